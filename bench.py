@@ -1,0 +1,426 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 k-mer counting front end.
+
+Workload (one step): the isolate-scale configuration — a synthetic 5 Mbp genome
+(GC 0.51, seven inserted 5 kb repeat copies at >= 99% identity), 150 bp pairs at
+100x (1.67M pairs), fragments N(350, 30), 0.5% substitutions, Phred 30-40 with the
+last 20 bases decaying to 15, ingested (trim/merge) into a ReadBank.  A step runs
+the genome estimator (ntHash k=21 + CMS 4 x 2^23 nibbles + two HLL p=14 over the
+first <= 150k raw pairs, with the reference's early stop) and then the build front
+end (pass-1 CMS 4 x 2^24 u16, pass-2 solid table, SolidKmerNode conversion) for
+the multi-k pass k = 21, 33, 55 (64/128-bit keys) and 77 (256-bit keys).
+
+Metric: k-mers/s = (estimator k-mer occurrences consumed + pass-1 and pass-2 k-mer
+occurrences of every k) / step time.  `value` keeps the bank and the estimator
+sample resident in HBM; `e2e` runs the same step through the C ABI from pinned
+host buffers (bank and sample uploaded, every solid table exported every step).
+
+--impl reference times the reference's algorithm on the host cores instead: the
+oracle's C++ restatement in its multithreaded (rayon-like) mode, on a bounded
+sample of the same workload per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+KS = [21, 33, 55, 77]
+WORKLOAD = dict(seed=43, genome_len=5_000_000, gc=0.51, n_repeats=7, repeat_len=5000, repeat_identity=0.99,
+                coverage=100.0, sub_rate=0.005, indel_rate=0.0)
+CMS_LOG2W = 24
+COUNTER_BITS = 16
+HLL_P = 14
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--counter-bits", type=int, default=COUNTER_BITS, choices=[4, 16])
+    ap.add_argument("--scale", type=float, default=1.0, help="coverage multiplier (quick runs)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def kmers_in(bank, k: int, min_len: int) -> int:
+    tot = 0
+    for a in bank.arenas:
+        L = a.lengths.astype(np.int64)
+        L = L[L >= min_len]
+        tot += int((L - k + 1).sum())
+    return tot
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.device), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def make_workload(rank: int, scale: float):
+    from fastbact_gb300 import api
+
+    wl = dict(WORKLOAD)
+    wl["seed"] = WORKLOAD["seed"] + 1000 * rank  # independent isolate per rank (weak scaling)
+    wl["coverage"] = WORKLOAD["coverage"] * scale
+    p = api.synth_params(**wl)
+    t0 = time.time()
+    bank, st, sample, n_sample, stats = api.synth_isolate(p, threads=0, sample_pairs=150_000)
+    gen_s = time.time() - t0
+    return p, bank, st, sample, n_sample, stats, gen_s
+
+
+def pinned_copy(a: np.ndarray) -> np.ndarray:
+    """Copy of `a` in page-locked host memory (torch allocator)."""
+    import torch
+
+    t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+    out = t.numpy().view(a.dtype)[: a.size]
+    out[...] = a
+    out._keepalive = t  # noqa: SLF001  (keeps the pinned block alive)
+    return out
+
+
+def pinned_bank(bank):
+    from fastbact_gb300 import api
+
+    arenas = []
+    for a in bank.arenas:
+        arenas.append(api.BitSeqArena(pinned_copy(a.data), pinned_copy(a.offsets), pinned_copy(a.lengths),
+                                      pinned_copy(a.pair_idx) if a.pair_idx is not None else None))
+    return api.ReadBank(*arenas)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world, local):
+    import torch
+
+    from fastbact_gb300 import api
+    from fastbact_gb300.build import build
+
+    build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    p, bank, ist, sample, n_sample, stats, gen_s = make_workload(rank, args.scale)
+    ctx = api.Context(local, pool_bytes=int(os.environ.get("FBK_POOL_BYTES", str(60 << 30))))
+    dbank = api.DeviceBank(ctx, bank)
+    dsample = api.DeviceBank(ctx, sample)
+    ctx.sync()
+    cb = args.counter_bits
+
+    def step(ctx, dbank, dsample, sample_lengths, export=False):
+        ge, _, _ = api.estimate_bank(ctx, dsample, sample_lengths, n_sample, stats, max_pairs=250_000, target_cov=110.0)
+        res = []
+        for k in KS:
+            t = api.build_cdbg_ext(dbank, k, None, ge.genome_size, ctx=ctx, counter_bits=cb, cms_log2_width=CMS_LOG2W)
+            info = t.info()
+            res.append((k, info[0], info[1], t.pushes()))
+            if export:
+                t.export()
+            t.release()
+        return ge, res
+
+    sample_len = np.ascontiguousarray(sample.lengths)
+    for _ in range(args.warmup):
+        ge, res = step(ctx, dbank, dsample, sample_len)
+    kmers_est = ge.m_sample
+    kmers_pass = {k: (kmers_in(bank, k, k), kmers_in(bank, k, k + 1)) for k in KS}
+    kmers_step = kmers_est + sum(a + b for a, b in kmers_pass.values())
+
+    # ---- device-resident timed region -------------------------------------------
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ctx.sync()
+    ctx.timing_reset()
+    ctx.set_timing(True)
+    launches0 = ctx.launch_count()
+    clocks.start()
+    ctx.record(0)
+    for _ in range(args.steps):
+        ge, res = step(ctx, dbank, dsample, sample_len)
+    ctx.record(1)
+    ms = ctx.elapsed_ms(0, 1)
+    clk = clocks.stop()
+    ctx.sync()
+    torch.cuda.synchronize()
+    launches = ctx.launch_count() - launches0
+    kernel_ms = {n: ctx.timing(n) for n in ("pass1", "pass2", "convert", "table_init", "est_", "clamp", "subsample")}
+    ctx.set_timing(False)
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    total_kmers = kmers_step * args.steps * world
+    value = total_kmers / (ms / 1e3)
+
+    # ---- roofline of the dominant kernel -------------------------------------------
+    c_b = 0.5 if cb == 4 else 2.0
+    bank_bytes = bank.total_bases() / 4.0
+    key_bytes = {21: 8, 33: 16, 55: 16, 77: 32}
+    pushes = {k: pu for (k, _, _, pu) in res}
+    alg = {
+        "pass1": sum(bank_bytes + kmers_pass[k][0] * 8 * c_b for k in KS),
+        "pass2": sum(bank_bytes + kmers_pass[k][1] * 4 * c_b + pushes[k] * 2 * (key_bytes[k] + 2 + 16) for k in KS),
+    }
+    dom = max(("pass1", "pass2"), key=lambda n: kernel_ms[n][0])
+    dom_ms, dom_launches = kernel_ms[dom]
+    per_launch_ms = dom_ms / max(dom_launches, 1)
+    per_launch_bytes = alg[dom] / len(KS)
+    achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
+    peaks_path = ROOT / "MEASURED_PEAKS.json"
+    if peaks_path.exists():
+        peak = json.loads(peaks_path.read_text())["hbm_gbs"]
+        peak_src = "measured"
+    else:
+        peak = 6800.0
+        peak_src = "fallback"
+    traffic = None
+    tpath = ROOT / "profiles" / "traffic.json"
+    if tpath.exists():
+        traffic = json.loads(tpath.read_text()).get(f"{dom}_{'u16' if cb == 16 else 'nibble'}")
+
+    # ---- end to end through the C ABI from pinned host memory ------------------------
+    e2e = None
+    if not args.no_e2e:
+        pb = pinned_bank(bank)
+        ps = api.BitSeqArena(pinned_copy(sample.data), pinned_copy(sample.offsets), pinned_copy(sample.lengths))
+        h2d = sum(a.data.nbytes + a.offsets.nbytes + a.lengths.nbytes + (a.pair_idx.nbytes if a.pair_idx is not None else 0)
+                  for a in pb.arenas) + ps.data.nbytes + ps.offsets.nbytes + ps.lengths.nbytes
+
+        def e2e_step():
+            db = api.DeviceBank(ctx, pb)
+            ds = api.DeviceBank(ctx, ps)
+            ge2, res2 = step(ctx, db, ds, ps.lengths, export=True)
+            db.release()
+            ds.release()
+            return ge2, res2
+
+        e2e_step()
+        if world > 1:
+            torch.distributed.barrier()
+        ctx.sync()
+        t0 = time.perf_counter()
+        ctx.record(2)
+        for _ in range(args.steps):
+            ge2, res2 = e2e_step()
+        ctx.record(3)
+        e_ms = ctx.elapsed_ms(2, 3)
+        wall = (time.perf_counter() - t0) * 1e3
+        e_ms = max(e_ms, wall)
+        if world > 1:
+            t = torch.tensor([e_ms], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e_ms = float(t.item())
+        d2h = sum(n_solid * ((key_bytes[k]) + 2 + 1) for (k, _, n_solid, _) in res2)
+        e2e = {"value": total_kmers / (e_ms / 1e3), "unit": "k-mers/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e_ms / args.steps}
+
+    # ---- CPU baseline (oracle restatement, bounded sample) ------------------------
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_arm(bank, sample, n_sample, stats, budget_s=args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": "k-mers/s ntHash+CMS+HLL+count (estimator + multi-k build front end)",
+            "value": value, "unit": "k-mers/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64/u16 integer", "data": "synthetic (seeded generator; no dataset)",
+            "config": {
+                "workload": "isolate-scale plain method: 5 Mbp genome GC 0.51, 7x5 kb repeats >=99% id, "
+                            "PE150 100x (1.67M pairs), N(350,30) fragments, 0.5% subs, Phred tail decay; "
+                            "multi-k 21,33,55 (64/128-bit) + 77 (256-bit)",
+                "genome_len": p.genome_len, "pairs": stats.exact_read_pairs, "bank_reads": bank.total_reads(),
+                "bank_bases": bank.total_bases(), "ks": KS, "cms": f"4 x 2^{CMS_LOG2W} {'u16' if cb == 16 else 'nibble'}",
+                "hll_p": HLL_P, "estimator_kmers": kmers_est,
+                "pass_kmers": {str(k): kmers_pass[k] for k in KS},
+                "solid": {str(k): n for (k, _, n, _) in res}, "table_keys": {str(k): n for (k, n, _, _) in res},
+                "genome_size_est": ge.genome_size, "parallelism": f"replicas x{world} (one isolate per GPU)",
+                "l2": "per-step working set exceeds L2 (bank 115 MB + CMS 128 MB + solid tables >= 1 GB)",
+                "generation_s": round(gen_s, 1),
+            },
+            "kernel_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in kernel_ms.items()},
+            "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+                         "alg_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    ctx.close()
+
+
+# ---------------------------------------------------------------------------
+# CPU arm: the oracle restatement of the reference algorithm, multithreaded
+# ---------------------------------------------------------------------------
+def cpu_arm(bank, sample, n_sample, stats, budget_s: float, threads: int = 0):
+    """Times the reference algorithm (estimator sample loop + build passes 1-2 for each
+    k) on a bounded prefix of the bank's reads; returns k-mers/s."""
+    from fastbact_gb300 import api
+    from oracle import orc
+
+    cores = threads or os.cpu_count() or 1
+    reads = [sample.extract_ascii(i) for i in range(2 * min(n_sample, 150_000))]
+    ost = orc.count_stats(**stats.__dict__)
+    t0 = time.perf_counter()
+    rc, oe, _, _ = orc.estimate_from_reads(reads, ost, 250_000, 110.0)
+    t_est = time.perf_counter() - t0
+    est_kmers = oe.m_sample
+
+    def sub_bank(frac):
+        arenas = []
+        for a in bank.arenas:
+            n = int(len(a) * frac)
+            if n == 0:
+                arenas.append(api.BitSeqArena())
+                continue
+            end_base = int(a.offsets[n - 1]) + int(a.lengths[n - 1])
+            nw = (end_base + 31) // 32
+            arenas.append(api.BitSeqArena(np.ascontiguousarray(a.data[:nw]), np.ascontiguousarray(a.offsets[:n]),
+                                          np.ascontiguousarray(a.lengths[:n])))
+        return api.ReadBank(*arenas)
+
+    # calibrate on 0.5% of the reads, then size the sample to the budget
+    def run(frac):
+        b = sub_bank(frac)
+        t = time.perf_counter()
+        km = 0
+        for k in KS:
+            kb = api.key_bits_for_k(k)
+            cms, tab, _, _ = orc.build_front(b, k, kb, CMS_LOG2W, 4, None, threads=cores)
+            del cms, tab
+            km += kmers_in(b, k, k) + kmers_in(b, k, k + 1)
+        return km, time.perf_counter() - t
+
+    km, dt = run(0.005)
+    rate = km / max(dt, 1e-6)
+    full = sum(kmers_in(bank, k, k) + kmers_in(bank, k, k + 1) for k in KS)
+    frac = min(1.0, max(0.005, (budget_s - t_est) * rate / max(full, 1)))
+    km, dt = run(frac)
+    value = (km + est_kmers) / (dt + t_est)
+    return {"value": value, "unit": "k-mers/s", "cores": cores, "kind": "port",
+            "sample": f"estimator sample loop ({est_kmers} k-mers, sequential as in the reference) + passes 1-2 at "
+                      f"k={KS} over the first {frac:.3%} of each arena's reads (nibble CMS, 64 mutex shards)",
+            "seconds": dt + t_est}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from fastbact_gb300.build import build
+
+    build()
+    _, bank, _, sample, n_sample, stats, _ = make_workload(0, args.scale)
+    per_step = max(5.0, min(20.0, 150.0 / max(args.steps + args.warmup, 1)))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_arm(bank, sample, n_sample, stats, budget_s=per_step)
+        if i >= args.warmup:
+            vals.append(r)
+    v = float(np.mean([r["value"] for r in vals]))
+    line = {"impl": "reference", "metric": "k-mers/s ntHash+CMS+HLL+count (estimator + multi-k build front end)",
+            "value": v, "unit": "k-mers/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean([r["seconds"] for r in vals])) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64/u8 integer", "data": "synthetic (seeded generator)",
+            "config": {"workload": "isolate-scale plain method (same as the GPU arm), bounded sample per step",
+                       "ks": KS},
+            "cpu_baseline": {"value": v, "unit": "k-mers/s", "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": "k-mers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

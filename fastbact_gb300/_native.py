@@ -1,0 +1,212 @@
+"""ctypes binding of the C ABI in include/fbk.h and include/fbk_synth.h.
+
+The library is loaded from fastbact_gb300/_lib/libfbk.so (built in-tree by
+fastbact_gb300.build).  There is no fallback: if the library is missing the
+import of anything that needs it raises, so no CPU path can stand in for the
+device kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libfbk.so"
+
+u8p = C.POINTER(C.c_uint8)
+u16p = C.POINTER(C.c_uint16)
+u32p = C.POINTER(C.c_uint32)
+u64p = C.POINTER(C.c_uint64)
+vp = C.c_void_p
+
+FBK_OK = 0
+STATUS_NAMES = {
+    0: "FBK_OK", 1: "FBK_ERR_INVALID", 2: "FBK_ERR_CUDA", 3: "FBK_ERR_OOM", 4: "FBK_ERR_TABLE_FULL",
+    5: "FBK_ERR_TIMEOUT", 6: "FBK_ERR_IO", 7: "FBK_ERR_FORMAT", 8: "FBK_ERR_EMPTY", 9: "FBK_ERR_BUSY",
+    10: "FBK_ERR_NOT_READY", 11: "FBK_ERR_NO_DEVICE",
+}
+
+
+class ArenaView(C.Structure):
+    _fields_ = [("data", u64p), ("n_words", C.c_uint64), ("offsets", u64p), ("lengths", u32p),
+                ("n_seqs", C.c_uint64), ("pair_idx", u32p)]
+
+
+class CountStats(C.Structure):
+    _fields_ = [("exact_read_pairs", C.c_uint64), ("total_bases_r1", C.c_uint64), ("total_bases_r2", C.c_uint64),
+                ("total_bases", C.c_uint64), ("min_read_len", C.c_uint64), ("max_read_len", C.c_uint64),
+                ("mean_read_len", C.c_double), ("median_read_len", C.c_uint64)]
+
+
+class GenomeEstimate(C.Structure):
+    _fields_ = [("genome_size", C.c_uint64), ("exact_read_pairs", C.c_uint64), ("total_bases", C.c_uint64),
+                ("median_read_len", C.c_uint64), ("max_read_len", C.c_uint64), ("estimated_cov", C.c_double),
+                ("subsample_factor", C.c_double), ("kmers", C.c_uint64 * 8), ("n_kmers", C.c_uint64),
+                ("confidence", C.c_int32), ("_pad", C.c_int32), ("u_ge_1", C.c_uint64), ("u_ge_2", C.c_uint64),
+                ("sample_kmer_depth", C.c_double), ("pairs_sampled", C.c_uint64), ("m_sample", C.c_uint64)]
+
+
+class EstimatorParams(C.Structure):
+    _fields_ = [("k", C.c_uint32), ("cms_log2_width", C.c_uint32), ("hll_p", C.c_uint32), ("_pad", C.c_uint32),
+                ("sample_cap", C.c_uint64), ("max_pairs", C.c_uint64), ("target_cov", C.c_double)]
+
+
+class Subsample(C.Structure):
+    _fields_ = [("factor", C.c_double), ("seed", C.c_uint64)]
+
+
+class BuildParams(C.Structure):
+    _fields_ = [("k", C.c_uint32), ("key_bits", C.c_uint32), ("cms_log2_width", C.c_uint32),
+                ("counter_bits", C.c_uint32), ("t_solid", C.c_uint32), ("min_trans_cov", C.c_uint32),
+                ("table_log2_cap", C.c_uint32), ("_pad", C.c_uint32), ("genome_size", C.c_uint64)]
+
+
+class SynthParams(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("genome_len", C.c_uint64), ("gc", C.c_double), ("n_repeats", C.c_uint32),
+                ("repeat_len", C.c_uint32), ("repeat_identity", C.c_double), ("tandem_copies", C.c_uint32),
+                ("tandem_unit", C.c_uint32), ("read_len", C.c_uint32), ("_pad", C.c_uint32),
+                ("coverage", C.c_double), ("frag_mean", C.c_double), ("frag_sd", C.c_double),
+                ("sub_rate", C.c_double), ("indel_rate", C.c_double), ("q_lo", C.c_uint32), ("q_hi", C.c_uint32),
+                ("tail_len", C.c_uint32), ("tail_q", C.c_uint32)]
+
+
+S = C.c_int  # fbk_status
+P = C.POINTER
+
+# name -> (restype, argtypes); every symbol the headers declare.
+SIGNATURES = {
+    "fbk_status_str": (C.c_char_p, [S]),
+    "fbk_version": (C.c_char_p, []),
+    "fbk_ctx_create": (S, [C.c_int, C.c_uint64, P(vp)]),
+    "fbk_ctx_destroy": (S, [vp]),
+    "fbk_last_error": (S, [vp, C.c_char_p, C.c_size_t]),
+    "fbk_ctx_sync": (S, [vp]),
+    "fbk_ctx_set_timing": (S, [vp, C.c_int]),
+    "fbk_ctx_timing": (S, [vp, C.c_char_p, P(C.c_double), u64p]),
+    "fbk_ctx_timing_reset": (S, [vp]),
+    "fbk_ctx_event_record": (S, [vp, C.c_int]),
+    "fbk_ctx_event_elapsed": (S, [vp, C.c_int, C.c_int, P(C.c_double)]),
+    "fbk_ctx_launch_count": (S, [vp, u64p]),
+    "fbk_ctx_mem_info": (S, [vp, u64p, u64p]),
+    "fbk_bank_upload": (S, [vp, P(ArenaView), P(vp)]),
+    "fbk_bank_info": (S, [vp, u64p, u64p]),
+    "fbk_bank_release": (S, [vp]),
+    "fbk_cms_width_for_genome_size": (C.c_uint64, [C.c_uint64]),
+    "fbk_cms_create": (S, [vp, C.c_uint32, C.c_uint32, P(vp)]),
+    "fbk_cms_clear": (S, [vp]),
+    "fbk_cms_add_keys": (S, [vp, u64p, C.c_uint64]),
+    "fbk_cms_estimate_keys": (S, [vp, u64p, C.c_uint64, u32p]),
+    "fbk_cms_add_bank": (S, [vp, vp, C.c_uint32, C.c_uint32, P(Subsample)]),
+    "fbk_cms_add_contigs": (S, [vp, u8p, u64p, C.c_uint64, C.c_uint32, C.c_uint32]),
+    "fbk_cms_nbytes": (S, [vp, u64p]),
+    "fbk_cms_export": (S, [vp, u8p, C.c_uint64]),
+    "fbk_cms_merge": (S, [vp, vp]),
+    "fbk_cms_release": (S, [vp]),
+    "fbk_hll_create": (S, [vp, C.c_uint32, P(vp)]),
+    "fbk_hll_add_hashes": (S, [vp, u64p, C.c_uint64]),
+    "fbk_hll_add_canonical_hashes": (S, [vp, u64p, C.c_uint64]),
+    "fbk_hll_merge": (S, [vp, vp]),
+    "fbk_hll_export": (S, [vp, u8p, C.c_uint64]),
+    "fbk_hll_estimate": (S, [vp, P(C.c_double)]),
+    "fbk_hll_release": (S, [vp]),
+    "fbk_hll_estimate_registers": (C.c_double, [u8p, C.c_uint32]),
+    "fbk_nthash_arena": (S, [vp, P(ArenaView), C.c_uint32, u64p, C.c_uint64, u64p]),
+    "fbk_canonical_kmers_arena": (S, [vp, P(ArenaView), C.c_uint32, C.c_uint32, u64p, u8p, C.c_uint64, u64p]),
+    "fbk_solid_build": (S, [vp, vp, vp, P(BuildParams), P(Subsample), u8p, u64p, C.c_uint64, P(vp)]),
+    "fbk_build_front": (S, [vp, vp, P(BuildParams), P(Subsample), u8p, u64p, C.c_uint64, P(vp), P(vp)]),
+    "fbk_table_info": (S, [vp, u64p, u64p, u64p]),
+    "fbk_table_export": (S, [vp, u64p, u16p, u8p, C.c_uint64, u64p]),
+    "fbk_table_export_acc": (S, [vp, u64p, u16p, u16p, C.c_uint64, u64p]),
+    "fbk_table_pushes": (S, [vp, u64p]),
+    "fbk_table_digest": (S, [vp, u64p, u64p]),
+    "fbk_table_release": (S, [vp]),
+    "fbk_estimator_defaults": (None, [P(EstimatorParams)]),
+    "fbk_estimate_sample": (S, [vp, P(ArenaView), C.c_uint64, P(CountStats), P(EstimatorParams), P(GenomeEstimate), u8p, u8p]),
+    "fbk_estimate_bank": (S, [vp, vp, u32p, C.c_uint64, P(CountStats), P(EstimatorParams), P(GenomeEstimate), u8p, u8p]),
+    "fbk_count_fastx_exact": (S, [C.c_char_p, C.c_char_p, P(CountStats), C.c_char_p, C.c_size_t]),
+    "fbk_estimate_genome": (S, [vp, C.c_char_p, C.c_char_p, C.c_uint64, C.c_double, P(GenomeEstimate)]),
+    "fbk_compute_dynamic_kmers": (C.c_int, [C.c_uint64, C.c_int64, u64p, C.c_int]),
+    "fbk_subsample_mask": (S, [vp, C.c_uint64, P(Subsample), u64p]),
+    "fbk_ingest_fastq": (S, [C.c_char_p, C.c_char_p, C.c_double, C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_uint64,
+                             P(vp), C.c_char_p, C.c_size_t]),
+    "fbk_hbank_arena": (S, [vp, C.c_int, P(ArenaView)]),
+    "fbk_hbank_stats": (S, [vp, u64p, u64p, u64p, u64p, u64p, u64p]),
+    "fbk_hbank_free": (None, [vp]),
+    "fbk_trim_adapter": (C.c_uint64, [u8p, C.c_uint64]),
+    "fbk_trim_quality": (C.c_int64, [u8p, u8p, C.c_uint64, C.c_uint32, C.c_uint64]),
+    "fbk_merge_read_pair": (C.c_int64, [u8p, u8p, C.c_uint64, u8p, u8p, C.c_uint64, C.c_uint64, C.c_double, u8p, u64p, u64p]),
+    "fbk_synth_defaults": (None, [P(SynthParams)]),
+    "fbk_synth_n_pairs": (C.c_uint64, [P(SynthParams)]),
+    "fbk_synth_genome": (S, [P(SynthParams), u8p]),
+    "fbk_synth_pairs": (S, [P(SynthParams), u8p, C.c_uint64, C.c_uint64, u8p, u8p, u8p, u8p]),
+    "fbk_synth_write_fastq": (S, [P(SynthParams), C.c_char_p, C.c_char_p]),
+    "fbk_synth_isolate": (S, [P(SynthParams), C.c_int, C.c_uint64, C.c_uint32, C.c_int, C.c_int, P(vp), C.c_uint64, P(vp),
+                              P(CountStats)]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads libfbk.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: run fastbact_gb300.build.build() (the device kernels have no fallback)")
+        L = C.CDLL(str(LIB_PATH), mode=C.RTLD_GLOBAL)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class FbkError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+        self.msg = msg
+
+
+def check(status: int, ctx=None, what: str = "") -> None:
+    if status == FBK_OK:
+        return
+    msg = what
+    if ctx is not None:
+        buf = C.create_string_buffer(4096)
+        lib().fbk_last_error(ctx, buf, len(buf))
+        if buf.value:
+            msg = f"{what}: {buf.value.decode(errors='replace')}" if what else buf.value.decode(errors="replace")
+    raise FbkError(status, msg)
+
+
+def ptr(a: np.ndarray | None, ctype=None):
+    """Pointer to a contiguous numpy array (None -> NULL)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "array must be contiguous"
+    t = ctype or {np.dtype(np.uint8): C.c_uint8, np.dtype(np.uint16): C.c_uint16,
+                  np.dtype(np.uint32): C.c_uint32, np.dtype(np.uint64): C.c_uint64}[a.dtype]
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def arena_view(data: np.ndarray, offsets: np.ndarray, lengths: np.ndarray, pair_idx: np.ndarray | None = None) -> ArenaView:
+    v = ArenaView()
+    v.data = ptr(data)
+    v.n_words = data.size
+    v.offsets = ptr(offsets)
+    v.lengths = ptr(lengths)
+    v.n_seqs = offsets.size
+    v.pair_idx = ptr(pair_idx) if pair_idx is not None else None
+    return v
+
+
+def exported_symbols() -> list[str]:
+    return sorted(SIGNATURES)
+
+
+os.environ.setdefault("CUDA_MODULE_LOADING", "LAZY")

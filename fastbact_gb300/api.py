@@ -1,0 +1,750 @@
+"""Python mirror of the reference's hot-path interface, backed by libfbk.so.
+
+Names, argument meaning and error behaviour follow the Rust entry points of
+fastBact (paths inside its repository):
+
+* ``ReadBank`` / ``BitSeqArena``          — src/common/bitseq.rs:145-399
+* ``CountMinSketch``                       — src/common/sketch.rs:121-253
+* ``HyperLogLog``                          — src/common/sketch.rs:24-115
+* ``count_fastx_exact``, ``estimate_genome``, ``compute_dynamic_kmers``
+                                           — src/ingest/estimator.rs:104-440
+* ``ingest_reads_ext_with_seed``           — src/ingest/trim_merge.rs:307-417
+* ``build_cdbg*``                          — src/graph/build.rs:37-328 (front end:
+  passes 1-2 and the SolidKmerNode conversion; the returned ``SolidTable`` is the
+  table the unitig compaction walks)
+
+Every computation on k-mers runs in the device kernels; this module only moves
+buffers and parameters across the C ABI.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+from ._native import check, ptr
+
+CONFIDENCE = {0: "HIGH", 1: "LOW_COVERAGE_WARNING", 2: "UNRELIABLE"}
+
+
+def key_bits_for_k(k: int) -> int:
+    """KmerInt width the reference dispatches to (src/main.rs:350-364)."""
+    if k <= 31:
+        return 64
+    if k <= 63:
+        return 128
+    if k <= 127:
+        return 256
+    raise ValueError(f"k={k} exceeds 127")
+
+
+def splitmix64(z: int) -> int:
+    z &= (1 << 64) - 1
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & ((1 << 64) - 1)
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & ((1 << 64) - 1)
+    return z ^ (z >> 31)
+
+
+# ---------------------------------------------------------------------------
+# context
+# ---------------------------------------------------------------------------
+class Context:
+    """One device, one stream, one (optional) memory pool."""
+
+    def __init__(self, device: int = 0, pool_bytes: int = 0):
+        self._h = C.c_void_p()
+        st = N.lib().fbk_ctx_create(device, pool_bytes, C.byref(self._h))
+        if st != N.FBK_OK:
+            raise N.FbkError(st, f"fbk_ctx_create(device={device})")
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            N.lib().fbk_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        check(N.lib().fbk_ctx_sync(self._h), self._h)
+
+    def set_timing(self, on: bool):
+        check(N.lib().fbk_ctx_set_timing(self._h, 1 if on else 0), self._h)
+
+    def timing(self, prefix: str = "") -> tuple[float, int]:
+        ms, n = C.c_double(), C.c_uint64()
+        check(N.lib().fbk_ctx_timing(self._h, prefix.encode(), C.byref(ms), C.byref(n)), self._h)
+        return ms.value, n.value
+
+    def timing_reset(self):
+        check(N.lib().fbk_ctx_timing_reset(self._h), self._h)
+
+    def record(self, slot: int) -> None:
+        check(N.lib().fbk_ctx_event_record(self._h, slot), self._h)
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_double()
+        check(N.lib().fbk_ctx_event_elapsed(self._h, a, b, C.byref(ms)), self._h)
+        return ms.value
+
+    def launch_count(self) -> int:
+        n = C.c_uint64()
+        check(N.lib().fbk_ctx_launch_count(self._h, C.byref(n)), self._h)
+        return n.value
+
+    def mem_info(self) -> tuple[int, int]:
+        u, s = C.c_uint64(), C.c_uint64()
+        check(N.lib().fbk_ctx_mem_info(self._h, C.byref(u), C.byref(s)), self._h)
+        return u.value, s.value
+
+
+_default_ctx: Context | None = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+# ---------------------------------------------------------------------------
+# read bank (host side)
+# ---------------------------------------------------------------------------
+_A2B = np.zeros(256, dtype=np.uint8)
+for _c, _v in ((b"C", 1), (b"c", 1), (b"G", 2), (b"g", 2), (b"T", 3), (b"t", 3)):
+    _A2B[_c[0]] = _v
+
+
+@dataclass
+class BitSeqArena:
+    """BitSeqArena: base i at bits 2*(i%32) of data[i/32] (bitseq.rs:145-222)."""
+    data: np.ndarray = field(default_factory=lambda: np.zeros(0, np.uint64))
+    offsets: np.ndarray = field(default_factory=lambda: np.zeros(0, np.uint64))
+    lengths: np.ndarray = field(default_factory=lambda: np.zeros(0, np.uint32))
+    pair_idx: np.ndarray | None = None
+
+    @staticmethod
+    def from_seqs(seqs: list[bytes], pair_idx: list[int] | None = None) -> "BitSeqArena":
+        lengths = np.array([len(s) for s in seqs], dtype=np.uint32)
+        offsets = np.zeros(len(seqs), dtype=np.uint64)
+        if len(seqs):
+            offsets[1:] = np.cumsum(lengths[:-1], dtype=np.uint64)
+        total = int(lengths.sum(dtype=np.uint64))
+        codes = _A2B[np.frombuffer(b"".join(seqs), dtype=np.uint8)] if total else np.zeros(0, np.uint8)
+        return BitSeqArena(pack_codes(codes), offsets, lengths,
+                           None if pair_idx is None else np.asarray(pair_idx, dtype=np.uint32))
+
+    def __len__(self):
+        return int(self.offsets.size)
+
+    def total_bases(self) -> int:
+        return int(self.lengths.sum(dtype=np.uint64))
+
+    def extract_ascii(self, i: int) -> bytes:
+        o, n = int(self.offsets[i]), int(self.lengths[i])
+        g = np.arange(o, o + n, dtype=np.uint64)
+        codes = (self.data[g >> np.uint64(5)] >> ((g & np.uint64(31)) << np.uint64(1))) & np.uint64(3)
+        return np.frombuffer(b"ACGT", dtype=np.uint8)[codes.astype(np.intp)].tobytes()
+
+    def view(self) -> N.ArenaView:
+        return N.arena_view(self.data, self.offsets, self.lengths, self.pair_idx)
+
+
+def pack_codes(codes: np.ndarray) -> np.ndarray:
+    """Packs 2-bit codes LSB-first, 32 per u64 word."""
+    n = codes.size
+    nw = (n + 31) // 32
+    padded = np.zeros(nw * 32, dtype=np.uint64)
+    padded[:n] = codes
+    shifts = (np.arange(32, dtype=np.uint64) * np.uint64(2))
+    return np.bitwise_or.reduce(padded.reshape(nw, 32) << shifts, axis=1).astype(np.uint64) if nw else np.zeros(0, np.uint64)
+
+
+@dataclass
+class IngestStats:
+    input_read_pairs: int = 0
+    retained_read_pairs: int = 0
+    merged_pairs_count: int = 0
+    unmerged_pairs_count: int = 0
+    bases_before_trim: int = 0
+    bases_after_trim: int = 0
+
+
+@dataclass
+class ReadBank:
+    """ReadBank (bitseq.rs:350-399): merged reads, then unmerged R1, then R2."""
+    merged_reads: BitSeqArena = field(default_factory=BitSeqArena)
+    pe_forward: BitSeqArena = field(default_factory=BitSeqArena)
+    pe_reverse: BitSeqArena = field(default_factory=BitSeqArena)
+
+    @property
+    def arenas(self):
+        return [self.merged_reads, self.pe_forward, self.pe_reverse]
+
+    def total_reads(self) -> int:
+        return sum(len(a) for a in self.arenas)
+
+    def total_bases(self) -> int:
+        return sum(a.total_bases() for a in self.arenas)
+
+    def views(self):
+        arr = (N.ArenaView * 3)()
+        for i, a in enumerate(self.arenas):
+            arr[i] = a.view()
+        return arr
+
+
+def _arena_from_view(v: N.ArenaView) -> BitSeqArena:
+    def cp(p, n, dt):
+        if n == 0 or not p:
+            return np.zeros(0, dt)
+        return np.ctypeslib.as_array(p, shape=(n,)).astype(dt, copy=True)
+
+    return BitSeqArena(cp(v.data, v.n_words, np.uint64), cp(v.offsets, v.n_seqs, np.uint64),
+                       cp(v.lengths, v.n_seqs, np.uint32), cp(v.pair_idx, v.n_seqs, np.uint32))
+
+
+def _bank_from_hbank(h) -> tuple[ReadBank, IngestStats]:
+    L = N.lib()
+    arenas = []
+    for i in range(3):
+        v = N.ArenaView()
+        check(L.fbk_hbank_arena(h, i, C.byref(v)))
+        arenas.append(_arena_from_view(v))
+    vals = [C.c_uint64() for _ in range(6)]
+    check(L.fbk_hbank_stats(h, *[C.byref(x) for x in vals]))
+    st = IngestStats(vals[0].value, vals[1].value, vals[2].value, vals[3].value, vals[4].value, vals[5].value)
+    return ReadBank(*arenas), st
+
+
+def ingest_reads_ext_with_seed(r1: str, r2: str, subsample_factor: float, min_len: int, min_qual: int,
+                               enable_trim: bool = True, enable_merge: bool = True, seed: int = 0):
+    """trim_merge.rs:307-417 (host-side CPU ingest producing the bank)."""
+    h = C.c_void_p()
+    err = C.create_string_buffer(1024)
+    st = N.lib().fbk_ingest_fastq(str(r1).encode(), str(r2).encode(), subsample_factor, min_len, min_qual,
+                                  int(enable_trim), int(enable_merge), seed, C.byref(h), err, len(err))
+    if st != N.FBK_OK:
+        raise N.FbkError(st, err.value.decode(errors="replace"))
+    try:
+        return _bank_from_hbank(h)
+    finally:
+        N.lib().fbk_hbank_free(h)
+
+
+# ---------------------------------------------------------------------------
+# estimator
+# ---------------------------------------------------------------------------
+@dataclass
+class ExactCountStats:
+    exact_read_pairs: int
+    total_bases_r1: int
+    total_bases_r2: int
+    total_bases: int
+    min_read_len: int
+    max_read_len: int
+    mean_read_len: float
+    median_read_len: int
+
+    @staticmethod
+    def from_c(s: N.CountStats) -> "ExactCountStats":
+        return ExactCountStats(s.exact_read_pairs, s.total_bases_r1, s.total_bases_r2, s.total_bases,
+                               s.min_read_len, s.max_read_len, s.mean_read_len, s.median_read_len)
+
+    def to_c(self) -> N.CountStats:
+        s = N.CountStats()
+        for f in ("exact_read_pairs", "total_bases_r1", "total_bases_r2", "total_bases", "min_read_len",
+                  "max_read_len", "mean_read_len", "median_read_len"):
+            setattr(s, f, getattr(self, f))
+        return s
+
+
+@dataclass
+class GenomeEstimate:
+    genome_size: int
+    exact_read_pairs: int
+    total_bases: int
+    median_read_len: int
+    max_read_len: int
+    estimated_cov: float
+    subsample_factor: float
+    kmers: list
+    confidence: str
+    u_ge_1: int
+    u_ge_2: int
+    sample_kmer_depth: float
+    pairs_sampled: int = 0
+    m_sample: int = 0
+
+    @staticmethod
+    def from_c(e: N.GenomeEstimate) -> "GenomeEstimate":
+        return GenomeEstimate(e.genome_size, e.exact_read_pairs, e.total_bases, e.median_read_len, e.max_read_len,
+                              e.estimated_cov, e.subsample_factor, [e.kmers[i] for i in range(e.n_kmers)],
+                              CONFIDENCE[e.confidence], e.u_ge_1, e.u_ge_2, e.sample_kmer_depth, e.pairs_sampled,
+                              e.m_sample)
+
+
+def count_fastx_exact(r1: str, r2: str) -> ExactCountStats:
+    s = N.CountStats()
+    err = C.create_string_buffer(2048)
+    st = N.lib().fbk_count_fastx_exact(str(r1).encode(), str(r2).encode(), C.byref(s), err, len(err))
+    if st != N.FBK_OK:
+        raise N.FbkError(st, err.value.decode(errors="replace"))
+    return ExactCountStats.from_c(s)
+
+
+def compute_dynamic_kmers(median_len: int, target_max_k: int | None = None) -> list[int]:
+    out = (C.c_uint64 * 16)()
+    n = N.lib().fbk_compute_dynamic_kmers(median_len, -1 if target_max_k is None else target_max_k, out, 16)
+    return [out[i] for i in range(n)]
+
+
+def estimator_params(**kw) -> N.EstimatorParams:
+    p = N.EstimatorParams()
+    N.lib().fbk_estimator_defaults(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def estimate_genome(r1: str, r2: str, max_pairs: int, target_cov: float, ctx: Context | None = None) -> GenomeEstimate:
+    """estimator.rs:286-440: FASTQ scan on the host, sample loop on the device."""
+    ctx = ctx or default_context()
+    e = N.GenomeEstimate()
+    check(N.lib().fbk_estimate_genome(ctx.handle, str(r1).encode(), str(r2).encode(), max_pairs, target_cov,
+                                      C.byref(e)), ctx.handle, "estimate_genome")
+    return GenomeEstimate.from_c(e)
+
+
+def estimate_sample(ctx: Context, sample: BitSeqArena, n_pairs: int, stats: ExactCountStats, **params):
+    """Device sample loop over packed raw reads (R1,R2 interleaved per pair).
+    Returns (GenomeEstimate, regs_total, regs_solid)."""
+    p = estimator_params(**params)
+    m = 1 << p.hll_p
+    rt = np.zeros(m, np.uint8)
+    rs = np.zeros(m, np.uint8)
+    v = sample.view()
+    cs = stats.to_c()
+    e = N.GenomeEstimate()
+    check(N.lib().fbk_estimate_sample(ctx.handle, C.byref(v), n_pairs, C.byref(cs), C.byref(p), C.byref(e), ptr(rt),
+                                      ptr(rs)), ctx.handle, "estimate_sample")
+    return GenomeEstimate.from_c(e), rt, rs
+
+
+def estimate_bank(ctx: Context, sample_bank: "DeviceBank", lengths: np.ndarray, n_pairs: int, stats: ExactCountStats,
+                  want_registers: bool = False, **params):
+    """estimate_sample on an already uploaded sample (R1,R2 interleaved)."""
+    p = estimator_params(**params)
+    m = 1 << p.hll_p
+    rt = np.zeros(m, np.uint8) if want_registers else None
+    rs = np.zeros(m, np.uint8) if want_registers else None
+    cs = stats.to_c()
+    e = N.GenomeEstimate()
+    check(N.lib().fbk_estimate_bank(ctx.handle, sample_bank.handle, ptr(lengths), n_pairs, C.byref(cs), C.byref(p),
+                                    C.byref(e), ptr(rt), ptr(rs)), ctx.handle, "estimate_bank")
+    return GenomeEstimate.from_c(e), rt, rs
+
+
+# ---------------------------------------------------------------------------
+# device objects
+# ---------------------------------------------------------------------------
+class DeviceBank:
+    """A ReadBank uploaded to device memory."""
+
+    def __init__(self, ctx: Context, bank: ReadBank | BitSeqArena):
+        self.ctx = ctx
+        if isinstance(bank, BitSeqArena):
+            bank = ReadBank(merged_reads=bank)
+        self._views = bank.views()
+        self._h = C.c_void_p()
+        check(N.lib().fbk_bank_upload(ctx.handle, self._views, C.byref(self._h)), ctx.handle, "bank upload")
+        self.n_bases = bank.total_bases()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def release(self):
+        if self._h:
+            N.lib().fbk_bank_release(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+def _subsample(ss):
+    if ss is None:
+        return None
+    factor, seed = ss
+    s = N.Subsample()
+    s.factor = factor
+    s.seed = seed
+    return C.byref(s)
+
+
+class CountMinSketch:
+    """4-row Count-Min Sketch on the device (sketch.rs:121-253).  counter_bits=4 is
+    the reference nibble layout; 16 gives u16 counters."""
+
+    def __init__(self, width: int, ctx: Context | None = None, counter_bits: int = 4):
+        self.ctx = ctx or default_context()
+        if width & (width - 1):
+            width = 1 << (width - 1).bit_length()  # sketch.rs:141-143
+        self.width = width
+        self.counter_bits = counter_bits
+        self._h = C.c_void_p()
+        check(N.lib().fbk_cms_create(self.ctx.handle, width.bit_length() - 1, counter_bits, C.byref(self._h)),
+              self.ctx.handle, "cms create")
+
+    @staticmethod
+    def width_for_genome_size(g: int) -> int:
+        return N.lib().fbk_cms_width_for_genome_size(g)
+
+    @classmethod
+    def for_genome_size(cls, g: int, ctx: Context | None = None, counter_bits: int = 4):
+        return cls(cls.width_for_genome_size(g), ctx, counter_bits)
+
+    def add(self, keys) -> None:
+        k = np.ascontiguousarray(np.atleast_1d(np.asarray(keys, dtype=np.uint64)))
+        check(N.lib().fbk_cms_add_keys(self._h, ptr(k), k.size), self.ctx.handle, "cms add")
+
+    def estimate(self, keys) -> np.ndarray:
+        k = np.ascontiguousarray(np.atleast_1d(np.asarray(keys, dtype=np.uint64)))
+        out = np.zeros(k.size, np.uint32)
+        check(N.lib().fbk_cms_estimate_keys(self._h, ptr(k), k.size, ptr(out)), self.ctx.handle, "cms estimate")
+        return out
+
+    def add_bank(self, bank: DeviceBank, k: int, key_bits: int | None = None, subsample=None) -> None:
+        check(N.lib().fbk_cms_add_bank(self._h, bank.handle, k, key_bits or key_bits_for_k(k), _subsample(subsample)),
+              self.ctx.handle, "cms pass 1")
+
+    def add_contigs(self, contigs: list[bytes], k: int, key_bits: int | None = None) -> None:
+        ascii, offs = _contig_buffers(contigs)
+        check(N.lib().fbk_cms_add_contigs(self._h, ptr(ascii), ptr(offs), len(contigs), k, key_bits or key_bits_for_k(k)),
+              self.ctx.handle, "cms contigs")
+
+    def export(self) -> np.ndarray:
+        n = C.c_uint64()
+        check(N.lib().fbk_cms_nbytes(self._h, C.byref(n)))
+        out = np.zeros(n.value, np.uint8)
+        check(N.lib().fbk_cms_export(self._h, ptr(out), n.value), self.ctx.handle, "cms export")
+        return out
+
+    def merge(self, other: "CountMinSketch") -> None:
+        check(N.lib().fbk_cms_merge(self._h, other._h), self.ctx.handle, "cms merge")
+
+    def clear(self) -> None:
+        check(N.lib().fbk_cms_clear(self._h), self.ctx.handle)
+
+    def release(self):
+        if self._h:
+            N.lib().fbk_cms_release(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class HyperLogLog:
+    """HyperLogLog on the device (sketch.rs:24-115); p = 14 in the reference."""
+
+    def __init__(self, p: int = 14, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.p = p
+        self._h = C.c_void_p()
+        check(N.lib().fbk_hll_create(self.ctx.handle, p, C.byref(self._h)), self.ctx.handle, "hll create")
+
+    def add_hash(self, h) -> None:
+        a = np.ascontiguousarray(np.atleast_1d(np.asarray(h, dtype=np.uint64)))
+        check(N.lib().fbk_hll_add_hashes(self._h, ptr(a), a.size), self.ctx.handle)
+
+    def add_canonical_hash(self, h) -> None:
+        a = np.ascontiguousarray(np.atleast_1d(np.asarray(h, dtype=np.uint64)))
+        check(N.lib().fbk_hll_add_canonical_hashes(self._h, ptr(a), a.size), self.ctx.handle)
+
+    def merge(self, other: "HyperLogLog") -> None:
+        check(N.lib().fbk_hll_merge(self._h, other._h), self.ctx.handle)
+
+    def registers(self) -> np.ndarray:
+        r = np.zeros(1 << self.p, np.uint8)
+        check(N.lib().fbk_hll_export(self._h, ptr(r), r.size), self.ctx.handle)
+        return r
+
+    def estimate(self) -> float:
+        d = C.c_double()
+        check(N.lib().fbk_hll_estimate(self._h, C.byref(d)), self.ctx.handle)
+        return d.value
+
+    def release(self):
+        if self._h:
+            N.lib().fbk_hll_release(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class SolidTable:
+    """Device-resident solid k-mer table (SolidKmerNode rows, build.rs:295-328)."""
+
+    def __init__(self, ctx: Context, handle, k: int, key_bits: int):
+        self.ctx, self._h, self.k, self.key_bits = ctx, handle, k, key_bits
+        self.nw = key_bits // 64
+
+    def info(self) -> tuple[int, int, int]:
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        check(N.lib().fbk_table_info(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def __len__(self):
+        return self.info()[1]
+
+    def export(self, sort: bool = False):
+        """(keys[n, nw] big-endian words, cov u16, mask u8)."""
+        n_solid = self.info()[1]
+        keys = np.zeros((n_solid, self.nw), np.uint64)
+        cov = np.zeros(n_solid, np.uint16)
+        mask = np.zeros(n_solid, np.uint8)
+        n = C.c_uint64()
+        check(N.lib().fbk_table_export(self._h, ptr(keys.reshape(-1)), ptr(cov), ptr(mask), n_solid, C.byref(n)),
+              self.ctx.handle, "table export")
+        return sort_rows(keys, cov, mask) if sort else (keys, cov, mask)
+
+    def export_acc(self, sort: bool = True):
+        """Every accumulated key: (keys[n, nw], cov u16, edge_counts[n, 8] u16)."""
+        n_keys = self.info()[0]
+        keys = np.zeros((n_keys, self.nw), np.uint64)
+        cov = np.zeros(n_keys, np.uint16)
+        edges = np.zeros((n_keys, 8), np.uint16)
+        n = C.c_uint64()
+        check(N.lib().fbk_table_export_acc(self._h, ptr(keys.reshape(-1)), ptr(cov), ptr(edges.reshape(-1)), n_keys,
+                                           C.byref(n)), self.ctx.handle, "table export_acc")
+        return sort_rows(keys, cov, edges) if sort else (keys, cov, edges)
+
+    def pushes(self) -> int:
+        n = C.c_uint64()
+        check(N.lib().fbk_table_pushes(self._h, C.byref(n)))
+        return n.value
+
+    def digest(self) -> tuple[int, int]:
+        d, n = C.c_uint64(), C.c_uint64()
+        check(N.lib().fbk_table_digest(self._h, C.byref(d), C.byref(n)))
+        return d.value, n.value
+
+    def release(self):
+        if self._h:
+            N.lib().fbk_table_release(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+def sort_rows(keys: np.ndarray, *cols):
+    """Sorts rows by key (big-endian word order = KmerInt's Ord)."""
+    if keys.shape[0] == 0:
+        return (keys, *cols)
+    order = np.lexsort(tuple(keys[:, j] for j in reversed(range(keys.shape[1]))))
+    return (keys[order], *[c[order] for c in cols])
+
+
+def _contig_buffers(contigs: list[bytes]):
+    ascii = np.frombuffer(b"".join(contigs), dtype=np.uint8).copy() if contigs else np.zeros(1, np.uint8)
+    offs = np.zeros(len(contigs) + 1, np.uint64)
+    if contigs:
+        offs[1:] = np.cumsum([len(c) for c in contigs], dtype=np.uint64)
+    return ascii, offs
+
+
+def build_params(k: int, target_solid_cov: int | None = None, genome_size: int | None = None, key_bits: int | None = None,
+                 counter_bits: int = 4, cms_log2_width: int = 0, table_log2_cap: int = 0) -> N.BuildParams:
+    p = N.BuildParams()
+    p.k = k
+    p.key_bits = key_bits or key_bits_for_k(k)
+    p.cms_log2_width = cms_log2_width
+    p.counter_bits = counter_bits
+    p.t_solid = 2 if target_solid_cov is None else target_solid_cov          # build.rs:141
+    p.min_trans_cov = 3 if target_solid_cov is None else target_solid_cov    # build.rs:302
+    p.table_log2_cap = table_log2_cap
+    p.genome_size = genome_size or 0
+    return p
+
+
+def build_cdbg_with_contigs_ext(bank, contigs: list[bytes], k: int, target_solid_cov: int | None = None,
+                                genome_size: int | None = None, *, ctx: Context | None = None, key_bits: int | None = None,
+                                counter_bits: int = 4, cms_log2_width: int = 0, subsample=None, keep_cms: bool = False):
+    """Front end of build_cdbg_with_contigs_ext (build.rs:67-328): CMS pass 1, the
+    CMS-gated transition pass 2 and the SolidKmerNode conversion, on the device.
+    Returns the SolidTable (and the pass-1 CountMinSketch when keep_cms)."""
+    ctx = ctx or default_context()
+    dbank = bank if isinstance(bank, DeviceBank) else DeviceBank(ctx, bank)
+    p = build_params(k, target_solid_cov, genome_size, key_bits, counter_bits, cms_log2_width)
+    ascii, offs = _contig_buffers(contigs)
+    t, c = C.c_void_p(), C.c_void_p()
+    check(N.lib().fbk_build_front(ctx.handle, dbank.handle, C.byref(p), _subsample(subsample), ptr(ascii), ptr(offs),
+                                  len(contigs), C.byref(t), C.byref(c) if keep_cms else None), ctx.handle, "build front")
+    table = SolidTable(ctx, t, k, p.key_bits)
+    if keep_cms:
+        cms = CountMinSketch.__new__(CountMinSketch)
+        cms.ctx, cms._h, cms.counter_bits = ctx, c, counter_bits
+        cms.width = 1 << p.cms_log2_width if p.cms_log2_width else None
+        return table, cms
+    return table
+
+
+def build_cdbg(bank, k: int, target_solid_cov: int | None = None, **kw):
+    return build_cdbg_with_contigs_ext(bank, [], k, target_solid_cov, None, **kw)
+
+
+def build_cdbg_ext(bank, k: int, target_solid_cov: int | None = None, genome_size: int | None = None, **kw):
+    return build_cdbg_with_contigs_ext(bank, [], k, target_solid_cov, genome_size, **kw)
+
+
+def build_cdbg_with_contigs(bank, contigs: list[bytes], k: int, target_solid_cov: int | None = None, **kw):
+    return build_cdbg_with_contigs_ext(bank, contigs, k, target_solid_cov, None, **kw)
+
+
+def solid_build(ctx: Context, bank: DeviceBank, cms: CountMinSketch, k: int, target_solid_cov: int | None = None,
+                key_bits: int | None = None, contigs: list[bytes] | None = None, subsample=None,
+                table_log2_cap: int = 0) -> SolidTable:
+    """Pass 2 + conversion against an existing pass-1 sketch."""
+    p = build_params(k, target_solid_cov, None, key_bits, cms.counter_bits, 0, table_log2_cap)
+    contigs = contigs or []
+    ascii, offs = _contig_buffers(contigs)
+    t = C.c_void_p()
+    check(N.lib().fbk_solid_build(ctx.handle, bank.handle, cms._h, C.byref(p), _subsample(subsample), ptr(ascii), ptr(offs),
+                                  len(contigs), C.byref(t)), ctx.handle, "solid build")
+    return SolidTable(ctx, t, k, p.key_bits)
+
+
+def subsample_mask(ctx: Context, n_pairs: int, factor: float, seed: int) -> np.ndarray:
+    out = np.zeros((n_pairs + 63) // 64, np.uint64)
+    s = N.Subsample()
+    s.factor, s.seed = factor, seed
+    check(N.lib().fbk_subsample_mask(ctx.handle, n_pairs, C.byref(s), ptr(out)), ctx.handle, "subsample")
+    return out
+
+
+def nthash_arena(ctx: Context, arena: BitSeqArena, k: int) -> np.ndarray:
+    total = int(np.maximum(arena.lengths.astype(np.int64) - k + 1, 0).sum())
+    out = np.zeros(max(total, 1), np.uint64)
+    n = C.c_uint64()
+    v = arena.view()
+    check(N.lib().fbk_nthash_arena(ctx.handle, C.byref(v), k, ptr(out), out.size, C.byref(n)), ctx.handle)
+    return out[:n.value]
+
+
+def canonical_kmers_arena(ctx: Context, arena: BitSeqArena, k: int, key_bits: int | None = None):
+    kb = key_bits or key_bits_for_k(k)
+    nw = kb // 64
+    total = int(np.maximum(arena.lengths.astype(np.int64) - k + 1, 0).sum())
+    out = np.zeros((max(total, 1), nw), np.uint64)
+    rc = np.zeros(max(total, 1), np.uint8)
+    n = C.c_uint64()
+    v = arena.view()
+    check(N.lib().fbk_canonical_kmers_arena(ctx.handle, C.byref(v), k, kb, ptr(out.reshape(-1)), ptr(rc), total,
+                                            C.byref(n)), ctx.handle)
+    return out[:n.value], rc[:n.value]
+
+
+# ---------------------------------------------------------------------------
+# synthetic isolates
+# ---------------------------------------------------------------------------
+def synth_params(**kw) -> N.SynthParams:
+    p = N.SynthParams()
+    N.lib().fbk_synth_defaults(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def synth_isolate(params: N.SynthParams, threads: int = 0, min_len: int = 30, min_qual: int = 20, enable_trim: bool = True,
+                  enable_merge: bool = True, sample_pairs: int = 150000):
+    """Generates an isolate and ingests it (trim/merge on the host).  Returns
+    (ReadBank with pair indices, IngestStats, raw estimator sample arena, n sample
+    pairs, ExactCountStats)."""
+    hb, hs = C.c_void_p(), C.c_void_p()
+    cs = N.CountStats()
+    check(N.lib().fbk_synth_isolate(C.byref(params), threads, min_len, min_qual, int(enable_trim), int(enable_merge),
+                                    C.byref(hb), sample_pairs, C.byref(hs) if sample_pairs else None, C.byref(cs)),
+          None, "synth isolate")
+    try:
+        bank, st = _bank_from_hbank(hb)
+        sample = None
+        if sample_pairs:
+            sbank, _ = _bank_from_hbank(hs)
+            sample = sbank.merged_reads
+    finally:
+        N.lib().fbk_hbank_free(hb)
+        if sample_pairs:
+            N.lib().fbk_hbank_free(hs)
+    n_sample = len(sample) // 2 if sample is not None else 0
+    return bank, st, sample, n_sample, ExactCountStats.from_c(cs)
+
+
+def synth_write_fastq(params: N.SynthParams, r1: str, r2: str) -> None:
+    check(N.lib().fbk_synth_write_fastq(C.byref(params), str(r1).encode(), str(r2).encode()), None, "synth fastq")
+
+
+def synth_genome(params: N.SynthParams) -> bytes:
+    g = np.zeros(params.genome_len, np.uint8)
+    check(N.lib().fbk_synth_genome(C.byref(params), ptr(g)))
+    return g.tobytes()
+
+
+def synth_pairs(params: N.SynthParams, genome: bytes, first: int, n: int):
+    L = params.read_len
+    bufs = [np.zeros(n * L, np.uint8) for _ in range(4)]
+    g = np.frombuffer(genome, np.uint8).copy()
+    check(N.lib().fbk_synth_pairs(C.byref(params), ptr(g), first, n, *[ptr(b) for b in bufs]))
+    return [b.reshape(n, L) for b in bufs]
+
+
+# single-pair ingest helpers (their known-answer tests mirror trim_merge.rs:423-508)
+def trim_adapter(seq: bytes) -> bytes:
+    a = np.frombuffer(seq, np.uint8).copy()
+    return seq[:N.lib().fbk_trim_adapter(ptr(a), a.size)]
+
+
+def trim_quality(seq: bytes, qual: bytes, min_qual: int, min_len: int):
+    a = np.frombuffer(seq, np.uint8).copy()
+    q = np.frombuffer(qual, np.uint8).copy()
+    n = N.lib().fbk_trim_quality(ptr(a), ptr(q), a.size, min_qual, min_len)
+    return None if n < 0 else (seq[:n], qual[:n])
+
+
+def merge_read_pair(r1: bytes, q1: bytes, r2: bytes, q2: bytes, min_overlap: int = 15, max_mismatch_ratio: float = 0.10):
+    """Returns (merged_seq, overlap_len, mismatches) or None when unmerged."""
+    a, qa = np.frombuffer(r1, np.uint8).copy(), np.frombuffer(q1, np.uint8).copy()
+    b, qb = np.frombuffer(r2, np.uint8).copy(), np.frombuffer(q2, np.uint8).copy()
+    out = np.zeros(len(r1) + len(r2) + 1, np.uint8)
+    ov, mm = C.c_uint64(), C.c_uint64()
+    n = N.lib().fbk_merge_read_pair(ptr(a), ptr(qa), a.size, ptr(b), ptr(qb), b.size, min_overlap, max_mismatch_ratio,
+                                    ptr(out), C.byref(ov), C.byref(mm))
+    if n < 0:
+        return None
+    return out[:n].tobytes(), ov.value, mm.value

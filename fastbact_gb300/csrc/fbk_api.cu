@@ -1,0 +1,1182 @@
+// fbk_api.cu — host side of the C ABI: contexts, device pool, bank upload, and the
+// CountMinSketch / HyperLogLog / solid-table objects with their build passes.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "fbk_device.cuh"
+#include "fbk_internal.h"
+
+using namespace fbk;
+
+// ===========================================================================
+// errors, pool, timing
+// ===========================================================================
+namespace fbk {
+
+fbk_status set_err(fbk_ctx* ctx, fbk_status st, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return st;
+}
+fbk_status cuda_err(fbk_ctx* ctx, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return set_err(ctx, e == cudaErrorMemoryAllocation ? FBK_ERR_OOM : FBK_ERR_CUDA, m);
+}
+
+bool DevicePool::init(uint64_t bytes, std::string& err) {
+    bytes = (bytes + 255) & ~255ULL;
+    cudaError_t e = cudaMalloc((void**)&base_, bytes);
+    if (e != cudaSuccess) {
+        err = std::string("pool cudaMalloc: ") + cudaGetErrorString(e);
+        base_ = nullptr;
+        return false;
+    }
+    size_ = bytes;
+    free_.clear();
+    live_.clear();
+    free_[0] = bytes;
+    used_bytes_ = 0;
+    return true;
+}
+void DevicePool::release() {
+    if (base_) cudaFree(base_);
+    base_ = nullptr;
+    size_ = used_bytes_ = 0;
+    free_.clear();
+    live_.clear();
+}
+void* DevicePool::alloc(uint64_t bytes) {
+    std::lock_guard<std::mutex> g(mu_);
+    bytes = std::max<uint64_t>(256, (bytes + 255) & ~255ULL);
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+        if (it->second >= bytes) {
+            uint64_t off = it->first, sz = it->second;
+            free_.erase(it);
+            if (sz > bytes) free_[off + bytes] = sz - bytes;
+            live_[off] = bytes;
+            used_bytes_ += bytes;
+            return base_ + off;
+        }
+    }
+    return nullptr;
+}
+void DevicePool::free(void* p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> g(mu_);
+    uint64_t off = (uint64_t)((char*)p - base_);
+    auto it = live_.find(off);
+    if (it == live_.end()) return;
+    uint64_t sz = it->second;
+    live_.erase(it);
+    used_bytes_ -= sz;
+    auto nx = free_.lower_bound(off);
+    if (nx != free_.end() && nx->first == off + sz) {
+        sz += nx->second;
+        free_.erase(nx);
+    }
+    auto pv = free_.lower_bound(off);
+    if (pv != free_.begin()) {
+        --pv;
+        if (pv->first + pv->second == off) {
+            pv->second += sz;
+            return;
+        }
+    }
+    free_[off] = sz;
+}
+uint64_t DevicePool::largest_free() const {
+    std::lock_guard<std::mutex> g(mu_);
+    uint64_t m = 0;
+    for (auto& f : free_) m = std::max(m, f.second);
+    return m;
+}
+
+void* dev_alloc(fbk_ctx* ctx, uint64_t bytes) {
+    if (bytes == 0) bytes = 256;
+    if (ctx->pool.active()) return ctx->pool.alloc(bytes);
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+void dev_free(fbk_ctx* ctx, void* p) {
+    if (!p) return;
+    if (ctx->pool.active()) ctx->pool.free(p);
+    else cudaFree(p);
+}
+
+Launch launch_cfg(fbk_ctx* ctx, int block, int grid) {
+    Launch L;
+    L.block = block;
+    L.grid = grid > 0 ? grid : ctx->num_sms * 4;
+    L.stream = ctx->stream;
+    return L;
+}
+
+void time_begin(fbk_ctx* ctx, const char* name, TimedLaunch& t) {
+    ctx->launches++;
+    t.name = name;
+    t.a = t.b = nullptr;
+    if (!ctx->timing) return;
+    for (cudaEvent_t* e : {&t.a, &t.b}) {
+        if (!ctx->free_events.empty()) {
+            *e = ctx->free_events.back();
+            ctx->free_events.pop_back();
+        } else {
+            cudaEventCreate(e);
+        }
+    }
+    cudaEventRecord(t.a, ctx->stream);
+}
+void time_end(fbk_ctx* ctx, TimedLaunch& t) {
+    if (!ctx->timing || !t.a) return;
+    cudaEventRecord(t.b, ctx->stream);
+    ctx->pending.push_back(t);
+}
+
+static void collect_timing(fbk_ctx* ctx) {
+    if (ctx->pending.empty()) return;
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& t : ctx->pending) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, t.a, t.b);
+        auto& acc = ctx->timed[t.name];
+        acc.first += ms;
+        acc.second += 1;
+        ctx->free_events.push_back(t.a);
+        ctx->free_events.push_back(t.b);
+    }
+    ctx->pending.clear();
+}
+
+fbk_status ctx_check_status(fbk_ctx* ctx, uint32_t* bits) {
+    uint32_t* h = (uint32_t*)ctx->h_pinned;
+    cudaError_t e = cudaMemcpyAsync(h, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "status readback");
+    *bits = h[0];
+    return FBK_OK;
+}
+
+BankDev bank_view(const fbk_bank* b, uint64_t r_begin, uint64_t r_end, const uint64_t* keep_bits) {
+    BankDev v;
+    v.data = b->data;
+    v.off = b->off;
+    v.len = b->len;
+    v.pair_idx = b->pair_idx;
+    v.keep_bits = keep_bits;
+    v.r_begin = r_begin;
+    v.r_end = r_end;
+    return v;
+}
+
+uint64_t f64_to_u64_sat(double x) {
+    if (!(x > 0.0)) return 0;
+    if (x >= 18446744073709551616.0) return UINT64_MAX;
+    return (uint64_t)x;
+}
+
+double hll_estimate_from_sum(double sum, uint64_t zeros, uint32_t p) {
+    const double m = (double)(1ULL << p);
+    const double alpha_m = 0.7213 / (1.0 + 1.079 / m);
+    const double raw = alpha_m * m * m / sum;
+    if (raw <= 2.5 * m) {
+        if (zeros > 0) return m * std::log(m / (double)zeros);
+        return raw;
+    } else if (raw <= (1.0 / 30.0) * 18446744073709551616.0) {
+        return raw;
+    }
+    const double two64 = 18446744073709551616.0;
+    return -two64 * std::log(1.0 - raw / two64);
+}
+
+}  // namespace fbk
+
+#define CK(ctx, call)                                         \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_err(ctx, e_, #call); \
+    } while (0)
+
+#define TIMED(ctx, name, call)              \
+    do {                                    \
+        TimedLaunch tl_;                    \
+        time_begin(ctx, name, tl_);         \
+        cudaError_t e_ = (call);            \
+        time_end(ctx, tl_);                 \
+        if (e_ != cudaSuccess) return cuda_err(ctx, e_, name); \
+    } while (0)
+
+// ===========================================================================
+// status, context
+// ===========================================================================
+extern "C" {
+
+FBK_API const char* fbk_status_str(fbk_status s) {
+    switch (s) {
+        case FBK_OK: return "ok";
+        case FBK_ERR_INVALID: return "invalid argument";
+        case FBK_ERR_CUDA: return "cuda error";
+        case FBK_ERR_OOM: return "out of device memory";
+        case FBK_ERR_TABLE_FULL: return "solid table full";
+        case FBK_ERR_TIMEOUT: return "device wait timed out";
+        case FBK_ERR_IO: return "i/o error";
+        case FBK_ERR_FORMAT: return "malformed input";
+        case FBK_ERR_EMPTY: return "no valid read pairs";
+        case FBK_ERR_BUSY: return "busy";
+        case FBK_ERR_NOT_READY: return "not ready";
+        case FBK_ERR_NO_DEVICE: return "no cuda device";
+        default: return "unknown status";
+    }
+}
+
+FBK_API const char* fbk_version(void) { return "fastbact_gb300 0.1.0 (sm_103a)"; }
+
+FBK_API fbk_status fbk_ctx_create(int device, uint64_t pool_bytes, fbk_ctx** out) {
+    if (!out) return FBK_ERR_INVALID;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return FBK_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= n) return FBK_ERR_INVALID;
+    fbk_ctx* c = new fbk_ctx();
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_status, 64);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_counts, 8 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_pinned, 65536);
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, 64);
+    if (e != cudaSuccess) {
+        fbk_ctx_destroy(c);
+        return FBK_ERR_CUDA;
+    }
+    if (pool_bytes > 0 && !c->pool.init(pool_bytes, c->err)) {
+        fbk_ctx_destroy(c);
+        return FBK_ERR_OOM;
+    }
+    *out = c;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_ctx_destroy(fbk_ctx* c) {
+    if (!c) return FBK_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& t : c->pending) {
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    for (auto e : c->free_events) cudaEventDestroy(e);
+    for (auto e : c->markers)
+        if (e) cudaEventDestroy(e);
+    c->pool.release();
+    if (c->d_status) cudaFree(c->d_status);
+    if (c->d_counts) cudaFree(c->d_counts);
+    if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_last_error(const fbk_ctx* ctx, char* buf, size_t len) {
+    if (!ctx || !buf || len == 0) return FBK_ERR_INVALID;
+    snprintf(buf, len, "%s", ctx->err.c_str());
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_ctx_sync(fbk_ctx* ctx) {
+    if (!ctx) return FBK_ERR_INVALID;
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_ctx_set_timing(fbk_ctx* ctx, int enable) {
+    if (!ctx) return FBK_ERR_INVALID;
+    ctx->timing = enable != 0;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_ctx_timing(fbk_ctx* ctx, const char* prefix, double* ms, uint64_t* launches) {
+    if (!ctx || !prefix || !ms || !launches) return FBK_ERR_INVALID;
+    collect_timing(ctx);
+    double t = 0;
+    uint64_t n = 0;
+    size_t pl = strlen(prefix);
+    for (auto& kv : ctx->timed)
+        if (kv.first.compare(0, pl, prefix) == 0) {
+            t += kv.second.first;
+            n += kv.second.second;
+        }
+    *ms = t;
+    *launches = n;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_ctx_timing_reset(fbk_ctx* ctx) {
+    if (!ctx) return FBK_ERR_INVALID;
+    collect_timing(ctx);
+    ctx->timed.clear();
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_ctx_event_record(fbk_ctx* ctx, int slot) {
+    if (!ctx || slot < 0 || slot >= 16) return FBK_ERR_INVALID;
+    if (!ctx->markers[slot]) CK(ctx, cudaEventCreate(&ctx->markers[slot]));
+    CK(ctx, cudaEventRecord(ctx->markers[slot], ctx->stream));
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_ctx_event_elapsed(fbk_ctx* ctx, int a, int b, double* ms) {
+    if (!ctx || !ms || a < 0 || a >= 16 || b < 0 || b >= 16 || !ctx->markers[a] || !ctx->markers[b]) return FBK_ERR_INVALID;
+    CK(ctx, cudaEventSynchronize(ctx->markers[b]));
+    float f = 0.f;
+    CK(ctx, cudaEventElapsedTime(&f, ctx->markers[a], ctx->markers[b]));
+    *ms = f;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_ctx_launch_count(const fbk_ctx* ctx, uint64_t* n) {
+    if (!ctx || !n) return FBK_ERR_INVALID;
+    *n = ctx->launches;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_ctx_mem_info(const fbk_ctx* ctx, uint64_t* used, uint64_t* size) {
+    if (!ctx || !used || !size) return FBK_ERR_INVALID;
+    *used = ctx->pool.used();
+    *size = ctx->pool.size();
+    return FBK_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// read bank
+// ===========================================================================
+namespace fbk {
+
+fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_arenas, fbk_bank** out) {
+    uint64_t n_words = 0, n_reads = 0, n_bases = 0;
+    bool all_pairs = true;
+    uint32_t max_len = 0;
+    uint64_t max_pair = 0;
+    for (int a = 0; a < n_arenas; ++a) {
+        const fbk_arena_view& v = arenas[a];
+        if (v.n_seqs && (!v.offsets || !v.lengths)) return set_err(ctx, FBK_ERR_INVALID, "arena has sequences but no offsets/lengths");
+        if (v.n_words && !v.data) return set_err(ctx, FBK_ERR_INVALID, "arena has words but no data pointer");
+        // Every sequence must lie inside its arena's words: the kernels read only there.
+        for (uint64_t i = 0; i < v.n_seqs; ++i) {
+            const uint64_t end = v.offsets[i] + (uint64_t)v.lengths[i];
+            if (v.lengths[i] && end > v.n_words * 32) return set_err(ctx, FBK_ERR_INVALID, "sequence extends past the arena data");
+            n_bases += v.lengths[i];
+            max_len = std::max(max_len, v.lengths[i]);
+            if (v.pair_idx) max_pair = std::max<uint64_t>(max_pair, v.pair_idx[i]);
+        }
+        if (v.n_seqs && !v.pair_idx) all_pairs = false;
+        n_words += v.n_words;
+        n_reads += v.n_seqs;
+    }
+    fbk_bank* b = new fbk_bank();
+    b->ctx = ctx;
+    b->n_reads = n_reads;
+    b->n_words = n_words;
+    b->n_bases = n_bases;
+    b->max_len = max_len;
+    b->n_pairs = all_pairs && n_reads ? max_pair + 1 : 0;
+    b->data = (uint64_t*)dev_alloc(ctx, (n_words + 8) * 8);
+    b->off = (uint64_t*)dev_alloc(ctx, std::max<uint64_t>(n_reads, 1) * 8);
+    b->len = (uint32_t*)dev_alloc(ctx, std::max<uint64_t>(n_reads, 1) * 4);
+    if (all_pairs && n_reads) b->pair_idx = (uint32_t*)dev_alloc(ctx, n_reads * 4);
+    if (!b->data || !b->off || !b->len || (all_pairs && n_reads && !b->pair_idx)) {
+        fbk_bank_release(b);
+        return set_err(ctx, FBK_ERR_OOM, "device memory for the read bank");
+    }
+    uint64_t wbase = 0, rbase = 0;
+    Launch L = launch_cfg(ctx, 256, 0);
+    for (int a = 0; a < n_arenas; ++a) {
+        const fbk_arena_view& v = arenas[a];
+        cudaError_t e = cudaSuccess;
+        if (v.n_words) e = cudaMemcpyAsync(b->data + wbase, v.data, v.n_words * 8, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess && v.n_seqs) e = cudaMemcpyAsync(b->off + rbase, v.offsets, v.n_seqs * 8, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess && v.n_seqs) e = cudaMemcpyAsync(b->len + rbase, v.lengths, v.n_seqs * 4, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess && v.n_seqs && b->pair_idx)
+            e = cudaMemcpyAsync(b->pair_idx + rbase, v.pair_idx, v.n_seqs * 4, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess && wbase && v.n_seqs) {
+            TimedLaunch tl;
+            time_begin(ctx, "bank_rebase", tl);
+            e = launch_add_u64(L, b->off + rbase, v.n_seqs, wbase * 32);
+            time_end(ctx, tl);
+        }
+        if (e != cudaSuccess) {
+            fbk_bank_release(b);
+            return cuda_err(ctx, e, "bank upload");
+        }
+        wbase += v.n_words;
+        rbase += v.n_seqs;
+    }
+    cudaError_t e = cudaMemsetAsync(b->data + n_words, 0, 8 * 8, ctx->stream);
+    if (e != cudaSuccess) {
+        fbk_bank_release(b);
+        return cuda_err(ctx, e, "bank padding");
+    }
+    // Read ranges whose total length stays below 2^31 bases: within one range no
+    // 32-bit edge counter can exceed 2^32 (see k_convert).
+    b->chunk_starts.push_back(0);
+    uint64_t acc = 0, r = 0;
+    for (int a = 0; a < n_arenas; ++a)
+        for (uint64_t i = 0; i < arenas[a].n_seqs; ++i, ++r) {
+            if (acc + arenas[a].lengths[i] >= (1ULL << 31)) {
+                b->chunk_starts.push_back(r);
+                acc = 0;
+            }
+            acc += arenas[a].lengths[i];
+        }
+    b->chunk_starts.push_back(n_reads);
+    *out = b;
+    return FBK_OK;
+}
+
+}  // namespace fbk
+
+extern "C" {
+
+FBK_API fbk_status fbk_bank_upload(fbk_ctx* ctx, const fbk_arena_view arenas[3], fbk_bank** out) {
+    if (!ctx || !arenas || !out) return FBK_ERR_INVALID;
+    CK(ctx, cudaSetDevice(ctx->device));
+    return bank_upload_impl(ctx, arenas, 3, out);
+}
+
+FBK_API fbk_status fbk_bank_info(const fbk_bank* b, uint64_t* n_reads, uint64_t* n_bases) {
+    if (!b) return FBK_ERR_INVALID;
+    if (n_reads) *n_reads = b->n_reads;
+    if (n_bases) *n_bases = b->n_bases;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_bank_release(fbk_bank* b) {
+    if (!b) return FBK_OK;
+    fbk_ctx* ctx = b->ctx;
+    cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, b->data);
+    dev_free(ctx, b->off);
+    dev_free(ctx, b->len);
+    dev_free(ctx, b->pair_idx);
+    delete b;
+    return FBK_OK;
+}
+
+// ===========================================================================
+// CountMinSketch
+// ===========================================================================
+FBK_API uint64_t fbk_cms_width_for_genome_size(uint64_t g) {
+    uint64_t x = g * 16, t = 1;
+    while (t < x) t <<= 1;
+    return std::min<uint64_t>(std::max<uint64_t>(t, 1ULL << 21), 1ULL << 27);
+}
+
+FBK_API fbk_status fbk_cms_create(fbk_ctx* ctx, uint32_t log2w, uint32_t cbits, fbk_cms** out) {
+    if (!ctx || !out || (cbits != 4 && cbits != 16) || log2w < 3 || log2w > 31)
+        return set_err(ctx, FBK_ERR_INVALID, "cms: counter_bits must be 4 or 16 and 3 <= log2_width <= 31");
+    CK(ctx, cudaSetDevice(ctx->device));
+    fbk_cms* c = new fbk_cms();
+    c->ctx = ctx;
+    c->log2w = log2w;
+    c->cbits = cbits;
+    const uint64_t w = 1ULL << log2w;
+    c->n_words = cbits == 4 ? (4 * w) / 8 : (4 * w) / 2;
+    c->words = (uint32_t*)dev_alloc(ctx, c->n_words * 4);
+    c->hll12 = (uint32_t*)dev_alloc(ctx, 4096 * 4);
+    if (!c->words || !c->hll12) {
+        dev_free(ctx, c->words);
+        dev_free(ctx, c->hll12);
+        delete c;
+        return set_err(ctx, FBK_ERR_OOM, "device memory for the count-min sketch");
+    }
+    CK(ctx, cudaMemsetAsync(c->words, 0, c->n_words * 4, ctx->stream));
+    CK(ctx, cudaMemsetAsync(c->hll12, 0, 4096 * 4, ctx->stream));
+    *out = c;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_cms_clear(fbk_cms* c) {
+    if (!c) return FBK_ERR_INVALID;
+    CK(c->ctx, cudaMemsetAsync(c->words, 0, c->n_words * 4, c->ctx->stream));
+    CK(c->ctx, cudaMemsetAsync(c->hll12, 0, 4096 * 4, c->ctx->stream));
+    return FBK_OK;
+}
+
+static fbk_status cms_keys_op(fbk_cms* c, const uint64_t* keys, uint64_t n, uint32_t* est, int add) {
+    if (!c || (n && !keys) || (!add && n && !est)) return FBK_ERR_INVALID;
+    if (n == 0) return FBK_OK;
+    fbk_ctx* ctx = c->ctx;
+    uint64_t* dk = (uint64_t*)dev_alloc(ctx, n * 8);
+    uint32_t* de = add ? nullptr : (uint32_t*)dev_alloc(ctx, n * 4);
+    if (!dk || (!add && !de)) {
+        dev_free(ctx, dk);
+        dev_free(ctx, de);
+        return set_err(ctx, FBK_ERR_OOM, "cms key buffer");
+    }
+    cudaError_t e = cudaMemcpyAsync(dk, keys, n * 8, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) {
+        TimedLaunch tl;
+        time_begin(ctx, add ? "cms_add_keys" : "cms_estimate_keys", tl);
+        // Sequential-add semantics only matter through the final counters, which are
+        // order independent; a single launch is therefore exact.
+        e = launch_cms_keys((int)c->cbits, launch_cfg(ctx, 256, 0), c->words, c->log2w, dk, n, de, add);
+        time_end(ctx, tl);
+    }
+    if (e == cudaSuccess && !add) e = cudaMemcpyAsync(est, de, n * 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, dk);
+    dev_free(ctx, de);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cms key op");
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_cms_add_keys(fbk_cms* c, const uint64_t* keys, uint64_t n) { return cms_keys_op(c, keys, n, nullptr, 1); }
+FBK_API fbk_status fbk_cms_estimate_keys(fbk_cms* c, const uint64_t* keys, uint64_t n, uint32_t* out) {
+    return cms_keys_op(c, keys, n, out, 0);
+}
+
+static int nw_of(uint32_t key_bits) { return key_bits == 64 ? 1 : key_bits == 128 ? 2 : key_bits == 256 ? 4 : 0; }
+static uint32_t max_k_of(uint32_t key_bits) { return key_bits == 64 ? 31 : key_bits == 128 ? 63 : 127; }
+
+// Builds the subsampler bitmap for a bank on the device (nullptr when keeping all).
+static fbk_status make_keep_bits(fbk_ctx* ctx, const fbk_bank* b, const fbk_subsample* ss, uint64_t** bits_out) {
+    *bits_out = nullptr;
+    if (!ss || !(ss->factor < 0.999)) return FBK_OK;
+    if (!b->pair_idx || b->n_pairs == 0)
+        return set_err(ctx, FBK_ERR_INVALID, "subsampling needs per-read pair indices in the bank");
+    uint64_t nw = (b->n_pairs + 63) / 64;
+    uint64_t* bits = (uint64_t*)dev_alloc(ctx, nw * 8);
+    if (!bits) return set_err(ctx, FBK_ERR_OOM, "subsample bitmap");
+    TIMED(ctx, "subsample", launch_subsample_mask(launch_cfg(ctx, 256, 0), b->n_pairs, ss->factor, ss->seed, bits));
+    *bits_out = bits;
+    return FBK_OK;
+}
+
+static fbk_status pass1_impl(fbk_cms* c, const fbk_bank* b, uint32_t k, uint32_t key_bits, const uint64_t* keep_bits,
+                             uint32_t mult) {
+    fbk_ctx* ctx = c->ctx;
+    const int nw = nw_of(key_bits);
+    if (!nw || k < 1 || k > max_k_of(key_bits)) return set_err(ctx, FBK_ERR_INVALID, "k out of range for key_bits");
+    Launch L = launch_cfg(ctx, ctx->block_pass1, ctx->grid_pass1);
+    TIMED(ctx, "pass1", launch_pass1(nw, (int)c->cbits, L, bank_view(b, 0, b->n_reads, keep_bits), k, c->words, c->log2w,
+                                     mult, c->hll12));
+    return FBK_OK;
+}
+
+// Distinct canonical keys added to the sketch by bank passes (p=12 HyperLogLog,
+// about 1.6% standard error); only used to size the solid table.
+static fbk_status cms_distinct(const fbk_cms* c, uint64_t* out) {
+    fbk_ctx* ctx = c->ctx;
+    uint32_t* h = (uint32_t*)ctx->h_pinned;
+    CK(ctx, cudaMemcpyAsync(h, c->hll12, 4096 * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    double sum = 0.0;
+    uint64_t zeros = 0;
+    for (int i = 0; i < 4096; ++i) {
+        sum += std::ldexp(1.0, -(int)h[i]);
+        zeros += h[i] == 0;
+    }
+    *out = (uint64_t)(hll_estimate_from_sum(sum, zeros, 12) * 1.05) + 1024;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_cms_add_bank(fbk_cms* c, const fbk_bank* b, uint32_t k, uint32_t key_bits, const fbk_subsample* ss) {
+    if (!c || !b) return FBK_ERR_INVALID;
+    fbk_ctx* ctx = c->ctx;
+    CK(ctx, cudaSetDevice(ctx->device));
+    uint64_t* keep = nullptr;
+    fbk_status st = make_keep_bits(ctx, b, ss, &keep);
+    if (st) return st;
+    st = pass1_impl(c, b, k, key_bits, keep, 1);
+    if (keep) {
+        cudaStreamSynchronize(ctx->stream);
+        dev_free(ctx, keep);
+    }
+    return st;
+}
+
+// Packs ASCII contigs into a one-arena device bank (ASCII_TO_2BIT, bitseq.rs:67-81).
+static fbk_status contig_bank(fbk_ctx* ctx, const uint8_t* ascii, const uint64_t* offs, uint64_t n, fbk_bank** out) {
+    std::vector<uint64_t> words, o(n);
+    std::vector<uint32_t> l(n);
+    uint64_t pos = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        uint64_t len = offs[i + 1] - offs[i];
+        if (len > 0xFFFFFFFFULL) return set_err(ctx, FBK_ERR_INVALID, "contig longer than 2^32-1 bases");
+        o[i] = pos;
+        l[i] = (uint32_t)len;
+        words.resize((pos + len + 31) / 32 + 1, 0);
+        for (uint64_t j = 0; j < len; ++j, ++pos) {
+            uint8_t ch = ascii[offs[i] + j];
+            uint64_t code = (ch == 'C' || ch == 'c') ? 1 : (ch == 'G' || ch == 'g') ? 2 : (ch == 'T' || ch == 't') ? 3 : 0;
+            words[pos >> 5] |= code << ((pos & 31) * 2);
+        }
+    }
+    fbk_arena_view v;
+    v.data = words.data();
+    v.n_words = words.size();
+    v.offsets = o.data();
+    v.lengths = l.data();
+    v.n_seqs = n;
+    v.pair_idx = nullptr;
+    fbk_status st = bank_upload_impl(ctx, &v, 1, out);
+    if (st == FBK_OK) cudaStreamSynchronize(ctx->stream);  // host vectors go out of scope
+    return st;
+}
+
+FBK_API fbk_status fbk_cms_add_contigs(fbk_cms* c, const uint8_t* ascii, const uint64_t* offs, uint64_t n, uint32_t k,
+                                       uint32_t key_bits) {
+    if (!c || (n && (!ascii || !offs))) return FBK_ERR_INVALID;
+    if (n == 0) return FBK_OK;
+    fbk_ctx* ctx = c->ctx;
+    fbk_bank* cb = nullptr;
+    fbk_status st = contig_bank(ctx, ascii, offs, n, &cb);
+    if (st) return st;
+    st = pass1_impl(c, cb, k, key_bits, nullptr, 10);
+    fbk_bank_release(cb);
+    return st;
+}
+
+FBK_API fbk_status fbk_cms_nbytes(const fbk_cms* c, uint64_t* nbytes) {
+    if (!c || !nbytes) return FBK_ERR_INVALID;
+    *nbytes = c->n_words * 4;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_cms_export(fbk_cms* c, uint8_t* out, uint64_t nbytes) {
+    if (!c || !out || nbytes != c->n_words * 4) return FBK_ERR_INVALID;
+    CK(c->ctx, cudaMemcpyAsync(out, c->words, nbytes, cudaMemcpyDeviceToHost, c->ctx->stream));
+    CK(c->ctx, cudaStreamSynchronize(c->ctx->stream));
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_cms_merge(fbk_cms* dst, const fbk_cms* src) {
+    if (!dst || !src || dst->cbits != src->cbits || dst->log2w != src->log2w) return FBK_ERR_INVALID;
+    fbk_ctx* ctx = dst->ctx;
+    if (src->ctx != ctx) CK(ctx, cudaStreamSynchronize(src->ctx->stream));
+    TIMED(ctx, "cms_merge", launch_cms_merge((int)dst->cbits, launch_cfg(ctx, 256, 0), dst->words, src->words, dst->n_words));
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_cms_release(fbk_cms* c) {
+    if (!c) return FBK_OK;
+    cudaStreamSynchronize(c->ctx->stream);
+    dev_free(c->ctx, c->words);
+    dev_free(c->ctx, c->hll12);
+    delete c;
+    return FBK_OK;
+}
+
+// ===========================================================================
+// HyperLogLog
+// ===========================================================================
+FBK_API fbk_status fbk_hll_create(fbk_ctx* ctx, uint32_t p, fbk_hll** out) {
+    if (!ctx || !out || p < 4 || p > 18) return set_err(ctx, FBK_ERR_INVALID, "hll: 4 <= p <= 18");
+    fbk_hll* h = new fbk_hll();
+    h->ctx = ctx;
+    h->p = p;
+    h->regs = (uint32_t*)dev_alloc(ctx, (1ULL << p) * 4);
+    if (!h->regs) {
+        delete h;
+        return set_err(ctx, FBK_ERR_OOM, "hll registers");
+    }
+    CK(ctx, cudaMemsetAsync(h->regs, 0, (1ULL << p) * 4, ctx->stream));
+    *out = h;
+    return FBK_OK;
+}
+
+static fbk_status hll_add(fbk_hll* h, const uint64_t* x, uint64_t n, int mix) {
+    if (!h || (n && !x)) return FBK_ERR_INVALID;
+    if (!n) return FBK_OK;
+    fbk_ctx* ctx = h->ctx;
+    uint64_t* d = (uint64_t*)dev_alloc(ctx, n * 8);
+    if (!d) return set_err(ctx, FBK_ERR_OOM, "hll hash buffer");
+    cudaError_t e = cudaMemcpyAsync(d, x, n * 8, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) {
+        TimedLaunch tl;
+        time_begin(ctx, "hll_add", tl);
+        e = launch_hll_add(launch_cfg(ctx, 256, 0), h->regs, h->p, d, n, mix);
+        time_end(ctx, tl);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, d);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "hll add");
+    return FBK_OK;
+}
+FBK_API fbk_status fbk_hll_add_hashes(fbk_hll* h, const uint64_t* x, uint64_t n) { return hll_add(h, x, n, 0); }
+FBK_API fbk_status fbk_hll_add_canonical_hashes(fbk_hll* h, const uint64_t* x, uint64_t n) { return hll_add(h, x, n, 1); }
+
+FBK_API fbk_status fbk_hll_merge(fbk_hll* dst, const fbk_hll* src) {
+    if (!dst || !src || dst->p != src->p) return FBK_ERR_INVALID;
+    fbk_ctx* ctx = dst->ctx;
+    TIMED(ctx, "hll_merge", launch_hll_merge(launch_cfg(ctx, 256, 0), dst->regs, src->regs, 1ULL << dst->p));
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_hll_export(fbk_hll* h, uint8_t* regs, uint64_t n) {
+    if (!h || !regs || n != (1ULL << h->p)) return FBK_ERR_INVALID;
+    std::vector<uint32_t> tmp(n);
+    CK(h->ctx, cudaMemcpyAsync(tmp.data(), h->regs, n * 4, cudaMemcpyDeviceToHost, h->ctx->stream));
+    CK(h->ctx, cudaStreamSynchronize(h->ctx->stream));
+    for (uint64_t i = 0; i < n; ++i) regs[i] = (uint8_t)tmp[i];
+    return FBK_OK;
+}
+
+FBK_API double fbk_hll_estimate_registers(const uint8_t* regs, uint32_t p) {
+    const uint64_t n = 1ULL << p;
+    double sum = 0.0;
+    uint64_t zeros = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        sum += std::ldexp(1.0, -(int)regs[i]);
+        zeros += regs[i] == 0;
+    }
+    return hll_estimate_from_sum(sum, zeros, p);
+}
+
+FBK_API fbk_status fbk_hll_estimate(fbk_hll* h, double* out) {
+    if (!h || !out) return FBK_ERR_INVALID;
+    std::vector<uint8_t> r(1ULL << h->p);
+    fbk_status st = fbk_hll_export(h, r.data(), r.size());
+    if (st) return st;
+    *out = fbk_hll_estimate_registers(r.data(), h->p);
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_hll_release(fbk_hll* h) {
+    if (!h) return FBK_OK;
+    cudaStreamSynchronize(h->ctx->stream);
+    dev_free(h->ctx, h->regs);
+    delete h;
+    return FBK_OK;
+}
+
+// ===========================================================================
+// solid table
+// ===========================================================================
+static void table_free_storage(fbk_table* t) {
+    fbk_ctx* ctx = t->ctx;
+    dev_free(ctx, t->keys);
+    dev_free(ctx, t->tags);
+    dev_free(ctx, t->cnt);
+    dev_free(ctx, t->cov);
+    t->keys = t->tags = nullptr;
+    t->cnt = t->cov = nullptr;
+}
+static void table_free_out(fbk_table* t) {
+    dev_free(t->ctx, t->out_keys);
+    dev_free(t->ctx, t->out_cov);
+    dev_free(t->ctx, t->out_mask);
+    t->out_keys = nullptr;
+    t->out_cov = nullptr;
+    t->out_mask = nullptr;
+    t->out_cap = 0;
+}
+
+static TableDev table_dev(const fbk_table* t) {
+    TableDev d;
+    d.keys = t->keys;
+    d.tags = t->tags;
+    d.cnt = t->cnt;
+    d.cov = t->cov;
+    d.mask = t->cap - 1;
+    d.max_probe = (uint32_t)std::min<uint64_t>(t->cap, 1u << 16);
+    d.spin_limit = 1u << 20;
+    return d;
+}
+
+static fbk_status table_alloc(fbk_table* t, uint64_t cap, bool with_cov) {
+    fbk_ctx* ctx = t->ctx;
+    t->cap = cap;
+    t->keys = (uint64_t*)dev_alloc(ctx, cap * 8 * t->nw);
+    if (t->nw > 1) t->tags = (uint64_t*)dev_alloc(ctx, cap * 8);
+    t->cnt = (uint32_t*)dev_alloc(ctx, cap * 32);
+    if (with_cov) t->cov = (uint32_t*)dev_alloc(ctx, cap * 4);
+    if (!t->keys || (t->nw > 1 && !t->tags) || !t->cnt || (with_cov && !t->cov)) {
+        table_free_storage(t);
+        return set_err(ctx, FBK_ERR_OOM, "device memory for the solid table (capacity " + std::to_string(cap) + ")");
+    }
+    TIMED(ctx, "table_init", launch_table_init((int)t->nw, launch_cfg(ctx, 256, 0), table_dev(t)));
+    CK(ctx, cudaMemsetAsync(t->cnt, 0, cap * 32, ctx->stream));
+    if (with_cov) CK(ctx, cudaMemsetAsync(t->cov, 0, cap * 4, ctx->stream));
+    return FBK_OK;
+}
+
+// Runs the conversion kernel, (re)allocating the compact output when needed.
+static fbk_status table_convert(fbk_table* t, uint64_t* acc_keys, uint16_t* acc_cov, uint16_t* acc_edges, uint64_t acc_cap) {
+    fbk_ctx* ctx = t->ctx;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        CK(ctx, cudaMemsetAsync(ctx->d_counts, 0, 4 * sizeof(unsigned long long), ctx->stream));
+        ConvOut o;
+        o.keys = t->out_keys;
+        o.cov = t->out_cov;
+        o.mask = t->out_mask;
+        o.cap_solid = t->out_cap;
+        o.acc_keys = acc_keys;
+        o.acc_cov = acc_cov;
+        o.acc_edges = acc_edges;
+        o.cap_acc = acc_cap;
+        o.counts = ctx->d_counts;
+        TIMED(ctx, "convert", launch_convert((int)t->nw, launch_cfg(ctx, 256, 0), table_dev(t), t->min_trans_cov, o));
+        unsigned long long* h = (unsigned long long*)ctx->h_pinned;
+        CK(ctx, cudaMemcpyAsync(h, ctx->d_counts, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(ctx, cudaStreamSynchronize(ctx->stream));
+        t->n_keys = h[0];
+        t->n_solid = h[1];
+        t->digest = h[2];
+        t->pushes = h[3];
+        if (t->n_solid <= t->out_cap) return FBK_OK;
+        table_free_out(t);
+        uint64_t cap = t->n_solid + 1024;
+        t->out_keys = (uint64_t*)dev_alloc(ctx, cap * 8 * t->nw);
+        t->out_cov = (uint16_t*)dev_alloc(ctx, cap * 2);
+        t->out_mask = (uint8_t*)dev_alloc(ctx, cap);
+        if (!t->out_keys || !t->out_cov || !t->out_mask) {
+            table_free_out(t);
+            return set_err(ctx, FBK_ERR_OOM, "solid table output");
+        }
+        t->out_cap = cap;
+    }
+    return FBK_OK;
+}
+
+static uint64_t next_pow2(uint64_t x) {
+    uint64_t t = 1;
+    while (t < x) t <<= 1;
+    return t;
+}
+
+// Pass 2 over every chunk of the read bank (and the prior contigs), with retries
+// at twice the capacity when the probe limit is hit.
+static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cms* cms, const fbk_build_params* p,
+                                   const uint64_t* keep_bits, const fbk_bank* contigs, uint64_t distinct_hint,
+                                   fbk_table** out) {
+    const int nw = nw_of(p->key_bits);
+    if (!nw || p->k < 1 || p->k > max_k_of(p->key_bits)) return set_err(ctx, FBK_ERR_INVALID, "k out of range for key_bits");
+    if (p->t_solid > 0xFFFF || p->min_trans_cov > 0xFFFF) return set_err(ctx, FBK_ERR_INVALID, "thresholds must fit u16");
+    uint64_t cap;
+    if (p->table_log2_cap) {
+        if (p->table_log2_cap < 10 || p->table_log2_cap > 34) return set_err(ctx, FBK_ERR_INVALID, "table_log2_cap out of range");
+        cap = 1ULL << p->table_log2_cap;
+    } else {
+        cap = next_pow2(std::max<uint64_t>(1024, (uint64_t)(2.2 * (double)distinct_hint) + 1024));
+    }
+    fbk_table* t = new fbk_table();
+    t->ctx = ctx;
+    t->nw = (uint32_t)nw;
+    t->k = p->k;
+    t->min_trans_cov = p->min_trans_cov;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        fbk_status st = table_alloc(t, cap, contigs != nullptr);
+        if (st) {
+            delete t;
+            return st;
+        }
+        CK(ctx, cudaMemsetAsync(ctx->d_status, 0, 4, ctx->stream));
+        TableDev td = table_dev(t);
+        Launch L = launch_cfg(ctx, ctx->block_pass2, ctx->grid_pass2);
+        Launch Lc = launch_cfg(ctx, 256, 0);
+        for (size_t c = 0; c + 1 < b->chunk_starts.size(); ++c) {
+            if (c > 0) TIMED(ctx, "clamp", launch_clamp_counters(Lc, t->cnt, cap * 8));
+            if (c > 0 && t->cov) TIMED(ctx, "clamp", launch_clamp_counters(Lc, t->cov, cap));
+            TIMED(ctx, "pass2",
+                  launch_pass2(nw, (int)cms->cbits, L, bank_view(b, b->chunk_starts[c], b->chunk_starts[c + 1], keep_bits), p->k,
+                               cms->words, cms->log2w, p->t_solid, 1, 1, 1, td, ctx->d_status));
+        }
+        if (contigs) {
+            // +1000 per edge push and +100 cov (build.rs:203-240); 4096-contig launches
+            // keep every 32-bit counter below 2^32 before the next clamp.
+            for (uint64_t r0 = 0; r0 < contigs->n_reads; r0 += 4096) {
+                TIMED(ctx, "clamp", launch_clamp_counters(Lc, t->cnt, cap * 8));
+                TIMED(ctx, "clamp", launch_clamp_counters(Lc, t->cov, cap));
+                TIMED(ctx, "pass2_contigs",
+                      launch_pass2(nw, (int)cms->cbits, L, bank_view(contigs, r0, std::min(contigs->n_reads, r0 + 4096), nullptr),
+                                   p->k, cms->words, cms->log2w, p->t_solid, 0, 1000, 100, td, ctx->d_status));
+            }
+        }
+        uint32_t bits = 0;
+        st = ctx_check_status(ctx, &bits);
+        if (st) {
+            table_free_storage(t);
+            delete t;
+            return st;
+        }
+        if (bits & ST_SPIN_TIMEOUT) {
+            table_free_storage(t);
+            delete t;
+            return set_err(ctx, FBK_ERR_TIMEOUT, "solid table: a bounded wait for a key publication gave up");
+        }
+        if (!(bits & ST_TABLE_FULL)) {
+            st = table_convert(t, nullptr, nullptr, nullptr, 0);
+            if (st) {
+                table_free_storage(t);
+                table_free_out(t);
+                delete t;
+                return st;
+            }
+            *out = t;
+            return FBK_OK;
+        }
+        table_free_storage(t);
+        cap *= 2;
+    }
+    delete t;
+    return set_err(ctx, FBK_ERR_TABLE_FULL, "solid table still full after growing it 3 times");
+}
+
+static fbk_status contig_bank_opt(fbk_ctx* ctx, const uint8_t* ascii, const uint64_t* offs, uint64_t n, fbk_bank** out) {
+    *out = nullptr;
+    if (n == 0) return FBK_OK;
+    if (!ascii || !offs) return set_err(ctx, FBK_ERR_INVALID, "contigs: null buffers");
+    return contig_bank(ctx, ascii, offs, n, out);
+}
+
+FBK_API fbk_status fbk_solid_build(fbk_ctx* ctx, const fbk_bank* b, const fbk_cms* cms, const fbk_build_params* p,
+                                   const fbk_subsample* ss, const uint8_t* contig_ascii, const uint64_t* contig_offs,
+                                   uint64_t n_contigs, fbk_table** out) {
+    if (!ctx || !b || !cms || !p || !out) return FBK_ERR_INVALID;
+    CK(ctx, cudaSetDevice(ctx->device));
+    uint64_t* keep = nullptr;
+    fbk_status st = make_keep_bits(ctx, b, ss, &keep);
+    if (st) return st;
+    fbk_bank* cb = nullptr;
+    st = contig_bank_opt(ctx, contig_ascii, contig_offs, n_contigs, &cb);
+    uint64_t distinct = 0;
+    if (st == FBK_OK && !p->table_log2_cap) st = cms_distinct(cms, &distinct);
+    if (st == FBK_OK) st = solid_build_impl(ctx, b, cms, p, keep, cb, distinct + (cb ? cb->n_bases : 0), out);
+    cudaStreamSynchronize(ctx->stream);
+    if (cb) fbk_bank_release(cb);
+    dev_free(ctx, keep);
+    return st;
+}
+
+FBK_API fbk_status fbk_build_front(fbk_ctx* ctx, const fbk_bank* b, const fbk_build_params* p, const fbk_subsample* ss,
+                                   const uint8_t* contig_ascii, const uint64_t* contig_offs, uint64_t n_contigs,
+                                   fbk_table** out, fbk_cms** cms_out) {
+    if (!ctx || !b || !p || !out) return FBK_ERR_INVALID;
+    CK(ctx, cudaSetDevice(ctx->device));
+    uint32_t log2w = p->cms_log2_width;
+    if (!log2w) {
+        // build.rs:74-84: explicit genome size (floored at 50 kb), else read bases / 60
+        uint64_t g = p->genome_size ? std::max<uint64_t>(p->genome_size, 50000) : std::max<uint64_t>(b->n_bases / 60, 50000);
+        uint64_t w = fbk_cms_width_for_genome_size(g);
+        log2w = 0;
+        while ((1ULL << log2w) < w) ++log2w;
+    }
+    fbk_cms* cms = nullptr;
+    fbk_status st = fbk_cms_create(ctx, log2w, p->counter_bits, &cms);
+    if (st) return st;
+    uint64_t* keep = nullptr;
+    fbk_bank* cb = nullptr;
+    st = make_keep_bits(ctx, b, ss, &keep);
+    if (st == FBK_OK) st = contig_bank_opt(ctx, contig_ascii, contig_offs, n_contigs, &cb);
+    if (st == FBK_OK) st = pass1_impl(cms, b, p->k, p->key_bits, keep, 1);
+    if (st == FBK_OK && cb) st = pass1_impl(cms, cb, p->k, p->key_bits, nullptr, 10);
+    uint64_t distinct = 0;
+    if (st == FBK_OK && !p->table_log2_cap) st = cms_distinct(cms, &distinct);
+    if (st == FBK_OK) st = solid_build_impl(ctx, b, cms, p, keep, cb, distinct, out);
+    cudaStreamSynchronize(ctx->stream);
+    if (cb) fbk_bank_release(cb);
+    dev_free(ctx, keep);
+    if (st == FBK_OK && cms_out) *cms_out = cms;
+    else fbk_cms_release(cms);
+    return st;
+}
+
+FBK_API fbk_status fbk_table_info(const fbk_table* t, uint64_t* n_keys, uint64_t* n_solid, uint64_t* capacity) {
+    if (!t) return FBK_ERR_INVALID;
+    if (n_keys) *n_keys = t->n_keys;
+    if (n_solid) *n_solid = t->n_solid;
+    if (capacity) *capacity = t->cap;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_table_export(fbk_table* t, uint64_t* keys, uint16_t* cov, uint8_t* mask, uint64_t cap, uint64_t* n_out) {
+    if (!t || !n_out) return FBK_ERR_INVALID;
+    fbk_ctx* ctx = t->ctx;
+    uint64_t n = std::min(cap, t->n_solid);
+    if (n && (!keys || !cov || !mask)) return FBK_ERR_INVALID;
+    if (n) {
+        CK(ctx, cudaMemcpyAsync(keys, t->out_keys, n * 8 * t->nw, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(ctx, cudaMemcpyAsync(cov, t->out_cov, n * 2, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(ctx, cudaMemcpyAsync(mask, t->out_mask, n, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    *n_out = t->n_solid;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_table_export_acc(fbk_table* t, uint64_t* keys, uint16_t* cov, uint16_t* edges, uint64_t cap, uint64_t* n_out) {
+    if (!t || !n_out) return FBK_ERR_INVALID;
+    fbk_ctx* ctx = t->ctx;
+    uint64_t n = std::min(cap, t->n_keys);
+    uint64_t* dk = nullptr;
+    uint16_t *dc = nullptr, *de = nullptr;
+    if (n) {
+        if (!keys || !cov || !edges) return FBK_ERR_INVALID;
+        dk = (uint64_t*)dev_alloc(ctx, n * 8 * t->nw);
+        dc = (uint16_t*)dev_alloc(ctx, n * 2);
+        de = (uint16_t*)dev_alloc(ctx, n * 16);
+        if (!dk || !dc || !de) {
+            dev_free(ctx, dk);
+            dev_free(ctx, dc);
+            dev_free(ctx, de);
+            return set_err(ctx, FBK_ERR_OOM, "accumulator export buffers");
+        }
+    }
+    fbk_status st = table_convert(t, dk, dc, de, n);
+    if (st == FBK_OK && n) {
+        cudaError_t e = cudaMemcpyAsync(keys, dk, n * 8 * t->nw, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(cov, dc, n * 2, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(edges, de, n * 16, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) st = cuda_err(ctx, e, "accumulator export");
+    }
+    dev_free(ctx, dk);
+    dev_free(ctx, dc);
+    dev_free(ctx, de);
+    *n_out = t->n_keys;
+    return st;
+}
+
+FBK_API fbk_status fbk_table_pushes(const fbk_table* t, uint64_t* pushes) {
+    if (!t || !pushes) return FBK_ERR_INVALID;
+    *pushes = t->pushes;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_table_digest(fbk_table* t, uint64_t* digest, uint64_t* n_solid) {
+    if (!t || !digest) return FBK_ERR_INVALID;
+    *digest = t->digest;
+    if (n_solid) *n_solid = t->n_solid;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_table_release(fbk_table* t) {
+    if (!t) return FBK_OK;
+    cudaStreamSynchronize(t->ctx->stream);
+    table_free_storage(t);
+    table_free_out(t);
+    delete t;
+    return FBK_OK;
+}
+
+// ===========================================================================
+// subsampler, ntHash / canonical k-mer dumps
+// ===========================================================================
+FBK_API fbk_status fbk_subsample_mask(fbk_ctx* ctx, uint64_t n_pairs, const fbk_subsample* ss, uint64_t* keep_bits) {
+    if (!ctx || !ss || (n_pairs && !keep_bits)) return FBK_ERR_INVALID;
+    if (!n_pairs) return FBK_OK;
+    const uint64_t nw = (n_pairs + 63) / 64;
+    uint64_t* d = (uint64_t*)dev_alloc(ctx, nw * 8);
+    if (!d) return set_err(ctx, FBK_ERR_OOM, "subsample bitmap");
+    cudaError_t e;
+    {
+        TimedLaunch tl;
+        time_begin(ctx, "subsample", tl);
+        e = launch_subsample_mask(launch_cfg(ctx, 256, 0), n_pairs, ss->factor, ss->seed, d);
+        time_end(ctx, tl);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(keep_bits, d, nw * 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, d);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "subsample mask");
+    return FBK_OK;
+}
+
+// Uploads one arena and the per-read window bases for the dump kernels.
+static fbk_status dump_prep(fbk_ctx* ctx, const fbk_arena_view* arena, uint32_t k, fbk_bank** bank, uint64_t** kbase,
+                            uint64_t* total) {
+    fbk_status st = bank_upload_impl(ctx, arena, 1, bank);
+    if (st) return st;
+    std::vector<uint64_t> kb(arena->n_seqs + 1, 0);
+    for (uint64_t i = 0; i < arena->n_seqs; ++i) kb[i + 1] = kb[i] + (arena->lengths[i] >= k ? arena->lengths[i] - k + 1 : 0);
+    *total = kb.back();
+    *kbase = (uint64_t*)dev_alloc(ctx, kb.size() * 8);
+    if (!*kbase) {
+        fbk_bank_release(*bank);
+        return set_err(ctx, FBK_ERR_OOM, "window base offsets");
+    }
+    CK(ctx, cudaMemcpyAsync(*kbase, kb.data(), kb.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_nthash_arena(fbk_ctx* ctx, const fbk_arena_view* arena, uint32_t k, uint64_t* out, uint64_t cap, uint64_t* n_out) {
+    if (!ctx || !arena || !n_out || k == 0) return FBK_ERR_INVALID;
+    CK(ctx, cudaSetDevice(ctx->device));
+    fbk_bank* b = nullptr;
+    uint64_t* kbase = nullptr;
+    uint64_t total = 0;
+    fbk_status st = dump_prep(ctx, arena, k, &b, &kbase, &total);
+    if (st) return st;
+    *n_out = total;
+    if (total > cap || (total && !out)) {
+        fbk_bank_release(b);
+        dev_free(ctx, kbase);
+        return total > cap ? set_err(ctx, FBK_ERR_INVALID, "output buffer too small") : FBK_ERR_INVALID;
+    }
+    uint64_t* d = (uint64_t*)dev_alloc(ctx, std::max<uint64_t>(total, 1) * 8);
+    cudaError_t e = d ? cudaSuccess : cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) {
+        TimedLaunch tl;
+        time_begin(ctx, "nthash_dump", tl);
+        e = launch_nthash_arena(launch_cfg(ctx, 256, 0), bank_view(b, 0, b->n_reads, nullptr), kbase, k, d);
+        time_end(ctx, tl);
+    }
+    if (e == cudaSuccess && total) e = cudaMemcpyAsync(out, d, total * 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, d);
+    dev_free(ctx, kbase);
+    fbk_bank_release(b);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "nthash dump");
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_canonical_kmers_arena(fbk_ctx* ctx, const fbk_arena_view* arena, uint32_t k, uint32_t key_bits,
+                                             uint64_t* out_words, uint8_t* out_is_rc, uint64_t cap, uint64_t* n_out) {
+    const int nw = nw_of(key_bits);
+    if (!ctx || !arena || !n_out || !nw || k == 0 || k > max_k_of(key_bits)) return FBK_ERR_INVALID;
+    CK(ctx, cudaSetDevice(ctx->device));
+    fbk_bank* b = nullptr;
+    uint64_t* kbase = nullptr;
+    uint64_t total = 0;
+    fbk_status st = dump_prep(ctx, arena, k, &b, &kbase, &total);
+    if (st) return st;
+    *n_out = total;
+    if (total > cap || (total && (!out_words || !out_is_rc))) {
+        fbk_bank_release(b);
+        dev_free(ctx, kbase);
+        return total > cap ? set_err(ctx, FBK_ERR_INVALID, "output buffer too small") : FBK_ERR_INVALID;
+    }
+    uint64_t* d = (uint64_t*)dev_alloc(ctx, std::max<uint64_t>(total, 1) * 8 * nw);
+    uint8_t* dr = (uint8_t*)dev_alloc(ctx, std::max<uint64_t>(total, 1));
+    cudaError_t e = (d && dr) ? cudaSuccess : cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) {
+        TimedLaunch tl;
+        time_begin(ctx, "canon_dump", tl);
+        e = launch_canon_arena(nw, launch_cfg(ctx, 256, 0), bank_view(b, 0, b->n_reads, nullptr), kbase, k, d, dr);
+        time_end(ctx, tl);
+    }
+    if (e == cudaSuccess && total) e = cudaMemcpyAsync(out_words, d, total * 8 * nw, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && total) e = cudaMemcpyAsync(out_is_rc, dr, total, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, d);
+    dev_free(ctx, dr);
+    dev_free(ctx, kbase);
+    fbk_bank_release(b);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "canonical k-mer dump");
+    return FBK_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,237 @@
+// fbk_device.cuh — device primitives of the k-mer counting front end (sm_103a).
+//
+// K-mers are read straight out of the 2-bit packed bank: the window of k bases that
+// starts at base g is the 2k-bit field at bit 2g of the LSB-first stream
+// (src/common/bitseq.rs:213-219).  From that field W:
+//   rc  = ~W masked to 2k bits          (kmer.rs:99-101, 158-178, 260-305)
+//   fwd = W with its 2-bit groups reversed, as the MSB-first integer of
+//         KmerInt::from_ascii (kmer.rs:73-81, 132-140, 210-222)
+// so every lane computes its own window with no rolling dependency; the values are
+// identical to RollingKmer::roll_next's (kmer.rs:104-112, 181-189, 307-329).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fbk {
+
+// splitmix64 finaliser — src/common/sketch.rs:13-18
+__host__ __device__ __forceinline__ uint64_t smix(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+// CMS row seeds — sketch.rs:122-127
+__host__ __device__ __forceinline__ uint64_t cms_seed(int r) {
+    return r == 0 ? 0x243f6a8885a308d3ULL : r == 1 ? 0x13198a2e03707344ULL : r == 2 ? 0xa4093822299f31d0ULL : 0x082efa98ec4e6c89ULL;
+}
+
+// ntHash seeds — kmer.rs:385-391 (REV[c] == FWD[3-c])
+__host__ __device__ __forceinline__ uint64_t nt_fwd(uint32_t c) {
+    return (c & 2) ? ((c & 1) ? 0x295c504fac61002eULL : 0x20323ee046061444ULL)
+                   : ((c & 1) ? 0x3193c18562a02b4cULL : 0x3c8bfbb395c60474ULL);
+}
+__host__ __device__ __forceinline__ uint64_t rotl64(uint64_t x, uint32_t r) {
+    r &= 63;
+    return (x << r) | (x >> ((64 - r) & 63));
+}
+__host__ __device__ __forceinline__ uint64_t rotr64(uint64_t x, uint32_t r) {
+    r &= 63;
+    return (x >> r) | (x << ((64 - r) & 63));
+}
+
+// Reverses the order of the 32 2-bit groups of x.
+__device__ __forceinline__ uint64_t rev2(uint64_t x) {
+    x = __brevll(x);
+    return ((x >> 1) & 0x5555555555555555ULL) | ((x & 0x5555555555555555ULL) << 1);
+}
+
+// 64 bits of the packed stream starting at base g (bases g .. g+31).  The bank
+// buffer carries 8 zero words of padding, so word g/32+1 always exists.
+__device__ __forceinline__ uint64_t bits_at(const uint64_t* __restrict__ d, uint64_t g) {
+    const uint64_t wi = g >> 5;
+    const uint32_t sh = (uint32_t)(g & 31) << 1;
+    const uint64_t lo = d[wi], hi = d[wi + 1];
+    return (lo >> sh) | ((hi << (63 - sh)) << 1);
+}
+__device__ __forceinline__ uint32_t base_at(const uint64_t* __restrict__ d, uint64_t g) {
+    return (uint32_t)(d[g >> 5] >> ((g & 31) << 1)) & 3u;
+}
+
+// Canonical k-mer of NW 64-bit words, big-endian (w[0] most significant), the word
+// order of [u64; 4] in kmer.rs:199.
+template <int NW>
+struct Key {
+    uint64_t w[NW];
+};
+
+template <int NW>
+__device__ __forceinline__ bool key_less(const Key<NW>& a, const Key<NW>& b) {
+#pragma unroll
+    for (int i = 0; i < NW; ++i)
+        if (a.w[i] != b.w[i]) return a.w[i] < b.w[i];
+    return false;
+}
+template <int NW>
+__device__ __forceinline__ bool key_eq(const Key<NW>& a, const Key<NW>& b) {
+    bool e = true;
+#pragma unroll
+    for (int i = 0; i < NW; ++i) e &= (a.w[i] == b.w[i]);
+    return e;
+}
+// KmerInt::to_u64 — kmer.rs:115-117 (u64), 192-194 (lo^hi), 332-334 (xor of 4 words)
+template <int NW>
+__device__ __forceinline__ uint64_t key_fold(const Key<NW>& a) {
+    uint64_t f = 0;
+#pragma unroll
+    for (int i = 0; i < NW; ++i) f ^= a.w[i];
+    return f;
+}
+
+// Mask for LSB-first word i of a 2k-bit field.
+__device__ __forceinline__ uint64_t field_mask(uint32_t k, int i) {
+    const int bits = (int)(2 * k) - 64 * i;
+    return bits >= 64 ? ~0ULL : bits <= 0 ? 0ULL : ((1ULL << bits) - 1);
+}
+
+// Canonical k-mer (min(fwd, rc), rc chosen iff rc < fwd — build.rs:102,258) of the
+// window starting at base g.  k <= 32*NW - 1.
+template <int NW>
+__device__ __forceinline__ void window_canonical(const uint64_t* __restrict__ d, uint64_t g, uint32_t k, Key<NW>& can,
+                                                 bool& is_rc) {
+    uint64_t W[NW];
+#pragma unroll
+    for (int i = 0; i < NW; ++i) W[i] = bits_at(d, g + 32ull * i);
+    // fwd: full group reversal of the NW*64-bit field (R.w[i] = rev2(W[i])), then a
+    // right shift by s = 64*NW - 2k bits (big-endian words).
+    uint64_t R[NW];
+#pragma unroll
+    for (int i = 0; i < NW; ++i) R[i] = rev2(W[i]);
+    const uint32_t s = 64u * NW - 2u * k;
+    const uint32_t ws = s >> 6, bs = s & 63;
+    Key<NW> fwd, rc;
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+        const int src = j - (int)ws;
+        uint64_t v = 0;
+        if (src >= 0) {
+            v = R[src] >> bs;
+            if (bs && src >= 1) v |= R[src - 1] << (64 - bs);
+        }
+        fwd.w[j] = v;
+    }
+    // rc: ~W masked to 2k bits; LSB-first word i is big-endian word NW-1-i.
+#pragma unroll
+    for (int i = 0; i < NW; ++i) rc.w[NW - 1 - i] = (~W[i]) & field_mask(k, i);
+    is_rc = key_less<NW>(rc, fwd);
+    can = is_rc ? rc : fwd;
+}
+
+// ---------------------------------------------------------------------------
+// Count-Min Sketch counters.  Nibble mode keeps the reference byte layout
+// (sketch.rs:131-157: counter c = r*w+col lives in byte c>>1, high nibble when c is
+// odd), viewed as little-endian 32-bit words: nibble c sits at bit 4*(c&7) of word
+// c>>3.  u16 mode: counter c is the half-word c&1 of word c>>1.
+// Saturating increments use a CAS loop that first skips saturated counters, the
+// device form of sketch.rs:199-221.  The loop is bounded: every failed CAS means
+// another increment of the same 32-bit word succeeded, and a word holds at most
+// 8*15 (nibble) or 2*65535 (u16) increments.
+// ---------------------------------------------------------------------------
+template <int CB>
+__device__ __forceinline__ void cms_counter_addr(uint64_t c, uint32_t*& word, uint32_t& shift);
+template <>
+__device__ __forceinline__ void cms_counter_addr<4>(uint64_t c, uint32_t*& word, uint32_t& shift) {
+    word += c >> 3;
+    shift = (uint32_t)(c & 7) << 2;
+}
+template <>
+__device__ __forceinline__ void cms_counter_addr<16>(uint64_t c, uint32_t*& word, uint32_t& shift) {
+    word += c >> 1;
+    shift = (uint32_t)(c & 1) << 4;
+}
+template <int CB>
+__device__ __forceinline__ uint32_t cms_cap() { return CB == 4 ? 15u : 0xFFFFu; }
+
+// Adds `n` (>= 1) to one counter, saturating at the cap.
+template <int CB>
+__device__ __forceinline__ void cms_sat_add(uint32_t* base, uint64_t c, uint32_t n) {
+    uint32_t* p = base;
+    uint32_t sh;
+    cms_counter_addr<CB>(c, p, sh);
+    const uint32_t cap = cms_cap<CB>();
+    uint32_t cur = *(volatile uint32_t*)p;
+    for (;;) {
+        const uint32_t v = (cur >> sh) & cap;
+        if (v >= cap) return;
+        const uint32_t nv = (v + n > cap) ? cap : v + n;
+        const uint32_t want = (cur & ~(cap << sh)) | (nv << sh);
+        const uint32_t old = atomicCAS(p, cur, want);
+        if (old == cur) return;
+        cur = old;
+    }
+}
+
+template <int CB>
+__device__ __forceinline__ uint32_t cms_read(const uint32_t* base, uint64_t c) {
+    uint32_t* p = const_cast<uint32_t*>(base);
+    uint32_t sh;
+    cms_counter_addr<CB>(c, p, sh);
+    return (*p >> sh) & cms_cap<CB>();
+}
+
+// Counter index of row r for key (sketch.rs:193-195).
+__device__ __forceinline__ uint64_t cms_index(uint64_t key, int r, uint32_t log2w) {
+    const uint64_t col = smix(key ^ cms_seed(r)) & ((1ULL << log2w) - 1);
+    return ((uint64_t)r << log2w) + col;
+}
+
+// CountMinSketch::add (sketch.rs:191-223)
+template <int CB>
+__device__ __forceinline__ void cms_add(uint32_t* t, uint64_t key, uint32_t log2w) {
+    uint64_t c[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) c[r] = cms_index(key, r, log2w);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) cms_sat_add<CB>(t, c[r], 1);
+}
+
+// CountMinSketch::estimate (sketch.rs:227-246).  The reference returns early at 0;
+// reading all four rows gives the same minimum.
+template <int CB>
+__device__ __forceinline__ uint32_t cms_estimate(const uint32_t* t, uint64_t key, uint32_t log2w) {
+    uint32_t v[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) v[r] = cms_read<CB>(t, cms_index(key, r, log2w));
+    uint32_t m = cms_cap<CB>();
+#pragma unroll
+    for (int r = 0; r < 4; ++r) m = v[r] < m ? v[r] : m;
+    return m;
+}
+
+// HyperLogLog register index and rank — sketch.rs:49-63 (p = 14 there).
+__device__ __forceinline__ void hll_idx_rho(uint64_t h, uint32_t p, uint32_t& idx, uint32_t& rho) {
+    idx = (uint32_t)(h >> (64 - p));
+    const uint64_t w = h & ((1ULL << (64 - p)) - 1);
+    rho = w == 0 ? (64 - p + 1) : ((uint32_t)__clzll(w) - p + 1);
+}
+
+// Canonical ntHash of the window of k bases at g (nthash_fwd/rev, kmer.rs:394-423).
+// Equal to RollingNtHash's rolled value for the same window (kmer.rs:447-464).
+__device__ __forceinline__ uint64_t nthash_canonical_at(const uint64_t* __restrict__ d, uint64_t g, uint32_t k) {
+    uint64_t hf = 0, hr = 0;
+    for (uint32_t j = 0; j < k; ++j) {
+        const uint32_t c = base_at(d, g + j);
+        hf ^= rotl64(nt_fwd(c), (k - 1 - j) & 63);
+        hr ^= rotl64(nt_fwd(3 - c), j & 63);
+    }
+    return hf < hr ? hf : hr;
+}
+
+// Device status bits, read by the host after each phase.
+enum : uint32_t {
+    ST_TABLE_FULL = 1u,
+    ST_SPIN_TIMEOUT = 2u,
+    ST_BAD_INPUT = 4u,
+};
+
+}  // namespace fbk

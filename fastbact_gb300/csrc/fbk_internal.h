@@ -1,0 +1,127 @@
+// fbk_internal.h — host-side internals shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/fbk.h"
+#include "fbk_kernels.cuh"
+
+namespace fbk {
+
+// First-fit device memory pool carved from one cudaMalloc (256-byte granules).
+class DevicePool {
+  public:
+    bool init(uint64_t bytes, std::string& err);
+    void release();
+    void* alloc(uint64_t bytes);
+    void free(void* p);
+    uint64_t used() const { return used_bytes_; }
+    uint64_t size() const { return size_; }
+    uint64_t largest_free() const;
+    bool active() const { return base_ != nullptr; }
+
+  private:
+    char* base_ = nullptr;
+    uint64_t size_ = 0, used_bytes_ = 0;
+    std::map<uint64_t, uint64_t> free_;  // offset -> size
+    std::map<uint64_t, uint64_t> live_;  // offset -> size
+    mutable std::mutex mu_;
+};
+
+struct TimedLaunch {
+    std::string name;
+    cudaEvent_t a, b;
+};
+
+}  // namespace fbk
+
+struct fbk_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    fbk::DevicePool pool;
+    uint32_t* d_status = nullptr;            // device status bits (4 words)
+    unsigned long long* d_counts = nullptr;  // conversion counters (4)
+    void* h_pinned = nullptr;                // 64 KiB pinned host scratch
+    std::string err;
+    bool timing = false;
+    std::vector<fbk::TimedLaunch> pending;
+    std::vector<cudaEvent_t> free_events;
+    std::map<std::string, std::pair<double, uint64_t>> timed;
+    uint64_t launches = 0;
+    cudaEvent_t markers[16] = {};
+    // launch shapes (block size; grid 0 = persistent grid from occupancy)
+    int block_pass1 = 256, grid_pass1 = 0;
+    int block_pass2 = 256, grid_pass2 = 0;
+    int block_misc = 256;
+};
+
+struct fbk_bank {
+    fbk_ctx* ctx = nullptr;
+    uint64_t* data = nullptr;
+    uint64_t* off = nullptr;
+    uint32_t* len = nullptr;
+    uint32_t* pair_idx = nullptr;
+    uint64_t n_reads = 0, n_words = 0, n_bases = 0, n_pairs = 0;
+    uint32_t max_len = 0;
+    std::vector<uint64_t> chunk_starts;  // read-range boundaries with < 2^31 bases each
+};
+
+struct fbk_cms {
+    fbk_ctx* ctx = nullptr;
+    uint32_t* words = nullptr;
+    uint32_t* hll12 = nullptr;  // p=12 registers of the keys added by bank passes (table sizing)
+    uint32_t log2w = 0;
+    uint32_t cbits = 4;
+    uint64_t n_words = 0;
+};
+
+struct fbk_hll {
+    fbk_ctx* ctx = nullptr;
+    uint32_t* regs = nullptr;
+    uint32_t p = 14;
+};
+
+struct fbk_table {
+    fbk_ctx* ctx = nullptr;
+    uint32_t nw = 1, k = 0, min_trans_cov = 3;
+    uint64_t cap = 0;
+    uint64_t* keys = nullptr;
+    uint64_t* tags = nullptr;
+    uint32_t* cnt = nullptr;
+    uint32_t* cov = nullptr;
+    // converted SolidKmerNode rows
+    uint64_t* out_keys = nullptr;
+    uint16_t* out_cov = nullptr;
+    uint8_t* out_mask = nullptr;
+    uint64_t out_cap = 0;
+    uint64_t n_keys = 0, n_solid = 0, digest = 0, pushes = 0;
+};
+
+namespace fbk {
+
+fbk_status set_err(fbk_ctx* ctx, fbk_status st, const std::string& msg);
+fbk_status cuda_err(fbk_ctx* ctx, cudaError_t e, const char* what);
+void* dev_alloc(fbk_ctx* ctx, uint64_t bytes);
+void dev_free(fbk_ctx* ctx, void* p);
+Launch launch_cfg(fbk_ctx* ctx, int block, int grid);
+// Brackets a launch with timing events when timing is on.
+void time_begin(fbk_ctx* ctx, const char* name, TimedLaunch& t);
+void time_end(fbk_ctx* ctx, TimedLaunch& t);
+fbk_status ctx_check_status(fbk_ctx* ctx, uint32_t* bits);
+
+// Upload of a packed arena set into a device bank (used by the estimator for its
+// sample and by prior-contig handling).
+fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_arenas, fbk_bank** out);
+BankDev bank_view(const fbk_bank* b, uint64_t r_begin, uint64_t r_end, const uint64_t* keep_bits);
+
+// host f64 HyperLogLog::estimate from the register sum and zero count (sketch.rs:83-114)
+double hll_estimate_from_sum(double sum, uint64_t zeros, uint32_t p);
+uint64_t f64_to_u64_sat(double x);
+
+}  // namespace fbk

@@ -1,0 +1,269 @@
+/*
+ * fbk.h — C ABI of the GB300 (sm_103a) k-mer counting front end for fastBact.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and returns an
+ * fbk_status (0 = FBK_OK).  fbk_last_error() gives the message of the most recent
+ * failure on a context.  The caller owns every host buffer; the library owns device
+ * objects until their *_release call.  A context is used from one host thread at a
+ * time; separate contexts are independent.  Each context owns one CUDA stream.
+ *
+ * Reference interfaces (paths inside the fastBact repository) that each group
+ * replaces are cited next to the declarations.  The Rust-side binding a maintainer
+ * adds to call these functions is shown in INTEGRATION.md.
+ */
+#ifndef FBK_H
+#define FBK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FBK_API __attribute__((visibility("default")))
+
+typedef int fbk_status;
+enum {
+    FBK_OK = 0,
+    FBK_ERR_INVALID = 1,     /* bad argument (size, k out of range, null pointer) */
+    FBK_ERR_CUDA = 2,        /* CUDA runtime error; message in fbk_last_error */
+    FBK_ERR_OOM = 3,         /* device pool or cudaMalloc exhausted */
+    FBK_ERR_TABLE_FULL = 4,  /* solid table probe limit hit (retried internally first) */
+    FBK_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
+    FBK_ERR_IO = 6,          /* file open/read failure */
+    FBK_ERR_FORMAT = 7,      /* malformed or desynchronised FASTQ */
+    FBK_ERR_EMPTY = 8,       /* no valid read pairs */
+    FBK_ERR_BUSY = 9,        /* admission refused: not enough free device memory / slots */
+    FBK_ERR_NOT_READY = 10,  /* asynchronous work not finished yet */
+    FBK_ERR_NO_DEVICE = 11   /* no CUDA device visible */
+};
+
+typedef struct fbk_ctx fbk_ctx;       /* device, stream, memory pool, status words */
+typedef struct fbk_bank fbk_bank;     /* device-resident ReadBank */
+typedef struct fbk_cms fbk_cms;       /* device-resident CountMinSketch */
+typedef struct fbk_table fbk_table;   /* device-resident solid k-mer table */
+typedef struct fbk_hll fbk_hll;       /* device-resident HyperLogLog */
+typedef struct fbk_hbank fbk_hbank;   /* host-resident ReadBank (ingest output) */
+
+/* One BitSeqArena (src/common/bitseq.rs:145-149): base i of the arena lives at bits
+ * 2*(i%32) of data[i/32] (LSB first, A=0 C=1 G=2 T=3); offsets[id] is the arena base
+ * index of sequence id, lengths[id] its length.  pair_idx (optional, may be NULL) is
+ * the 0-based input pair each read came from, used by the subsampler. */
+typedef struct {
+    const uint64_t* data;
+    uint64_t n_words;
+    const uint64_t* offsets;
+    const uint32_t* lengths;
+    uint64_t n_seqs;
+    const uint32_t* pair_idx;
+} fbk_arena_view;
+
+/* ExactCountStats — src/ingest/estimator.rs:34-51 */
+typedef struct {
+    uint64_t exact_read_pairs;
+    uint64_t total_bases_r1;
+    uint64_t total_bases_r2;
+    uint64_t total_bases;
+    uint64_t min_read_len;
+    uint64_t max_read_len;
+    double mean_read_len;
+    uint64_t median_read_len;
+} fbk_count_stats;
+
+/* GenomeEstimate — src/ingest/estimator.rs:55-83 (kmers is the Vec<usize> ladder;
+ * confidence: 0 High, 1 LowCoverageWarning, 2 Unreliable). */
+typedef struct {
+    uint64_t genome_size;
+    uint64_t exact_read_pairs;
+    uint64_t total_bases;
+    uint64_t median_read_len;
+    uint64_t max_read_len;
+    double estimated_cov;
+    double subsample_factor;
+    uint64_t kmers[8];
+    uint64_t n_kmers;
+    int32_t confidence;
+    int32_t _pad;
+    uint64_t u_ge_1;
+    uint64_t u_ge_2;
+    double sample_kmer_depth;
+    uint64_t pairs_sampled; /* pairs consumed before the sample loop ended */
+    uint64_t m_sample;      /* k-mer occurrences in the consumed pairs */
+} fbk_genome_estimate;
+
+/* Estimator parameters.  fbk_estimator_defaults() fills the reference constants:
+ * k = 21, CMS width 1<<23 nibbles, HLL p = 14, sample cap 150000 pairs,
+ * checkpoints every 2000 pairs from 6000 (src/ingest/estimator.rs:299-375). */
+typedef struct {
+    uint32_t k;
+    uint32_t cms_log2_width;
+    uint32_t hll_p;          /* 14 (reference) or 16 */
+    uint32_t _pad;
+    uint64_t sample_cap;     /* 150000 */
+    uint64_t max_pairs;      /* estimate_genome's max_pairs argument */
+    double target_cov;       /* estimate_genome's target_cov argument */
+} fbk_estimator_params;
+
+/* Subsampler (src/ingest/trim_merge.rs:324-348): input pair i (1-based) is kept iff
+ * factor >= 0.999 or splitmix64(i ^ seed) <= (u64)(factor * 2^64). */
+typedef struct {
+    double factor;
+    uint64_t seed;
+} fbk_subsample;
+
+/* Front-end build parameters (src/graph/build.rs:67-328).  t_solid is the CMS gate
+ * (target_solid_cov.unwrap_or(2)); min_trans_cov the per-edge mask threshold
+ * (target_solid_cov or 3).  counter_bits 4 = reference nibble CMS, 16 = u16 CMS. */
+typedef struct {
+    uint32_t k;
+    uint32_t key_bits;        /* 64 (k<=31), 128 (k<=63), 256 (k<=127) */
+    uint32_t cms_log2_width;  /* 0 = width_for_genome_size(genome_size) */
+    uint32_t counter_bits;    /* 4 or 16 */
+    uint32_t t_solid;
+    uint32_t min_trans_cov;
+    uint32_t table_log2_cap;  /* 0 = sized from the pass-1 distinct-k-mer sketch */
+    uint32_t _pad;
+    uint64_t genome_size;     /* used when cms_log2_width == 0 (build.rs:74-84) */
+} fbk_build_params;
+
+/* ---- status, context ------------------------------------------------------- */
+FBK_API const char* fbk_status_str(fbk_status s);
+FBK_API const char* fbk_version(void);
+/* pool_bytes = 0: objects are allocated one by one; > 0: carved from one pool. */
+FBK_API fbk_status fbk_ctx_create(int device, uint64_t pool_bytes, fbk_ctx** out);
+FBK_API fbk_status fbk_ctx_destroy(fbk_ctx* ctx);
+FBK_API fbk_status fbk_last_error(const fbk_ctx* ctx, char* buf, size_t len);
+FBK_API fbk_status fbk_ctx_sync(fbk_ctx* ctx);
+/* Kernel timing with CUDA events on the context's stream (off by default). */
+FBK_API fbk_status fbk_ctx_set_timing(fbk_ctx* ctx, int enable);
+/* Sum of event-timed milliseconds and launch count of kernels whose name starts
+ * with `prefix` since the last reset ("" = all kernels). */
+FBK_API fbk_status fbk_ctx_timing(fbk_ctx* ctx, const char* prefix, double* ms, uint64_t* launches);
+FBK_API fbk_status fbk_ctx_timing_reset(fbk_ctx* ctx);
+/* CUDA events on the context stream: record marker `slot` (0..15) now; elapsed
+ * milliseconds between two recorded markers (waits for the later one). */
+FBK_API fbk_status fbk_ctx_event_record(fbk_ctx* ctx, int slot);
+FBK_API fbk_status fbk_ctx_event_elapsed(fbk_ctx* ctx, int slot_a, int slot_b, double* ms);
+/* Number of kernels launched on this context since creation. */
+FBK_API fbk_status fbk_ctx_launch_count(const fbk_ctx* ctx, uint64_t* n);
+FBK_API fbk_status fbk_ctx_mem_info(const fbk_ctx* ctx, uint64_t* pool_used, uint64_t* pool_size);
+
+/* ---- read bank (ReadBank, src/common/bitseq.rs:350-399) ---------------------- */
+/* arenas[0..3] = merged_reads, pe_forward, pe_reverse (iteration order of
+ * build.rs:90).  Copies host data to the device (pinned host memory is copied
+ * asynchronously on the context stream). */
+FBK_API fbk_status fbk_bank_upload(fbk_ctx* ctx, const fbk_arena_view arenas[3], fbk_bank** out);
+FBK_API fbk_status fbk_bank_info(const fbk_bank* b, uint64_t* n_reads, uint64_t* n_bases);
+FBK_API fbk_status fbk_bank_release(fbk_bank* b);
+
+/* ---- CountMinSketch (src/common/sketch.rs:121-253) -------------------------- */
+FBK_API uint64_t fbk_cms_width_for_genome_size(uint64_t genome_size); /* sketch.rs:165-168 */
+FBK_API fbk_status fbk_cms_create(fbk_ctx* ctx, uint32_t log2_width, uint32_t counter_bits, fbk_cms** out);
+FBK_API fbk_status fbk_cms_clear(fbk_cms* c);
+/* CountMinSketch::add over host keys (sketch.rs:191-223). */
+FBK_API fbk_status fbk_cms_add_keys(fbk_cms* c, const uint64_t* keys, uint64_t n);
+/* CountMinSketch::estimate over host keys (sketch.rs:227-246). */
+FBK_API fbk_status fbk_cms_estimate_keys(fbk_cms* c, const uint64_t* keys, uint64_t n, uint32_t* out);
+/* Pass 1 of build_cdbg_with_contigs_ext (build.rs:90-116): add the canonical
+ * k-mer fold of every k-mer of every read with len >= k.  ss may be NULL. */
+FBK_API fbk_status fbk_cms_add_bank(fbk_cms* c, const fbk_bank* b, uint32_t k, uint32_t key_bits, const fbk_subsample* ss);
+/* Prior contigs add x10 per k-mer (build.rs:118-138); ascii concatenated, offs has n+1 entries. */
+FBK_API fbk_status fbk_cms_add_contigs(fbk_cms* c, const uint8_t* ascii, const uint64_t* offs, uint64_t n, uint32_t k, uint32_t key_bits);
+/* Raw table in the reference byte layout (4*w/2 bytes, nibble) or 4*w u16 (LE). */
+FBK_API fbk_status fbk_cms_nbytes(const fbk_cms* c, uint64_t* nbytes);
+FBK_API fbk_status fbk_cms_export(fbk_cms* c, uint8_t* out, uint64_t nbytes);
+/* dst = min(cap, dst + src) counter by counter: merging sketches of disjoint read
+ * sets equals the sketch of their union. */
+FBK_API fbk_status fbk_cms_merge(fbk_cms* dst, const fbk_cms* src);
+FBK_API fbk_status fbk_cms_release(fbk_cms* c);
+
+/* ---- HyperLogLog (src/common/sketch.rs:24-115) ------------------------------ */
+FBK_API fbk_status fbk_hll_create(fbk_ctx* ctx, uint32_t p, fbk_hll** out);
+FBK_API fbk_status fbk_hll_add_hashes(fbk_hll* h, const uint64_t* hashes, uint64_t n);           /* add_hash */
+FBK_API fbk_status fbk_hll_add_canonical_hashes(fbk_hll* h, const uint64_t* hashes, uint64_t n); /* add_canonical_hash */
+FBK_API fbk_status fbk_hll_merge(fbk_hll* dst, const fbk_hll* src);
+FBK_API fbk_status fbk_hll_export(fbk_hll* h, uint8_t* regs, uint64_t n);
+FBK_API fbk_status fbk_hll_estimate(fbk_hll* h, double* out);
+FBK_API fbk_status fbk_hll_release(fbk_hll* h);
+/* HyperLogLog::estimate over host registers (f64, register order). */
+FBK_API double fbk_hll_estimate_registers(const uint8_t* regs, uint32_t p);
+
+/* ---- ntHash (src/common/kmer.rs:385-477) --------------------------------------
+ * Canonical ntHash of every window of length k of each read in the arena
+ * (RollingNtHash::new + roll), computed on the device.  out has one entry per window,
+ * reads in order; returns the number written in *n_out. */
+FBK_API fbk_status fbk_nthash_arena(fbk_ctx* ctx, const fbk_arena_view* arena, uint32_t k, uint64_t* out, uint64_t cap, uint64_t* n_out);
+/* Canonical k-mers (big-endian words, key_bits/64 per window) and is_rc flags of
+ * every window of each read (RollingKmer::roll_next, kmer.rs:344-378). */
+FBK_API fbk_status fbk_canonical_kmers_arena(fbk_ctx* ctx, const fbk_arena_view* arena, uint32_t k, uint32_t key_bits, uint64_t* out_words, uint8_t* out_is_rc, uint64_t cap, uint64_t* n_out);
+
+/* ---- solid table (build.rs:141-328) ----------------------------------------- */
+/* Pass 2 + conversion: CMS-gated transitions accumulated in an open-addressing
+ * device table, then the SolidKmerNode conversion (mask, cov).  ss may be NULL. */
+FBK_API fbk_status fbk_solid_build(fbk_ctx* ctx, const fbk_bank* b, const fbk_cms* cms, const fbk_build_params* p,
+                                   const fbk_subsample* ss, const uint8_t* contig_ascii, const uint64_t* contig_offs,
+                                   uint64_t n_contigs, fbk_table** out);
+/* Passes 1 + 2 + conversion in one call: the front end of build_cdbg_with_contigs_ext
+ * (build.rs:67-328).  cms_out (optional) keeps the pass-1 sketch alive. */
+FBK_API fbk_status fbk_build_front(fbk_ctx* ctx, const fbk_bank* b, const fbk_build_params* p, const fbk_subsample* ss,
+                                   const uint8_t* contig_ascii, const uint64_t* contig_offs, uint64_t n_contigs,
+                                   fbk_table** out, fbk_cms** cms_out);
+/* n_keys: accumulated keys; n_solid: SolidKmerNode entries (mask != 0). */
+FBK_API fbk_status fbk_table_info(const fbk_table* t, uint64_t* n_keys, uint64_t* n_solid, uint64_t* capacity);
+/* Converted entries in device order (unsorted): keys (key_bits/64 big-endian words
+ * each), cov, mask.  cap = rows the buffers hold. */
+FBK_API fbk_status fbk_table_export(fbk_table* t, uint64_t* keys, uint16_t* cov, uint8_t* mask, uint64_t cap, uint64_t* n_out);
+/* Every accumulated key with its KmerAcc (cov and edge_counts[8], saturated at 65535). */
+FBK_API fbk_status fbk_table_export_acc(fbk_table* t, uint64_t* keys, uint16_t* cov, uint16_t* edges, uint64_t cap, uint64_t* n_out);
+/* Sum over every key of its raw edge counters (= transition pushes made by pass 2,
+ * weighted by the per-push increment); used for the algorithmic-bytes count. */
+FBK_API fbk_status fbk_table_pushes(const fbk_table* t, uint64_t* pushes);
+/* Order-independent digest of the converted entries (same formula as the oracle's). */
+FBK_API fbk_status fbk_table_digest(fbk_table* t, uint64_t* digest, uint64_t* n_solid);
+FBK_API fbk_status fbk_table_release(fbk_table* t);
+
+/* ---- estimator (src/ingest/estimator.rs:104-440) ----------------------------- */
+FBK_API void fbk_estimator_defaults(fbk_estimator_params* p);
+/* Sample loop on the device + f64 post-math on the host.  sample holds raw (untrimmed)
+ * reads interleaved R1,R2 per pair (2*n_pairs sequences); stats is count_fastx_exact
+ * over the whole input.  regs_total / regs_solid (optional, 1<<p bytes) receive the
+ * HLL registers at the point the sample loop stopped. */
+FBK_API fbk_status fbk_estimate_sample(fbk_ctx* ctx, const fbk_arena_view* sample, uint64_t n_pairs,
+                                       const fbk_count_stats* stats, const fbk_estimator_params* p,
+                                       fbk_genome_estimate* out, uint8_t* regs_total, uint8_t* regs_solid);
+/* Same as fbk_estimate_sample with the sample already resident: reads 0 .. 2*n_pairs-1
+ * of `sample` are R1,R2 interleaved per pair; read_lengths is the host copy of their
+ * lengths (used for the window bases and m_sample). */
+FBK_API fbk_status fbk_estimate_bank(fbk_ctx* ctx, const fbk_bank* sample, const uint32_t* read_lengths, uint64_t n_pairs,
+                                     const fbk_count_stats* stats, const fbk_estimator_params* p, fbk_genome_estimate* out,
+                                     uint8_t* regs_total, uint8_t* regs_solid);
+/* count_fastx_exact (estimator.rs:167-283), host-side FASTQ scan. */
+FBK_API fbk_status fbk_count_fastx_exact(const char* r1, const char* r2, fbk_count_stats* out, char* err, size_t errlen);
+/* estimate_genome (estimator.rs:286-440): FASTQ scan on the host, sample on the device. */
+FBK_API fbk_status fbk_estimate_genome(fbk_ctx* ctx, const char* r1, const char* r2, uint64_t max_pairs, double target_cov,
+                                       fbk_genome_estimate* out);
+FBK_API int fbk_compute_dynamic_kmers(uint64_t median_len, int64_t target_max_k, uint64_t* out, int cap); /* estimator.rs:104-161 */
+
+/* ---- subsampler (trim_merge.rs:324-348) -------------------------------------- */
+/* Bit i of keep_bits (host, ceil(n_pairs/64) words) = input pair i (0-based) kept. */
+FBK_API fbk_status fbk_subsample_mask(fbk_ctx* ctx, uint64_t n_pairs, const fbk_subsample* ss, uint64_t* keep_bits);
+
+/* ---- host ingest (trim_merge.rs:17-417), CPU side ----------------------------- */
+FBK_API fbk_status fbk_ingest_fastq(const char* r1, const char* r2, double subsample_factor, uint64_t min_len, uint32_t min_qual,
+                                    int enable_trim, int enable_merge, uint64_t seed, fbk_hbank** out, char* err, size_t errlen);
+FBK_API fbk_status fbk_hbank_arena(const fbk_hbank* hb, int arena, fbk_arena_view* view);
+FBK_API fbk_status fbk_hbank_stats(const fbk_hbank* hb, uint64_t* input_pairs, uint64_t* retained_pairs, uint64_t* merged_pairs,
+                                   uint64_t* unmerged_pairs, uint64_t* bases_before_trim, uint64_t* bases_after_trim);
+FBK_API void fbk_hbank_free(fbk_hbank* hb);
+/* Single-pair helpers exposed for their known-answer tests. */
+FBK_API uint64_t fbk_trim_adapter(const uint8_t* seq, uint64_t len);
+FBK_API int64_t fbk_trim_quality(const uint8_t* seq, const uint8_t* qual, uint64_t len, uint32_t min_qual, uint64_t min_len);
+FBK_API int64_t fbk_merge_read_pair(const uint8_t* r1, const uint8_t* q1, uint64_t l1, const uint8_t* r2, const uint8_t* q2,
+                                    uint64_t l2, uint64_t min_overlap, double max_mismatch_ratio, uint8_t* merged_out,
+                                    uint64_t* overlap_len, uint64_t* mismatches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FBK_H */

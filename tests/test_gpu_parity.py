@@ -1,0 +1,301 @@
+"""Parity of the device kernels (through the C ABI) with the oracle on the same
+seeded inputs.  Integer results must be bit-identical; the estimator's f64 outputs
+too (same operation order, same libm on the same host).  Tolerance: exact (0)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from fastbact_gb300 import api
+from oracle import orc
+
+pytestmark = pytest.mark.gpu
+M64 = (1 << 64) - 1
+
+
+def splitmix_py(z):
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
+    return z ^ (z >> 31)
+
+
+def rand_seqs(seed, n, lo, hi, alphabet=b"ACGT"):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        L = int(rng.integers(lo, hi + 1))
+        out.append(bytes(np.frombuffer(alphabet, np.uint8)[rng.integers(0, len(alphabet), L)]))
+    return out
+
+
+def oracle_rolling(seq: bytes, k: int, kb: int):
+    nw = kb // 64
+    n = len(seq) - k + 1
+    if n <= 0:
+        return np.zeros((0, nw), np.uint64), np.zeros(0, np.uint8)
+    out = np.zeros(n * nw, np.uint64)
+    rc = np.zeros(n, np.uint8)
+    a = np.frombuffer(seq, np.uint8).copy()
+    assert orc.lib().orc_rolling_canonicals(kb, orc.p(a), len(seq), k, orc.p(out), orc.p(rc)) == n
+    return out.reshape(n, nw), rc
+
+
+@pytest.fixture(scope="module")
+def small_isolate():
+    p = api.synth_params(seed=101, genome_len=60_000, coverage=30.0, gc=0.5)
+    return api.synth_isolate(p, threads=0, sample_pairs=150_000)
+
+
+@pytest.fixture(scope="module")
+def repeat_isolate():
+    # repeats + tandem array + indels + 1% errors: stresses the saturating counters
+    p = api.synth_params(seed=202, genome_len=50_000, coverage=60.0, gc=0.66, n_repeats=4, repeat_len=2000,
+                         tandem_copies=60, tandem_unit=60, sub_rate=0.01, indel_rate=0.0005)
+    return api.synth_isolate(p, threads=0, sample_pairs=150_000)
+
+
+# ---------------------------------------------------------------------------
+# k-mer extraction and ntHash
+# ---------------------------------------------------------------------------
+KS = [(1, 64), (5, 64), (21, 64), (31, 64), (21, 128), (33, 128), (55, 128), (63, 128), (31, 256), (65, 256),
+      (77, 256), (99, 256), (127, 256)]
+
+
+@pytest.mark.parametrize("k,kb", KS)
+def test_canonical_kmers_match_rolling(ctx, k, kb):
+    seqs = rand_seqs(k * 7 + kb, 60, 1, 400) + [b"A" * 200, b"ACGT" * 60, b"T" * (k + 1), b"G" * k]
+    arena = api.BitSeqArena.from_seqs(seqs)
+    got, got_rc = api.canonical_kmers_arena(ctx, arena, k, kb)
+    exp = [oracle_rolling(s, k, kb) for s in seqs]
+    exp_k = np.concatenate([e[0] for e in exp])
+    exp_rc = np.concatenate([e[1] for e in exp])
+    assert got.shape == exp_k.shape
+    assert np.array_equal(got, exp_k)
+    assert np.array_equal(got_rc, exp_rc)
+
+
+@pytest.mark.parametrize("k", [1, 15, 21, 31, 64, 65, 127])
+def test_nthash_matches_rolling(ctx, k):
+    seqs = rand_seqs(k, 80, 1, 300) + [b"N" * 50 + b"ACGT" * 20]
+    # N maps to A in the hash (ASCII_TO_2BIT); the packed arena stores it as A too
+    arena = api.BitSeqArena.from_seqs(seqs)
+    got = api.nthash_arena(ctx, arena, k)
+    exp = []
+    for s in seqs:
+        if len(s) < k:
+            continue
+        o = np.zeros(len(s) - k + 1, np.uint64)
+        a = np.frombuffer(s, np.uint8).copy()
+        orc.lib().orc_nthash_rolling_all(orc.p(a), len(s), k, orc.p(o))
+        exp.append(o)
+    assert np.array_equal(got, np.concatenate(exp))
+
+
+# ---------------------------------------------------------------------------
+# sketches
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("cb", [4, 16])
+def test_cms_keys_and_saturation(ctx, cb):
+    rng = np.random.default_rng(cb)
+    keys = rng.integers(0, 1 << 63, 20000, dtype=np.uint64)
+    hot = np.repeat(keys[:40], 40)  # counters beyond 15
+    allk = np.concatenate([keys, hot])
+    cms = api.CountMinSketch(1 << 12, ctx, counter_bits=cb)
+    cms.add(allk)
+    ref = orc.Cms(1 << 12, cb)
+    ref.add(allk)
+    assert np.array_equal(cms.export(), ref.export())
+    est = cms.estimate(keys[:3000])
+    assert [int(x) for x in est] == [ref.estimate(int(x)) for x in keys[:3000]]
+    c2 = api.CountMinSketch(1024, ctx, counter_bits=cb)  # sketch.rs:305-319
+    assert int(c2.estimate([42])[0]) == 0
+    c2.add([42] * 5)
+    assert int(c2.estimate([42])[0]) == 5
+    c2.add([42] * 20)
+    assert int(c2.estimate([42])[0]) == (15 if cb == 4 else 25)
+
+
+@pytest.mark.parametrize("cb", [4, 16])
+def test_cms_merge_equals_union(ctx, cb):
+    rng = np.random.default_rng(5)
+    a = rng.integers(0, 1 << 20, 30000, dtype=np.uint64)
+    b = rng.integers(0, 1 << 20, 30000, dtype=np.uint64)
+    ca, cbm, cu = (api.CountMinSketch(1 << 10, ctx, cb) for _ in range(3))
+    ca.add(a)
+    cbm.add(b)
+    cu.add(np.concatenate([a, b]))
+    ca.merge(cbm)
+    assert np.array_equal(ca.export(), cu.export())
+
+
+@pytest.mark.parametrize("p", [14, 16])
+def test_hll_registers_and_estimate(ctx, p):
+    n = 300_000
+    xs = np.array([splitmix_py(i) for i in range(n)], np.uint64)
+    h = api.HyperLogLog(p, ctx)
+    h.add_hash(xs)
+    r = orc.Hll(p)
+    r.add_hash(xs)
+    assert np.array_equal(h.registers(), r.registers())
+    assert h.estimate() == r.estimate()
+    h2, r2 = api.HyperLogLog(p, ctx), orc.Hll(p)
+    h2.add_canonical_hash(xs[:1000])
+    r2.add_canonical_hash(xs[:1000])
+    h.merge(h2)
+    r.merge(r2)
+    assert np.array_equal(h.registers(), r.registers())
+
+
+# ---------------------------------------------------------------------------
+# build front end
+# ---------------------------------------------------------------------------
+def compare_build(ctx, bank, k, kb, cb, tsc, log2w, contigs=None, subsample=None, keep_mask=None):
+    dbank = api.DeviceBank(ctx, bank)
+    table, cms = api.build_cdbg_with_contigs_ext(dbank, contigs or [], k, tsc, None, ctx=ctx, key_bits=kb,
+                                                 counter_bits=cb, cms_log2_width=log2w, subsample=subsample,
+                                                 keep_cms=True)
+    o_cms, o_tab, t_solid, mtc = orc.build_front(bank, k, kb, log2w, cb, tsc, threads=4, keep_mask=keep_mask,
+                                                 contigs=contigs)
+    assert np.array_equal(cms.export(), o_cms.export()), "pass-1 CMS bytes differ"
+    gk, gc, ge = table.export_acc(sort=True)
+    ok, oc, oe = api.sort_rows(*o_tab.export_acc())
+    assert gk.shape == ok.shape, (gk.shape, ok.shape)
+    assert np.array_equal(gk, ok) and np.array_equal(gc, oc) and np.array_equal(ge, oe)
+    sk, sc, sm = table.export(sort=True)
+    xk, xc, xm = api.sort_rows(*o_tab.export_solid(mtc))
+    assert np.array_equal(sk, xk) and np.array_equal(sc, xc) and np.array_equal(sm, xm)
+    assert table.digest() == o_tab.digest(mtc)
+    return table, len(sk)
+
+
+@pytest.mark.parametrize("k,kb", [(21, 64), (31, 64), (33, 128), (55, 128), (77, 256), (127, 256)])
+@pytest.mark.parametrize("cb", [4, 16])
+def test_build_front_matches_oracle(ctx, small_isolate, k, kb, cb):
+    bank = small_isolate[0]
+    _, n_solid = compare_build(ctx, bank, k, kb, cb, None, 16)
+    assert n_solid > 1000
+
+
+@pytest.mark.parametrize("tsc", [None, 1, 5, 15])
+def test_build_thresholds(ctx, repeat_isolate, tsc):
+    compare_build(ctx, repeat_isolate[0], 31, 64, 4, tsc, 14)
+
+
+def test_build_saturation_and_repeats(ctx, repeat_isolate):
+    # small CMS (many collisions, saturated nibbles) + repeat-rich bank, both widths
+    for k, kb in [(21, 64), (45, 128), (99, 256)]:
+        compare_build(ctx, repeat_isolate[0], k, kb, 4, None, 10)
+        compare_build(ctx, repeat_isolate[0], k, kb, 16, None, 10)
+
+
+def test_build_with_subsampling(ctx, repeat_isolate):
+    bank = repeat_isolate[0]
+    n_pairs = int(max(int(a.pair_idx.max()) for a in bank.arenas if len(a))) + 1
+    keep = api.subsample_mask(ctx, n_pairs, 0.35, 1234)
+    thr = int(0.35 * 2.0 ** 64)
+    exp = np.zeros_like(keep)
+    for q in range(n_pairs):
+        if splitmix_py((q + 1) ^ 1234) <= thr:
+            exp[q >> 6] |= np.uint64(1 << (q & 63))
+    assert np.array_equal(keep, exp)
+    compare_build(ctx, bank, 31, 64, 4, None, 16, subsample=(0.35, 1234), keep_mask=keep)
+
+
+def test_build_with_prior_contigs(ctx, small_isolate):
+    bank = small_isolate[0]
+    contigs = rand_seqs(9, 30, 20, 3000) + [b"ACGT" * 100]
+    compare_build(ctx, bank, 31, 64, 4, None, 16, contigs=contigs)
+    compare_build(ctx, bank, 33, 128, 16, 4, 16, contigs=contigs)
+    compare_build(ctx, bank, 79, 256, 4, 4, 16, contigs=contigs)
+
+
+def test_build_edge_cases(ctx):
+    k = 31
+    seqs = [b"", b"A", b"ACGT" * 7, b"C" * 31, b"G" * 32, b"T" * 1000, b"ACGTTGCA" * 600] + rand_seqs(3, 50, 1, 70)
+    bank = api.ReadBank(api.BitSeqArena.from_seqs(seqs[:4]), api.BitSeqArena.from_seqs(seqs[4:30]),
+                        api.BitSeqArena.from_seqs(seqs[30:]))
+    compare_build(ctx, bank, k, 64, 4, None, 12)
+    compare_build(ctx, bank, k, 64, 4, 1, 12)
+    compare_build(ctx, bank, 127, 256, 16, 1, 12)
+    empty = api.ReadBank()
+    t = api.build_cdbg_ext(empty, 31, None, 100000, ctx=ctx)
+    assert t.info()[:2] == (0, 0)
+
+
+def test_build_rc_bank_invariance(ctx, small_isolate):
+    """Size-independent property: the bank of reverse-complemented reads yields the
+    same CMS and the same solid table."""
+    bank = small_isolate[0]
+    seqs = [bank.pe_forward.extract_ascii(i) for i in range(min(3000, len(bank.pe_forward)))]
+    rcs = [s[::-1].translate(bytes.maketrans(b"ACGT", b"TGCA")) for s in seqs]
+    b1 = api.ReadBank(pe_forward=api.BitSeqArena.from_seqs(seqs))
+    b2 = api.ReadBank(pe_forward=api.BitSeqArena.from_seqs(rcs))
+    t1, c1 = api.build_cdbg_ext(b1, 31, None, None, ctx=ctx, cms_log2_width=16, keep_cms=True)
+    t2, c2 = api.build_cdbg_ext(b2, 31, None, None, ctx=ctx, cms_log2_width=16, keep_cms=True)
+    assert np.array_equal(c1.export(), c2.export())
+    assert t1.digest() == t2.digest()
+
+
+# ---------------------------------------------------------------------------
+# estimator
+# ---------------------------------------------------------------------------
+def sample_reads(sample: api.BitSeqArena, n_pairs: int):
+    return [sample.extract_ascii(i) for i in range(2 * n_pairs)]
+
+
+@pytest.mark.parametrize("max_pairs", [3000, 6000, 9000, 250000])
+def test_estimator_matches_oracle(ctx, small_isolate, max_pairs):
+    bank, st, sample, n_sample, cs = small_isolate
+    reads = sample_reads(sample, n_sample)
+    ost = orc.count_stats(**cs.__dict__)
+    rc, oe, ort, ors = orc.estimate_from_reads(reads, ost, max_pairs, 110.0)
+    assert rc == 0
+    ge, rt, rs = api.estimate_sample(ctx, sample, n_sample, cs, max_pairs=max_pairs, target_cov=110.0)
+    assert np.array_equal(rt, ort) and np.array_equal(rs, ors)
+    for f in ("genome_size", "exact_read_pairs", "total_bases", "median_read_len", "max_read_len", "estimated_cov",
+              "subsample_factor", "u_ge_1", "u_ge_2", "sample_kmer_depth", "pairs_sampled", "m_sample"):
+        assert getattr(ge, f) == getattr(oe, f), f
+    assert ge.kmers == [oe.kmers[i] for i in range(oe.n_kmers)]
+    assert {"HIGH": 0, "LOW_COVERAGE_WARNING": 1, "UNRELIABLE": 2}[ge.confidence] == oe.confidence
+
+
+def test_estimator_early_stop_and_p16(ctx, repeat_isolate):
+    bank, st, sample, n_sample, cs = repeat_isolate
+    reads = sample_reads(sample, n_sample)
+    ost = orc.count_stats(**cs.__dict__)
+    for p in (14, 16):
+        rc, oe, ort, ors = orc.estimate_from_reads(reads, ost, 250000, 0.0, hll_p=p)
+        ge, rt, rs = api.estimate_sample(ctx, sample, n_sample, cs, max_pairs=250000, hll_p=p)
+        assert np.array_equal(rt, ort) and np.array_equal(rs, ors)
+        assert (ge.genome_size, ge.u_ge_1, ge.u_ge_2, ge.pairs_sampled) == (oe.genome_size, oe.u_ge_1, oe.u_ge_2,
+                                                                            oe.pairs_sampled)
+        assert ge.sample_kmer_depth == oe.sample_kmer_depth
+
+
+def test_estimate_genome_from_fastq(ctx, tmp_path):
+    p = api.synth_params(seed=303, genome_len=80_000, coverage=40.0)
+    r1, r2 = tmp_path / "e_1.fq", tmp_path / "e_2.fq"
+    api.synth_write_fastq(p, r1, r2)
+    ge = api.estimate_genome(r1, r2, 250000, 30.0, ctx=ctx)
+    oe = orc.OrcEstimate()
+    err = C.create_string_buffer(256)
+    assert orc.lib().orc_estimate_genome(str(r1).encode(), str(r2).encode(), 250000, 30.0, C.byref(oe), None, None, err,
+                                         256) == 0
+    assert (ge.genome_size, ge.u_ge_1, ge.u_ge_2, ge.estimated_cov, ge.subsample_factor) == \
+           (oe.genome_size, oe.u_ge_1, oe.u_ge_2, oe.estimated_cov, oe.subsample_factor)
+    assert ge.confidence in ("HIGH", "LOW_COVERAGE_WARNING", "UNRELIABLE")
+    assert 0.7 * 80_000 < ge.genome_size < 1.3 * 80_000
+
+
+def test_estimator_reads_with_n_and_short(ctx):
+    seqs = []
+    for i in range(7000):
+        a, b = rand_seqs(i, 2, 10, 150, alphabet=b"ACGTN")
+        seqs += [a, b]
+    arena = api.BitSeqArena.from_seqs(seqs)
+    stats = api.ExactCountStats(7000, 1, 1, sum(map(len, seqs)), 10, 150, sum(map(len, seqs)) / 14000, 80)
+    ge, rt, rs = api.estimate_sample(ctx, arena, 7000, stats, max_pairs=250000)
+    rc, oe, ort, ors = orc.estimate_from_reads([s.replace(b"N", b"A") for s in seqs], orc.count_stats(**stats.__dict__),
+                                               250000, 0.0)
+    assert np.array_equal(rt, ort) and np.array_equal(rs, ors)
+    assert (ge.genome_size, ge.u_ge_2, ge.pairs_sampled) == (oe.genome_size, oe.u_ge_2, oe.pairs_sampled)
