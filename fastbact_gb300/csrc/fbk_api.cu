@@ -882,6 +882,16 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
             delete t;
             return st;
         }
+        if (!t->out_keys) {
+            // Converted rows are a subset of the distinct keys: size the output from
+            // the estimate (table_convert grows it and reruns if the estimate was low).
+            const uint64_t oc = std::min<uint64_t>(cap, (uint64_t)(1.1 * (double)distinct_hint) + 4096);
+            t->out_keys = (uint64_t*)dev_alloc(ctx, oc * 8 * t->nw);
+            t->out_cov = (uint16_t*)dev_alloc(ctx, oc * 2);
+            t->out_mask = (uint8_t*)dev_alloc(ctx, oc);
+            if (!t->out_keys || !t->out_cov || !t->out_mask) table_free_out(t);
+            else t->out_cap = oc;
+        }
         CK(ctx, cudaMemsetAsync(ctx->d_status, 0, 4, ctx->stream));
         TableDev td = table_dev(t);
         Launch L = launch_cfg(ctx, ctx->block_pass2, ctx->grid_pass2);
@@ -908,11 +918,13 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
         st = ctx_check_status(ctx, &bits);
         if (st) {
             table_free_storage(t);
+            table_free_out(t);
             delete t;
             return st;
         }
         if (bits & ST_SPIN_TIMEOUT) {
             table_free_storage(t);
+            table_free_out(t);
             delete t;
             return set_err(ctx, FBK_ERR_TIMEOUT, "solid table: a bounded wait for a key publication gave up");
         }
@@ -930,6 +942,7 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
         table_free_storage(t);
         cap *= 2;
     }
+    table_free_out(t);
     delete t;
     return set_err(ctx, FBK_ERR_TABLE_FULL, "solid table still full after growing it 3 times");
 }
