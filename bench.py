@@ -143,14 +143,17 @@ def make_workload(rank: int, scale: float):
     return p, bank, st, sample, n_sample, stats, gen_s
 
 
+_PINNED: list = []  # keeps the page-locked blocks alive for the process
+
+
 def pinned_copy(a: np.ndarray) -> np.ndarray:
     """Copy of `a` in page-locked host memory (torch allocator)."""
     import torch
 
-    t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+    t = torch.empty(max(a.nbytes, 8), dtype=torch.uint8, pin_memory=True)
+    _PINNED.append(t)
     out = t.numpy().view(a.dtype)[: a.size]
     out[...] = a
-    out._keepalive = t  # noqa: SLF001  (keeps the pinned block alive)
     return out
 
 
