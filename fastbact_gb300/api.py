@@ -19,6 +19,7 @@ buffers and parameters across the C ABI.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -51,10 +52,14 @@ def splitmix64(z: int) -> int:
 # context
 # ---------------------------------------------------------------------------
 class Context:
-    """One device, one stream, one (optional) memory pool."""
+    """One device, one stream, one (optional) memory pool.
+
+    Device objects created on a context register with it; closing the context
+    releases them first, so no object outlives the context it points into."""
 
     def __init__(self, device: int = 0, pool_bytes: int = 0):
         self._h = C.c_void_p()
+        self._children = weakref.WeakSet()
         st = N.lib().fbk_ctx_create(device, pool_bytes, C.byref(self._h))
         if st != N.FBK_OK:
             raise N.FbkError(st, f"fbk_ctx_create(device={device})")
@@ -64,8 +69,17 @@ class Context:
     def handle(self):
         return self._h
 
+    @property
+    def alive(self) -> bool:
+        return bool(self._h)
+
+    def adopt(self, obj) -> None:
+        self._children.add(obj)
+
     def close(self):
         if self._h:
+            for child in list(self._children):
+                child.release()
             N.lib().fbk_ctx_destroy(self._h)
             self._h = C.c_void_p()
 
@@ -369,6 +383,7 @@ class DeviceBank:
         self._views = bank.views()
         self._h = C.c_void_p()
         check(N.lib().fbk_bank_upload(ctx.handle, self._views, C.byref(self._h)), ctx.handle, "bank upload")
+        ctx.adopt(self)
         self.n_bases = bank.total_bases()
 
     @property
@@ -376,9 +391,9 @@ class DeviceBank:
         return self._h
 
     def release(self):
-        if self._h:
+        if self._h and self.ctx.alive:
             N.lib().fbk_bank_release(self._h)
-            self._h = C.c_void_p()
+        self._h = C.c_void_p()
 
     def __del__(self):
         try:
@@ -410,6 +425,7 @@ class CountMinSketch:
         self._h = C.c_void_p()
         check(N.lib().fbk_cms_create(self.ctx.handle, width.bit_length() - 1, counter_bits, C.byref(self._h)),
               self.ctx.handle, "cms create")
+        self.ctx.adopt(self)
 
     @staticmethod
     def width_for_genome_size(g: int) -> int:
@@ -452,9 +468,9 @@ class CountMinSketch:
         check(N.lib().fbk_cms_clear(self._h), self.ctx.handle)
 
     def release(self):
-        if self._h:
+        if self._h and self.ctx.alive:
             N.lib().fbk_cms_release(self._h)
-            self._h = C.c_void_p()
+        self._h = C.c_void_p()
 
     def __del__(self):
         try:
@@ -471,6 +487,7 @@ class HyperLogLog:
         self.p = p
         self._h = C.c_void_p()
         check(N.lib().fbk_hll_create(self.ctx.handle, p, C.byref(self._h)), self.ctx.handle, "hll create")
+        self.ctx.adopt(self)
 
     def add_hash(self, h) -> None:
         a = np.ascontiguousarray(np.atleast_1d(np.asarray(h, dtype=np.uint64)))
@@ -494,9 +511,9 @@ class HyperLogLog:
         return d.value
 
     def release(self):
-        if self._h:
+        if self._h and self.ctx.alive:
             N.lib().fbk_hll_release(self._h)
-            self._h = C.c_void_p()
+        self._h = C.c_void_p()
 
     def __del__(self):
         try:
@@ -511,6 +528,7 @@ class SolidTable:
     def __init__(self, ctx: Context, handle, k: int, key_bits: int):
         self.ctx, self._h, self.k, self.key_bits = ctx, handle, k, key_bits
         self.nw = key_bits // 64
+        ctx.adopt(self)
 
     def info(self) -> tuple[int, int, int]:
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
@@ -553,9 +571,9 @@ class SolidTable:
         return d.value, n.value
 
     def release(self):
-        if self._h:
+        if self._h and self.ctx.alive:
             N.lib().fbk_table_release(self._h)
-            self._h = C.c_void_p()
+        self._h = C.c_void_p()
 
     def __del__(self):
         try:
@@ -611,6 +629,7 @@ def build_cdbg_with_contigs_ext(bank, contigs: list[bytes], k: int, target_solid
     if keep_cms:
         cms = CountMinSketch.__new__(CountMinSketch)
         cms.ctx, cms._h, cms.counter_bits = ctx, c, counter_bits
+        ctx.adopt(cms)
         cms.width = 1 << p.cms_log2_width if p.cms_log2_width else None
         return table, cms
     return table

@@ -816,7 +816,7 @@ static fbk_status table_alloc(fbk_table* t, uint64_t cap, bool with_cov) {
 static fbk_status table_convert(fbk_table* t, uint64_t* acc_keys, uint16_t* acc_cov, uint16_t* acc_edges, uint64_t acc_cap) {
     fbk_ctx* ctx = t->ctx;
     for (int attempt = 0; attempt < 2; ++attempt) {
-        CK(ctx, cudaMemsetAsync(ctx->d_counts, 0, 4 * sizeof(unsigned long long), ctx->stream));
+        CK(ctx, cudaMemsetAsync(ctx->d_counts, 0, 8 * sizeof(unsigned long long), ctx->stream));
         ConvOut o;
         o.keys = t->out_keys;
         o.cov = t->out_cov;

@@ -204,90 +204,142 @@ __global__ void __launch_bounds__(256) k_pass2(BankDev b, uint32_t k, const uint
 // pushes: min(65535, sum of edges) — the clamp commutes because the increments
 // are positive — or the separate cov counter when prior contigs were added.
 // ---------------------------------------------------------------------------
+// Each block handles tiles of 256 threads x 8 consecutive slots; output rows are
+// reserved with one atomic per tile (block-wide prefix sums in shared memory), and
+// the key count, digest and raw edge total are accumulated per thread and added
+// once per warp at the end.
+constexpr int CONV_SLOTS = 8;
+
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp, uint32_t& total) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < nwarp ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= (uint32_t)o) w += y;
+        }
+        if (lane < nwarp) s_warp[lane] = w;  // inclusive prefix of warp totals
+    }
+    __syncthreads();
+    total = s_warp[nwarp - 1];
+    const uint32_t before = warp ? s_warp[warp - 1] : 0;
+    __syncthreads();
+    return before + x - v;
+}
+
 template <int NW>
 __global__ void __launch_bounds__(256) k_convert(TableDev t, uint32_t min_trans_cov, ConvOut o) {
-    const uint32_t lane = threadIdx.x & 31;
+    __shared__ uint32_t s_warp[32];
+    __shared__ unsigned long long s_base[2];
     const uint64_t cap = t.mask + 1;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    unsigned long long digest = 0, raw_total = 0;
-    for (uint64_t base = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~31ULL; base < cap; base += stride) {
-        const uint64_t s = base + lane;
-        bool occ = false;
-        Key<NW> key;
-        if (s < cap) {
-            if constexpr (NW == 1) {
-                key.w[0] = t.keys[s];
-                occ = key.w[0] != KEY_EMPTY;
-            } else {
-                occ = t.tags[s] != 0;
-                if (occ) {
+    const uint64_t tile = (uint64_t)blockDim.x * CONV_SLOTS;
+    unsigned long long n_keys = 0, digest = 0, raw_total = 0;
+    for (uint64_t base = (uint64_t)blockIdx.x * tile; base < cap; base += (uint64_t)gridDim.x * tile) {
+        const uint64_t s0 = base + (uint64_t)threadIdx.x * CONV_SLOTS;
+        uint32_t occ_bits = 0, keep_bits = 0;
 #pragma unroll
-                    for (int i = 0; i < NW; ++i) key.w[i] = t.keys[s * NW + i];
-                }
-            }
+        for (int j = 0; j < CONV_SLOTS; ++j) {
+            const uint64_t s = s0 + j;
+            if (s >= cap) break;
+            const bool occ = NW == 1 ? (t.keys[s] != KEY_EMPTY) : (t.tags[s] != 0);
+            occ_bits |= (uint32_t)occ << j;
         }
-        uint32_t e[8];
-        uint32_t mask = 0, cov16 = 0;
-        if (occ) {
+        // mask per occupied slot (needs the counters)
+        uint8_t masks[CONV_SLOTS];
+        uint16_t covs[CONV_SLOTS];
+#pragma unroll
+        for (int j = 0; j < CONV_SLOTS; ++j) {
+            masks[j] = 0;
+            covs[j] = 0;
+            if (!((occ_bits >> j) & 1u)) continue;
+            const uint64_t s = s0 + j;
             const uint4* c4 = reinterpret_cast<const uint4*>(t.cnt + s * 8);
             const uint4 a = c4[0], bq = c4[1];
-            e[0] = a.x; e[1] = a.y; e[2] = a.z; e[3] = a.w;
-            e[4] = bq.x; e[5] = bq.y; e[6] = bq.z; e[7] = bq.w;
-            uint32_t sum = 0;
+            const uint32_t e[8] = {a.x, a.y, a.z, a.w, bq.x, bq.y, bq.z, bq.w};
+            uint32_t sum = 0, m = 0;
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
                 raw_total += e[i];
-                e[i] = e[i] > 0xFFFFu ? 0xFFFFu : e[i];
-                sum += e[i];
-                if (e[i] >= min_trans_cov) mask |= 1u << i;
+                const uint32_t ec = e[i] > 0xFFFFu ? 0xFFFFu : e[i];
+                sum += ec;
+                if (ec >= min_trans_cov) m |= 1u << i;
             }
             if (t.cov) sum = t.cov[s];
-            cov16 = sum > 0xFFFFu ? 0xFFFFu : sum;
+            covs[j] = (uint16_t)(sum > 0xFFFFu ? 0xFFFFu : sum);
+            masks[j] = (uint8_t)m;
+            keep_bits |= (uint32_t)(m != 0) << j;
         }
-        // every accumulated key (optional)
-        const uint32_t occ_bal = __ballot_sync(0xffffffffu, occ);
-        unsigned long long abase = 0;
-        if (lane == 0 && occ_bal) abase = atomicAdd(&o.counts[0], (unsigned long long)__popc(occ_bal));
-        abase = __shfl_sync(0xffffffffu, abase, 0);
-        if (occ && o.acc_keys) {
-            const uint64_t idx = abase + __popc(occ_bal & ((1u << lane) - 1));
-            if (idx < o.cap_acc) {
-#pragma unroll
-                for (int i = 0; i < NW; ++i) o.acc_keys[idx * NW + i] = key.w[i];
-                o.acc_cov[idx] = (uint16_t)cov16;
-#pragma unroll
-                for (int i = 0; i < 8; ++i) o.acc_edges[idx * 8 + i] = (uint16_t)e[i];
-            }
+        n_keys += __popc(occ_bits);
+        uint32_t tot_keep = 0, tot_acc = 0;
+        const uint32_t my_keep = __popc(keep_bits);
+        const uint32_t off_keep = block_excl_scan(my_keep, s_warp, tot_keep);
+        uint32_t off_acc = 0;
+        if (o.acc_keys) off_acc = block_excl_scan(__popc(occ_bits), s_warp, tot_acc);
+        if (threadIdx.x == 0) {
+            s_base[0] = tot_keep ? atomicAdd(&o.counts[1], (unsigned long long)tot_keep) : 0;
+            s_base[1] = (o.acc_keys && tot_acc) ? atomicAdd(&o.counts[4], (unsigned long long)tot_acc) : 0;
         }
-        // SolidKmerNode entries: mask != 0, cov = max(1, cov / 2)
-        const bool keep = occ && mask != 0;
-        const uint32_t kb = __ballot_sync(0xffffffffu, keep);
-        unsigned long long sbase = 0;
-        if (lane == 0 && kb) sbase = atomicAdd(&o.counts[1], (unsigned long long)__popc(kb));
-        sbase = __shfl_sync(0xffffffffu, sbase, 0);
-        if (keep) {
-            uint32_t cv = cov16 / 2;
-            cv = cv < 1 ? 1 : cv;
-            const uint64_t idx = sbase + __popc(kb & ((1u << lane) - 1));
-            if (o.keys && idx < o.cap_solid) {
+        __syncthreads();
+        uint64_t wk = s_base[0] + off_keep, wa = s_base[1] + off_acc;
+        __syncthreads();
+        if (!occ_bits) continue;
 #pragma unroll
-                for (int i = 0; i < NW; ++i) o.keys[idx * NW + i] = key.w[i];
-                o.cov[idx] = (uint16_t)cv;
-                o.mask[idx] = (uint8_t)mask;
+        for (int j = 0; j < CONV_SLOTS; ++j) {
+            if (!((occ_bits >> j) & 1u)) continue;
+            const uint64_t s = s0 + j;
+            Key<NW> key;
+#pragma unroll
+            for (int i = 0; i < NW; ++i) key.w[i] = t.keys[s * NW + i];
+            if (o.acc_keys) {
+                if (wa < o.cap_acc) {
+#pragma unroll
+                    for (int i = 0; i < NW; ++i) o.acc_keys[wa * NW + i] = key.w[i];
+                    o.acc_cov[wa] = covs[j];
+                    const uint4* c4 = reinterpret_cast<const uint4*>(t.cnt + s * 8);
+                    const uint4 a = c4[0], bq = c4[1];
+                    const uint32_t e[8] = {a.x, a.y, a.z, a.w, bq.x, bq.y, bq.z, bq.w};
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) o.acc_edges[wa * 8 + i] = (uint16_t)(e[i] > 0xFFFFu ? 0xFFFFu : e[i]);
+                }
+                wa++;
             }
-            uint64_t kd = 0;
+            if ((keep_bits >> j) & 1u) {
+                uint32_t cv = covs[j] / 2u;
+                cv = cv < 1 ? 1 : cv;
+                if (o.keys && wk < o.cap_solid) {
 #pragma unroll
-            for (int i = 0; i < NW; ++i) kd = smix(kd ^ key.w[i]);
-            digest += smix(kd ^ smix(((uint64_t)cv << 8) | mask));
+                    for (int i = 0; i < NW; ++i) o.keys[wk * NW + i] = key.w[i];
+                    o.cov[wk] = (uint16_t)cv;
+                    o.mask[wk] = masks[j];
+                }
+                wk++;
+                uint64_t kd = 0;
+#pragma unroll
+                for (int i = 0; i < NW; ++i) kd = smix(kd ^ key.w[i]);
+                digest += smix(kd ^ smix(((uint64_t)cv << 8) | masks[j]));
+            }
         }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         digest += __shfl_down_sync(0xffffffffu, digest, off);
         raw_total += __shfl_down_sync(0xffffffffu, raw_total, off);
+        n_keys += __shfl_down_sync(0xffffffffu, n_keys, off);
     }
-    if (lane == 0 && digest) atomicAdd(&o.counts[2], digest);
-    if (lane == 0 && raw_total) atomicAdd(&o.counts[3], raw_total);
+    if ((threadIdx.x & 31) == 0) {
+        if (n_keys) atomicAdd(&o.counts[0], n_keys);
+        if (digest) atomicAdd(&o.counts[2], digest);
+        if (raw_total) atomicAdd(&o.counts[3], raw_total);
+    }
 }
 
 __global__ void k_clamp(uint32_t* cnt, uint64_t n) {

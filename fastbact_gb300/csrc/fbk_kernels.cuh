@@ -51,7 +51,7 @@ struct ConvOut {
     uint64_t* acc_keys;         // optional: every accumulated key
     uint16_t* acc_cov;
     uint16_t* acc_edges;        // 8 per key
-    unsigned long long* counts; // [0] n_keys, [1] n_solid, [2] digest, [3] raw edge total
+    unsigned long long* counts; // [0] n_keys, [1] n_solid, [2] digest, [3] raw edge total, [4] acc rows
     uint64_t cap_solid, cap_acc;
 };
 

@@ -4,7 +4,8 @@
  * Every entry point is `extern "C"`, takes plain pointers and sizes, and returns an
  * fbk_status (0 = FBK_OK).  fbk_last_error() gives the message of the most recent
  * failure on a context.  The caller owns every host buffer; the library owns device
- * objects until their *_release call.  A context is used from one host thread at a
+ * objects until their *_release call.  Every object (bank, sketch, table) must be
+ * released before the context it was created on is destroyed.  A context is used from one host thread at a
  * time; separate contexts are independent.  Each context owns one CUDA stream.
  *
  * Reference interfaces (paths inside the fastBact repository) that each group
