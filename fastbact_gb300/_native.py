@@ -125,6 +125,8 @@ SIGNATURES = {
     "fbk_estimator_defaults": (None, [P(EstimatorParams)]),
     "fbk_estimate_sample": (S, [vp, P(ArenaView), C.c_uint64, P(CountStats), P(EstimatorParams), P(GenomeEstimate), u8p, u8p]),
     "fbk_estimate_bank": (S, [vp, vp, u32p, C.c_uint64, P(CountStats), P(EstimatorParams), P(GenomeEstimate), u8p, u8p]),
+    "fbk_estimate_sample_noalloc": (S, [C.c_int, vp, P(ArenaView), C.c_uint64, P(CountStats), P(EstimatorParams),
+                                        P(GenomeEstimate), u8p, u8p, C.c_char_p, C.c_size_t]),
     "fbk_count_fastx_exact": (S, [C.c_char_p, C.c_char_p, P(CountStats), C.c_char_p, C.c_size_t]),
     "fbk_estimate_genome": (S, [vp, C.c_char_p, C.c_char_p, C.c_uint64, C.c_double, P(GenomeEstimate)]),
     "fbk_compute_dynamic_kmers": (C.c_int, [C.c_uint64, C.c_int64, u64p, C.c_int]),
