@@ -81,6 +81,8 @@ SIGNATURES = {
     "fbk_version": (C.c_char_p, []),
     "fbk_ctx_create": (S, [C.c_int, C.c_uint64, P(vp)]),
     "fbk_ctx_destroy": (S, [vp]),
+    "fbk_ctx_fork": (S, [vp, P(vp)]),
+    "fbk_ctx_pool_free": (S, [vp, u64p, u64p]),
     "fbk_last_error": (S, [vp, C.c_char_p, C.c_size_t]),
     "fbk_ctx_sync": (S, [vp]),
     "fbk_ctx_set_timing": (S, [vp, C.c_int]),
@@ -88,6 +90,8 @@ SIGNATURES = {
     "fbk_ctx_timing_reset": (S, [vp]),
     "fbk_ctx_event_record": (S, [vp, C.c_int]),
     "fbk_ctx_event_elapsed": (S, [vp, C.c_int, C.c_int, P(C.c_double)]),
+    "fbk_ctx_set_tuning": (S, [vp, C.c_char_p, C.c_double]),
+    "fbk_ctx_get_tuning": (S, [vp, C.c_char_p, P(C.c_double)]),
     "fbk_ctx_launch_count": (S, [vp, u64p]),
     "fbk_ctx_mem_info": (S, [vp, u64p, u64p]),
     "fbk_bank_upload": (S, [vp, P(ArenaView), P(vp)]),

@@ -103,6 +103,15 @@ class Context:
     def timing_reset(self):
         check(N.lib().fbk_ctx_timing_reset(self._h), self._h)
 
+    def set_tuning(self, **kw) -> None:
+        for name, v in kw.items():
+            check(N.lib().fbk_ctx_set_tuning(self._h, name.encode(), float(v)), self._h, "set_tuning")
+
+    def get_tuning(self, name: str) -> float:
+        v = C.c_double()
+        check(N.lib().fbk_ctx_get_tuning(self._h, name.encode(), C.byref(v)), self._h, "get_tuning")
+        return v.value
+
     def record(self, slot: int) -> None:
         check(N.lib().fbk_ctx_event_record(self._h, slot), self._h)
 

@@ -95,7 +95,7 @@ uint64_t DevicePool::largest_free() const {
 
 void* dev_alloc(fbk_ctx* ctx, uint64_t bytes) {
     if (bytes == 0) bytes = 256;
-    if (ctx->pool.active()) return ctx->pool.alloc(bytes);
+    if (ctx->pool && ctx->pool->active()) return ctx->pool->alloc(bytes);
     void* p = nullptr;
     if (cudaMalloc(&p, bytes) != cudaSuccess) {
         cudaGetLastError();
@@ -105,7 +105,7 @@ void* dev_alloc(fbk_ctx* ctx, uint64_t bytes) {
 }
 void dev_free(fbk_ctx* ctx, void* p) {
     if (!p) return;
-    if (ctx->pool.active()) ctx->pool.free(p);
+    if (ctx->pool && ctx->pool->active()) ctx->pool->free(p);
     else cudaFree(p);
 }
 
@@ -114,6 +114,12 @@ Launch launch_cfg(fbk_ctx* ctx, int block, int grid) {
     L.block = block;
     L.grid = grid > 0 ? grid : ctx->num_sms * 4;
     L.stream = ctx->stream;
+    L.sms = ctx->num_sms;
+    return L;
+}
+Launch launch_cfg_persistent(fbk_ctx* ctx, int block, int grid) {
+    Launch L = launch_cfg(ctx, block, grid);
+    L.grid = grid;
     return L;
 }
 
@@ -258,7 +264,8 @@ FBK_API fbk_status fbk_ctx_create(int device, uint64_t pool_bytes, fbk_ctx** out
         fbk_ctx_destroy(c);
         return FBK_ERR_CUDA;
     }
-    if (pool_bytes > 0 && !c->pool.init(pool_bytes, c->err)) {
+    c->pool = std::make_shared<DevicePool>();
+    if (pool_bytes > 0 && !c->pool->init(pool_bytes, c->err)) {
         fbk_ctx_destroy(c);
         return FBK_ERR_OOM;
     }
@@ -277,12 +284,58 @@ FBK_API fbk_status fbk_ctx_destroy(fbk_ctx* c) {
     for (auto e : c->free_events) cudaEventDestroy(e);
     for (auto e : c->markers)
         if (e) cudaEventDestroy(e);
-    c->pool.release();
+    c->pool.reset();  // the pool memory goes when its last context does
     if (c->d_status) cudaFree(c->d_status);
     if (c->d_counts) cudaFree(c->d_counts);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_ctx_fork(fbk_ctx* parent, fbk_ctx** out) {
+    if (!parent || !out) return FBK_ERR_INVALID;
+    *out = nullptr;
+    fbk_ctx* c = new fbk_ctx();
+    c->device = parent->device;
+    c->num_sms = parent->num_sms;
+    c->pool = parent->pool;
+    c->sweep_bytes = parent->sweep_bytes;
+    c->bucket_bytes = parent->bucket_bytes;
+    c->stripes = parent->stripes;
+    c->load_factor = parent->load_factor;
+    c->pass2_mode = parent->pass2_mode;
+    c->record_factor = parent->record_factor;
+    c->block_pass1 = parent->block_pass1;
+    c->grid_pass1 = parent->grid_pass1;
+    c->block_pass2 = parent->block_pass2;
+    c->grid_pass2 = parent->grid_pass2;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_status, 64);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_counts, 8 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_pinned, 65536);
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, 64);
+    if (e != cudaSuccess) {
+        fbk_ctx_destroy(c);
+        return cuda_err(parent, e, "fbk_ctx_fork");
+    }
+    *out = c;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_ctx_pool_free(const fbk_ctx* ctx, uint64_t* free_bytes, uint64_t* largest_block) {
+    if (!ctx || !free_bytes) return FBK_ERR_INVALID;
+    if (ctx->pool && ctx->pool->active()) {
+        *free_bytes = ctx->pool->free_bytes();
+        if (largest_block) *largest_block = ctx->pool->largest_free();
+    } else {
+        size_t f = 0, t = 0;
+        cudaSetDevice(ctx->device);
+        cudaMemGetInfo(&f, &t);
+        *free_bytes = f;
+        if (largest_block) *largest_block = f;
+    }
     return FBK_OK;
 }
 
@@ -343,6 +396,41 @@ FBK_API fbk_status fbk_ctx_event_elapsed(fbk_ctx* ctx, int a, int b, double* ms)
     return FBK_OK;
 }
 
+FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) {
+    if (!ctx || !name) return FBK_ERR_INVALID;
+    const std::string n(name);
+    if (n == "sweep_bytes" && v >= 4096) ctx->sweep_bytes = (uint64_t)v;
+    else if (n == "bucket_bytes" && v >= 4096) ctx->bucket_bytes = (uint64_t)v;
+    else if (n == "stripes" && v >= 1 && v <= 256) ctx->stripes = (uint32_t)v;
+    else if (n == "load_factor" && v >= 0.1 && v <= 0.9) ctx->load_factor = v;
+    else if (n == "pass2_mode" && (v == 0 || v == 1)) ctx->pass2_mode = (int)v;
+    else if (n == "record_factor" && v > 0 && v <= 16) ctx->record_factor = v;
+    // the pass kernels are compiled for blocks of at most 256 threads
+    else if (n == "block_pass1" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_pass1 = (int)v;
+    else if (n == "grid_pass1" && v >= 0) ctx->grid_pass1 = (int)v;
+    else if (n == "block_pass2" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_pass2 = (int)v;
+    else if (n == "grid_pass2" && v >= 0) ctx->grid_pass2 = (int)v;
+    else return set_err(ctx, FBK_ERR_INVALID, "unknown tuning name or value out of range: " + n);
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, double* v) {
+    if (!ctx || !name || !v) return FBK_ERR_INVALID;
+    const std::string n(name);
+    if (n == "sweep_bytes") *v = (double)ctx->sweep_bytes;
+    else if (n == "bucket_bytes") *v = (double)ctx->bucket_bytes;
+    else if (n == "stripes") *v = ctx->stripes;
+    else if (n == "load_factor") *v = ctx->load_factor;
+    else if (n == "pass2_mode") *v = ctx->pass2_mode;
+    else if (n == "record_factor") *v = ctx->record_factor;
+    else if (n == "block_pass1") *v = ctx->block_pass1;
+    else if (n == "grid_pass1") *v = ctx->grid_pass1;
+    else if (n == "block_pass2") *v = ctx->block_pass2;
+    else if (n == "grid_pass2") *v = ctx->grid_pass2;
+    else return FBK_ERR_INVALID;
+    return FBK_OK;
+}
+
 FBK_API fbk_status fbk_ctx_launch_count(const fbk_ctx* ctx, uint64_t* n) {
     if (!ctx || !n) return FBK_ERR_INVALID;
     *n = ctx->launches;
@@ -351,8 +439,8 @@ FBK_API fbk_status fbk_ctx_launch_count(const fbk_ctx* ctx, uint64_t* n) {
 
 FBK_API fbk_status fbk_ctx_mem_info(const fbk_ctx* ctx, uint64_t* used, uint64_t* size) {
     if (!ctx || !used || !size) return FBK_ERR_INVALID;
-    *used = ctx->pool.used();
-    *size = ctx->pool.size();
+    *used = ctx->pool ? ctx->pool->used() : 0;
+    *size = ctx->pool ? ctx->pool->size() : 0;
     return FBK_OK;
 }
 
@@ -363,7 +451,7 @@ FBK_API fbk_status fbk_ctx_mem_info(const fbk_ctx* ctx, uint64_t* used, uint64_t
 // ===========================================================================
 namespace fbk {
 
-fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_arenas, fbk_bank** out) {
+fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_arenas, fbk_bank** out, uint64_t chunk_bases) {
     uint64_t n_words = 0, n_reads = 0, n_bases = 0;
     bool all_pairs = true;
     uint32_t max_len = 0;
@@ -427,19 +515,30 @@ fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_ar
         fbk_bank_release(b);
         return cuda_err(ctx, e, "bank padding");
     }
-    // Read ranges whose total length stays below 2^31 bases: within one range no
-    // 32-bit edge counter can exceed 2^32 (see k_convert).
+    // Read ranges with fewer than chunk_bases bases: one launch over a range adds
+    // at most (bases x weight) to any 32-bit counter, which the callers keep below
+    // 2^32 - 2^17 (counters start each launch at <= 65535).
     b->chunk_starts.push_back(0);
     uint64_t acc = 0, r = 0;
     for (int a = 0; a < n_arenas; ++a)
         for (uint64_t i = 0; i < arenas[a].n_seqs; ++i, ++r) {
-            if (acc + arenas[a].lengths[i] >= (1ULL << 31)) {
+            if (acc && acc + arenas[a].lengths[i] >= chunk_bases) {
                 b->chunk_starts.push_back(r);
+                b->max_chunk = std::max(b->max_chunk, acc);
                 acc = 0;
             }
             acc += arenas[a].lengths[i];
         }
+    b->max_chunk = std::max(b->max_chunk, acc);
     b->chunk_starts.push_back(n_reads);
+    const uint64_t bins = std::min<uint64_t>((uint64_t)max_len + 2, 1ULL << 16);
+    b->len_hist.assign(bins, 0);
+    for (int a = 0; a < n_arenas; ++a)
+        for (uint64_t i = 0; i < arenas[a].n_seqs; ++i) {
+            const uint64_t L = arenas[a].lengths[i];
+            if (L < bins - 1) b->len_hist[L]++;
+            else b->long_bases += L;
+        }
     *out = b;
     return FBK_OK;
 }
@@ -483,24 +582,23 @@ FBK_API uint64_t fbk_cms_width_for_genome_size(uint64_t g) {
 }
 
 FBK_API fbk_status fbk_cms_create(fbk_ctx* ctx, uint32_t log2w, uint32_t cbits, fbk_cms** out) {
-    if (!ctx || !out || (cbits != 4 && cbits != 16) || log2w < 3 || log2w > 31)
-        return set_err(ctx, FBK_ERR_INVALID, "cms: counter_bits must be 4 or 16 and 3 <= log2_width <= 31");
+    if (!ctx || !out || (cbits != 4 && cbits != 16) || log2w < 3 || log2w > 30)
+        return set_err(ctx, FBK_ERR_INVALID, "cms: counter_bits must be 4 or 16 and 3 <= log2_width <= 30");
     CK(ctx, cudaSetDevice(ctx->device));
     fbk_cms* c = new fbk_cms();
     c->ctx = ctx;
     c->log2w = log2w;
     c->cbits = cbits;
-    const uint64_t w = 1ULL << log2w;
-    c->n_words = cbits == 4 ? (4 * w) / 8 : (4 * w) / 2;
-    c->words = (uint32_t*)dev_alloc(ctx, c->n_words * 4);
+    c->n = 4ULL << log2w;
+    c->cnt = (uint32_t*)dev_alloc(ctx, c->n * 4);
     c->hll12 = (uint32_t*)dev_alloc(ctx, 4096 * 4);
-    if (!c->words || !c->hll12) {
-        dev_free(ctx, c->words);
+    if (!c->cnt || !c->hll12) {
+        dev_free(ctx, c->cnt);
         dev_free(ctx, c->hll12);
         delete c;
         return set_err(ctx, FBK_ERR_OOM, "device memory for the count-min sketch");
     }
-    CK(ctx, cudaMemsetAsync(c->words, 0, c->n_words * 4, ctx->stream));
+    CK(ctx, cudaMemsetAsync(c->cnt, 0, c->n * 4, ctx->stream));
     CK(ctx, cudaMemsetAsync(c->hll12, 0, 4096 * 4, ctx->stream));
     *out = c;
     return FBK_OK;
@@ -508,8 +606,15 @@ FBK_API fbk_status fbk_cms_create(fbk_ctx* ctx, uint32_t log2w, uint32_t cbits, 
 
 FBK_API fbk_status fbk_cms_clear(fbk_cms* c) {
     if (!c) return FBK_ERR_INVALID;
-    CK(c->ctx, cudaMemsetAsync(c->words, 0, c->n_words * 4, c->ctx->stream));
+    CK(c->ctx, cudaMemsetAsync(c->cnt, 0, c->n * 4, c->ctx->stream));
     CK(c->ctx, cudaMemsetAsync(c->hll12, 0, 4096 * 4, c->ctx->stream));
+    return FBK_OK;
+}
+
+// Keeps every count <= 65535 between calls (exact below every cap).
+static fbk_status cms_clamp(fbk_cms* c) {
+    fbk_ctx* ctx = c->ctx;
+    TIMED(ctx, "cms_clamp", launch_clamp_counters(launch_cfg(ctx, 256, 0), c->cnt, c->n));
     return FBK_OK;
 }
 
@@ -517,24 +622,30 @@ static fbk_status cms_keys_op(fbk_cms* c, const uint64_t* keys, uint64_t n, uint
     if (!c || (n && !keys) || (!add && n && !est)) return FBK_ERR_INVALID;
     if (n == 0) return FBK_OK;
     fbk_ctx* ctx = c->ctx;
-    uint64_t* dk = (uint64_t*)dev_alloc(ctx, n * 8);
-    uint32_t* de = add ? nullptr : (uint32_t*)dev_alloc(ctx, n * 4);
+    const uint64_t chunk = 1ULL << 30;  // adds per launch stay far below 2^32 - 2^17
+    uint64_t* dk = (uint64_t*)dev_alloc(ctx, std::min(n, chunk) * 8);
+    uint32_t* de = add ? nullptr : (uint32_t*)dev_alloc(ctx, std::min(n, chunk) * 4);
     if (!dk || (!add && !de)) {
         dev_free(ctx, dk);
         dev_free(ctx, de);
         return set_err(ctx, FBK_ERR_OOM, "cms key buffer");
     }
-    cudaError_t e = cudaMemcpyAsync(dk, keys, n * 8, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) {
-        TimedLaunch tl;
-        time_begin(ctx, add ? "cms_add_keys" : "cms_estimate_keys", tl);
-        // Sequential-add semantics only matter through the final counters, which are
-        // order independent; a single launch is therefore exact.
-        e = launch_cms_keys((int)c->cbits, launch_cfg(ctx, 256, 0), c->words, c->log2w, dk, n, de, add);
-        time_end(ctx, tl);
+    cudaError_t e = cudaSuccess;
+    for (uint64_t s0 = 0; s0 < n && e == cudaSuccess; s0 += chunk) {
+        const uint64_t m = std::min(chunk, n - s0);
+        e = cudaMemcpyAsync(dk, keys + s0, m * 8, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) {
+            TimedLaunch tl;
+            time_begin(ctx, add ? "cms_add_keys" : "cms_estimate_keys", tl);
+            // The final counts of a batch of adds do not depend on their order, so one
+            // launch reproduces the sequential adds exactly.
+            e = launch_cms_keys(launch_cfg(ctx, 256, 0), c->cnt, c->log2w, c->cap(), dk, m, de, add);
+            time_end(ctx, tl);
+        }
+        if (e == cudaSuccess && add) e = launch_clamp_counters(launch_cfg(ctx, 256, 0), c->cnt, c->n);
+        if (e == cudaSuccess && !add) e = cudaMemcpyAsync(est + s0, de, m * 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     }
-    if (e == cudaSuccess && !add) e = cudaMemcpyAsync(est, de, n * 4, cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     dev_free(ctx, dk);
     dev_free(ctx, de);
     if (e != cudaSuccess) return cuda_err(ctx, e, "cms key op");
@@ -563,14 +674,42 @@ static fbk_status make_keep_bits(fbk_ctx* ctx, const fbk_bank* b, const fbk_subs
     return FBK_OK;
 }
 
+// Sweep plan: each sweep touches at most ctx->sweep_bytes of the sketch — several
+// whole rows when they fit, else a column range of one row.  Fewer sweeps mean fewer
+// scans of the bank; smaller slices stay resident in L2.
+struct SweepPlan {
+    uint32_t rows_per;   // rows per sweep (1, 2 or 4)
+    uint64_t cols_per;   // columns per sweep (all when rows_per > 1)
+};
+static SweepPlan sweep_plan(const fbk_ctx* ctx, uint32_t log2w) {
+    const uint64_t w = 1ULL << log2w, row_bytes = w * 4;
+    SweepPlan sp;
+    if (ctx->sweep_bytes >= 4 * row_bytes) sp = {4, w};
+    else if (ctx->sweep_bytes >= 2 * row_bytes) sp = {2, w};
+    else sp = {1, std::min(w, std::max<uint64_t>(1024, ctx->sweep_bytes / 4))};
+    return sp;
+}
+
 static fbk_status pass1_impl(fbk_cms* c, const fbk_bank* b, uint32_t k, uint32_t key_bits, const uint64_t* keep_bits,
                              uint32_t mult) {
     fbk_ctx* ctx = c->ctx;
     const int nw = nw_of(key_bits);
     if (!nw || k < 1 || k > max_k_of(key_bits)) return set_err(ctx, FBK_ERR_INVALID, "k out of range for key_bits");
-    Launch L = launch_cfg(ctx, ctx->block_pass1, ctx->grid_pass1);
-    TIMED(ctx, "pass1", launch_pass1(nw, (int)c->cbits, L, bank_view(b, 0, b->n_reads, keep_bits), k, c->words, c->log2w,
-                                     mult, c->hll12));
+    if ((uint64_t)mult * b->max_chunk_bases() >= (1ULL << 32) - (1ULL << 17))
+        return set_err(ctx, FBK_ERR_INVALID, "pass 1: read chunk too large for this weight");
+    Launch L = launch_cfg_persistent(ctx, ctx->block_pass1, ctx->grid_pass1);
+    const uint64_t w = 1ULL << c->log2w;
+    const SweepPlan sp = sweep_plan(ctx, c->log2w);
+    for (size_t ch = 0; ch + 1 < b->chunk_starts.size(); ++ch) {
+        const BankDev bv = bank_view(b, b->chunk_starts[ch], b->chunk_starts[ch + 1], keep_bits);
+        for (uint32_t row = 0; row < 4; row += sp.rows_per)
+            for (uint64_t c0 = 0; c0 < w; c0 += sp.cols_per)
+                TIMED(ctx, "pass1", launch_pass1_sweep(nw, L, bv, k, c->cnt, c->log2w, row, row + sp.rows_per, c0,
+                                                       std::min(w, c0 + sp.cols_per), mult,
+                                                       (row == 0 && c0 == 0) ? c->hll12 : nullptr));
+        fbk_status st = cms_clamp(c);
+        if (st) return st;
+    }
     return FBK_OK;
 }
 
@@ -606,6 +745,10 @@ FBK_API fbk_status fbk_cms_add_bank(fbk_cms* c, const fbk_bank* b, uint32_t k, u
     return st;
 }
 
+// Prior contigs are counted with weights up to 1000 per push, so their bank is cut
+// into ranges of fewer than 4M bases (1000 x 4M < 2^32 - 2^17).
+static const uint64_t CONTIG_CHUNK_BASES = 4000000;
+
 // Packs ASCII contigs into a one-arena device bank (ASCII_TO_2BIT, bitseq.rs:67-81).
 static fbk_status contig_bank(fbk_ctx* ctx, const uint8_t* ascii, const uint64_t* offs, uint64_t n, fbk_bank** out) {
     std::vector<uint64_t> words, o(n);
@@ -613,7 +756,7 @@ static fbk_status contig_bank(fbk_ctx* ctx, const uint8_t* ascii, const uint64_t
     uint64_t pos = 0;
     for (uint64_t i = 0; i < n; ++i) {
         uint64_t len = offs[i + 1] - offs[i];
-        if (len > 0xFFFFFFFFULL) return set_err(ctx, FBK_ERR_INVALID, "contig longer than 2^32-1 bases");
+        if (len >= CONTIG_CHUNK_BASES) return set_err(ctx, FBK_ERR_INVALID, "contig of 4M bases or more");
         o[i] = pos;
         l[i] = (uint32_t)len;
         words.resize((pos + len + 31) / 32 + 1, 0);
@@ -630,7 +773,7 @@ static fbk_status contig_bank(fbk_ctx* ctx, const uint8_t* ascii, const uint64_t
     v.lengths = l.data();
     v.n_seqs = n;
     v.pair_idx = nullptr;
-    fbk_status st = bank_upload_impl(ctx, &v, 1, out);
+    fbk_status st = bank_upload_impl(ctx, &v, 1, out, CONTIG_CHUNK_BASES);
     if (st == FBK_OK) cudaStreamSynchronize(ctx->stream);  // host vectors go out of scope
     return st;
 }
@@ -650,14 +793,27 @@ FBK_API fbk_status fbk_cms_add_contigs(fbk_cms* c, const uint8_t* ascii, const u
 
 FBK_API fbk_status fbk_cms_nbytes(const fbk_cms* c, uint64_t* nbytes) {
     if (!c || !nbytes) return FBK_ERR_INVALID;
-    *nbytes = c->n_words * 4;
+    *nbytes = c->cbits == 4 ? c->n / 2 : c->n * 2;
     return FBK_OK;
 }
 
 FBK_API fbk_status fbk_cms_export(fbk_cms* c, uint8_t* out, uint64_t nbytes) {
-    if (!c || !out || nbytes != c->n_words * 4) return FBK_ERR_INVALID;
-    CK(c->ctx, cudaMemcpyAsync(out, c->words, nbytes, cudaMemcpyDeviceToHost, c->ctx->stream));
-    CK(c->ctx, cudaStreamSynchronize(c->ctx->stream));
+    uint64_t want = 0;
+    if (!c || !out || fbk_cms_nbytes(c, &want) != FBK_OK || nbytes != want) return FBK_ERR_INVALID;
+    fbk_ctx* ctx = c->ctx;
+    uint8_t* d = (uint8_t*)dev_alloc(ctx, nbytes);
+    if (!d) return set_err(ctx, FBK_ERR_OOM, "cms export buffer");
+    cudaError_t e;
+    {
+        TimedLaunch tl;
+        time_begin(ctx, "cms_export", tl);
+        e = launch_cms_export((int)c->cbits, launch_cfg(ctx, 256, 0), c->cnt, c->n, d);
+        time_end(ctx, tl);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, nbytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, d);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cms export");
     return FBK_OK;
 }
 
@@ -665,14 +821,14 @@ FBK_API fbk_status fbk_cms_merge(fbk_cms* dst, const fbk_cms* src) {
     if (!dst || !src || dst->cbits != src->cbits || dst->log2w != src->log2w) return FBK_ERR_INVALID;
     fbk_ctx* ctx = dst->ctx;
     if (src->ctx != ctx) CK(ctx, cudaStreamSynchronize(src->ctx->stream));
-    TIMED(ctx, "cms_merge", launch_cms_merge((int)dst->cbits, launch_cfg(ctx, 256, 0), dst->words, src->words, dst->n_words));
+    TIMED(ctx, "cms_merge", launch_cms_merge(launch_cfg(ctx, 256, 0), dst->cnt, src->cnt, dst->n));
     return FBK_OK;
 }
 
 FBK_API fbk_status fbk_cms_release(fbk_cms* c) {
     if (!c) return FBK_OK;
     cudaStreamSynchronize(c->ctx->stream);
-    dev_free(c->ctx, c->words);
+    dev_free(c->ctx, c->cnt);
     dev_free(c->ctx, c->hll12);
     delete c;
     return FBK_OK;
@@ -789,7 +945,7 @@ static TableDev table_dev(const fbk_table* t) {
     d.tags = t->tags;
     d.cnt = t->cnt;
     d.cov = t->cov;
-    d.mask = t->cap - 1;
+    d.cap = t->cap;
     d.max_probe = (uint32_t)std::min<uint64_t>(t->cap, 1u << 16);
     d.spin_limit = 1u << 20;
     return d;
@@ -799,10 +955,10 @@ static fbk_status table_alloc(fbk_table* t, uint64_t cap, bool with_cov) {
     fbk_ctx* ctx = t->ctx;
     t->cap = cap;
     t->keys = (uint64_t*)dev_alloc(ctx, cap * 8 * t->nw);
-    if (t->nw > 1) t->tags = (uint64_t*)dev_alloc(ctx, cap * 8);
+    if (t->nw > 2) t->tags = (uint64_t*)dev_alloc(ctx, cap * 8);
     t->cnt = (uint32_t*)dev_alloc(ctx, cap * 32);
     if (with_cov) t->cov = (uint32_t*)dev_alloc(ctx, cap * 4);
-    if (!t->keys || (t->nw > 1 && !t->tags) || !t->cnt || (with_cov && !t->cov)) {
+    if (!t->keys || (t->nw > 2 && !t->tags) || !t->cnt || (with_cov && !t->cov)) {
         table_free_storage(t);
         return set_err(ctx, FBK_ERR_OOM, "device memory for the solid table (capacity " + std::to_string(cap) + ")");
     }
@@ -856,29 +1012,107 @@ static uint64_t next_pow2(uint64_t x) {
     return t;
 }
 
-// Pass 2 over every chunk of the read bank (and the prior contigs), with retries
-// at twice the capacity when the probe limit is hit.
+// Solidity bitmap of a bank (bit = first base of a window, 1 = passes the CMS gate):
+// starts all ones, one sweep per row slice clears the failing windows.
+static fbk_status solidity_bitmap(fbk_ctx* ctx, const fbk_bank* b, const fbk_cms* cms, const fbk_build_params* p, int nw,
+                                  const uint64_t* keep_bits, uint32_t** bm_out) {
+    const uint64_t n_bm = b->n_words + 9;
+    uint32_t* bm = (uint32_t*)dev_alloc(ctx, n_bm * 4);
+    if (!bm) return set_err(ctx, FBK_ERR_OOM, "solidity bitmap");
+    *bm_out = bm;
+    CK(ctx, cudaMemsetAsync(bm, 0xFF, n_bm * 4, ctx->stream));
+    Launch L = launch_cfg_persistent(ctx, ctx->block_pass2, ctx->grid_pass2);
+    const uint64_t w = 1ULL << cms->log2w;
+    const SweepPlan sp = sweep_plan(ctx, cms->log2w);
+    const BankDev bv = bank_view(b, 0, b->n_reads, keep_bits);
+    for (uint32_t row = 0; row < 4; row += sp.rows_per)
+        for (uint64_t c0 = 0; c0 < w; c0 += sp.cols_per)
+            TIMED(ctx, "solid", launch_solid_sweep(nw, L, bv, p->k, cms->cnt, cms->log2w, row, row + sp.rows_per, c0,
+                                                   std::min(w, c0 + sp.cols_per), p->t_solid, cms->cap(), bm));
+    return FBK_OK;
+}
+
+// Record buckets of pass 2: bucket b covers home slots [b << shift, (b+1) << shift),
+// a table range of about ctx->bucket_bytes, so a bucket's upserts stay in L2.
+struct Buckets {
+    fbk_ctx* ctx = nullptr;
+    BucketDev d{};
+    uint32_t* overflow = nullptr;
+    ~Buckets() {
+        if (!ctx) return;
+        cudaStreamSynchronize(ctx->stream);
+        dev_free(ctx, d.recs);
+        dev_free(ctx, d.fill);
+        dev_free(ctx, overflow);
+    }
+};
+
+static fbk_status buckets_alloc(fbk_ctx* ctx, uint64_t cap, uint64_t slot_bytes, int nw, uint64_t max_records, Buckets& bk) {
+    // at most 64 buckets (the emit kernel's per-warp staging holds 64 counters)
+    uint32_t shift = 0;
+    while (shift < 40 && (2ULL << shift) * slot_bytes <= ctx->bucket_bytes) ++shift;
+    while (((cap + (1ULL << shift) - 1) >> shift) > 64) ++shift;
+    const uint32_t P = (uint32_t)((cap + (1ULL << shift) - 1) >> shift);
+    const uint32_t S = std::max<uint32_t>(1, std::min<uint32_t>(256, ctx->stripes));
+    const uint64_t per_stripe = (uint64_t)(ctx->record_factor * (double)max_records / ((double)P * S)) +
+                                (ctx->record_factor >= 1.0 ? 4096 : 0);
+    bk.ctx = ctx;
+    bk.d.shift = shift;
+    bk.d.n_buckets = P;
+    bk.d.stripes = S;
+    bk.d.stripe_cap = per_stripe;
+    bk.d.recs = (uint64_t*)dev_alloc(ctx, (uint64_t)P * S * per_stripe * 8 * (nw + 1));
+    bk.d.fill = (unsigned long long*)dev_alloc(ctx, (uint64_t)P * S * 8);
+    bk.overflow = (uint32_t*)dev_alloc(ctx, 256);
+    bk.d.overflow = bk.overflow;
+    if (!bk.d.recs || !bk.d.fill || !bk.overflow) return set_err(ctx, FBK_ERR_OOM, "pass-2 record buckets");
+    CK(ctx, cudaMemsetAsync(bk.overflow, 0, 4, ctx->stream));
+    return FBK_OK;
+}
+
+// Pass 2 for every read chunk (and the prior contigs), with retries at twice the
+// capacity when the probe limit is hit.  Reads go through record buckets; if a
+// bucket stripe overflows, the chunk is redone by the direct sweep.
 static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cms* cms, const fbk_build_params* p,
                                    const uint64_t* keep_bits, const fbk_bank* contigs, uint64_t distinct_hint,
                                    fbk_table** out) {
     const int nw = nw_of(p->key_bits);
     if (!nw || p->k < 1 || p->k > max_k_of(p->key_bits)) return set_err(ctx, FBK_ERR_INVALID, "k out of range for key_bits");
     if (p->t_solid > 0xFFFF || p->min_trans_cov > 0xFFFF) return set_err(ctx, FBK_ERR_INVALID, "thresholds must fit u16");
+    if (2 * b->max_chunk_bases() >= (1ULL << 32) - (1ULL << 17))
+        return set_err(ctx, FBK_ERR_INVALID, "pass 2: read chunk too large");
     uint64_t cap;
     if (p->table_log2_cap) {
         if (p->table_log2_cap < 10 || p->table_log2_cap > 34) return set_err(ctx, FBK_ERR_INVALID, "table_log2_cap out of range");
         cap = 1ULL << p->table_log2_cap;
     } else {
-        cap = next_pow2(std::max<uint64_t>(1024, (uint64_t)(2.2 * (double)distinct_hint) + 1024));
+        cap = std::max<uint64_t>(1024, (uint64_t)((double)distinct_hint / ctx->load_factor) + 1024);
     }
+    uint32_t* bm = nullptr;
+    fbk_status st = solidity_bitmap(ctx, b, cms, p, nw, keep_bits, &bm);
+    if (st) {
+        dev_free(ctx, bm);
+        return st;
+    }
+    struct BmGuard {
+        fbk_ctx* c;
+        uint32_t* p;
+        ~BmGuard() {
+            cudaStreamSynchronize(c->stream);
+            dev_free(c, p);
+        }
+    } bmg{ctx, bm};
     fbk_table* t = new fbk_table();
     t->ctx = ctx;
     t->nw = (uint32_t)nw;
     t->k = p->k;
     t->min_trans_cov = p->min_trans_cov;
+    const uint64_t slot_bytes = 8ULL * nw + (nw > 2 ? 8 : 0) + 32 + (contigs ? 4 : 0);
+    const uint64_t max_records = std::min(b->windows(p->k, p->k + 1), b->max_chunk_bases());
     for (int attempt = 0; attempt < 4; ++attempt) {
-        fbk_status st = table_alloc(t, cap, contigs != nullptr);
+        st = table_alloc(t, cap, contigs != nullptr);
         if (st) {
+            table_free_out(t);
             delete t;
             return st;
         }
@@ -894,24 +1128,63 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
         }
         CK(ctx, cudaMemsetAsync(ctx->d_status, 0, 4, ctx->stream));
         TableDev td = table_dev(t);
-        Launch L = launch_cfg(ctx, ctx->block_pass2, ctx->grid_pass2);
+        Launch L = launch_cfg_persistent(ctx, ctx->block_pass2, ctx->grid_pass2);
         Launch Lc = launch_cfg(ctx, 256, 0);
-        for (size_t c = 0; c + 1 < b->chunk_starts.size(); ++c) {
-            if (c > 0) TIMED(ctx, "clamp", launch_clamp_counters(Lc, t->cnt, cap * 8));
-            if (c > 0 && t->cov) TIMED(ctx, "clamp", launch_clamp_counters(Lc, t->cov, cap));
-            TIMED(ctx, "pass2",
-                  launch_pass2(nw, (int)cms->cbits, L, bank_view(b, b->chunk_starts[c], b->chunk_starts[c + 1], keep_bits), p->k,
-                               cms->words, cms->log2w, p->t_solid, 1, 1, 1, td, ctx->d_status));
+        auto clamp = [&]() -> cudaError_t {
+            cudaError_t e = launch_clamp_counters(Lc, t->cnt, cap * 8);
+            if (e == cudaSuccess && t->cov) e = launch_clamp_counters(Lc, t->cov, cap);
+            return e;
+        };
+        Buckets bk;
+        const bool use_buckets = max_records && ctx->pass2_mode == 1;
+        st = use_buckets ? buckets_alloc(ctx, cap, slot_bytes, nw, max_records, bk) : FBK_OK;
+        if (st) {
+            table_free_storage(t);
+            table_free_out(t);
+            delete t;
+            return st;
+        }
+        bool first_launch = true;
+        for (size_t c = 0; c + 1 < b->chunk_starts.size() && use_buckets; ++c) {
+            if (!first_launch) TIMED(ctx, "clamp", clamp());
+            first_launch = false;
+            const BankDev bv = bank_view(b, b->chunk_starts[c], b->chunk_starts[c + 1], keep_bits);
+            CK(ctx, cudaMemsetAsync(bk.d.fill, 0, (uint64_t)bk.d.n_buckets * bk.d.stripes * 8, ctx->stream));
+            TIMED(ctx, "pass2_emit", launch_emit(nw, L, bv, p->k, bm, 1, td, bk.d));
+            for (uint32_t bu = 0; bu < bk.d.n_buckets; ++bu)
+                TIMED(ctx, "pass2_upsert", launch_upsert(nw, L, bk.d, bu, 1, 1, td, ctx->d_status));
+        }
+        uint32_t ovf = use_buckets ? 0 : 1;  // without buckets every chunk takes the direct sweep
+        if (use_buckets) {
+            CK(ctx, cudaMemcpyAsync(ctx->h_pinned, bk.overflow, 4, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(ctx, cudaStreamSynchronize(ctx->stream));
+            ovf = *(uint32_t*)ctx->h_pinned;
+        }
+        if (ovf && max_records) {
+            if (use_buckets) {
+                // A stripe ran out of room: recount every chunk with the direct sweep.
+                table_free_storage(t);
+                st = table_alloc(t, cap, contigs != nullptr);
+                if (st) {
+                    table_free_out(t);
+                    delete t;
+                    return st;
+                }
+                td = table_dev(t);
+            }
+            for (size_t c = 0; c + 1 < b->chunk_starts.size(); ++c) {
+                if (c > 0) TIMED(ctx, "clamp", clamp());
+                TIMED(ctx, "pass2_direct", launch_pass2_sweep(nw, L, bank_view(b, b->chunk_starts[c], b->chunk_starts[c + 1], keep_bits),
+                                                              p->k, bm, 1, 0, cap, 1, 1, td, ctx->d_status));
+            }
         }
         if (contigs) {
-            // +1000 per edge push and +100 cov (build.rs:203-240); 4096-contig launches
-            // keep every 32-bit counter below 2^32 before the next clamp.
-            for (uint64_t r0 = 0; r0 < contigs->n_reads; r0 += 4096) {
-                TIMED(ctx, "clamp", launch_clamp_counters(Lc, t->cnt, cap * 8));
-                TIMED(ctx, "clamp", launch_clamp_counters(Lc, t->cov, cap));
+            // +1000 per edge push and +100 cov (build.rs:203-240)
+            for (size_t c = 0; c + 1 < contigs->chunk_starts.size(); ++c) {
+                TIMED(ctx, "clamp", clamp());
                 TIMED(ctx, "pass2_contigs",
-                      launch_pass2(nw, (int)cms->cbits, L, bank_view(contigs, r0, std::min(contigs->n_reads, r0 + 4096), nullptr),
-                                   p->k, cms->words, cms->log2w, p->t_solid, 0, 1000, 100, td, ctx->d_status));
+                      launch_pass2_sweep(nw, L, bank_view(contigs, contigs->chunk_starts[c], contigs->chunk_starts[c + 1], nullptr),
+                                         p->k, nullptr, 0, 0, cap, 1000, 100, td, ctx->d_status));
             }
         }
         uint32_t bits = 0;

@@ -127,85 +127,10 @@ __device__ __forceinline__ void window_canonical(const uint64_t* __restrict__ d,
     can = is_rc ? rc : fwd;
 }
 
-// ---------------------------------------------------------------------------
-// Count-Min Sketch counters.  Nibble mode keeps the reference byte layout
-// (sketch.rs:131-157: counter c = r*w+col lives in byte c>>1, high nibble when c is
-// odd), viewed as little-endian 32-bit words: nibble c sits at bit 4*(c&7) of word
-// c>>3.  u16 mode: counter c is the half-word c&1 of word c>>1.
-// Saturating increments use a CAS loop that first skips saturated counters, the
-// device form of sketch.rs:199-221.  The loop is bounded: every failed CAS means
-// another increment of the same 32-bit word succeeded, and a word holds at most
-// 8*15 (nibble) or 2*65535 (u16) increments.
-// ---------------------------------------------------------------------------
-template <int CB>
-__device__ __forceinline__ void cms_counter_addr(uint64_t c, uint32_t*& word, uint32_t& shift);
-template <>
-__device__ __forceinline__ void cms_counter_addr<4>(uint64_t c, uint32_t*& word, uint32_t& shift) {
-    word += c >> 3;
-    shift = (uint32_t)(c & 7) << 2;
-}
-template <>
-__device__ __forceinline__ void cms_counter_addr<16>(uint64_t c, uint32_t*& word, uint32_t& shift) {
-    word += c >> 1;
-    shift = (uint32_t)(c & 1) << 4;
-}
-template <int CB>
-__device__ __forceinline__ uint32_t cms_cap() { return CB == 4 ? 15u : 0xFFFFu; }
-
-// Adds `n` (>= 1) to one counter, saturating at the cap.
-template <int CB>
-__device__ __forceinline__ void cms_sat_add(uint32_t* base, uint64_t c, uint32_t n) {
-    uint32_t* p = base;
-    uint32_t sh;
-    cms_counter_addr<CB>(c, p, sh);
-    const uint32_t cap = cms_cap<CB>();
-    uint32_t cur = *(volatile uint32_t*)p;
-    for (;;) {
-        const uint32_t v = (cur >> sh) & cap;
-        if (v >= cap) return;
-        const uint32_t nv = (v + n > cap) ? cap : v + n;
-        const uint32_t want = (cur & ~(cap << sh)) | (nv << sh);
-        const uint32_t old = atomicCAS(p, cur, want);
-        if (old == cur) return;
-        cur = old;
-    }
-}
-
-template <int CB>
-__device__ __forceinline__ uint32_t cms_read(const uint32_t* base, uint64_t c) {
-    uint32_t* p = const_cast<uint32_t*>(base);
-    uint32_t sh;
-    cms_counter_addr<CB>(c, p, sh);
-    return (*p >> sh) & cms_cap<CB>();
-}
-
-// Counter index of row r for key (sketch.rs:193-195).
+// Counter index of row r for key in a 4 x 2^log2w Count-Min Sketch (sketch.rs:193-195).
 __device__ __forceinline__ uint64_t cms_index(uint64_t key, int r, uint32_t log2w) {
     const uint64_t col = smix(key ^ cms_seed(r)) & ((1ULL << log2w) - 1);
     return ((uint64_t)r << log2w) + col;
-}
-
-// CountMinSketch::add (sketch.rs:191-223)
-template <int CB>
-__device__ __forceinline__ void cms_add(uint32_t* t, uint64_t key, uint32_t log2w) {
-    uint64_t c[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) c[r] = cms_index(key, r, log2w);
-#pragma unroll
-    for (int r = 0; r < 4; ++r) cms_sat_add<CB>(t, c[r], 1);
-}
-
-// CountMinSketch::estimate (sketch.rs:227-246).  The reference returns early at 0;
-// reading all four rows gives the same minimum.
-template <int CB>
-__device__ __forceinline__ uint32_t cms_estimate(const uint32_t* t, uint64_t key, uint32_t log2w) {
-    uint32_t v[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) v[r] = cms_read<CB>(t, cms_index(key, r, log2w));
-    uint32_t m = cms_cap<CB>();
-#pragma unroll
-    for (int r = 0; r < 4; ++r) m = v[r] < m ? v[r] : m;
-    return m;
 }
 
 // HyperLogLog register index and rank — sketch.rs:49-63 (p = 14 there).

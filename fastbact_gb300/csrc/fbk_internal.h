@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -23,7 +24,9 @@ class DevicePool {
     uint64_t used() const { return used_bytes_; }
     uint64_t size() const { return size_; }
     uint64_t largest_free() const;
+    uint64_t free_bytes() const { return size_ - used_bytes_; }
     bool active() const { return base_ != nullptr; }
+    ~DevicePool() { release(); }
 
   private:
     char* base_ = nullptr;
@@ -44,7 +47,7 @@ struct fbk_ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
-    fbk::DevicePool pool;
+    std::shared_ptr<fbk::DevicePool> pool;  // shared by contexts forked from this one
     uint32_t* d_status = nullptr;            // device status bits (4 words)
     unsigned long long* d_counts = nullptr;  // conversion counters (4)
     void* h_pinned = nullptr;                // 64 KiB pinned host scratch
@@ -55,10 +58,18 @@ struct fbk_ctx {
     std::map<std::string, std::pair<double, uint64_t>> timed;
     uint64_t launches = 0;
     cudaEvent_t markers[16] = {};
-    // launch shapes (block size; grid 0 = persistent grid from occupancy)
+    // launch shapes (block size; grid 0 = 4 blocks per SM)
     int block_pass1 = 256, grid_pass1 = 0;
     int block_pass2 = 256, grid_pass2 = 0;
     int block_misc = 256;
+    // sweep sizing: bytes of sketch per pass-1 / solidity sweep, and bytes of table
+    // per pass-2 slot range (the hot part of a range must stay L2-resident)
+    uint64_t sweep_bytes = 64ull << 20;
+    uint64_t bucket_bytes = 256ull << 20;  // table bytes per pass-2 record bucket
+    uint32_t stripes = 64;                // append stripes per bucket
+    double load_factor = 0.62;            // solid table keys / slots when sized from the estimate
+    int pass2_mode = 1;                   // 1 = record buckets, 0 = direct sweep
+    double record_factor = 1.25;          // bucket capacity / expected records per stripe
 };
 
 struct fbk_bank {
@@ -69,16 +80,28 @@ struct fbk_bank {
     uint32_t* pair_idx = nullptr;
     uint64_t n_reads = 0, n_words = 0, n_bases = 0, n_pairs = 0;
     uint32_t max_len = 0;
-    std::vector<uint64_t> chunk_starts;  // read-range boundaries with < 2^31 bases each
+    std::vector<uint64_t> chunk_starts;  // read-range boundaries (see bank_upload_impl)
+    uint64_t max_chunk = 0;              // most bases in one range
+    uint64_t max_chunk_bases() const { return max_chunk; }
+    std::vector<uint64_t> len_hist;      // read-length histogram (last bin: all longer reads)
+    uint64_t long_bases = 0;             // bases of reads in the last bin
+    // upper bound of the windows of length k in reads with len >= min_len
+    uint64_t windows(uint32_t k, uint32_t min_len) const {
+        uint64_t w = 0;
+        const uint64_t last = len_hist.empty() ? 0 : len_hist.size() - 1;
+        for (uint64_t L = std::max<uint64_t>(min_len, k); L < last; ++L) w += len_hist[L] * (L - k + 1);
+        return w + long_bases;
+    }
 };
 
 struct fbk_cms {
     fbk_ctx* ctx = nullptr;
-    uint32_t* words = nullptr;
+    uint32_t* cnt = nullptr;    // exact u32 count per (row, column), 4 rows of 2^log2w; <= 65535 between calls
     uint32_t* hll12 = nullptr;  // p=12 registers of the keys added by bank passes (table sizing)
     uint32_t log2w = 0;
-    uint32_t cbits = 4;
-    uint64_t n_words = 0;
+    uint32_t cbits = 4;         // reference layout and cap: 4 -> nibbles / 15, 16 -> u16 / 65535
+    uint64_t n = 0;             // 4 << log2w counters
+    uint32_t cap() const { return cbits == 4 ? 15u : 0xFFFFu; }
 };
 
 struct fbk_hll {
@@ -110,6 +133,8 @@ fbk_status cuda_err(fbk_ctx* ctx, cudaError_t e, const char* what);
 void* dev_alloc(fbk_ctx* ctx, uint64_t bytes);
 void dev_free(fbk_ctx* ctx, void* p);
 Launch launch_cfg(fbk_ctx* ctx, int block, int grid);
+// grid <= 0 is left to the launcher: resident blocks per SM x SMs
+Launch launch_cfg_persistent(fbk_ctx* ctx, int block, int grid);
 // Brackets a launch with timing events when timing is on.
 void time_begin(fbk_ctx* ctx, const char* name, TimedLaunch& t);
 void time_end(fbk_ctx* ctx, TimedLaunch& t);
@@ -117,7 +142,9 @@ fbk_status ctx_check_status(fbk_ctx* ctx, uint32_t* bits);
 
 // Upload of a packed arena set into a device bank (used by the estimator for its
 // sample and by prior-contig handling).
-fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_arenas, fbk_bank** out);
+// chunk_bases: read ranges are cut so that each holds fewer bases than this.
+fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_arenas, fbk_bank** out,
+                            uint64_t chunk_bases = 1ull << 30);
 BankDev bank_view(const fbk_bank* b, uint64_t r_begin, uint64_t r_end, const uint64_t* keep_bits);
 
 // host f64 HyperLogLog::estimate from the register sum and zero count (sketch.rs:83-114)

@@ -138,30 +138,48 @@ __global__ void k_subsample(uint64_t n_pairs, uint64_t threshold, uint64_t seed,
     }
 }
 
-template <int CB>
-__global__ void k_cms_keys(uint32_t* cms, uint32_t log2w, const uint64_t* __restrict__ keys, uint64_t n, uint32_t* est,
-                           int add) {
+// CountMinSketch::add / estimate (sketch.rs:191-246) over device keys, on the exact
+// u32 counts: add is a RED.ADD per row, estimate the minimum over rows capped at cap.
+__global__ void k_cms_keys(uint32_t* cnt, uint32_t log2w, uint32_t cap, const uint64_t* __restrict__ keys, uint64_t n,
+                           uint32_t* est, int add) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        if (add) cms_add<CB>(cms, keys[i], log2w);
-        else est[i] = cms_estimate<CB>(cms, keys[i], log2w);
+        const uint64_t key = keys[i];
+        if (add) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) atomicAdd(cnt + cms_index(key, r, log2w), 1u);
+        } else {
+            uint32_t m = cap;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const uint32_t c = cnt[cms_index(key, r, log2w)];
+                m = c < m ? c : m;
+            }
+            est[i] = m;
+        }
     }
 }
 
-// dst = min(cap, dst + src) per counter field of each 32-bit word.
-template <int CB>
-__global__ void k_cms_merge(uint32_t* dst, const uint32_t* src, uint64_t n_words) {
-    const uint32_t cap = cms_cap<CB>();
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_words; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t a = dst[i], b = src[i];
-        uint32_t out = 0;
-#pragma unroll
-        for (int f = 0; f < 32 / CB; ++f) {
-            const uint32_t sh = f * CB;
-            uint32_t v = ((a >> sh) & cap) + ((b >> sh) & cap);
-            v = v > cap ? cap : v;
-            out |= v << sh;
-        }
-        dst[i] = out;
+// dst = min(65535, dst + src): counts stay exact below every cap (<= 65535).
+__global__ void k_cms_merge(uint32_t* dst, const uint32_t* src, uint64_t n) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t v = (uint64_t)dst[i] + src[i];
+        dst[i] = v > 0xFFFFu ? 0xFFFFu : (uint32_t)v;
+    }
+}
+
+// Reference layout: nibble byte b holds counters 2b (low) and 2b+1 (high), capped at
+// 15 (sketch.rs:131-157); u16 mode writes min(65535, count) little-endian.
+__global__ void k_cms_export_nib(const uint32_t* __restrict__ cnt, uint64_t n_bytes, uint8_t* out) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_bytes; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint2 v = reinterpret_cast<const uint2*>(cnt)[i];
+        const uint32_t lo = v.x < 15u ? v.x : 15u, hi = v.y < 15u ? v.y : 15u;
+        out[i] = (uint8_t)(lo | (hi << 4));
+    }
+}
+__global__ void k_cms_export_u16(const uint32_t* __restrict__ cnt, uint64_t n, uint16_t* out) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = cnt[i];
+        out[i] = (uint16_t)(v < 0xFFFFu ? v : 0xFFFFu);
     }
 }
 
@@ -239,15 +257,18 @@ cudaError_t launch_subsample_mask(const Launch& L, uint64_t n_pairs, double fact
     k_subsample<<<L.grid, L.block, 0, L.stream>>>(n_pairs, thr, seed, keep_all, bits);
     return cudaGetLastError();
 }
-cudaError_t launch_cms_keys(int cb, const Launch& L, uint32_t* cms, uint32_t log2w, const uint64_t* keys, uint64_t n,
+cudaError_t launch_cms_keys(const Launch& L, uint32_t* cnt, uint32_t log2w, uint32_t cap, const uint64_t* keys, uint64_t n,
                             uint32_t* est_out, int add) {
-    if (cb == 4) k_cms_keys<4><<<L.grid, L.block, 0, L.stream>>>(cms, log2w, keys, n, est_out, add);
-    else k_cms_keys<16><<<L.grid, L.block, 0, L.stream>>>(cms, log2w, keys, n, est_out, add);
+    k_cms_keys<<<L.grid, L.block, 0, L.stream>>>(cnt, log2w, cap, keys, n, est_out, add);
     return cudaGetLastError();
 }
-cudaError_t launch_cms_merge(int cb, const Launch& L, uint32_t* dst, const uint32_t* src, uint64_t n_words) {
-    if (cb == 4) k_cms_merge<4><<<L.grid, L.block, 0, L.stream>>>(dst, src, n_words);
-    else k_cms_merge<16><<<L.grid, L.block, 0, L.stream>>>(dst, src, n_words);
+cudaError_t launch_cms_merge(const Launch& L, uint32_t* dst, const uint32_t* src, uint64_t n) {
+    k_cms_merge<<<L.grid, L.block, 0, L.stream>>>(dst, src, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_cms_export(int cb, const Launch& L, const uint32_t* cnt, uint64_t n, uint8_t* out) {
+    if (cb == 4) k_cms_export_nib<<<L.grid, L.block, 0, L.stream>>>(cnt, n / 2, out);
+    else k_cms_export_u16<<<L.grid, L.block, 0, L.stream>>>(cnt, n, reinterpret_cast<uint16_t*>(out));
     return cudaGetLastError();
 }
 cudaError_t launch_nthash_arena(const Launch& L, const BankDev& b, const uint64_t* kbase, uint32_t k, uint64_t* out) {

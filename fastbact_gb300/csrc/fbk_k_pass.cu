@@ -1,6 +1,6 @@
-// fbk_k_pass.cu — build front-end kernels: pass 1 (CMS update), pass 2 (CMS-gated
-// transitions into the open-addressing solid table) and the SolidKmerNode
-// conversion (src/graph/build.rs:84-328).
+// fbk_k_pass.cu — build front-end kernels: pass 1 (CMS update), the CMS gate as a
+// solidity bitmap, pass 2 (gated transitions into the open-addressing solid table)
+// and the SolidKmerNode conversion (src/graph/build.rs:84-328).
 //
 // Work split: one warp per read (reads are ~150-300 bases), lane j handles the
 // k-mer windows j, j+32, ... of the read, each computed directly from the packed
@@ -19,18 +19,33 @@ static constexpr uint64_t TAG_READY = 1ULL << 63;
 static constexpr uint64_t KEY_EMPTY = ~0ULL;
 
 // ---------------------------------------------------------------------------
+// Count-Min Sketch on the device.  The sketch keeps an exact u32 count per
+// (row, column) — count_r(col) — and every reader applies the reference's cap:
+// the nibble value is min(15, count), the u16 value min(65535, count).  This is
+// the same as the reference's saturating increments (sketch.rs:199-221) because
+// increments are positive: min(cap, min(cap, a) + b) = min(cap, a + b).  Counts are
+// clamped to 65535 between launches, and a launch adds less than 2^32 - 2^17 in
+// total, so no u32 wraps.  The gain: an increment is one fire-and-forget RED.ADD
+// instead of a load + CAS round trip.
+//
 // Pass 1 — build.rs:90-116 (mult = 1) and the prior-contig weighting x10
-// (build.rs:118-138, mult = 10: ten saturating increments == one add of 10).
+// (build.rs:118-138, mult = 10).  One launch is one sweep over the bank that adds
+// only the k-mers whose column in row `row` falls in [c0, c1): the host sizes the
+// column range so the sweep's slice of the sketch (~64 MB) stays resident in L2,
+// and runs the sweeps for all rows and ranges back to back.
 // ---------------------------------------------------------------------------
-template <int NW, int CB>
-__global__ void __launch_bounds__(256) k_pass1(BankDev b, uint32_t k, uint32_t* __restrict__ cms, uint32_t log2w,
-                                               uint32_t mult, uint32_t* __restrict__ hll12) {
+template <int NW>
+__global__ void __launch_bounds__(256) k_pass1_sweep(BankDev b, uint32_t k, uint32_t* __restrict__ cnt, uint32_t log2w,
+                                                     uint32_t r0, uint32_t r1, uint64_t c0, uint64_t c1, uint32_t mult,
+                                                     uint32_t* __restrict__ hll12) {
     __shared__ uint32_t s_hll[4096];
     const bool do_hll = hll12 != nullptr;
     if (do_hll) {
         for (int i = threadIdx.x; i < 4096; i += blockDim.x) s_hll[i] = 0;
         __syncthreads();
     }
+    const uint64_t wmask = (1ULL << log2w) - 1, span = c1 - c0, seed0 = cms_seed((int)r0);
+    uint32_t* row0 = cnt + ((uint64_t)r0 << log2w);
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -44,13 +59,17 @@ __global__ void __launch_bounds__(256) k_pass1(BankDev b, uint32_t k, uint32_t* 
             bool rc;
             window_canonical<NW>(b.data, off + i, k, can, rc);
             const uint64_t key = key_fold<NW>(can);
-            uint64_t c[4];
-#pragma unroll
-            for (int rr = 0; rr < 4; ++rr) c[rr] = cms_index(key, rr, log2w);
-#pragma unroll
-            for (int rr = 0; rr < 4; ++rr) cms_sat_add<CB>(cms, c[rr], mult);
+            if (r1 == r0 + 1) {
+                const uint64_t col = smix(key ^ seed0) & wmask;
+                if (col - c0 < span) atomicAdd(row0 + col, mult);
+            } else {
+                for (uint32_t row = r0; row < r1; ++row) {
+                    const uint64_t col = smix(key ^ cms_seed((int)row)) & wmask;
+                    if (col - c0 < span) atomicAdd(cnt + ((uint64_t)row << log2w) + col, mult);
+                }
+            }
             if (do_hll) {
-                // Any bijective hash of the key serves the distinct count.
+                // any bijective hash of the key serves the distinct count
                 uint32_t idx, rho;
                 hll_idx_rho(smix(key ^ cms_seed(0)), 12, idx, rho);
                 if (s_hll[idx] < rho) atomicMax(&s_hll[idx], rho);
@@ -67,10 +86,73 @@ __global__ void __launch_bounds__(256) k_pass1(BankDev b, uint32_t k, uint32_t* 
 }
 
 // ---------------------------------------------------------------------------
-// Solid table probing
+// Solidity bitmap — the CMS gate of pass 2 (build.rs:259-267): window q of a read
+// is solid iff min_r min(cap, count_r) >= t_solid, i.e. iff every row's capped count
+// is >= t_solid.  Bit (off + q) of the bitmap (indexed by the window's first base in
+// the bank) starts at 1; each sweep clears the bits of windows whose column in its
+// row slice fails the test.  A warp's 32 windows are 32 consecutive bits, so one
+// ballot becomes at most two atomicAnd.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int64_t table_slot1(const TableDev& t, uint64_t key, uint32_t* status) {
-    uint64_t s = smix(key ^ TABLE_SALT) & t.mask;
+template <int NW>
+__global__ void __launch_bounds__(256) k_solid_sweep(BankDev b, uint32_t k, const uint32_t* __restrict__ cnt, uint32_t log2w,
+                                                     uint32_t r0, uint32_t r1, uint64_t c0, uint64_t c1, uint32_t t_solid,
+                                                     uint32_t cap, uint32_t* __restrict__ bm) {
+    const uint64_t wmask = (1ULL << log2w) - 1, span = c1 - c0, seed0 = cms_seed((int)r0);
+    const uint32_t* row0 = cnt + ((uint64_t)r0 << log2w);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t r = b.r_begin + gw; r < b.r_end; r += nwarps) {
+        const uint32_t len = b.len[r];
+        if (len < k + 1 || !bank_keep(b, r)) continue;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        for (uint32_t it = 0; it < ((nk + 31) >> 5); ++it) {
+            const uint32_t q = (it << 5) + lane;
+            bool clr = false;
+            if (q < nk) {
+                Key<NW> can;
+                bool rc;
+                window_canonical<NW>(b.data, off + q, k, can, rc);
+                const uint64_t key = key_fold<NW>(can);
+                if (r1 == r0 + 1) {
+                    const uint64_t col = smix(key ^ seed0) & wmask;
+                    if (col - c0 < span) {
+                        uint32_t c = __ldg(row0 + col);
+                        c = c < cap ? c : cap;
+                        clr = c < t_solid;
+                    }
+                } else {
+                    for (uint32_t row = r0; row < r1; ++row) {
+                        const uint64_t col = smix(key ^ cms_seed((int)row)) & wmask;
+                        if (col - c0 < span) {
+                            uint32_t c = __ldg(cnt + ((uint64_t)row << log2w) + col);
+                            c = c < cap ? c : cap;
+                            clr |= c < t_solid;
+                        }
+                    }
+                }
+            }
+            const uint32_t m = __ballot_sync(0xffffffffu, clr);
+            if (lane == 0 && m) {
+                const uint64_t g0 = off + ((uint64_t)it << 5);
+                const uint32_t sh = (uint32_t)(g0 & 31);
+                atomicAnd(&bm[g0 >> 5], ~(m << sh));
+                if (sh) atomicAnd(&bm[(g0 >> 5) + 1], ~(m >> (32 - sh)));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Solid table probing from a precomputed home slot
+// ---------------------------------------------------------------------------
+// Home slot of a key: the high 64 bits of mix(fold) * cap (any capacity).
+__device__ __forceinline__ uint64_t home_slot(uint64_t fold, uint64_t cap) {
+    return __umul64hi(smix(fold ^ TABLE_SALT), cap);
+}
+
+__device__ __forceinline__ int64_t table_slot1(const TableDev& t, uint64_t key, uint64_t s, uint32_t* status) {
     for (uint32_t probe = 0; probe < t.max_probe; ++probe) {
         const uint64_t cur = __ldcg(&t.keys[s]);
         if (cur == key) return (int64_t)s;
@@ -78,16 +160,45 @@ __device__ __forceinline__ int64_t table_slot1(const TableDev& t, uint64_t key, 
             const uint64_t old = atomicCAS((unsigned long long*)&t.keys[s], KEY_EMPTY, key);
             if (old == KEY_EMPTY || old == key) return (int64_t)s;
         }
-        s = (s + 1) & t.mask;
+        s = s + 1 == t.cap ? 0 : s + 1;
+    }
+    atomicOr(status, ST_TABLE_FULL);
+    return -1;
+}
+
+// 16-byte compare-and-swap (sm_90 and later): the 128-bit key of a slot goes from
+// EMPTY (all ones: a k <= 63 key leaves its top two bits zero) to the key in one
+// atomic step, so a slot never holds half a key and no publication wait is needed.
+__device__ __forceinline__ void cas128(uint64_t* addr, uint64_t cmp_lo, uint64_t cmp_hi, uint64_t new_lo, uint64_t new_hi,
+                                       uint64_t& old_lo, uint64_t& old_hi) {
+    asm volatile(
+        "{\n\t.reg .b128 c, n, d;\n\t"
+        "mov.b128 c, {%2, %3};\n\t"
+        "mov.b128 n, {%4, %5};\n\t"
+        "atom.global.cas.b128 d, [%6], c, n;\n\t"
+        "mov.b128 {%0, %1}, d;\n\t}"
+        : "=l"(old_lo), "=l"(old_hi)
+        : "l"(cmp_lo), "l"(cmp_hi), "l"(new_lo), "l"(new_hi), "l"(addr)
+        : "memory");
+}
+
+__device__ __forceinline__ int64_t table_slot2(const TableDev& t, const Key<2>& key, uint64_t s, uint32_t* status) {
+    for (uint32_t probe = 0; probe < t.max_probe; ++probe) {
+        uint64_t* a = t.keys + s * 2;
+        const uint64_t c0 = __ldcg(a), c1 = __ldcg(a + 1);
+        if (c0 == key.w[0] && c1 == key.w[1]) return (int64_t)s;
+        // Anything but our key or EMPTY may be a slot being written: decide with the CAS.
+        uint64_t o0, o1;
+        cas128(a, KEY_EMPTY, KEY_EMPTY, key.w[0], key.w[1], o0, o1);
+        if ((o0 == KEY_EMPTY && o1 == KEY_EMPTY) || (o0 == key.w[0] && o1 == key.w[1])) return (int64_t)s;
+        s = s + 1 == t.cap ? 0 : s + 1;
     }
     atomicOr(status, ST_TABLE_FULL);
     return -1;
 }
 
 template <int NW>
-__device__ __forceinline__ int64_t table_slotw(const TableDev& t, const Key<NW>& key, uint32_t* status) {
-    const uint64_t f = key_fold<NW>(key);
-    uint64_t s = smix(f ^ TABLE_SALT) & t.mask;
+__device__ __forceinline__ int64_t table_slotw(const TableDev& t, const Key<NW>& key, uint64_t f, uint64_t s, uint32_t* status) {
     const uint64_t fp = (smix(f ^ FP_SALT) | 1ULL) & ~TAG_READY;
     for (uint32_t probe = 0; probe < t.max_probe; ++probe) {
         cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> tag_ref(*(unsigned long long*)&t.tags[s]);
@@ -119,16 +230,10 @@ __device__ __forceinline__ int64_t table_slotw(const TableDev& t, const Key<NW>&
             for (int i = 0; i < NW; ++i) eq &= (__ldcg(&t.keys[s * NW + i]) == key.w[i]);
             if (eq) return (int64_t)s;
         }
-        s = (s + 1) & t.mask;
+        s = s + 1 == t.cap ? 0 : s + 1;
     }
     atomicOr(status, ST_TABLE_FULL);
     return -1;
-}
-
-template <int NW>
-__device__ __forceinline__ int64_t table_slot(const TableDev& t, const Key<NW>& key, uint32_t* status) {
-    if constexpr (NW == 1) return table_slot1(t, key.w[0], status);
-    else return table_slotw<NW>(t, key, status);
 }
 
 // ---------------------------------------------------------------------------
@@ -137,15 +242,21 @@ __device__ __forceinline__ int64_t table_slot(const TableDev& t, const Key<NW>& 
 //
 // For the transition (u, v) between windows q and q+1 the reference pushes
 // (u_can, base(q+k) + 4*u_rc) and (v_can, (3 - base(q)) + 4*!v_rc), each push adding
-// to cov and to one edge counter.  Here the owner lane of window q performs both
-// pushes that concern its own key: as u of (q, q+1) and as v of (q-1, q).  The
-// solidity of the neighbours comes from warp ballots; a window's pushes are issued
-// one iteration later, once the ballot of the next 32 windows is known.
+// to cov and to one edge counter.  Here the lane of window q makes both pushes that
+// concern its own key — as u of (q, q+1) and as v of (q-1, q) — with one probe.
+// Solidity comes from the bitmap.  One launch handles the keys whose home slot lies
+// in [s0, s1): the host splits the table into slot ranges whose hot part fits L2 and
+// sweeps the bank once per range; every occurrence of a key lands in the same sweep.
 // ---------------------------------------------------------------------------
-template <int NW, int CB>
-__global__ void __launch_bounds__(256) k_pass2(BankDev b, uint32_t k, const uint32_t* __restrict__ cms, uint32_t log2w,
-                                               uint32_t t_solid, int gate, uint32_t w_edge, uint32_t w_cov, TableDev t,
-                                               uint32_t* status) {
+__device__ __forceinline__ bool bm_bit(const uint32_t* __restrict__ bm, uint64_t g) {
+    return (__ldg(&bm[g >> 5]) >> (g & 31)) & 1u;
+}
+
+template <int NW>
+__global__ void __launch_bounds__(256) k_pass2_sweep(BankDev b, uint32_t k, const uint32_t* __restrict__ bm, int gate,
+                                                     uint64_t s0, uint64_t s1, uint32_t w_edge, uint32_t w_cov, TableDev t,
+                                                     uint32_t* status) {
+    const uint64_t span = s1 - s0;
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -154,46 +265,181 @@ __global__ void __launch_bounds__(256) k_pass2(BankDev b, uint32_t k, const uint
         if (len < k + 1 || !bank_keep(b, r)) continue;
         const uint64_t off = b.off[r];
         const uint32_t nk = len - k + 1;
-        const uint32_t n_it = (nk + 31) >> 5;
-        uint32_t m_prev2 = 0, m_prev = 0;
-        Key<NW> pkey;
-#pragma unroll
-        for (int i = 0; i < NW; ++i) pkey.w[i] = 0;
-        bool prc = false;
-        for (uint32_t it = 0; it <= n_it; ++it) {
-            uint32_t m_cur = 0;
-            Key<NW> ckey;
-#pragma unroll
-            for (int i = 0; i < NW; ++i) ckey.w[i] = 0;
-            bool crc = false;
-            if (it < n_it) {
-                const uint32_t p = (it << 5) + lane;
-                bool solid = false;
-                if (p < nk) {
-                    window_canonical<NW>(b.data, off + p, k, ckey, crc);
-                    solid = !gate || cms_estimate<CB>(cms, key_fold<NW>(ckey), log2w) >= t_solid;
-                }
-                m_cur = __ballot_sync(0xffffffffu, solid);
+        for (uint32_t q = lane; q < nk; q += 32) {
+            const uint64_t g = off + q;
+            bool sq = true, sl = q > 0, sr = q + 1 < nk;
+            if (gate) {
+                sq = bm_bit(bm, g);
+                sl = sl && bm_bit(bm, g - 1);
+                sr = sr && bm_bit(bm, g + 1);
             }
-            if (it > 0 && ((m_prev >> lane) & 1u)) {
-                const uint32_t q = ((it - 1) << 5) + lane;
-                const bool sl = lane > 0 ? ((m_prev >> (lane - 1)) & 1u) : ((m_prev2 >> 31) & 1u);
-                const bool sr = lane < 31 ? ((m_prev >> (lane + 1)) & 1u) : (m_cur & 1u);
-                if (sl || sr) {
-                    const int64_t s = table_slot<NW>(t, pkey, status);
-                    if (s >= 0) {
-                        uint32_t* c = t.cnt + (uint64_t)s * 8;
-                        if (sr) atomicAdd(&c[base_at(b.data, off + q + k) + (prc ? 4u : 0u)], w_edge);
-                        if (sl) atomicAdd(&c[(3u - base_at(b.data, off + q - 1)) + (prc ? 0u : 4u)], w_edge);
-                        if (t.cov) atomicAdd(&t.cov[s], w_cov * ((sl ? 1u : 0u) + (sr ? 1u : 0u)));
-                    }
-                }
-            }
-            m_prev2 = m_prev;
-            m_prev = m_cur;
-            pkey = ckey;
-            prc = crc;
+            if (!sq || !(sl || sr)) continue;
+            Key<NW> key;
+            bool rc;
+            window_canonical<NW>(b.data, g, k, key, rc);
+            const uint64_t f = key_fold<NW>(key);
+            const uint64_t home = home_slot(f, t.cap);
+            if (home - s0 >= span) continue;
+            int64_t s;
+            if constexpr (NW == 1) s = table_slot1(t, key.w[0], home, status);
+            else if constexpr (NW == 2) s = table_slot2(t, key, home, status);
+            else s = table_slotw<NW>(t, key, f, home, status);
+            if (s < 0) continue;
+            uint32_t* c = t.cnt + (uint64_t)s * 8;
+            if (sr) atomicAdd(&c[base_at(b.data, g + k) + (rc ? 4u : 0u)], w_edge);
+            if (sl) atomicAdd(&c[(3u - base_at(b.data, g - 1)) + (rc ? 0u : 4u)], w_edge);
+            if (t.cov) atomicAdd(&t.cov[s], w_cov * ((sl ? 1u : 0u) + (sr ? 1u : 0u)));
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pass 2, record form.  k_emit scans the bank once: every window that is solid and
+// has a solid neighbour inside its read yields one record (its canonical key and the
+// one or two pushes it makes, same rules as k_pass2_sweep) appended to the bucket of
+// its home slot.  k_upsert then processes one bucket per launch: every lane owns a
+// record, probes from the home slot and adds the pushes.
+// ---------------------------------------------------------------------------
+// Records are staged per warp in shared memory (EMIT_BUF of them) and flushed
+// bucket by bucket: one atomic per (flush, bucket) reserves room for all of the
+// warp's records of that bucket, which are then written as one run.
+constexpr uint32_t EMIT_BUF = 128;
+constexpr uint32_t EMIT_MAX_BUCKETS = 64;
+// staging words per warp: records, bucket bytes, ranks (u16), histogram (64 u32),
+// reservation bases (64 u64)
+#define EMIT_WARP_WORDS(NW) (EMIT_BUF * ((NW) + 1) + EMIT_BUF / 8 + EMIT_BUF / 4 + EMIT_MAX_BUCKETS / 2 + EMIT_MAX_BUCKETS)
+
+// Warp counting sort of the staged records by bucket: a shared-memory histogram
+// (one atomic per record), one parallel round of global reservations (lane j
+// reserves for bucket j, j+32, ...), then every lane copies records to
+// region[bucket] + rank.  Cost does not grow with the number of buckets.
+template <int NW>
+__device__ __forceinline__ void emit_flush(const BucketDev& bk, uint32_t stripe, uint32_t lane, uint64_t* buf, const uint8_t* bbuf,
+                                           uint32_t n_buf, uint32_t* hist, unsigned long long* gbase, uint16_t* rank) {
+    for (uint32_t bu = lane; bu < bk.n_buckets; bu += 32) hist[bu] = 0;
+    __syncwarp();
+    for (uint32_t j = lane; j < n_buf; j += 32) rank[j] = (uint16_t)atomicAdd(&hist[bbuf[j]], 1u);
+    __syncwarp();
+    for (uint32_t bu = lane; bu < bk.n_buckets; bu += 32) {
+        const uint32_t c = hist[bu];
+        gbase[bu] = c ? atomicAdd(bk.fill + (uint64_t)bu * bk.stripes + stripe, (unsigned long long)c) : 0;
+    }
+    __syncwarp();
+    for (uint32_t j = lane; j < n_buf; j += 32) {
+        const uint32_t bu = bbuf[j];
+        const unsigned long long pos = gbase[bu] + rank[j];
+        if (pos < bk.stripe_cap) {
+            uint64_t* dst = bk.recs + (((uint64_t)bu * bk.stripes + stripe) * bk.stripe_cap + pos) * (NW + 1);
+#pragma unroll
+            for (int i = 0; i <= NW; ++i) dst[i] = buf[j * (NW + 1) + i];
+        } else {
+            atomicOr(bk.overflow, 1u);
+        }
+    }
+    __syncwarp();
+}
+
+template <int NW>
+__global__ void __launch_bounds__(256) k_emit(BankDev b, uint32_t k, const uint32_t* __restrict__ bm, int gate, TableDev t,
+                                              BucketDev bk) {
+    extern __shared__ uint64_t emit_smem[];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint64_t* buf = emit_smem + (uint64_t)wib * EMIT_WARP_WORDS(NW);
+    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + EMIT_BUF * (NW + 1));      // EMIT_BUF bytes
+    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + EMIT_BUF);              // EMIT_BUF u16
+    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + EMIT_BUF);              // EMIT_MAX_BUCKETS u32
+    unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t stripe = (uint32_t)(gw % bk.stripes);
+    uint32_t n_buf = 0;  // warp-uniform
+    for (uint64_t r = b.r_begin + gw; r < b.r_end; r += nwarps) {
+        const uint32_t len = b.len[r];
+        if (len < k + 1 || !bank_keep(b, r)) continue;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        for (uint32_t it = 0; it < ((nk + 31) >> 5); ++it) {
+            const uint32_t q = (it << 5) + lane;
+            bool emit = false;
+            Key<NW> key;
+            uint32_t info = 0, bucket = 0;
+            if (q < nk) {
+                const uint64_t g = off + q;
+                bool sq = true, sl = q > 0, sr = q + 1 < nk;
+                if (gate) {
+                    sq = bm_bit(bm, g);
+                    sl = sl && bm_bit(bm, g - 1);
+                    sr = sr && bm_bit(bm, g + 1);
+                }
+                emit = sq && (sl || sr);
+                if (emit) {
+                    bool rc;
+                    window_canonical<NW>(b.data, g, k, key, rc);
+                    if (sr) info |= 8u | (base_at(b.data, g + k) + (rc ? 4u : 0u));
+                    if (sl) info |= (8u | ((3u - base_at(b.data, g - 1)) + (rc ? 0u : 4u))) << 4;
+                    bucket = (uint32_t)(home_slot(key_fold<NW>(key), t.cap) >> bk.shift);
+                }
+            }
+            const uint32_t active = __ballot_sync(0xffffffffu, emit);
+            if (emit) {
+                const uint32_t pos = n_buf + __popc(active & ((1u << lane) - 1));
+#pragma unroll
+                for (int i = 0; i < NW; ++i) buf[pos * (NW + 1) + i] = key.w[i];
+                buf[pos * (NW + 1) + NW] = info;
+                bbuf[pos] = (uint8_t)bucket;
+            }
+            n_buf += __popc(active);
+            if (n_buf > EMIT_BUF - 32) {
+                __syncwarp();
+                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+                n_buf = 0;
+            }
+        }
+    }
+    __syncwarp();
+    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+}
+
+template <int NW>
+__global__ void __launch_bounds__(256) k_upsert(BucketDev bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov, TableDev t,
+                                                uint32_t* status) {
+    __shared__ unsigned long long s_pre[257];
+    const uint32_t S = bk.stripes;  // <= 256
+    if (threadIdx.x == 0) {
+        unsigned long long acc = 0;
+        for (uint32_t i = 0; i < S; ++i) {
+            s_pre[i] = acc;
+            unsigned long long f = bk.fill[(uint64_t)bucket * S + i];
+            acc += f < bk.stripe_cap ? f : bk.stripe_cap;
+        }
+        s_pre[S] = acc;
+    }
+    __syncthreads();
+    const uint64_t n = s_pre[S];
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = S;  // stripe: last s with s_pre[s] <= i
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (s_pre[mid] <= i) lo = mid;
+            else hi = mid;
+        }
+        const uint64_t* rec = bk.recs + (((uint64_t)bucket * S + lo) * bk.stripe_cap + (i - s_pre[lo])) * (NW + 1);
+        Key<NW> key;
+#pragma unroll
+        for (int j = 0; j < NW; ++j) key.w[j] = __ldcs(rec + j);
+        const uint32_t info = (uint32_t)__ldcs(rec + NW);
+        const uint64_t f = key_fold<NW>(key);
+        const uint64_t home = home_slot(f, t.cap);
+        int64_t s;
+        if constexpr (NW == 1) s = table_slot1(t, key.w[0], home, status);
+        else if constexpr (NW == 2) s = table_slot2(t, key, home, status);
+        else s = table_slotw<NW>(t, key, f, home, status);
+        if (s < 0) continue;
+        uint32_t* c = t.cnt + (uint64_t)s * 8;
+        const uint32_t nu = (info >> 3) & 1u, nv = (info >> 7) & 1u;
+        if (nu) atomicAdd(&c[info & 7u], w_edge);
+        if (nv) atomicAdd(&c[(info >> 4) & 7u], w_edge);
+        if (t.cov) atomicAdd(&t.cov[s], w_cov * (nu + nv));
     }
 }
 
@@ -240,7 +486,7 @@ template <int NW>
 __global__ void __launch_bounds__(256) k_convert(TableDev t, uint32_t min_trans_cov, ConvOut o) {
     __shared__ uint32_t s_warp[32];
     __shared__ unsigned long long s_base[2];
-    const uint64_t cap = t.mask + 1;
+    const uint64_t cap = t.cap;
     const uint64_t tile = (uint64_t)blockDim.x * CONV_SLOTS;
     unsigned long long n_keys = 0, digest = 0, raw_total = 0;
     for (uint64_t base = (uint64_t)blockIdx.x * tile; base < cap; base += (uint64_t)gridDim.x * tile) {
@@ -250,7 +496,7 @@ __global__ void __launch_bounds__(256) k_convert(TableDev t, uint32_t min_trans_
         for (int j = 0; j < CONV_SLOTS; ++j) {
             const uint64_t s = s0 + j;
             if (s >= cap) break;
-            const bool occ = NW == 1 ? (t.keys[s] != KEY_EMPTY) : (t.tags[s] != 0);
+            const bool occ = NW <= 2 ? (t.keys[s * NW] != KEY_EMPTY) : (t.tags[s] != 0);
             occ_bits |= (uint32_t)occ << j;
         }
         // mask per occupied slot (needs the counters)
@@ -355,32 +601,88 @@ __global__ void k_table_init(uint64_t* keys, uint64_t n_keys_words, uint64_t fil
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-template <int NW>
-static cudaError_t pass1_nw(int cb, const Launch& L, const BankDev& b, uint32_t k, uint32_t* cms, uint32_t log2w,
-                            uint32_t mult, uint32_t* hll12) {
-    if (cb == 4) k_pass1<NW, 4><<<L.grid, L.block, 0, L.stream>>>(b, k, cms, log2w, mult, hll12);
-    else k_pass1<NW, 16><<<L.grid, L.block, 0, L.stream>>>(b, k, cms, log2w, mult, hll12);
-    return cudaGetLastError();
-}
-cudaError_t launch_pass1(int nw, int cb, const Launch& L, const BankDev& b, uint32_t k, uint32_t* cms, uint32_t log2w,
-                         uint32_t mult, uint32_t* hll12) {
-    if (nw == 1) return pass1_nw<1>(cb, L, b, k, cms, log2w, mult, hll12);
-    if (nw == 2) return pass1_nw<2>(cb, L, b, k, cms, log2w, mult, hll12);
-    return pass1_nw<4>(cb, L, b, k, cms, log2w, mult, hll12);
+// Persistent grid: resident blocks per SM for this kernel and block size, times SMs.
+template <class K>
+static int grid_for(K kernel, const Launch& L) {
+    if (L.grid > 0) return L.grid;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, L.block, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+    return per_sm * (L.sms > 0 ? L.sms : 1);
 }
 
 template <int NW>
-static cudaError_t pass2_nw(int cb, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* cms, uint32_t log2w,
-                            uint32_t t_solid, int gate, uint32_t we, uint32_t wc, const TableDev& t, uint32_t* status) {
-    if (cb == 4) k_pass2<NW, 4><<<L.grid, L.block, 0, L.stream>>>(b, k, cms, log2w, t_solid, gate, we, wc, t, status);
-    else k_pass2<NW, 16><<<L.grid, L.block, 0, L.stream>>>(b, k, cms, log2w, t_solid, gate, we, wc, t, status);
+static cudaError_t pass1_nw(const Launch& L, const BankDev& b, uint32_t k, uint32_t* cnt, uint32_t log2w, uint32_t r0,
+                            uint32_t r1, uint64_t c0, uint64_t c1, uint32_t mult, uint32_t* hll12) {
+    k_pass1_sweep<NW><<<grid_for(k_pass1_sweep<NW>, L), L.block, 0, L.stream>>>(b, k, cnt, log2w, r0, r1, c0, c1, mult, hll12);
     return cudaGetLastError();
 }
-cudaError_t launch_pass2(int nw, int cb, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* cms, uint32_t log2w,
-                         uint32_t t_solid, int gate, uint32_t w_edge, uint32_t w_cov, const TableDev& t, uint32_t* status) {
-    if (nw == 1) return pass2_nw<1>(cb, L, b, k, cms, log2w, t_solid, gate, w_edge, w_cov, t, status);
-    if (nw == 2) return pass2_nw<2>(cb, L, b, k, cms, log2w, t_solid, gate, w_edge, w_cov, t, status);
-    return pass2_nw<4>(cb, L, b, k, cms, log2w, t_solid, gate, w_edge, w_cov, t, status);
+cudaError_t launch_pass1_sweep(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* cnt, uint32_t log2w,
+                               uint32_t r0, uint32_t r1, uint64_t c0, uint64_t c1, uint32_t mult, uint32_t* hll12) {
+    if (nw == 1) return pass1_nw<1>(L, b, k, cnt, log2w, r0, r1, c0, c1, mult, hll12);
+    if (nw == 2) return pass1_nw<2>(L, b, k, cnt, log2w, r0, r1, c0, c1, mult, hll12);
+    return pass1_nw<4>(L, b, k, cnt, log2w, r0, r1, c0, c1, mult, hll12);
+}
+
+template <int NW>
+static cudaError_t solid_nw(const Launch& L, const BankDev& b, uint32_t k, const uint32_t* cnt, uint32_t log2w, uint32_t r0,
+                            uint32_t r1, uint64_t c0, uint64_t c1, uint32_t t_solid, uint32_t cap, uint32_t* bm) {
+    k_solid_sweep<NW><<<grid_for(k_solid_sweep<NW>, L), L.block, 0, L.stream>>>(b, k, cnt, log2w, r0, r1, c0, c1, t_solid, cap, bm);
+    return cudaGetLastError();
+}
+cudaError_t launch_solid_sweep(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* cnt, uint32_t log2w,
+                               uint32_t r0, uint32_t r1, uint64_t c0, uint64_t c1, uint32_t t_solid, uint32_t cap, uint32_t* bm) {
+    if (nw == 1) return solid_nw<1>(L, b, k, cnt, log2w, r0, r1, c0, c1, t_solid, cap, bm);
+    if (nw == 2) return solid_nw<2>(L, b, k, cnt, log2w, r0, r1, c0, c1, t_solid, cap, bm);
+    return solid_nw<4>(L, b, k, cnt, log2w, r0, r1, c0, c1, t_solid, cap, bm);
+}
+
+template <int NW>
+static cudaError_t pass2_nw(const Launch& L, const BankDev& b, uint32_t k, const uint32_t* bm, int gate, uint64_t s0,
+                            uint64_t s1, uint32_t we, uint32_t wc, const TableDev& t, uint32_t* status) {
+    k_pass2_sweep<NW><<<grid_for(k_pass2_sweep<NW>, L), L.block, 0, L.stream>>>(b, k, bm, gate, s0, s1, we, wc, t, status);
+    return cudaGetLastError();
+}
+cudaError_t launch_pass2_sweep(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* bm, int gate,
+                               uint64_t s0, uint64_t s1, uint32_t w_edge, uint32_t w_cov, const TableDev& t,
+                               uint32_t* status) {
+    if (nw == 1) return pass2_nw<1>(L, b, k, bm, gate, s0, s1, w_edge, w_cov, t, status);
+    if (nw == 2) return pass2_nw<2>(L, b, k, bm, gate, s0, s1, w_edge, w_cov, t, status);
+    return pass2_nw<4>(L, b, k, bm, gate, s0, s1, w_edge, w_cov, t, status);
+}
+
+template <int NW>
+static cudaError_t emit_nw(const Launch& L, const BankDev& b, uint32_t k, const uint32_t* bm, int gate, const TableDev& t,
+                           const BucketDev& bk) {
+    const size_t smem = (size_t)(L.block / 32) * EMIT_WARP_WORDS(NW) * 8;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_emit<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int grid = L.grid;
+    if (grid <= 0) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit<NW>, L.block, smem) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        grid = per_sm * (L.sms > 0 ? L.sms : 1);
+    }
+    k_emit<NW><<<grid, L.block, smem, L.stream>>>(b, k, bm, gate, t, bk);
+    return cudaGetLastError();
+}
+cudaError_t launch_emit(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* bm, int gate, const TableDev& t,
+                        const BucketDev& bk) {
+    if (nw == 1) return emit_nw<1>(L, b, k, bm, gate, t, bk);
+    if (nw == 2) return emit_nw<2>(L, b, k, bm, gate, t, bk);
+    return emit_nw<4>(L, b, k, bm, gate, t, bk);
+}
+
+template <int NW>
+static cudaError_t upsert_nw(const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t we, uint32_t wc, const TableDev& t,
+                             uint32_t* status) {
+    k_upsert<NW><<<grid_for(k_upsert<NW>, L), L.block, 0, L.stream>>>(bk, bucket, we, wc, t, status);
+    return cudaGetLastError();
+}
+cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov,
+                          const TableDev& t, uint32_t* status) {
+    if (nw == 1) return upsert_nw<1>(L, bk, bucket, w_edge, w_cov, t, status);
+    if (nw == 2) return upsert_nw<2>(L, bk, bucket, w_edge, w_cov, t, status);
+    return upsert_nw<4>(L, bk, bucket, w_edge, w_cov, t, status);
 }
 
 cudaError_t launch_convert(int nw, const Launch& L, const TableDev& t, uint32_t min_trans_cov, const ConvOut& o) {
@@ -396,9 +698,9 @@ cudaError_t launch_clamp_counters(const Launch& L, uint32_t* cnt, uint64_t n) {
 }
 
 cudaError_t launch_table_init(int nw, const Launch& L, const TableDev& t) {
-    const uint64_t cap = t.mask + 1;
-    if (nw == 1) {
-        k_table_init<<<L.grid, L.block, 0, L.stream>>>(t.keys, cap, KEY_EMPTY);
+    const uint64_t cap = t.cap;
+    if (nw <= 2) {
+        k_table_init<<<L.grid, L.block, 0, L.stream>>>(t.keys, cap * nw, KEY_EMPTY);
         return cudaGetLastError();
     }
     return cudaMemsetAsync(t.tags, 0, cap * sizeof(uint64_t), L.stream);

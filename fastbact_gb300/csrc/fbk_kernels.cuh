@@ -30,17 +30,32 @@ __host__ __device__ inline bool bank_keep(const BankDev& b, uint64_t r) {
 }
 
 // Open-addressing solid table.  NW == 1: keys[] holds the key itself (EMPTY = ~0;
-// a k <= 31 key uses 62 bits).  NW > 1: tags[] claims slots (0 empty, fingerprint,
-// fingerprint|READY once the key words are published) and keys[] holds NW words per
-// slot.  cnt[] holds 8 edge counters (u32) per slot, 32-byte aligned.
+// a k <= 31 key uses 62 bits).  NW == 2: keys[] holds the two words, claimed with one
+// 16-byte CAS (EMPTY = all ones).  NW == 4: tags[] claims slots (0 empty,
+// fingerprint, fingerprint|READY once the key words are published) and keys[] holds
+// the four words.  cnt[] holds 8 edge counters (u32) per slot, 32-byte aligned.
 struct TableDev {
     uint64_t* keys;
     uint64_t* tags;
     uint32_t* cnt;
     uint32_t* cov;       // separate cov counters, only when prior contigs are used
-    uint64_t mask;       // capacity - 1
+    uint64_t cap;        // slots (any size: home slot = high 64 bits of hash * cap)
     uint32_t max_probe;
     uint32_t spin_limit;
+};
+
+// Pass-2 records, grouped by the slot range of their key's home slot.  Bucket b
+// holds S stripes of stripe_cap records; warps append to stripe (warp % S) with one
+// atomic per (warp iteration, bucket).  A record is the canonical key (NW words)
+// and the pushes it makes: bits 0-2 edge as u, bit 3 present; bits 4-6 edge as v,
+// bit 7 present.
+struct BucketDev {
+    uint64_t* recs;              // (NW + 1) words per record
+    unsigned long long* fill;    // P * S append counters
+    uint64_t stripe_cap;
+    uint32_t shift;              // bucket of a home slot = home >> shift
+    uint32_t n_buckets, stripes;
+    uint32_t* overflow;          // set when a stripe runs out of room
 };
 
 // Output of the SolidKmerNode conversion.
@@ -56,22 +71,35 @@ struct ConvOut {
 };
 
 struct Launch {
-    int grid;
+    int grid;     // <= 0: occupancy-derived persistent grid (resident blocks x SMs)
     int block;
     cudaStream_t stream;
+    int sms;
 };
 
 // ---- build passes (fbk_k_pass.cu) -------------------------------------------
-// Pass 1: every k-mer of every kept read with len >= k adds `mult` (saturating) to
-// its four CMS counters.  hll12 (optional, 4096 u32) collects a p=12 HyperLogLog
-// of the keys, used only to size the solid table.
-cudaError_t launch_pass1(int nw, int cb, const Launch& L, const BankDev& b, uint32_t k, uint32_t* cms, uint32_t log2w,
-                         uint32_t mult, uint32_t* hll12);
-// Pass 2: transitions between adjacent k-mers; with gate != 0 both ends must have
-// CMS estimate >= t_solid.  Each push adds w_edge to an edge counter (and w_cov to
-// the cov counter when the table keeps one).
-cudaError_t launch_pass2(int nw, int cb, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* cms, uint32_t log2w,
-                         uint32_t t_solid, int gate, uint32_t w_edge, uint32_t w_cov, const TableDev& t, uint32_t* status);
+// Pass 1 sweep: for every k-mer of every kept read with len >= k and every row in
+// [r0, r1), a column in [c0, c1) gets `mult` added to its u32 count.  hll12
+// (optional, 4096 u32) collects a p=12 HyperLogLog of the keys (table sizing only).
+cudaError_t launch_pass1_sweep(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* cnt, uint32_t log2w,
+                               uint32_t r0, uint32_t r1, uint64_t c0, uint64_t c1, uint32_t mult, uint32_t* hll12);
+// Solidity sweep: clears bitmap bit (first base of window) when, in any row of
+// [r0, r1) whose column lies in [c0, c1), the window's capped count is below t_solid.
+cudaError_t launch_solid_sweep(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* cnt, uint32_t log2w,
+                               uint32_t r0, uint32_t r1, uint64_t c0, uint64_t c1, uint32_t t_solid, uint32_t cap,
+                               uint32_t* bm);
+// Pass 2 sweep over the keys whose home slot lies in [s0, s1): each push adds
+// w_edge to an edge counter (and w_cov to the cov counter when the table keeps one).
+cudaError_t launch_pass2_sweep(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* bm, int gate,
+                               uint64_t s0, uint64_t s1, uint32_t w_edge, uint32_t w_cov, const TableDev& t,
+                               uint32_t* status);
+// Pass 2 in two phases: one scan emits the records of solid windows into slot-range
+// buckets; then one launch per bucket upserts its records (the bucket's table range
+// stays L2-resident while every lane works on its own record).
+cudaError_t launch_emit(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* bm, int gate, const TableDev& t,
+                        const BucketDev& bk);
+cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov,
+                          const TableDev& t, uint32_t* status);
 cudaError_t launch_convert(int nw, const Launch& L, const TableDev& t, uint32_t min_trans_cov, const ConvOut& o);
 cudaError_t launch_clamp_counters(const Launch& L, uint32_t* cnt, uint64_t n);
 cudaError_t launch_table_init(int nw, const Launch& L, const TableDev& t);
@@ -87,9 +115,13 @@ cudaError_t launch_est_sums(const Launch& L, const uint32_t* regs_total, const u
 cudaError_t launch_hll_add(const Launch& L, uint32_t* regs, uint32_t p, const uint64_t* hashes, uint64_t n, int mix);
 cudaError_t launch_hll_merge(const Launch& L, uint32_t* dst, const uint32_t* src, uint64_t n);
 cudaError_t launch_subsample_mask(const Launch& L, uint64_t n_pairs, double factor, uint64_t seed, uint64_t* bits);
-cudaError_t launch_cms_keys(int cb, const Launch& L, uint32_t* cms, uint32_t log2w, const uint64_t* keys, uint64_t n,
+// Count-Min Sketch of exact u32 counts (4 rows of 2^log2w); readers cap at `cap`.
+cudaError_t launch_cms_keys(const Launch& L, uint32_t* cnt, uint32_t log2w, uint32_t cap, const uint64_t* keys, uint64_t n,
                             uint32_t* est_out, int add);
-cudaError_t launch_cms_merge(int cb, const Launch& L, uint32_t* dst, const uint32_t* src, uint64_t n_words);
+cudaError_t launch_cms_merge(const Launch& L, uint32_t* dst, const uint32_t* src, uint64_t n);
+// Reference byte layout: counter_bits 4 = nibbles (byte c>>1, high nibble for odd c),
+// 16 = little-endian u16; values min(cap, count).
+cudaError_t launch_cms_export(int cb, const Launch& L, const uint32_t* cnt, uint64_t n, uint8_t* out);
 cudaError_t launch_nthash_arena(const Launch& L, const BankDev& b, const uint64_t* kbase, uint32_t k, uint64_t* out);
 cudaError_t launch_canon_arena(int nw, const Launch& L, const BankDev& b, const uint64_t* kbase, uint32_t k,
                                uint64_t* out_words, uint8_t* out_rc);

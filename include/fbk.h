@@ -134,6 +134,13 @@ FBK_API const char* fbk_version(void);
 /* pool_bytes = 0: objects are allocated one by one; > 0: carved from one pool. */
 FBK_API fbk_status fbk_ctx_create(int device, uint64_t pool_bytes, fbk_ctx** out);
 FBK_API fbk_status fbk_ctx_destroy(fbk_ctx* ctx);
+/* A second context on the same device with its own stream, sharing the parent's
+ * memory pool (work on the two streams may overlap).  Destroy forks before or after
+ * the parent; the pool lives until its last context is destroyed. */
+FBK_API fbk_status fbk_ctx_fork(fbk_ctx* parent, fbk_ctx** out);
+/* Free bytes and the largest free block of the context's pool (device free memory
+ * when the context has no pool). */
+FBK_API fbk_status fbk_ctx_pool_free(const fbk_ctx* ctx, uint64_t* free_bytes, uint64_t* largest_block);
 FBK_API fbk_status fbk_last_error(const fbk_ctx* ctx, char* buf, size_t len);
 FBK_API fbk_status fbk_ctx_sync(fbk_ctx* ctx);
 /* Kernel timing with CUDA events on the context's stream (off by default). */
@@ -146,6 +153,15 @@ FBK_API fbk_status fbk_ctx_timing_reset(fbk_ctx* ctx);
  * milliseconds between two recorded markers (waits for the later one). */
 FBK_API fbk_status fbk_ctx_event_record(fbk_ctx* ctx, int slot);
 FBK_API fbk_status fbk_ctx_event_elapsed(fbk_ctx* ctx, int slot_a, int slot_b, double* ms);
+/* Launch and sizing parameters (the autotuner sets these): "sweep_bytes" (sketch
+ * bytes per pass-1 / solidity sweep), "bucket_bytes" (table bytes per pass-2 record
+ * bucket), "stripes", "load_factor", "pass2_mode" (1 buckets, 0 direct sweep),
+ * "record_factor" (record capacity over the expected count; a full bucket falls back
+ * to the direct sweep),
+ * "block_pass1", "grid_pass1", "block_pass2", "grid_pass2" (blocks of 32..256 threads in
+ * steps of 32; grid 0 = occupancy). */
+FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double value);
+FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, double* value);
 /* Number of kernels launched on this context since creation. */
 FBK_API fbk_status fbk_ctx_launch_count(const fbk_ctx* ctx, uint64_t* n);
 FBK_API fbk_status fbk_ctx_mem_info(const fbk_ctx* ctx, uint64_t* pool_used, uint64_t* pool_size);

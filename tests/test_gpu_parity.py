@@ -176,9 +176,11 @@ def test_build_front_matches_oracle(ctx, small_isolate, k, kb, cb):
     assert n_solid > 1000
 
 
-@pytest.mark.parametrize("tsc", [None, 1, 5, 15])
+@pytest.mark.parametrize("tsc", [None, 1, 5, 15, 20])
 def test_build_thresholds(ctx, repeat_isolate, tsc):
+    # tsc = 20 is above the nibble cap: the reference's capped estimate never reaches it
     compare_build(ctx, repeat_isolate[0], 31, 64, 4, tsc, 14)
+    compare_build(ctx, repeat_isolate[0], 31, 64, 16, tsc, 14)
 
 
 def test_build_saturation_and_repeats(ctx, repeat_isolate):
@@ -299,3 +301,26 @@ def test_estimator_reads_with_n_and_short(ctx):
                                                250000, 0.0)
     assert np.array_equal(rt, ort) and np.array_equal(rs, ors)
     assert (ge.genome_size, ge.u_ge_2, ge.pairs_sampled) == (oe.genome_size, oe.u_ge_2, oe.pairs_sampled)
+
+
+# ---------------------------------------------------------------------------
+# launch / sizing variants must not change any result
+# ---------------------------------------------------------------------------
+TUNINGS = [
+    dict(pass2_mode=0),                                   # direct sweep
+    dict(sweep_bytes=1 << 20, bucket_bytes=1 << 20),      # many column slices, 64 buckets
+    dict(sweep_bytes=1 << 31, bucket_bytes=1 << 30),      # one sweep over all rows, one bucket
+    dict(stripes=1, record_factor=0.05),                  # stripes overflow -> direct fallback
+    dict(load_factor=0.85, block_pass1=128, block_pass2=64, grid_pass1=37, grid_pass2=91),
+]
+
+
+@pytest.mark.parametrize("tune", TUNINGS)
+def test_build_tuning_variants(repeat_isolate, tune):
+    c = api.Context(0)
+    try:
+        c.set_tuning(**tune)
+        for k, kb, cb in [(31, 64, 4), (45, 128, 16), (99, 256, 4)]:
+            compare_build(c, repeat_isolate[0], k, kb, cb, None, 14)
+    finally:
+        c.close()

@@ -212,3 +212,8 @@ def test_ingest_subsample_matches_keep_rule(tmp_path):
         assert list(a_sub.pair_idx) == [int(a_full.pair_idx[j]) for j in sel]
         assert [a_sub.extract_ascii(i) for i in range(min(20, len(a_sub)))] == \
                [a_full.extract_ascii(j) for j in sel[:20]]
+
+
+def test_tuning_rejects_out_of_range_without_device():
+    # validation happens before any device work; a NULL context is rejected outright
+    assert N.lib().fbk_ctx_set_tuning(None, b"sweep_bytes", 1e6) == 1
