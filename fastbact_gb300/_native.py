@@ -63,6 +63,35 @@ class BuildParams(C.Structure):
                 ("table_log2_cap", C.c_uint32), ("_pad", C.c_uint32), ("genome_size", C.c_uint64)]
 
 
+class SubsamplePolicy(C.Structure):
+    _fields_ = [("no_subsample", C.c_int32), ("enable_auto_subsample", C.c_int32), ("has_genome_size", C.c_int32),
+                ("_pad", C.c_int32), ("genome_size", C.c_uint64), ("depth", C.c_double), ("threshold_ratio", C.c_double)]
+
+
+class BatchParams(C.Structure):
+    _fields_ = [("k", C.c_uint32), ("key_bits", C.c_uint32), ("cms_log2_width", C.c_uint32), ("counter_bits", C.c_uint32),
+                ("t_solid", C.c_uint32), ("min_trans_cov", C.c_uint32), ("use_graphs", C.c_uint32), ("autotune", C.c_uint32),
+                ("keep_sketch", C.c_uint32), ("max_wave", C.c_uint32), ("est_max_pairs", C.c_uint64),
+                ("subsample_seed", C.c_uint64), ("max_wave_bytes", C.c_uint64), ("policy", SubsamplePolicy)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("state", C.c_int32), ("subsample_reason", C.c_int32), ("fallback", C.c_int32), ("wave", C.c_int32),
+                ("subsample_factor", C.c_double), ("estimate", GenomeEstimate), ("n_keys", C.c_uint64),
+                ("n_solid", C.c_uint64), ("digest", C.c_uint64), ("pushes", C.c_uint64), ("kmers", C.c_uint64),
+                ("table_capacity", C.c_uint64), ("status", C.c_int32), ("_pad", C.c_int32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("isolates_done", C.c_uint64), ("waves", C.c_uint64), ("fallbacks", C.c_uint64),
+                ("graph_launches", C.c_uint64), ("kernel_launches", C.c_uint64), ("ms_estimate", C.c_double),
+                ("ms_phase_a", C.c_double), ("ms_phase_b", C.c_double), ("ms_host", C.c_double),
+                ("pass1_block", C.c_int32), ("pass1_grid", C.c_int32), ("pass1_rows", C.c_int32),
+                ("solid_block", C.c_int32), ("solid_grid", C.c_int32), ("solid_rows", C.c_int32),
+                ("emit_block", C.c_int32), ("emit_grid", C.c_int32), ("upsert_block", C.c_int32),
+                ("upsert_grid", C.c_int32), ("tuned", C.c_int32), ("_pad", C.c_int32), ("tune_ms", C.c_double)]
+
+
 class SynthParams(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("genome_len", C.c_uint64), ("gc", C.c_double), ("n_repeats", C.c_uint32),
                 ("repeat_len", C.c_uint32), ("repeat_identity", C.c_double), ("tandem_copies", C.c_uint32),
@@ -135,6 +164,17 @@ SIGNATURES = {
     "fbk_estimate_genome": (S, [vp, C.c_char_p, C.c_char_p, C.c_uint64, C.c_double, P(GenomeEstimate)]),
     "fbk_compute_dynamic_kmers": (C.c_int, [C.c_uint64, C.c_int64, u64p, C.c_int]),
     "fbk_subsample_mask": (S, [vp, C.c_uint64, P(Subsample), u64p]),
+    "fbk_subsample_policy_defaults": (None, [P(SubsamplePolicy)]),
+    "fbk_subsample_decide": (S, [P(SubsamplePolicy), P(GenomeEstimate), P(C.c_double), P(C.c_int32)]),
+    "fbk_batch_defaults": (None, [P(BatchParams)]),
+    "fbk_batch_create": (S, [vp, P(BatchParams), P(vp)]),
+    "fbk_batch_submit": (S, [vp, P(ArenaView), P(ArenaView), C.c_uint64, P(CountStats), u64p]),
+    "fbk_batch_run": (S, [vp]),
+    "fbk_batch_get_result": (S, [vp, C.c_uint64, P(BatchResult)]),
+    "fbk_batch_take_table": (S, [vp, C.c_uint64, P(vp)]),
+    "fbk_batch_drop": (S, [vp, C.c_uint64]),
+    "fbk_batch_get_stats": (S, [vp, P(BatchStats)]),
+    "fbk_batch_release": (S, [vp]),
     "fbk_ingest_fastq": (S, [C.c_char_p, C.c_char_p, C.c_double, C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_uint64,
                              P(vp), C.c_char_p, C.c_size_t]),
     "fbk_hbank_arena": (S, [vp, C.c_int, P(ArenaView)]),

@@ -317,6 +317,17 @@ class GenomeEstimate:
                               CONFIDENCE[e.confidence], e.u_ge_1, e.u_ge_2, e.sample_kmer_depth, e.pairs_sampled,
                               e.m_sample)
 
+    def to_c(self) -> N.GenomeEstimate:
+        e = N.GenomeEstimate()
+        for f in ("genome_size", "exact_read_pairs", "total_bases", "median_read_len", "max_read_len", "estimated_cov",
+                  "subsample_factor", "u_ge_1", "u_ge_2", "sample_kmer_depth", "pairs_sampled", "m_sample"):
+            setattr(e, f, getattr(self, f))
+        for i, k in enumerate(self.kmers[:8]):
+            e.kmers[i] = k
+        e.n_kmers = min(8, len(self.kmers))
+        e.confidence = {v: c for c, v in CONFIDENCE.items()}[self.confidence]
+        return e
+
 
 def count_fastx_exact(r1: str, r2: str) -> ExactCountStats:
     s = N.CountStats()
@@ -697,6 +708,105 @@ def canonical_kmers_arena(ctx: Context, arena: BitSeqArena, k: int, key_bits: in
     check(N.lib().fbk_canonical_kmers_arena(ctx.handle, C.byref(v), k, kb, ptr(out.reshape(-1)), ptr(rc), total,
                                             C.byref(n)), ctx.handle)
     return out[:n.value], rc[:n.value]
+
+
+# ---------------------------------------------------------------------------
+# subsampling policy and batches
+# ---------------------------------------------------------------------------
+SUBSAMPLE_REASONS = [
+    "EXPLICIT_NO_SUBSAMPLE_FLAG", "EXPLICIT_GENOME_SIZE_ZERO_INVALID", "AUTO_SUBSAMPLE_EXPLICIT_GENOME_SIZE",
+    "AUTO_SUBSAMPLE_EXPLICIT_GENOME_SIZE_WITHIN_TARGET", "AUTO_SUBSAMPLE_HIGH_CONFIDENCE",
+    "AUTO_SUBSAMPLE_HIGH_CONFIDENCE_WITHIN_TARGET", "AUTO_SUBSAMPLE_INTERCEPTED_LOW_COVERAGE_WARNING",
+    "AUTO_SUBSAMPLE_INTERCEPTED_UNRELIABLE", "GENOME_SIZE_PRIOR_PROVIDED_SUBSAMPLING_NOT_ENABLED",
+    "DISABLED_BY_DEFAULT_SAFE_FALLBACK",
+]
+
+
+def subsample_policy(no_subsample: bool = False, enable_auto_subsample: bool = False, genome_size: int | None = None,
+                     depth: float = 120.0, threshold_ratio: float = 1.5) -> N.SubsamplePolicy:
+    """The pipeline driver's subsampling options (src/main.rs:76-180, cli.rs:30-72)."""
+    p = N.SubsamplePolicy()
+    N.lib().fbk_subsample_policy_defaults(C.byref(p))
+    p.no_subsample = int(no_subsample)
+    p.enable_auto_subsample = int(enable_auto_subsample)
+    p.has_genome_size = int(genome_size is not None)
+    p.genome_size = genome_size or 0
+    p.depth = depth
+    p.threshold_ratio = threshold_ratio
+    return p
+
+
+def subsample_decide(policy: N.SubsamplePolicy, estimate: GenomeEstimate) -> tuple[float, str]:
+    """(subsample factor, reason) for an estimate, as main.rs:84-180 decides them."""
+    e = estimate.to_c()
+    f, r = C.c_double(), C.c_int32()
+    check(N.lib().fbk_subsample_decide(C.byref(policy), C.byref(e), C.byref(f), C.byref(r)), None, "subsample_decide")
+    return f.value, SUBSAMPLE_REASONS[r.value]
+
+
+def batch_params(policy: N.SubsamplePolicy | None = None, **kw) -> N.BatchParams:
+    p = N.BatchParams()
+    N.lib().fbk_batch_defaults(C.byref(p))
+    if policy is not None:
+        p.policy = policy
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class Batch:
+    """Many isolates counted together (fbk_batch_*): per isolate the estimate, the
+    subsampling decision and the build front end at one k, each phase one launch
+    over every isolate of a wave."""
+
+    def __init__(self, ctx: Context, params: N.BatchParams | None = None, **kw):
+        self.ctx = ctx
+        self.params = params if params is not None else batch_params(**kw)
+        self.key_bits = self.params.key_bits
+        self._h = C.c_void_p()
+        check(N.lib().fbk_batch_create(ctx.handle, C.byref(self.params), C.byref(self._h)), ctx.handle, "batch create")
+        ctx.adopt(self)
+
+    def submit(self, bank: ReadBank, sample: BitSeqArena, sample_pairs: int, stats: ExactCountStats) -> int:
+        views = bank.views()
+        sv = sample.view()
+        cs = stats.to_c()
+        i = C.c_uint64()
+        check(N.lib().fbk_batch_submit(self._h, views, C.byref(sv), sample_pairs, C.byref(cs), C.byref(i)),
+              self.ctx.handle, "batch submit")
+        return i.value
+
+    def run(self) -> None:
+        check(N.lib().fbk_batch_run(self._h), self.ctx.handle, "batch run")
+
+    def result(self, i: int) -> N.BatchResult:
+        r = N.BatchResult()
+        check(N.lib().fbk_batch_get_result(self._h, i, C.byref(r)), self.ctx.handle, "batch result")
+        return r
+
+    def take_table(self, i: int) -> SolidTable:
+        h = C.c_void_p()
+        check(N.lib().fbk_batch_take_table(self._h, i, C.byref(h)), self.ctx.handle, "batch take table")
+        return SolidTable(self.ctx, h, self.params.k, self.key_bits)
+
+    def drop(self, i: int) -> None:
+        check(N.lib().fbk_batch_drop(self._h, i), self.ctx.handle, "batch drop")
+
+    def stats(self) -> N.BatchStats:
+        s = N.BatchStats()
+        check(N.lib().fbk_batch_get_stats(self._h, C.byref(s)), self.ctx.handle, "batch stats")
+        return s
+
+    def release(self):
+        if self._h and self.ctx.alive:
+            N.lib().fbk_batch_release(self._h)
+        self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------

@@ -127,7 +127,7 @@ void time_begin(fbk_ctx* ctx, const char* name, TimedLaunch& t) {
     ctx->launches++;
     t.name = name;
     t.a = t.b = nullptr;
-    if (!ctx->timing) return;
+    if (!ctx->timing || ctx->capturing) return;
     for (cudaEvent_t* e : {&t.a, &t.b}) {
         if (!ctx->free_events.empty()) {
             *e = ctx->free_events.back();
@@ -202,20 +202,6 @@ double hll_estimate_from_sum(double sum, uint64_t zeros, uint32_t p) {
 
 }  // namespace fbk
 
-#define CK(ctx, call)                                         \
-    do {                                                      \
-        cudaError_t e_ = (call);                              \
-        if (e_ != cudaSuccess) return cuda_err(ctx, e_, #call); \
-    } while (0)
-
-#define TIMED(ctx, name, call)              \
-    do {                                    \
-        TimedLaunch tl_;                    \
-        time_begin(ctx, name, tl_);         \
-        cudaError_t e_ = (call);            \
-        time_end(ctx, tl_);                 \
-        if (e_ != cudaSuccess) return cuda_err(ctx, e_, name); \
-    } while (0)
 
 // ===========================================================================
 // status, context
@@ -1305,6 +1291,7 @@ FBK_API fbk_status fbk_table_export(fbk_table* t, uint64_t* keys, uint16_t* cov,
 FBK_API fbk_status fbk_table_export_acc(fbk_table* t, uint64_t* keys, uint16_t* cov, uint16_t* edges, uint64_t cap, uint64_t* n_out) {
     if (!t || !n_out) return FBK_ERR_INVALID;
     fbk_ctx* ctx = t->ctx;
+    if (!t->cnt) return set_err(ctx, FBK_ERR_INVALID, "the accumulator slots of this table were released after conversion");
     uint64_t n = std::min(cap, t->n_keys);
     uint64_t* dk = nullptr;
     uint16_t *dc = nullptr, *de = nullptr;
@@ -1466,3 +1453,21 @@ FBK_API fbk_status fbk_canonical_kmers_arena(fbk_ctx* ctx, const fbk_arena_view*
 }
 
 }  // extern "C"
+
+// Entry points of the table and pass helpers for the multi-isolate host code.
+namespace fbk {
+int key_words(uint32_t key_bits) { return nw_of(key_bits); }
+uint32_t key_k_max(uint32_t key_bits) { return max_k_of(key_bits); }
+fbk_status keep_bits_for(fbk_ctx* ctx, const fbk_bank* b, const fbk_subsample* ss, uint64_t** bits_out) {
+    return make_keep_bits(ctx, b, ss, bits_out);
+}
+TableDev tbl_dev(const fbk_table* t) { return table_dev(t); }
+fbk_status tbl_alloc(fbk_table* t, uint64_t cap, bool with_cov) { return table_alloc(t, cap, with_cov); }
+void tbl_free_storage(fbk_table* t) { table_free_storage(t); }
+void tbl_free_out(fbk_table* t) { table_free_out(t); }
+fbk_status tbl_convert(fbk_table* t) { return table_convert(t, nullptr, nullptr, nullptr, 0); }
+fbk_status solid_build(fbk_ctx* ctx, const fbk_bank* b, const fbk_cms* cms, const fbk_build_params* p, const uint64_t* keep_bits,
+                       uint64_t distinct_hint, fbk_table** out) {
+    return solid_build_impl(ctx, b, cms, p, keep_bits, nullptr, distinct_hint, out);
+}
+}  // namespace fbk

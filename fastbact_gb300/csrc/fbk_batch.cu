@@ -1,0 +1,880 @@
+// fbk_batch.cu — many isolates per launch: the counting stages of the reference
+// pipeline (src/main.rs stage 1 estimate + subsampling policy, then the build front
+// end src/graph/build.rs:84-328 at one k) for every isolate of a batch.
+//
+// Flow of fbk_batch_run:
+//   1. estimator per isolate (fbk_estimate_bank on its raw sample pairs), the
+//      subsampling policy (main.rs:76-180) and the subsampler bitmap;
+//   2. phase A for a wave of isolates: sketch clear, pass 1, solidity bitmap and
+//      the record / k-mer counts — one multi-isolate launch per step;
+//   3. the host reads each isolate's distinct-key estimate and record count and
+//      carves tables and record buckets for as many isolates as the pool holds;
+//   4. phase B per sub-wave: table init, record emit, record prefix, upsert — one
+//      multi-isolate launch each — and the SolidKmerNode conversion per isolate;
+//   5. isolates whose buckets or table overflowed are redone by the
+//      single-isolate path, which grows what overflowed.
+// Each phase can run as one CUDA graph (captured on the context's stream).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "fbk_device.cuh"
+#include "fbk_internal.h"
+
+using namespace fbk;
+
+namespace {
+
+struct BatchIso {
+    uint64_t id = 0;
+    fbk_bank* bank = nullptr;
+    fbk_bank* sample = nullptr;
+    std::vector<uint32_t> sample_len;
+    uint64_t sample_pairs = 0;
+    fbk_count_stats stats{};
+    fbk_batch_result res{};
+    uint64_t* keep = nullptr;
+    uint32_t* cnt = nullptr;
+    uint32_t* hll12 = nullptr;
+    uint32_t* bm = nullptr;
+    uint64_t distinct = 0, records = 0;
+    fbk_table* table = nullptr;
+    // phase-B storage
+    uint64_t* recs = nullptr;
+    unsigned long long* fill = nullptr;
+    BucketDev bk{};
+};
+
+struct Shape {
+    int block, grid, rows;
+};
+
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+struct fbk_batch {
+    fbk_ctx* ctx = nullptr;
+    fbk_batch_params p{};
+    int nw = 1;
+    std::vector<std::unique_ptr<BatchIso>> isos;
+    fbk_batch_stats stats{};
+    Shape pass1{256, 0, 4}, solid{256, 0, 4}, emit{256, 0, 0}, upsert{256, 0, 0};
+    bool tuned = false;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    void* h_stage = nullptr;  // pinned staging for descriptors and read-backs
+    uint64_t h_stage_bytes = 0;
+};
+
+namespace {
+
+constexpr uint32_t BATCH_STRIPES = 64;
+
+uint32_t cms_cap_of(uint32_t cbits) { return cbits == 4 ? 15u : 0xFFFFu; }
+
+void free_counting(fbk_batch* B, BatchIso* it, bool keep_sketch) {
+    fbk_ctx* ctx = B->ctx;
+    if (!keep_sketch) {
+        dev_free(ctx, it->cnt);
+        it->cnt = nullptr;
+    }
+    dev_free(ctx, it->hll12);
+    dev_free(ctx, it->bm);
+    it->hll12 = nullptr;
+    it->bm = nullptr;
+}
+
+void free_buckets(fbk_batch* B, BatchIso* it) {
+    dev_free(B->ctx, it->recs);
+    dev_free(B->ctx, it->fill);
+    it->recs = nullptr;
+    it->fill = nullptr;
+}
+
+void free_iso(fbk_batch* B, BatchIso* it) {
+    fbk_ctx* ctx = B->ctx;
+    cudaStreamSynchronize(ctx->stream);
+    free_buckets(B, it);
+    free_counting(B, it, false);
+    dev_free(ctx, it->keep);
+    it->keep = nullptr;
+    if (it->table) fbk_table_release(it->table);
+    it->table = nullptr;
+    if (it->bank) fbk_bank_release(it->bank);
+    if (it->sample) fbk_bank_release(it->sample);
+    it->bank = it->sample = nullptr;
+}
+
+fbk_status stage(fbk_batch* B, uint64_t bytes) {
+    if (bytes <= B->h_stage_bytes) return FBK_OK;
+    if (B->h_stage) cudaFreeHost(B->h_stage);
+    B->h_stage = nullptr;
+    B->h_stage_bytes = 0;
+    const uint64_t nb = std::max<uint64_t>(bytes, 1 << 20);
+    CK(B->ctx, cudaMallocHost(&B->h_stage, nb));
+    B->h_stage_bytes = nb;
+    return FBK_OK;
+}
+
+// Runs body() on the context's stream — captured as one CUDA graph when the batch
+// uses graphs — and adds the phase's device time to *ms.
+template <class F>
+fbk_status run_phase(fbk_batch* B, double* ms, F&& body) {
+    fbk_ctx* ctx = B->ctx;
+    if (!B->p.use_graphs) {
+        CK(ctx, cudaEventRecord(B->ev[0], ctx->stream));
+        fbk_status st = body();
+        if (st) return st;
+        CK(ctx, cudaEventRecord(B->ev[1], ctx->stream));
+    } else {
+        CK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        ctx->capturing = true;
+        fbk_status st = body();
+        ctx->capturing = false;
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        if (st) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return cuda_err(ctx, e, "batch phase capture");
+        cudaGraphExec_t x = nullptr;
+        e = cudaGraphInstantiate(&x, g, 0);
+        if (e == cudaSuccess) e = cudaEventRecord(B->ev[0], ctx->stream);
+        if (e == cudaSuccess) e = cudaGraphLaunch(x, ctx->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(B->ev[1], ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (x) cudaGraphExecDestroy(x);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_err(ctx, e, "batch phase graph");
+        B->stats.graph_launches++;
+    }
+    CK(ctx, cudaEventSynchronize(B->ev[1]));
+    float t = 0.f;
+    CK(ctx, cudaEventElapsedTime(&t, B->ev[0], B->ev[1]));
+    *ms += t;
+    return FBK_OK;
+}
+
+Launch shape_launch(fbk_ctx* ctx, const Shape& s) { return launch_cfg_persistent(ctx, s.block, s.grid); }
+
+// Stage 1: estimate, subsampling decision and subsampler bitmap of one isolate.
+fbk_status estimate_one(fbk_batch* B, BatchIso* it) {
+    fbk_ctx* ctx = B->ctx;
+    fbk_estimator_params ep;
+    fbk_estimator_defaults(&ep);
+    ep.max_pairs = B->p.est_max_pairs;
+    ep.target_cov = B->p.policy.depth;
+    fbk_status st = fbk_estimate_bank(ctx, it->sample, it->sample_len.data(), it->sample_pairs, &it->stats, &ep,
+                                      &it->res.estimate, nullptr, nullptr);
+    if (st) return st;
+    st = fbk_subsample_decide(&B->p.policy, &it->res.estimate, &it->res.subsample_factor, &it->res.subsample_reason);
+    if (st) return set_err(ctx, st, "invalid subsampling policy");
+    fbk_subsample ss{it->res.subsample_factor, B->p.subsample_seed};
+    st = keep_bits_for(ctx, it->bank, &ss, &it->keep);
+    if (st) return st;
+    // the estimator's sample is no longer needed
+    fbk_bank_release(it->sample);
+    it->sample = nullptr;
+    it->res.state = 1;
+    return FBK_OK;
+}
+
+IsoDev iso_dev(const fbk_batch* B, const BatchIso* it, unsigned long long* nrec, uint32_t* status) {
+    IsoDev d{};
+    d.b = bank_view(it->bank, 0, it->bank->n_reads, it->keep);
+    d.cnt = it->cnt;
+    d.hll12 = it->hll12;
+    d.bm = it->bm;
+    d.n_records = nrec;
+    d.log2w = B->p.cms_log2_width;
+    d.t_solid = B->p.t_solid;
+    d.cap = cms_cap_of(B->p.counter_bits);
+    d.status = status;
+    if (it->table) d.t = tbl_dev(it->table);
+    d.bk = it->bk;
+    return d;
+}
+
+// Per-wave device scratch: descriptors, read bases, counters.
+struct WaveBufs {
+    fbk_ctx* ctx = nullptr;
+    IsoDev* iso = nullptr;
+    unsigned long long* rb = nullptr;
+    unsigned long long* cnt = nullptr;   // 8 per isolate: [0..2] record/k-mer counts, [3..7] conversion counts
+    uint32_t* status = nullptr;          // 2 per isolate: status bits, bucket overflow
+    unsigned long long* unit_pre = nullptr;
+    unsigned long long* stripe_pre = nullptr;
+    ~WaveBufs() {
+        if (!ctx) return;
+        cudaStreamSynchronize(ctx->stream);
+        dev_free(ctx, iso);
+        dev_free(ctx, rb);
+        dev_free(ctx, cnt);
+        dev_free(ctx, status);
+        dev_free(ctx, unit_pre);
+        dev_free(ctx, stripe_pre);
+    }
+};
+
+fbk_status wave_bufs(fbk_batch* B, uint32_t n, bool phase_b, WaveBufs& w) {
+    fbk_ctx* ctx = B->ctx;
+    w.ctx = ctx;
+    w.iso = (IsoDev*)dev_alloc(ctx, n * sizeof(IsoDev));
+    w.rb = (unsigned long long*)dev_alloc(ctx, (n + 1) * 8);
+    w.cnt = (unsigned long long*)dev_alloc(ctx, (uint64_t)n * 8 * 8);
+    w.status = (uint32_t*)dev_alloc(ctx, (uint64_t)n * 2 * 4);
+    if (phase_b) {
+        w.unit_pre = (unsigned long long*)dev_alloc(ctx, ((uint64_t)n * 64 + 1) * 8);
+        w.stripe_pre = (unsigned long long*)dev_alloc(ctx, (uint64_t)n * 64 * (BATCH_STRIPES + 1) * 8);
+    }
+    if (!w.iso || !w.rb || !w.cnt || !w.status || (phase_b && (!w.unit_pre || !w.stripe_pre)))
+        return set_err(ctx, FBK_ERR_OOM, "batch wave descriptors");
+    return FBK_OK;
+}
+
+// Copies descriptors and read bases of a wave to the device (before any capture).
+fbk_status upload_wave(fbk_batch* B, const std::vector<BatchIso*>& W, WaveBufs& w) {
+    fbk_ctx* ctx = B->ctx;
+    const uint32_t n = (uint32_t)W.size();
+    fbk_status st = stage(B, n * sizeof(IsoDev) + (n + 1) * 8);
+    if (st) return st;
+    IsoDev* hd = (IsoDev*)B->h_stage;
+    unsigned long long* hb = (unsigned long long*)((char*)B->h_stage + n * sizeof(IsoDev));
+    hb[0] = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        hd[i] = iso_dev(B, W[i], w.cnt + 8 * i, w.status + 2 * i);
+        hd[i].bk.overflow = w.status + 2 * i + 1;
+        hb[i + 1] = hb[i] + W[i]->bank->n_reads;
+    }
+    CK(ctx, cudaMemcpyAsync(w.iso, hd, n * sizeof(IsoDev), cudaMemcpyHostToDevice, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(w.rb, hb, (n + 1) * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));  // the staging buffer is reused next
+    return FBK_OK;
+}
+
+uint64_t phase_a_bytes(const fbk_batch* B, const BatchIso* it) {
+    return (4ULL << B->p.cms_log2_width) * 4 + 4096 * 4 + (it->bank->n_words + 9) * 4 + 4096;
+}
+
+// Autotuner: times candidate launch shapes of the pass-1 and solidity kernels on one
+// isolate (its own sketch and bitmap as scratch) and keeps the fastest.
+fbk_status autotune(fbk_batch* B, BatchIso* it) {
+    fbk_ctx* ctx = B->ctx;
+    const double t0 = now_ms();
+    WaveBufs w;
+    fbk_status st = wave_bufs(B, 1, false, w);
+    if (st) return st;
+    std::vector<BatchIso*> one{it};
+    st = upload_wave(B, one, w);
+    if (st) return st;
+    const uint64_t cms_bytes = (4ULL << B->p.cms_log2_width) * 4;
+    const int blocks[] = {128, 256};
+    const int per_sm[] = {0, 2, 4};
+    const int rows[] = {4, 2, 1};
+    auto timed = [&](auto&& launch, float* ms) -> fbk_status {
+        CK(ctx, cudaEventRecord(B->ev[0], ctx->stream));
+        fbk_status s2 = launch();
+        if (s2) return s2;
+        CK(ctx, cudaEventRecord(B->ev[1], ctx->stream));
+        CK(ctx, cudaEventSynchronize(B->ev[1]));
+        CK(ctx, cudaEventElapsedTime(ms, B->ev[0], B->ev[1]));
+        return FBK_OK;
+    };
+    float best = 1e30f;
+    Shape best1 = B->pass1;
+    for (int rp : rows)
+        for (int bl : blocks)
+            for (int ps : per_sm) {
+                Shape s{bl, ps ? ps * ctx->num_sms : 0, rp};
+                CK(ctx, cudaMemsetAsync(it->cnt, 0, cms_bytes, ctx->stream));
+                float ms = 0;
+                st = timed([&]() -> fbk_status {
+                    for (uint32_t r = 0; r < 4; r += (uint32_t)rp)
+                        TIMED(ctx, "tune_pass1", launch_batch_pass1(B->nw, shape_launch(ctx, s), w.iso, w.rb, 1, B->p.k, r, r + rp, 0));
+                    return FBK_OK;
+                }, &ms);
+                if (st) return st;
+                if (ms < best) {
+                    best = ms;
+                    best1 = s;
+                }
+            }
+    // the sketch now holds the isolate's full counts: tune the solidity sweep on it
+    const uint64_t bm_bytes = (it->bank->n_words + 9) * 4;
+    best = 1e30f;
+    Shape best2 = B->solid;
+    for (int rp : rows)
+        for (int bl : blocks)
+            for (int ps : per_sm) {
+                Shape s{bl, ps ? ps * ctx->num_sms : 0, rp};
+                CK(ctx, cudaMemsetAsync(it->bm, 0xFF, bm_bytes, ctx->stream));
+                float ms = 0;
+                st = timed([&]() -> fbk_status {
+                    for (uint32_t r = 0; r < 4; r += (uint32_t)rp)
+                        TIMED(ctx, "tune_solid", launch_batch_solid(B->nw, shape_launch(ctx, s), w.iso, w.rb, 1, B->p.k, r, r + rp));
+                    return FBK_OK;
+                }, &ms);
+                if (st) return st;
+                if (ms < best) {
+                    best = ms;
+                    best2 = s;
+                }
+            }
+    B->pass1 = best1;
+    B->solid = best2;
+    B->tuned = true;
+    B->stats.tuned = 1;
+    B->stats.tune_ms += now_ms() - t0;
+    return FBK_OK;
+}
+
+// Phase A of a wave: pass 1, solidity bitmap, counts; then the host reads each
+// isolate's distinct-key estimate and record count.
+fbk_status phase_a(fbk_batch* B, const std::vector<BatchIso*>& W) {
+    fbk_ctx* ctx = B->ctx;
+    const uint32_t n = (uint32_t)W.size();
+    const uint64_t cms_bytes = (4ULL << B->p.cms_log2_width) * 4;
+    for (BatchIso* it : W) {
+        it->cnt = (uint32_t*)dev_alloc(ctx, cms_bytes);
+        it->hll12 = (uint32_t*)dev_alloc(ctx, 4096 * 4);
+        it->bm = (uint32_t*)dev_alloc(ctx, (it->bank->n_words + 9) * 4);
+        if (!it->cnt || !it->hll12 || !it->bm) return set_err(ctx, FBK_ERR_OOM, "batch sketches");
+    }
+    if (B->p.autotune && !B->tuned) {
+        BatchIso* big = *std::max_element(W.begin(), W.end(), [](const BatchIso* a, const BatchIso* b) {
+            return a->bank->n_bases < b->bank->n_bases;
+        });
+        fbk_status st = autotune(B, big);
+        if (st) return st;
+    }
+    WaveBufs w;
+    fbk_status st = wave_bufs(B, n, false, w);
+    if (st) return st;
+    st = upload_wave(B, W, w);
+    if (st) return st;
+    const uint32_t k = B->p.k;
+    st = run_phase(B, &B->stats.ms_phase_a, [&]() -> fbk_status {
+        for (BatchIso* it : W) {
+            CK(ctx, cudaMemsetAsync(it->cnt, 0, cms_bytes, ctx->stream));
+            CK(ctx, cudaMemsetAsync(it->hll12, 0, 4096 * 4, ctx->stream));
+            CK(ctx, cudaMemsetAsync(it->bm, 0xFF, (it->bank->n_words + 9) * 4, ctx->stream));
+        }
+        CK(ctx, cudaMemsetAsync(w.cnt, 0, (uint64_t)n * 64, ctx->stream));
+        CK(ctx, cudaMemsetAsync(w.status, 0, (uint64_t)n * 8, ctx->stream));
+        for (uint32_t r = 0; r < 4; r += (uint32_t)B->pass1.rows)
+            TIMED(ctx, "batch_pass1", launch_batch_pass1(B->nw, shape_launch(ctx, B->pass1), w.iso, w.rb, n, k, r,
+                                                         r + (uint32_t)B->pass1.rows, r == 0));
+        for (uint32_t r = 0; r < 4; r += (uint32_t)B->solid.rows)
+            TIMED(ctx, "batch_solid", launch_batch_solid(B->nw, shape_launch(ctx, B->solid), w.iso, w.rb, n, k, r,
+                                                         r + (uint32_t)B->solid.rows));
+        TIMED(ctx, "batch_count", launch_batch_count(shape_launch(ctx, B->solid), w.iso, w.rb, n, k));
+        return FBK_OK;
+    });
+    if (st) return st;
+    // read back the HyperLogLog registers and counts
+    const double h0 = now_ms();
+    st = stage(B, (uint64_t)n * (4096 * 4 + 64));
+    if (st) return st;
+    uint32_t* hr = (uint32_t*)B->h_stage;
+    unsigned long long* hc = (unsigned long long*)(hr + (uint64_t)n * 4096);
+    for (uint32_t i = 0; i < n; ++i)
+        CK(ctx, cudaMemcpyAsync(hr + (uint64_t)i * 4096, W[i]->hll12, 4096 * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(hc, w.cnt, (uint64_t)n * 64, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    for (uint32_t i = 0; i < n; ++i) {
+        BatchIso* it = W[i];
+        double sum = 0.0;
+        uint64_t zeros = 0;
+        for (int j = 0; j < 4096; ++j) {
+            const uint32_t v = hr[(uint64_t)i * 4096 + j];
+            sum += std::ldexp(1.0, -(int)v);
+            zeros += v == 0;
+        }
+        it->distinct = (uint64_t)(hll_estimate_from_sum(sum, zeros, 12) * 1.05) + 1024;
+        it->records = hc[8 * i];
+        it->res.kmers = hc[8 * i + 1] + hc[8 * i + 2];
+        it->res.state = 2;
+    }
+    B->stats.ms_host += now_ms() - h0;
+    return FBK_OK;
+}
+
+uint64_t slot_bytes_of(int nw) { return 8ULL * nw + (nw > 2 ? 8 : 0) + 32; }
+
+// Table capacity, bucket geometry and device bytes of phase B for one isolate.
+struct PlanB {
+    uint64_t cap, out_cap, per_stripe, bytes;
+    uint32_t shift, n_buckets;
+};
+
+PlanB plan_b(const fbk_batch* B, const BatchIso* it) {
+    const fbk_ctx* ctx = B->ctx;
+    PlanB q;
+    q.cap = std::max<uint64_t>(1024, (uint64_t)((double)it->distinct / ctx->load_factor) + 1024);
+    q.out_cap = std::min<uint64_t>(q.cap, (uint64_t)(1.1 * (double)it->distinct) + 4096);
+    const uint64_t sb = slot_bytes_of(B->nw);
+    uint32_t shift = 0;
+    while (shift < 40 && (2ULL << shift) * sb <= ctx->bucket_bytes) ++shift;
+    while (((q.cap + (1ULL << shift) - 1) >> shift) > 64) ++shift;
+    q.shift = shift;
+    q.n_buckets = (uint32_t)((q.cap + (1ULL << shift) - 1) >> shift);
+    q.per_stripe = (uint64_t)(1.15 * (double)it->records / ((double)q.n_buckets * BATCH_STRIPES)) + 2048;
+    q.bytes = q.cap * sb + q.out_cap * (8ULL * B->nw + 3) + (uint64_t)q.n_buckets * BATCH_STRIPES * (q.per_stripe * 8 * (B->nw + 1) + 8) +
+              8192;
+    return q;
+}
+
+// Allocates an isolate's table, output rows and record buckets.
+fbk_status alloc_b(fbk_batch* B, BatchIso* it, const PlanB& q) {
+    fbk_ctx* ctx = B->ctx;
+    fbk_table* t = new fbk_table();
+    t->ctx = ctx;
+    t->nw = (uint32_t)B->nw;
+    t->k = B->p.k;
+    t->min_trans_cov = B->p.min_trans_cov;
+    it->table = t;
+    t->cap = q.cap;
+    t->keys = (uint64_t*)dev_alloc(ctx, q.cap * 8 * t->nw);
+    if (t->nw > 2) t->tags = (uint64_t*)dev_alloc(ctx, q.cap * 8);
+    t->cnt = (uint32_t*)dev_alloc(ctx, q.cap * 32);
+    t->out_keys = (uint64_t*)dev_alloc(ctx, q.out_cap * 8 * t->nw);
+    t->out_cov = (uint16_t*)dev_alloc(ctx, q.out_cap * 2);
+    t->out_mask = (uint8_t*)dev_alloc(ctx, q.out_cap);
+    t->out_cap = q.out_cap;
+    it->recs = (uint64_t*)dev_alloc(ctx, (uint64_t)q.n_buckets * BATCH_STRIPES * q.per_stripe * 8 * (B->nw + 1));
+    it->fill = (unsigned long long*)dev_alloc(ctx, (uint64_t)q.n_buckets * BATCH_STRIPES * 8);
+    if (!t->keys || (t->nw > 2 && !t->tags) || !t->cnt || !t->out_keys || !t->out_cov || !t->out_mask || !it->recs || !it->fill)
+        return set_err(ctx, FBK_ERR_OOM, "batch table");
+    it->bk = BucketDev{};
+    it->bk.recs = it->recs;
+    it->bk.fill = it->fill;
+    it->bk.stripe_cap = q.per_stripe;
+    it->bk.shift = q.shift;
+    it->bk.n_buckets = q.n_buckets;
+    it->bk.stripes = BATCH_STRIPES;
+    return FBK_OK;
+}
+
+void release_b(fbk_batch* B, BatchIso* it) {
+    free_buckets(B, it);
+    if (it->table) fbk_table_release(it->table);
+    it->table = nullptr;
+}
+
+void finish_iso(fbk_batch* B, BatchIso* it);
+
+// The single-isolate path for an isolate whose wave buckets or table overflowed.
+fbk_status fallback(fbk_batch* B, BatchIso* it) {
+    fbk_ctx* ctx = B->ctx;
+    release_b(B, it);
+    fbk_cms view;
+    view.ctx = ctx;
+    view.cnt = it->cnt;
+    view.log2w = B->p.cms_log2_width;
+    view.cbits = B->p.counter_bits;
+    view.n = 4ULL << view.log2w;
+    fbk_build_params bp{};
+    bp.k = B->p.k;
+    bp.key_bits = B->p.key_bits;
+    bp.cms_log2_width = B->p.cms_log2_width;
+    bp.counter_bits = B->p.counter_bits;
+    bp.t_solid = B->p.t_solid;
+    bp.min_trans_cov = B->p.min_trans_cov;
+    fbk_status st = solid_build(ctx, it->bank, &view, &bp, it->keep, it->distinct * 2, &it->table);
+    view.cnt = nullptr;
+    if (st) return st;
+    it->res.fallback = 1;
+    B->stats.fallbacks++;
+    return FBK_OK;
+}
+
+// Phase B of a sub-wave: tables, emit, prefix, upsert, conversion; then per-isolate
+// checks and clean-up.
+fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
+    fbk_ctx* ctx = B->ctx;
+    const uint32_t n = (uint32_t)V.size();
+    WaveBufs w;
+    fbk_status st = wave_bufs(B, n, true, w);
+    if (st) return st;
+    st = upload_wave(B, V, w);
+    if (st) return st;
+    const uint32_t k = B->p.k;
+    st = run_phase(B, &B->stats.ms_phase_b, [&]() -> fbk_status {
+        CK(ctx, cudaMemsetAsync(w.cnt, 0, (uint64_t)n * 64, ctx->stream));
+        CK(ctx, cudaMemsetAsync(w.status, 0, (uint64_t)n * 8, ctx->stream));
+        for (BatchIso* it : V) {
+            TIMED(ctx, "table_init", launch_table_init(B->nw, launch_cfg(ctx, 256, 0), tbl_dev(it->table)));
+            CK(ctx, cudaMemsetAsync(it->table->cnt, 0, it->table->cap * 32, ctx->stream));
+            CK(ctx, cudaMemsetAsync(it->fill, 0, (uint64_t)it->bk.n_buckets * BATCH_STRIPES * 8, ctx->stream));
+        }
+        TIMED(ctx, "batch_emit", launch_batch_emit(B->nw, shape_launch(ctx, B->emit), w.iso, w.rb, n, k, BATCH_STRIPES));
+        TIMED(ctx, "batch_prefix", launch_batch_prefix(launch_cfg(ctx, 1024, 1), w.iso, n, BATCH_STRIPES, w.unit_pre, w.stripe_pre));
+        TIMED(ctx, "batch_upsert", launch_batch_upsert(B->nw, shape_launch(ctx, B->upsert), w.iso, n, BATCH_STRIPES, w.unit_pre,
+                                                       w.stripe_pre));
+        for (uint32_t i = 0; i < n; ++i) {
+            fbk_table* t = V[i]->table;
+            ConvOut o{};
+            o.keys = t->out_keys;
+            o.cov = t->out_cov;
+            o.mask = t->out_mask;
+            o.cap_solid = t->out_cap;
+            o.counts = w.cnt + 8 * i + 3;
+            TIMED(ctx, "convert", launch_convert(B->nw, launch_cfg(ctx, 256, 0), tbl_dev(t), t->min_trans_cov, o));
+        }
+        return FBK_OK;
+    });
+    if (st) return st;
+    st = stage(B, (uint64_t)n * 72);
+    if (st) return st;
+    unsigned long long* hc = (unsigned long long*)B->h_stage;
+    uint32_t* hs = (uint32_t*)(hc + 8ULL * n);
+    CK(ctx, cudaMemcpyAsync(hc, w.cnt, (uint64_t)n * 64, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(hs, w.status, (uint64_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<unsigned long long> counts(hc, hc + 8ULL * n);
+    std::vector<uint32_t> stat(hs, hs + 2ULL * n);
+    for (uint32_t i = 0; i < n; ++i) {
+        BatchIso* it = V[i];
+        const uint32_t bits = stat[2 * i], ovf = stat[2 * i + 1];
+        if (bits & ST_SPIN_TIMEOUT) {
+            release_b(B, it);
+            return set_err(ctx, FBK_ERR_TIMEOUT, "batch: a bounded wait for a key publication gave up");
+        }
+        if ((bits & ST_TABLE_FULL) || ovf) {
+            st = fallback(B, it);
+            if (st) return st;
+        } else {
+            fbk_table* t = it->table;
+            t->n_keys = counts[8 * i + 3];
+            t->n_solid = counts[8 * i + 4];
+            t->digest = counts[8 * i + 5];
+            t->pushes = counts[8 * i + 6];
+            free_buckets(B, it);
+            if (t->n_solid > t->out_cap) {
+                st = tbl_convert(t);
+                if (st) return st;
+            }
+        }
+        finish_iso(B, it);
+    }
+    return FBK_OK;
+}
+
+// Records the finished table of an isolate in its result and frees what the table
+// no longer needs.
+void finish_iso(fbk_batch* B, BatchIso* it) {
+    fbk_table* t = it->table;
+    tbl_free_storage(t);  // the accumulator slots are not needed once the rows are converted
+    it->res.n_keys = t->n_keys;
+    it->res.n_solid = t->n_solid;
+    it->res.digest = t->digest;
+    it->res.pushes = t->pushes;
+    it->res.table_capacity = t->cap;
+    free_counting(B, it, B->p.keep_sketch != 0);
+    dev_free(B->ctx, it->keep);
+    it->keep = nullptr;
+    it->res.state = 3;
+    B->stats.isolates_done++;
+}
+
+// Phase B for isolates whose phase A is done, in sub-waves that fit the free pool
+// memory; an isolate that does not fit even alone takes the single-isolate path.
+fbk_status drain_b(fbk_batch* B, const std::vector<BatchIso*>& W) {
+    fbk_ctx* ctx = B->ctx;
+    const uint32_t max_wave = std::max<uint32_t>(1, std::min<uint32_t>(BATCH_MAX_ISO, B->p.max_wave ? B->p.max_wave : 64));
+    size_t j = 0;
+    fbk_status st = FBK_OK;
+    while (j < W.size()) {
+        const double h0 = now_ms();
+        uint64_t free_b = 0, largest = 0;
+        fbk_ctx_pool_free(ctx, &free_b, &largest);
+        if (B->p.max_wave_bytes) free_b = std::min(free_b, B->p.max_wave_bytes);
+        std::vector<BatchIso*> V;
+        uint64_t bytes = 0;
+        while (j < W.size() && V.size() < max_wave) {
+            const PlanB q = plan_b(B, W[j]);
+            if (!V.empty() && bytes + q.bytes + (64ULL << 20) > free_b) break;
+            st = alloc_b(B, W[j], q);
+            if (st) {
+                release_b(B, W[j]);
+                ctx->err.clear();
+                if (!V.empty()) break;
+                st = fallback(B, W[j]);
+                if (st) break;
+                finish_iso(B, W[j]);
+                ++j;
+                continue;
+            }
+            bytes += q.bytes;
+            V.push_back(W[j++]);
+        }
+        B->stats.ms_host += now_ms() - h0;
+        if (st == FBK_OK && !V.empty()) st = phase_b(B, V);
+        if (st) {
+            for (BatchIso* it : W) {
+                if (it->res.state == 3) continue;
+                release_b(B, it);
+                free_counting(B, it, false);
+                it->res.state = -1;
+                it->res.status = st;
+            }
+            return st;
+        }
+    }
+    return FBK_OK;
+}
+
+fbk_status run_impl(fbk_batch* B) {
+    fbk_ctx* ctx = B->ctx;
+    CK(ctx, cudaSetDevice(ctx->device));
+    // stage 1: estimates
+    for (auto& up : B->isos) {
+        BatchIso* it = up.get();
+        if (it->res.state != 0) continue;
+        CK(ctx, cudaEventRecord(B->ev[0], ctx->stream));
+        fbk_status st = estimate_one(B, it);
+        if (st) {
+            it->res.state = -1;
+            it->res.status = st;
+            continue;
+        }
+        CK(ctx, cudaEventRecord(B->ev[1], ctx->stream));
+        CK(ctx, cudaEventSynchronize(B->ev[1]));
+        float t = 0.f;
+        cudaEventElapsedTime(&t, B->ev[0], B->ev[1]);
+        B->stats.ms_estimate += t;
+    }
+    std::vector<BatchIso*> todo;
+    for (auto& up : B->isos)
+        if (up->res.state == 1) todo.push_back(up.get());
+    const uint32_t max_wave = std::max<uint32_t>(1, std::min<uint32_t>(BATCH_MAX_ISO, B->p.max_wave ? B->p.max_wave : 64));
+    size_t next = 0;
+    while (next < todo.size()) {
+        // phase-A wave: isolates whose sketches and bitmaps fill at most half of the
+        // free pool memory; the rest is left for phase-B tables and record buckets
+        uint64_t free_b = 0, largest = 0;
+        fbk_ctx_pool_free(ctx, &free_b, &largest);
+        if (B->p.max_wave_bytes) free_b = std::min(free_b, B->p.max_wave_bytes);
+        std::vector<BatchIso*> W;
+        uint64_t used = 0;
+        while (next < todo.size() && W.size() < max_wave) {
+            const uint64_t need = phase_a_bytes(B, todo[next]);
+            if (!W.empty() && (used + need) * 2 > free_b) break;
+            W.push_back(todo[next++]);
+            used += need;
+        }
+        const uint32_t wave_no = (uint32_t)B->stats.waves;
+        for (BatchIso* it : W) it->res.wave = (int32_t)wave_no;
+        fbk_status st = phase_a(B, W);
+        if (st) {
+            for (BatchIso* it : W) {
+                free_counting(B, it, false);
+                it->res.state = -1;
+                it->res.status = st;
+            }
+            return st;
+        }
+        B->stats.waves++;
+        st = drain_b(B, W);
+        if (st) return st;
+    }
+    return FBK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+FBK_API void fbk_subsample_policy_defaults(fbk_subsample_policy* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->depth = 120.0;
+    p->threshold_ratio = 1.5;
+}
+
+// src/main.rs:76-180, branch for branch.
+FBK_API fbk_status fbk_subsample_decide(const fbk_subsample_policy* p, const fbk_genome_estimate* e, double* factor,
+                                        int32_t* reason) {
+    if (!p || !e || !factor) return FBK_ERR_INVALID;
+    if (!std::isfinite(p->threshold_ratio) || p->threshold_ratio < 1.0) return FBK_ERR_INVALID;
+    const double trigger_mult = p->threshold_ratio;
+    double f = 1.0;
+    int32_t why;
+    if (p->no_subsample) {
+        why = 0;
+    } else if (p->enable_auto_subsample) {
+        if (p->has_genome_size) {
+            if (p->genome_size == 0) {
+                why = 1;
+            } else {
+                const double explicit_cov = (double)e->total_bases / (double)p->genome_size;
+                const double trigger_cov = trigger_mult * p->depth;
+                if (p->depth > 0.0 && explicit_cov > trigger_cov) {
+                    f = std::min(1.0, std::max(0.01, p->depth / explicit_cov));
+                    why = 2;
+                } else {
+                    why = 3;
+                }
+            }
+        } else if (e->confidence == 0) {
+            const double est_cov = e->estimated_cov;
+            const double trigger_cov = trigger_mult * p->depth;
+            if (p->depth > 0.0 && est_cov > trigger_cov) {
+                f = std::min(1.0, std::max(0.01, p->depth / est_cov));
+                why = 4;
+            } else {
+                why = 5;
+            }
+        } else if (e->confidence == 1) {
+            why = 6;
+        } else {
+            why = 7;
+        }
+    } else if (p->has_genome_size) {
+        why = 8;
+    } else {
+        why = 9;
+    }
+    *factor = f;
+    if (reason) *reason = why;
+    return FBK_OK;
+}
+
+FBK_API void fbk_batch_defaults(fbk_batch_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->k = 31;
+    p->key_bits = 64;
+    p->cms_log2_width = 22;
+    p->counter_bits = 16;
+    p->t_solid = 2;
+    p->min_trans_cov = 3;
+    p->use_graphs = 1;
+    p->autotune = 1;
+    p->max_wave = 64;
+    p->est_max_pairs = 250000;
+    fbk_subsample_policy_defaults(&p->policy);
+}
+
+FBK_API fbk_status fbk_batch_create(fbk_ctx* ctx, const fbk_batch_params* p, fbk_batch** out) {
+    if (!ctx || !p || !out) return FBK_ERR_INVALID;
+    *out = nullptr;
+    const int nw = key_words(p->key_bits);
+    if (!nw || p->k < 1 || p->k > key_k_max(p->key_bits)) return set_err(ctx, FBK_ERR_INVALID, "batch: k out of range for key_bits");
+    if (p->cms_log2_width < 10 || p->cms_log2_width > 28) return set_err(ctx, FBK_ERR_INVALID, "batch: cms_log2_width out of range");
+    if (p->counter_bits != 4 && p->counter_bits != 16) return set_err(ctx, FBK_ERR_INVALID, "batch: counter_bits must be 4 or 16");
+    if (p->t_solid > 0xFFFF || p->min_trans_cov > 0xFFFF) return set_err(ctx, FBK_ERR_INVALID, "batch: thresholds must fit u16");
+    if (p->max_wave > BATCH_MAX_ISO) return set_err(ctx, FBK_ERR_INVALID, "batch: max_wave above 256");
+    if (!std::isfinite(p->policy.threshold_ratio) || p->policy.threshold_ratio < 1.0)
+        return set_err(ctx, FBK_ERR_INVALID, "Invalid --subsample-threshold-ratio: must be a finite float >= 1.0");
+    fbk_batch* B = new fbk_batch();
+    B->ctx = ctx;
+    B->p = *p;
+    B->nw = nw;
+    B->pass1 = {ctx->block_pass1, ctx->grid_pass1, 4};
+    B->solid = {ctx->block_pass2, ctx->grid_pass2, 4};
+    B->emit = {ctx->block_pass2, ctx->grid_pass2, 0};
+    B->upsert = {ctx->block_pass2, ctx->grid_pass2, 0};
+    // whole rows per sweep while they fit the context's sweep size
+    const uint64_t row_bytes = (1ULL << p->cms_log2_width) * 4;
+    const int rows = ctx->sweep_bytes >= 4 * row_bytes ? 4 : ctx->sweep_bytes >= 2 * row_bytes ? 2 : 1;
+    B->pass1.rows = B->solid.rows = rows;
+    cudaSetDevice(ctx->device);
+    if (cudaEventCreate(&B->ev[0]) != cudaSuccess || cudaEventCreate(&B->ev[1]) != cudaSuccess) {
+        fbk_batch_release(B);
+        return set_err(ctx, FBK_ERR_CUDA, "batch events");
+    }
+    *out = B;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_batch_submit(fbk_batch* B, const fbk_arena_view bank[3], const fbk_arena_view* sample, uint64_t sample_pairs,
+                                    const fbk_count_stats* stats, uint64_t* id) {
+    if (!B || !bank || !sample || !stats) return FBK_ERR_INVALID;
+    fbk_ctx* ctx = B->ctx;
+    CK(ctx, cudaSetDevice(ctx->device));
+    if (sample->n_seqs < 2 * sample_pairs) return set_err(ctx, FBK_ERR_INVALID, "sample holds fewer than 2*sample_pairs reads");
+    auto it = std::make_unique<BatchIso>();
+    it->id = B->isos.size();
+    it->stats = *stats;
+    it->sample_pairs = sample_pairs;
+    it->sample_len.assign(sample->lengths, sample->lengths + 2 * sample_pairs);
+    fbk_status st = bank_upload_impl(ctx, bank, 3, &it->bank);
+    if (st) return st;
+    if (it->bank->n_bases >= (1ULL << 31)) {
+        fbk_bank_release(it->bank);
+        return set_err(ctx, FBK_ERR_INVALID, "batch: an isolate of 2^31 bases or more takes the single-isolate path");
+    }
+    fbk_arena_view v = *sample;
+    v.n_seqs = 2 * sample_pairs;
+    v.pair_idx = nullptr;
+    st = bank_upload_impl(ctx, &v, 1, &it->sample);
+    if (st) {
+        fbk_bank_release(it->bank);
+        return st;
+    }
+    if (id) *id = it->id;
+    B->isos.push_back(std::move(it));
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_batch_run(fbk_batch* B) {
+    if (!B) return FBK_ERR_INVALID;
+    return run_impl(B);
+}
+
+FBK_API fbk_status fbk_batch_get_result(const fbk_batch* B, uint64_t id, fbk_batch_result* out) {
+    if (!B || !out || id >= B->isos.size()) return FBK_ERR_INVALID;
+    *out = B->isos[id]->res;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_batch_take_table(fbk_batch* B, uint64_t id, fbk_table** out) {
+    if (!B || !out || id >= B->isos.size()) return FBK_ERR_INVALID;
+    BatchIso* it = B->isos[id].get();
+    if (it->res.state != 3 || !it->table) return set_err(B->ctx, FBK_ERR_INVALID, "batch: isolate has no table to take");
+    *out = it->table;
+    it->table = nullptr;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_batch_drop(fbk_batch* B, uint64_t id) {
+    if (!B || id >= B->isos.size()) return FBK_ERR_INVALID;
+    free_iso(B, B->isos[id].get());
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_batch_get_stats(const fbk_batch* B, fbk_batch_stats* out) {
+    if (!B || !out) return FBK_ERR_INVALID;
+    *out = B->stats;
+    out->pass1_block = B->pass1.block;
+    out->pass1_grid = B->pass1.grid;
+    out->pass1_rows = B->pass1.rows;
+    out->solid_block = B->solid.block;
+    out->solid_grid = B->solid.grid;
+    out->solid_rows = B->solid.rows;
+    out->emit_block = B->emit.block;
+    out->emit_grid = B->emit.grid;
+    out->upsert_block = B->upsert.block;
+    out->upsert_grid = B->upsert.grid;
+    out->kernel_launches = B->ctx->launches;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_batch_release(fbk_batch* B) {
+    if (!B) return FBK_OK;
+    for (auto& up : B->isos) free_iso(B, up.get());
+    for (cudaEvent_t e : B->ev)
+        if (e) cudaEventDestroy(e);
+    if (B->h_stage) cudaFreeHost(B->h_stage);
+    delete B;
+    return FBK_OK;
+}
+
+}  // extern "C"

@@ -70,6 +70,7 @@ struct fbk_ctx {
     double load_factor = 0.62;            // solid table keys / slots when sized from the estimate
     int pass2_mode = 1;                   // 1 = record buckets, 0 = direct sweep
     double record_factor = 1.25;          // bucket capacity / expected records per stripe
+    bool capturing = false;               // launches are being captured into a CUDA graph
 };
 
 struct fbk_bank {
@@ -147,8 +148,35 @@ fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_ar
                             uint64_t chunk_bases = 1ull << 30);
 BankDev bank_view(const fbk_bank* b, uint64_t r_begin, uint64_t r_end, const uint64_t* keep_bits);
 
+// Single-isolate pieces reused by the multi-isolate host code (fbk_api.cu).
+int key_words(uint32_t key_bits);     // 64 -> 1, 128 -> 2, 256 -> 4, else 0
+uint32_t key_k_max(uint32_t key_bits);
+fbk_status keep_bits_for(fbk_ctx* ctx, const fbk_bank* b, const fbk_subsample* ss, uint64_t** bits_out);
+TableDev tbl_dev(const fbk_table* t);
+fbk_status tbl_alloc(fbk_table* t, uint64_t cap, bool with_cov);
+void tbl_free_storage(fbk_table* t);
+void tbl_free_out(fbk_table* t);
+fbk_status tbl_convert(fbk_table* t);  // conversion, growing the output when it was too small
+fbk_status solid_build(fbk_ctx* ctx, const fbk_bank* b, const fbk_cms* cms, const fbk_build_params* p, const uint64_t* keep_bits,
+                       uint64_t distinct_hint, fbk_table** out);
+
 // host f64 HyperLogLog::estimate from the register sum and zero count (sketch.rs:83-114)
 double hll_estimate_from_sum(double sum, uint64_t zeros, uint32_t p);
 uint64_t f64_to_u64_sat(double x);
 
 }  // namespace fbk
+
+#define CK(ctx, call)                                               \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return fbk::cuda_err(ctx, e_, #call); \
+    } while (0)
+
+#define TIMED(ctx, name, call)                                      \
+    do {                                                            \
+        fbk::TimedLaunch tl_;                                       \
+        fbk::time_begin(ctx, name, tl_);                            \
+        cudaError_t e_ = (call);                                    \
+        fbk::time_end(ctx, tl_);                                    \
+        if (e_ != cudaSuccess) return fbk::cuda_err(ctx, e_, name); \
+    } while (0)

@@ -1,0 +1,457 @@
+// fbk_k_batch.cu — multi-isolate forms of the build kernels (one launch per phase
+// for every isolate of a wave).
+//
+// The reads of all isolates in a wave form one global index R: isolate i owns
+// R in [read_base[i], read_base[i+1]).  Warps stride over R exactly like the
+// single-isolate kernels stride over one bank, so at any moment the resident warps
+// work on a narrow band of R — one or two isolates — and the sketch or table slice
+// they touch stays L2-resident.  A warp's R only grows, so it finds its isolate by
+// walking forward through read_base (shared memory) and reloads the isolate's
+// descriptor only when it crosses a boundary.
+#include "fbk_device.cuh"
+#include "fbk_kernels.cuh"
+#include "fbk_table.cuh"
+
+namespace fbk {
+
+__device__ __forceinline__ uint32_t iso_walk(const unsigned long long* s_base, uint32_t n_iso, uint32_t i, uint64_t R) {
+    while (i + 1 < n_iso && R >= s_base[i + 1]) ++i;
+    return i;
+}
+
+__device__ __forceinline__ uint32_t load_bases(const unsigned long long* read_base, uint32_t n_iso, unsigned long long* s_base) {
+    for (uint32_t i = threadIdx.x; i <= n_iso; i += blockDim.x) s_base[i] = read_base[i];
+    __syncthreads();
+    return 0;
+}
+
+// Pass 1 (build.rs:90-116) for rows [r0, r1) of every isolate's sketch, plus the
+// p=12 HyperLogLog of its keys when do_hll (registers are only raised, so a stale
+// cached read merely costs an extra atomicMax).
+template <int NW>
+__global__ void __launch_bounds__(256) k_batch_pass1(const IsoDev* __restrict__ iso, const unsigned long long* __restrict__ read_base,
+                                                     uint32_t n_iso, uint32_t k, uint32_t r0, uint32_t r1, int do_hll) {
+    __shared__ unsigned long long s_base[BATCH_MAX_ISO + 1];
+    load_bases(read_base, n_iso, s_base);
+    const uint64_t total = s_base[n_iso];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    uint32_t ci = 0, cur = 0xFFFFFFFFu;
+    BankDev b{};
+    uint32_t* cnt = nullptr;
+    uint32_t* hll = nullptr;
+    uint64_t wmask = 0, base = 0;
+    uint32_t log2w = 0;
+    for (uint64_t R = gw; R < total; R += nwarps) {
+        ci = iso_walk(s_base, n_iso, ci, R);
+        if (ci != cur) {
+            cur = ci;
+            b = iso[ci].b;
+            cnt = iso[ci].cnt;
+            log2w = iso[ci].log2w;
+            wmask = (1ULL << log2w) - 1;
+            hll = do_hll ? iso[ci].hll12 : nullptr;
+            base = s_base[ci];
+        }
+        const uint64_t r = R - base;
+        const uint32_t len = b.len[r];
+        if (len < k || !bank_keep(b, r)) continue;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        for (uint32_t i = lane; i < nk; i += 32) {
+            Key<NW> can;
+            bool rc;
+            window_canonical<NW>(b.data, off + i, k, can, rc);
+            const uint64_t key = key_fold<NW>(can);
+            for (uint32_t row = r0; row < r1; ++row) {
+                const uint64_t col = smix(key ^ cms_seed((int)row)) & wmask;
+                atomicAdd(cnt + ((uint64_t)row << log2w) + col, 1u);
+            }
+            if (hll) {
+                uint32_t idx, rho;
+                hll_idx_rho(smix(key ^ cms_seed(0)), 12, idx, rho);
+                if (__ldg(&hll[idx]) < rho) atomicMax(&hll[idx], rho);
+            }
+        }
+    }
+}
+
+// Solidity bitmap (build.rs:259-267) for rows [r0, r1) of every isolate: a window's
+// bit is cleared when its capped count in any of these rows is below t_solid.
+template <int NW>
+__global__ void __launch_bounds__(256) k_batch_solid(const IsoDev* __restrict__ iso, const unsigned long long* __restrict__ read_base,
+                                                     uint32_t n_iso, uint32_t k, uint32_t r0, uint32_t r1) {
+    __shared__ unsigned long long s_base[BATCH_MAX_ISO + 1];
+    load_bases(read_base, n_iso, s_base);
+    const uint64_t total = s_base[n_iso];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    uint32_t ci = 0, cur = 0xFFFFFFFFu;
+    BankDev b{};
+    const uint32_t* cnt = nullptr;
+    uint32_t* bm = nullptr;
+    uint64_t wmask = 0, base = 0;
+    uint32_t log2w = 0, t_solid = 0, cap = 0;
+    for (uint64_t R = gw; R < total; R += nwarps) {
+        ci = iso_walk(s_base, n_iso, ci, R);
+        if (ci != cur) {
+            cur = ci;
+            b = iso[ci].b;
+            cnt = iso[ci].cnt;
+            bm = iso[ci].bm;
+            log2w = iso[ci].log2w;
+            wmask = (1ULL << log2w) - 1;
+            t_solid = iso[ci].t_solid;
+            cap = iso[ci].cap;
+            base = s_base[ci];
+        }
+        const uint64_t r = R - base;
+        const uint32_t len = b.len[r];
+        if (len < k + 1 || !bank_keep(b, r)) continue;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        for (uint32_t it = 0; it < ((nk + 31) >> 5); ++it) {
+            const uint32_t q = (it << 5) + lane;
+            bool clr = false;
+            if (q < nk) {
+                Key<NW> can;
+                bool rc;
+                window_canonical<NW>(b.data, off + q, k, can, rc);
+                const uint64_t key = key_fold<NW>(can);
+                for (uint32_t row = r0; row < r1; ++row) {
+                    const uint64_t col = smix(key ^ cms_seed((int)row)) & wmask;
+                    uint32_t c = __ldg(cnt + ((uint64_t)row << log2w) + col);
+                    c = c < cap ? c : cap;
+                    clr |= c < t_solid;
+                }
+            }
+            const uint32_t m = __ballot_sync(0xffffffffu, clr);
+            if (lane == 0 && m) {
+                const uint64_t g0 = off + ((uint64_t)it << 5);
+                const uint32_t sh = (uint32_t)(g0 & 31);
+                atomicAnd(&bm[g0 >> 5], ~(m << sh));
+                if (sh) atomicAnd(&bm[(g0 >> 5) + 1], ~(m >> (32 - sh)));
+            }
+        }
+    }
+}
+
+// Exact number of pass-2 records of every isolate (windows that are solid and have
+// a solid neighbour inside their read), which sizes the record buckets, and the
+// k-mer occurrences of the two passes over kept reads: n_records[0] records,
+// [1] windows of reads with len >= k, [2] windows of reads with len >= k + 1.
+__global__ void __launch_bounds__(256) k_batch_count(const IsoDev* __restrict__ iso, const unsigned long long* __restrict__ read_base,
+                                                     uint32_t n_iso, uint32_t k) {
+    __shared__ unsigned long long s_base[BATCH_MAX_ISO + 1];
+    load_bases(read_base, n_iso, s_base);
+    const uint64_t total = s_base[n_iso];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    uint32_t ci = 0, cur = 0xFFFFFFFFu;
+    BankDev b{};
+    const uint32_t* bm = nullptr;
+    uint64_t base = 0;
+    unsigned long long acc = 0, w1 = 0, w2 = 0;
+    for (uint64_t R = gw; R < total; R += nwarps) {
+        ci = iso_walk(s_base, n_iso, ci, R);
+        if (ci != cur) {
+            if (lane == 0 && cur != 0xFFFFFFFFu) {
+                atomicAdd(iso[cur].n_records, acc);
+                atomicAdd(iso[cur].n_records + 1, w1);
+                atomicAdd(iso[cur].n_records + 2, w2);
+            }
+            acc = w1 = w2 = 0;
+            cur = ci;
+            b = iso[ci].b;
+            bm = iso[ci].bm;
+            base = s_base[ci];
+        }
+        const uint64_t r = R - base;
+        const uint32_t len = b.len[r];
+        if (len < k || !bank_keep(b, r)) continue;
+        w1 += len - k + 1;
+        if (len < k + 1) continue;
+        w2 += len - k + 1;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        for (uint32_t q = lane; q < ((nk + 31) & ~31u); q += 32) {
+            bool e = false;
+            if (q < nk) {
+                const uint64_t g = off + q;
+                e = bm_bit(bm, g) && ((q > 0 && bm_bit(bm, g - 1)) || (q + 1 < nk && bm_bit(bm, g + 1)));
+            }
+            acc += __popc(__ballot_sync(0xffffffffu, e));
+        }
+    }
+    if (lane == 0 && cur != 0xFFFFFFFFu) {
+        atomicAdd(iso[cur].n_records, acc);
+        atomicAdd(iso[cur].n_records + 1, w1);
+        atomicAdd(iso[cur].n_records + 2, w2);
+    }
+}
+
+// Pass 2, record form (build.rs:242-289): the records of every isolate go to that
+// isolate's buckets; a warp flushes its staging buffer when it moves to the next
+// isolate.
+template <int NW>
+__global__ void __launch_bounds__(256) k_batch_emit(const IsoDev* __restrict__ iso, const unsigned long long* __restrict__ read_base,
+                                                    uint32_t n_iso, uint32_t k, uint32_t stripes) {
+    extern __shared__ uint64_t emit_smem[];
+    __shared__ unsigned long long s_base[BATCH_MAX_ISO + 1];
+    load_bases(read_base, n_iso, s_base);
+    const uint64_t total = s_base[n_iso];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint64_t* buf = emit_smem + (uint64_t)wib * EMIT_WARP_WORDS(NW);
+    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + EMIT_BUF * (NW + 1));
+    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + EMIT_BUF);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + EMIT_BUF);
+    unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t stripe = (uint32_t)(gw % stripes);
+    uint32_t ci = 0, cur = 0xFFFFFFFFu, n_buf = 0;
+    BankDev b{};
+    const uint32_t* bm = nullptr;
+    BucketDev bk{};
+    uint64_t cap = 0, base = 0;
+    for (uint64_t R = gw; R < total; R += nwarps) {
+        ci = iso_walk(s_base, n_iso, ci, R);
+        if (ci != cur) {
+            if (n_buf) {
+                __syncwarp();
+                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+                n_buf = 0;
+            }
+            cur = ci;
+            b = iso[ci].b;
+            bm = iso[ci].bm;
+            bk = iso[ci].bk;
+            cap = iso[ci].t.cap;
+            base = s_base[ci];
+        }
+        const uint64_t r = R - base;
+        const uint32_t len = b.len[r];
+        if (len < k + 1 || !bank_keep(b, r)) continue;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        for (uint32_t it = 0; it < ((nk + 31) >> 5); ++it) {
+            const uint32_t q = (it << 5) + lane;
+            bool emit = false;
+            Key<NW> key;
+            uint32_t info = 0, bucket = 0;
+            if (q < nk) {
+                const uint64_t g = off + q;
+                const bool sq = bm_bit(bm, g);
+                const bool sl = q > 0 && bm_bit(bm, g - 1);
+                const bool sr = q + 1 < nk && bm_bit(bm, g + 1);
+                emit = sq && (sl || sr);
+                if (emit) {
+                    bool rc;
+                    window_canonical<NW>(b.data, g, k, key, rc);
+                    if (sr) info |= 8u | (base_at(b.data, g + k) + (rc ? 4u : 0u));
+                    if (sl) info |= (8u | ((3u - base_at(b.data, g - 1)) + (rc ? 0u : 4u))) << 4;
+                    bucket = (uint32_t)(home_slot(key_fold<NW>(key), cap) >> bk.shift);
+                }
+            }
+            const uint32_t active = __ballot_sync(0xffffffffu, emit);
+            if (emit) {
+                const uint32_t pos = n_buf + __popc(active & ((1u << lane) - 1));
+#pragma unroll
+                for (int i = 0; i < NW; ++i) buf[pos * (NW + 1) + i] = key.w[i];
+                buf[pos * (NW + 1) + NW] = info;
+                bbuf[pos] = (uint8_t)bucket;
+            }
+            n_buf += __popc(active);
+            if (n_buf > EMIT_BUF - 32) {
+                __syncwarp();
+                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+                n_buf = 0;
+            }
+        }
+    }
+    __syncwarp();
+    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+}
+
+// Record totals of every (isolate, bucket) unit: stripe_pre[u * (S + 1) + s] is the
+// number of records in stripes < s of unit u (fills capped at the stripe size), and
+// unit_pre[u] the records of all units before u.  One block.
+__global__ void k_batch_prefix(const IsoDev* __restrict__ iso, uint32_t n_iso, uint32_t stripes,
+                               unsigned long long* __restrict__ unit_pre, unsigned long long* __restrict__ stripe_pre) {
+    const uint32_t n_units = n_iso * EMIT_MAX_BUCKETS, S = stripes;
+    for (uint32_t u = threadIdx.x; u < n_units; u += blockDim.x) {
+        const IsoDev& d = iso[u / EMIT_MAX_BUCKETS];
+        const uint32_t bu = u % EMIT_MAX_BUCKETS;
+        unsigned long long acc = 0;
+        unsigned long long* sp = stripe_pre + (uint64_t)u * (S + 1);
+        for (uint32_t s = 0; s < S; ++s) {
+            sp[s] = acc;
+            if (bu < d.bk.n_buckets) {
+                const unsigned long long f = d.bk.fill[(uint64_t)bu * S + s];
+                acc += f < d.bk.stripe_cap ? f : d.bk.stripe_cap;
+            }
+        }
+        sp[S] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long acc = 0;
+        for (uint32_t u = 0; u < n_units; ++u) {
+            unit_pre[u] = acc;
+            acc += stripe_pre[(uint64_t)u * (S + 1) + S];
+        }
+        unit_pre[n_units] = acc;
+    }
+}
+
+// Upsert of every record of every unit, units in order (isolate-major, then
+// bucket): resident blocks work on consecutive records, i.e. on one bucket's table
+// range at a time.  Each block takes tiles of blockDim records; the tile's units are
+// found once per tile.
+template <int NW>
+__global__ void __launch_bounds__(256) k_batch_upsert(const IsoDev* __restrict__ iso, uint32_t n_iso, uint32_t stripes,
+                                                      const unsigned long long* __restrict__ unit_pre,
+                                                      const unsigned long long* __restrict__ stripe_pre) {
+    __shared__ uint32_t s_u[2];
+    const uint32_t n_units = n_iso * EMIT_MAX_BUCKETS, S = stripes;
+    const uint64_t total = unit_pre[n_units];
+    const uint64_t tile = blockDim.x;
+    for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < total; t0 += (uint64_t)gridDim.x * tile) {
+        if (threadIdx.x < 2) {
+            const uint64_t x = threadIdx.x == 0 ? t0 : (t0 + tile - 1 < total ? t0 + tile - 1 : total - 1);
+            uint32_t lo = 0, hi = n_units;  // last u with unit_pre[u] <= x
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (unit_pre[mid] <= x) lo = mid;
+                else hi = mid;
+            }
+            s_u[threadIdx.x] = lo;
+        }
+        __syncthreads();
+        const uint64_t i = t0 + threadIdx.x;
+        uint32_t ulo = s_u[0], uhi = s_u[1] + 1;
+        __syncthreads();
+        if (i >= total) continue;
+        while (uhi - ulo > 1) {
+            const uint32_t mid = (ulo + uhi) >> 1;
+            if (unit_pre[mid] <= i) ulo = mid;
+            else uhi = mid;
+        }
+        const uint32_t u = ulo;
+        const uint64_t j = i - unit_pre[u];
+        const unsigned long long* sp = stripe_pre + (uint64_t)u * (S + 1);
+        uint32_t lo = 0, hi = S;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (sp[mid] <= j) lo = mid;
+            else hi = mid;
+        }
+        const IsoDev& d = iso[u / EMIT_MAX_BUCKETS];
+        const uint32_t bucket = u % EMIT_MAX_BUCKETS;
+        const uint64_t* rec = d.bk.recs + (((uint64_t)bucket * S + lo) * d.bk.stripe_cap + (j - sp[lo])) * (NW + 1);
+        Key<NW> key;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) key.w[w] = __ldcs(rec + w);
+        const uint32_t info = (uint32_t)__ldcs(rec + NW);
+        const TableDev t = d.t;
+        const uint64_t f = key_fold<NW>(key);
+        const uint64_t home = home_slot(f, t.cap);
+        int64_t s;
+        if constexpr (NW == 1) s = table_slot1(t, key.w[0], home, d.status);
+        else if constexpr (NW == 2) s = table_slot2(t, key, home, d.status);
+        else s = table_slotw<NW>(t, key, f, home, d.status);
+        if (s < 0) continue;
+        uint32_t* c = t.cnt + (uint64_t)s * 8;
+        if ((info >> 3) & 1u) atomicAdd(&c[info & 7u], 1u);
+        if ((info >> 7) & 1u) atomicAdd(&c[(info >> 4) & 7u], 1u);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <class K>
+static int grid_of(K kernel, const Launch& L, size_t smem) {
+    if (L.grid > 0) return L.grid;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, L.block, smem) != cudaSuccess || per_sm < 1) per_sm = 1;
+    return per_sm * (L.sms > 0 ? L.sms : 1);
+}
+
+template <int NW>
+static cudaError_t bpass1(const Launch& L, const IsoDev* iso, const unsigned long long* rb, uint32_t n, uint32_t k, uint32_t r0,
+                          uint32_t r1, int hll) {
+    k_batch_pass1<NW><<<grid_of(k_batch_pass1<NW>, L, 0), L.block, 0, L.stream>>>(iso, rb, n, k, r0, r1, hll);
+    return cudaGetLastError();
+}
+cudaError_t launch_batch_pass1(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
+                               uint32_t k, uint32_t r0, uint32_t r1, int do_hll) {
+    if (n_iso > BATCH_MAX_ISO) return cudaErrorInvalidValue;
+    if (nw == 1) return bpass1<1>(L, iso, read_base, n_iso, k, r0, r1, do_hll);
+    if (nw == 2) return bpass1<2>(L, iso, read_base, n_iso, k, r0, r1, do_hll);
+    return bpass1<4>(L, iso, read_base, n_iso, k, r0, r1, do_hll);
+}
+
+template <int NW>
+static cudaError_t bsolid(const Launch& L, const IsoDev* iso, const unsigned long long* rb, uint32_t n, uint32_t k, uint32_t r0,
+                          uint32_t r1) {
+    k_batch_solid<NW><<<grid_of(k_batch_solid<NW>, L, 0), L.block, 0, L.stream>>>(iso, rb, n, k, r0, r1);
+    return cudaGetLastError();
+}
+cudaError_t launch_batch_solid(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
+                               uint32_t k, uint32_t r0, uint32_t r1) {
+    if (n_iso > BATCH_MAX_ISO) return cudaErrorInvalidValue;
+    if (nw == 1) return bsolid<1>(L, iso, read_base, n_iso, k, r0, r1);
+    if (nw == 2) return bsolid<2>(L, iso, read_base, n_iso, k, r0, r1);
+    return bsolid<4>(L, iso, read_base, n_iso, k, r0, r1);
+}
+
+cudaError_t launch_batch_count(const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso, uint32_t k) {
+    if (n_iso > BATCH_MAX_ISO) return cudaErrorInvalidValue;
+    k_batch_count<<<grid_of(k_batch_count, L, 0), L.block, 0, L.stream>>>(iso, read_base, n_iso, k);
+    return cudaGetLastError();
+}
+
+template <int NW>
+static cudaError_t bemit(const Launch& L, const IsoDev* iso, const unsigned long long* rb, uint32_t n, uint32_t k, uint32_t S) {
+    const size_t smem = (size_t)(L.block / 32) * EMIT_WARP_WORDS(NW) * 8;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_batch_emit<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_batch_emit<NW><<<grid_of(k_batch_emit<NW>, L, smem), L.block, smem, L.stream>>>(iso, rb, n, k, S);
+    return cudaGetLastError();
+}
+cudaError_t launch_batch_emit(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
+                              uint32_t k, uint32_t stripes) {
+    if (n_iso > BATCH_MAX_ISO || stripes == 0 || stripes > 256) return cudaErrorInvalidValue;
+    if (nw == 1) return bemit<1>(L, iso, read_base, n_iso, k, stripes);
+    if (nw == 2) return bemit<2>(L, iso, read_base, n_iso, k, stripes);
+    return bemit<4>(L, iso, read_base, n_iso, k, stripes);
+}
+
+cudaError_t launch_batch_prefix(const Launch& L, const IsoDev* iso, uint32_t n_iso, uint32_t stripes, unsigned long long* unit_pre,
+                                unsigned long long* stripe_pre) {
+    if (n_iso > BATCH_MAX_ISO || stripes == 0 || stripes > 256) return cudaErrorInvalidValue;
+    k_batch_prefix<<<1, 1024, 0, L.stream>>>(iso, n_iso, stripes, unit_pre, stripe_pre);
+    return cudaGetLastError();
+}
+
+template <int NW>
+static cudaError_t bupsert(const Launch& L, const IsoDev* iso, uint32_t n, uint32_t S, const unsigned long long* up,
+                           const unsigned long long* sp) {
+    k_batch_upsert<NW><<<grid_of(k_batch_upsert<NW>, L, 0), L.block, 0, L.stream>>>(iso, n, S, up, sp);
+    return cudaGetLastError();
+}
+cudaError_t launch_batch_upsert(int nw, const Launch& L, const IsoDev* iso, uint32_t n_iso, uint32_t stripes,
+                                const unsigned long long* unit_pre, const unsigned long long* stripe_pre) {
+    if (n_iso > BATCH_MAX_ISO || stripes == 0 || stripes > 256) return cudaErrorInvalidValue;
+    if (nw == 1) return bupsert<1>(L, iso, n_iso, stripes, unit_pre, stripe_pre);
+    if (nw == 2) return bupsert<2>(L, iso, n_iso, stripes, unit_pre, stripe_pre);
+    return bupsert<4>(L, iso, n_iso, stripes, unit_pre, stripe_pre);
+}
+
+}  // namespace fbk

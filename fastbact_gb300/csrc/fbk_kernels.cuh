@@ -70,6 +70,20 @@ struct ConvOut {
     uint64_t cap_solid, cap_acc;
 };
 
+// One isolate of a multi-isolate wave (fbk_k_batch.cu).
+constexpr uint32_t BATCH_MAX_ISO = 256;
+struct IsoDev {
+    BankDev b;                      // r_begin = 0, r_end = the isolate's reads
+    uint32_t* cnt;                  // exact u32 sketch, 4 rows of 2^log2w
+    uint32_t* hll12;                // p=12 registers of the keys (table sizing)
+    uint32_t* bm;                   // solidity bitmap
+    unsigned long long* n_records;  // [0] pass-2 records, [1] pass-1 and [2] pass-2 k-mer occurrences
+    uint32_t log2w, t_solid, cap, _pad;
+    TableDev t;
+    BucketDev bk;
+    uint32_t* status;               // ST_* bits of this isolate
+};
+
 struct Launch {
     int grid;     // <= 0: occupancy-derived persistent grid (resident blocks x SMs)
     int block;
@@ -103,6 +117,21 @@ cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t
 cudaError_t launch_convert(int nw, const Launch& L, const TableDev& t, uint32_t min_trans_cov, const ConvOut& o);
 cudaError_t launch_clamp_counters(const Launch& L, uint32_t* cnt, uint64_t n);
 cudaError_t launch_table_init(int nw, const Launch& L, const TableDev& t);
+
+// ---- multi-isolate waves (fbk_k_batch.cu) ----------------------------------------
+// read_base: n_iso + 1 global read indices (isolate i owns [read_base[i], read_base[i+1])).
+cudaError_t launch_batch_pass1(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
+                               uint32_t k, uint32_t r0, uint32_t r1, int do_hll);
+cudaError_t launch_batch_solid(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
+                               uint32_t k, uint32_t r0, uint32_t r1);
+cudaError_t launch_batch_count(const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso, uint32_t k);
+cudaError_t launch_batch_emit(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
+                              uint32_t k, uint32_t stripes);
+// unit_pre: n_iso * 64 + 1 entries; stripe_pre: n_iso * 64 * (stripes + 1) entries.
+cudaError_t launch_batch_prefix(const Launch& L, const IsoDev* iso, uint32_t n_iso, uint32_t stripes, unsigned long long* unit_pre,
+                                unsigned long long* stripe_pre);
+cudaError_t launch_batch_upsert(int nw, const Launch& L, const IsoDev* iso, uint32_t n_iso, uint32_t stripes,
+                                const unsigned long long* unit_pre, const unsigned long long* stripe_pre);
 
 // ---- estimator and utilities (fbk_k_est.cu) -----------------------------------
 cudaError_t launch_est_firstpos(const Launch& L, const BankDev& b, const uint64_t* kbase, uint32_t k, uint32_t* first,

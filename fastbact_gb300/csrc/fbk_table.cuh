@@ -1,0 +1,153 @@
+// fbk_table.cuh — device pieces shared by the single-isolate and the multi-isolate
+// build kernels: open-addressing probes of the solid table, the solidity-bitmap
+// test, and the per-warp record staging of pass 2.
+#pragma once
+#include <cuda/atomic>
+
+#include "fbk_device.cuh"
+#include "fbk_kernels.cuh"
+
+namespace fbk {
+
+static constexpr uint64_t TABLE_SALT = 0x6a09e667f3bcc908ULL;
+static constexpr uint64_t FP_SALT = 0xbb67ae8584caa73bULL;
+static constexpr uint64_t TAG_READY = 1ULL << 63;
+static constexpr uint64_t KEY_EMPTY = ~0ULL;
+
+// ---------------------------------------------------------------------------
+// Solid table probing from a precomputed home slot
+// ---------------------------------------------------------------------------
+// Home slot of a key: the high 64 bits of mix(fold) * cap (any capacity).
+__device__ __forceinline__ uint64_t home_slot(uint64_t fold, uint64_t cap) {
+    return __umul64hi(smix(fold ^ TABLE_SALT), cap);
+}
+
+__device__ __forceinline__ int64_t table_slot1(const TableDev& t, uint64_t key, uint64_t s, uint32_t* status) {
+    for (uint32_t probe = 0; probe < t.max_probe; ++probe) {
+        const uint64_t cur = __ldcg(&t.keys[s]);
+        if (cur == key) return (int64_t)s;
+        if (cur == KEY_EMPTY) {
+            const uint64_t old = atomicCAS((unsigned long long*)&t.keys[s], KEY_EMPTY, key);
+            if (old == KEY_EMPTY || old == key) return (int64_t)s;
+        }
+        s = s + 1 == t.cap ? 0 : s + 1;
+    }
+    atomicOr(status, ST_TABLE_FULL);
+    return -1;
+}
+
+// 16-byte compare-and-swap (sm_90 and later): the 128-bit key of a slot goes from
+// EMPTY (all ones: a k <= 63 key leaves its top two bits zero) to the key in one
+// atomic step, so a slot never holds half a key and no publication wait is needed.
+__device__ __forceinline__ void cas128(uint64_t* addr, uint64_t cmp_lo, uint64_t cmp_hi, uint64_t new_lo, uint64_t new_hi,
+                                       uint64_t& old_lo, uint64_t& old_hi) {
+    asm volatile(
+        "{\n\t.reg .b128 c, n, d;\n\t"
+        "mov.b128 c, {%2, %3};\n\t"
+        "mov.b128 n, {%4, %5};\n\t"
+        "atom.global.cas.b128 d, [%6], c, n;\n\t"
+        "mov.b128 {%0, %1}, d;\n\t}"
+        : "=l"(old_lo), "=l"(old_hi)
+        : "l"(cmp_lo), "l"(cmp_hi), "l"(new_lo), "l"(new_hi), "l"(addr)
+        : "memory");
+}
+
+__device__ __forceinline__ int64_t table_slot2(const TableDev& t, const Key<2>& key, uint64_t s, uint32_t* status) {
+    for (uint32_t probe = 0; probe < t.max_probe; ++probe) {
+        uint64_t* a = t.keys + s * 2;
+        const uint64_t c0 = __ldcg(a), c1 = __ldcg(a + 1);
+        if (c0 == key.w[0] && c1 == key.w[1]) return (int64_t)s;
+        // Anything but our key or EMPTY may be a slot being written: decide with the CAS.
+        uint64_t o0, o1;
+        cas128(a, KEY_EMPTY, KEY_EMPTY, key.w[0], key.w[1], o0, o1);
+        if ((o0 == KEY_EMPTY && o1 == KEY_EMPTY) || (o0 == key.w[0] && o1 == key.w[1])) return (int64_t)s;
+        s = s + 1 == t.cap ? 0 : s + 1;
+    }
+    atomicOr(status, ST_TABLE_FULL);
+    return -1;
+}
+
+template <int NW>
+__device__ __forceinline__ int64_t table_slotw(const TableDev& t, const Key<NW>& key, uint64_t f, uint64_t s, uint32_t* status) {
+    const uint64_t fp = (smix(f ^ FP_SALT) | 1ULL) & ~TAG_READY;
+    for (uint32_t probe = 0; probe < t.max_probe; ++probe) {
+        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> tag_ref(*(unsigned long long*)&t.tags[s]);
+        uint64_t tag = tag_ref.load(cuda::memory_order_acquire);
+        if (tag == 0) {
+            const uint64_t old = atomicCAS((unsigned long long*)&t.tags[s], 0ULL, fp);
+            if (old == 0) {
+#pragma unroll
+                for (int i = 0; i < NW; ++i) __stcg(&t.keys[s * NW + i], key.w[i]);
+                tag_ref.fetch_or(TAG_READY, cuda::memory_order_release);
+                return (int64_t)s;
+            }
+            tag = old;
+        }
+        if ((tag & ~TAG_READY) == fp) {
+            // Same fingerprint: wait (bounded) until the claiming thread has published
+            // the key words, then compare them.
+            uint32_t spins = 0;
+            while (!(tag & TAG_READY)) {
+                if (++spins > t.spin_limit) {
+                    atomicOr(status, ST_SPIN_TIMEOUT);
+                    return -1;
+                }
+                __nanosleep(64);
+                tag = tag_ref.load(cuda::memory_order_acquire);
+            }
+            bool eq = true;
+#pragma unroll
+            for (int i = 0; i < NW; ++i) eq &= (__ldcg(&t.keys[s * NW + i]) == key.w[i]);
+            if (eq) return (int64_t)s;
+        }
+        s = s + 1 == t.cap ? 0 : s + 1;
+    }
+    atomicOr(status, ST_TABLE_FULL);
+    return -1;
+}
+
+
+__device__ __forceinline__ bool bm_bit(const uint32_t* __restrict__ bm, uint64_t g) {
+    return (__ldg(&bm[g >> 5]) >> (g & 31)) & 1u;
+}
+
+// Records are staged per warp in shared memory (EMIT_BUF of them) and flushed
+// bucket by bucket: one atomic per (flush, bucket) reserves room for all of the
+// warp's records of that bucket, which are then written as one run.
+constexpr uint32_t EMIT_BUF = 128;
+constexpr uint32_t EMIT_MAX_BUCKETS = 64;
+// staging words per warp: records, bucket bytes, ranks (u16), histogram (64 u32),
+// reservation bases (64 u64)
+#define EMIT_WARP_WORDS(NW) (EMIT_BUF * ((NW) + 1) + EMIT_BUF / 8 + EMIT_BUF / 4 + EMIT_MAX_BUCKETS / 2 + EMIT_MAX_BUCKETS)
+
+// Warp counting sort of the staged records by bucket: a shared-memory histogram
+// (one atomic per record), one parallel round of global reservations (lane j
+// reserves for bucket j, j+32, ...), then every lane copies records to
+// region[bucket] + rank.  Cost does not grow with the number of buckets.
+template <int NW>
+__device__ __forceinline__ void emit_flush(const BucketDev& bk, uint32_t stripe, uint32_t lane, uint64_t* buf, const uint8_t* bbuf,
+                                           uint32_t n_buf, uint32_t* hist, unsigned long long* gbase, uint16_t* rank) {
+    for (uint32_t bu = lane; bu < bk.n_buckets; bu += 32) hist[bu] = 0;
+    __syncwarp();
+    for (uint32_t j = lane; j < n_buf; j += 32) rank[j] = (uint16_t)atomicAdd(&hist[bbuf[j]], 1u);
+    __syncwarp();
+    for (uint32_t bu = lane; bu < bk.n_buckets; bu += 32) {
+        const uint32_t c = hist[bu];
+        gbase[bu] = c ? atomicAdd(bk.fill + (uint64_t)bu * bk.stripes + stripe, (unsigned long long)c) : 0;
+    }
+    __syncwarp();
+    for (uint32_t j = lane; j < n_buf; j += 32) {
+        const uint32_t bu = bbuf[j];
+        const unsigned long long pos = gbase[bu] + rank[j];
+        if (pos < bk.stripe_cap) {
+            uint64_t* dst = bk.recs + (((uint64_t)bu * bk.stripes + stripe) * bk.stripe_cap + pos) * (NW + 1);
+#pragma unroll
+            for (int i = 0; i <= NW; ++i) dst[i] = buf[j * (NW + 1) + i];
+        } else {
+            atomicOr(bk.overflow, 1u);
+        }
+    }
+    __syncwarp();
+}
+
+}  // namespace fbk

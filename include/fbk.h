@@ -283,6 +283,96 @@ FBK_API int fbk_compute_dynamic_kmers(uint64_t median_len, int64_t target_max_k,
 /* Bit i of keep_bits (host, ceil(n_pairs/64) words) = input pair i (0-based) kept. */
 FBK_API fbk_status fbk_subsample_mask(fbk_ctx* ctx, uint64_t n_pairs, const fbk_subsample* ss, uint64_t* keep_bits);
 
+/* Subsampling policy of the pipeline driver (src/main.rs:76-180): decides the
+ * subsample factor from an estimate.  reason: 0 EXPLICIT_NO_SUBSAMPLE_FLAG,
+ * 1 EXPLICIT_GENOME_SIZE_ZERO_INVALID, 2 AUTO_SUBSAMPLE_EXPLICIT_GENOME_SIZE,
+ * 3 AUTO_SUBSAMPLE_EXPLICIT_GENOME_SIZE_WITHIN_TARGET, 4 AUTO_SUBSAMPLE_HIGH_CONFIDENCE,
+ * 5 AUTO_SUBSAMPLE_HIGH_CONFIDENCE_WITHIN_TARGET, 6 AUTO_SUBSAMPLE_INTERCEPTED_LOW_COVERAGE_WARNING,
+ * 7 AUTO_SUBSAMPLE_INTERCEPTED_UNRELIABLE, 8 GENOME_SIZE_PRIOR_PROVIDED_SUBSAMPLING_NOT_ENABLED,
+ * 9 DISABLED_BY_DEFAULT_SAFE_FALLBACK.  An invalid threshold ratio (not finite or
+ * below 1) is FBK_ERR_INVALID, as main.rs:76-81 bails. */
+typedef struct {
+    int32_t no_subsample;           /* --no-subsample */
+    int32_t enable_auto_subsample;  /* --enable-auto-subsample */
+    int32_t has_genome_size;        /* --genome-size given */
+    int32_t _pad;
+    uint64_t genome_size;           /* its value */
+    double depth;                   /* --depth (120 by default) */
+    double threshold_ratio;         /* --subsample-threshold-ratio (1.5 by default) */
+} fbk_subsample_policy;
+FBK_API void fbk_subsample_policy_defaults(fbk_subsample_policy* p);
+FBK_API fbk_status fbk_subsample_decide(const fbk_subsample_policy* p, const fbk_genome_estimate* e, double* factor,
+                                        int32_t* reason);
+
+/* ---- batches: many isolates per launch ------------------------------------------
+ * The reference runs one isolate per process (src/main.rs: estimate_genome, the
+ * subsampling policy, ingest, then build_cdbg per k).  A batch runs those counting
+ * stages for many isolates at once; it has no counterpart in the reference.  Per
+ * isolate it computes exactly what the single-isolate calls compute
+ * (fbk_estimate_bank, fbk_subsample_decide, fbk_build_front with the batch's k,
+ * sketch width and thresholds); the sketches, bitmaps, tables and record buckets
+ * are carved from the context's pool, and each phase is one launch over every
+ * isolate of a wave (optionally one CUDA graph per phase).  Waves are sized by the
+ * free pool memory.  A batch belongs to one context and one host thread. */
+typedef struct fbk_batch fbk_batch;
+typedef struct {
+    uint32_t k;               /* 31 */
+    uint32_t key_bits;        /* 64 */
+    uint32_t cms_log2_width;  /* 22 */
+    uint32_t counter_bits;    /* 16 */
+    uint32_t t_solid;         /* 2: target_solid_cov.unwrap_or(2) */
+    uint32_t min_trans_cov;   /* 3 */
+    uint32_t use_graphs;      /* 1: each phase of a wave runs as one CUDA graph */
+    uint32_t autotune;        /* 1: launch shapes chosen by timing candidates on the first wave */
+    uint32_t keep_sketch;     /* 1: keep each isolate's sketch until the batch is released */
+    uint32_t max_wave;        /* isolates per wave (<= 256) */
+    uint64_t est_max_pairs;   /* estimate_genome's max_pairs: 250000 (main.rs:65) */
+    uint64_t subsample_seed;  /* --subsample-seed: 0 */
+    uint64_t max_wave_bytes;  /* 0: all free pool memory */
+    fbk_subsample_policy policy;
+} fbk_batch_params;
+
+typedef struct {
+    int32_t state;            /* 0 queued, 1 estimated, 2 counted, 3 done, -1 failed */
+    int32_t subsample_reason;
+    int32_t fallback;         /* 1: redone by the single-isolate path (bucket or table overflow) */
+    int32_t wave;
+    double subsample_factor;
+    fbk_genome_estimate estimate;
+    uint64_t n_keys, n_solid, digest, pushes;
+    uint64_t kmers;           /* k-mer occurrences of pass 1 + pass 2 (kept reads) */
+    uint64_t table_capacity;
+    fbk_status status;        /* error of a failed isolate */
+    int32_t _pad;
+} fbk_batch_result;
+
+typedef struct {
+    uint64_t isolates_done, waves, fallbacks, graph_launches, kernel_launches;
+    double ms_estimate, ms_phase_a, ms_phase_b, ms_host;   /* device time (events) and host planning */
+    /* launch shapes in use: block, grid (0 = occupancy), and sketch rows per sweep */
+    int32_t pass1_block, pass1_grid, pass1_rows, solid_block, solid_grid, solid_rows;
+    int32_t emit_block, emit_grid, upsert_block, upsert_grid;
+    int32_t tuned, _pad;
+    double tune_ms;
+} fbk_batch_stats;
+
+FBK_API void fbk_batch_defaults(fbk_batch_params* p);
+FBK_API fbk_status fbk_batch_create(fbk_ctx* ctx, const fbk_batch_params* p, fbk_batch** out);
+/* Uploads one isolate: its ReadBank (3 arenas, pair indices needed for subsampling),
+ * the raw sample pairs for the estimator (R1,R2 interleaved, sample_pairs pairs) and
+ * its count_fastx_exact statistics.  The host buffers may be reused on return. */
+FBK_API fbk_status fbk_batch_submit(fbk_batch* b, const fbk_arena_view bank[3], const fbk_arena_view* sample, uint64_t sample_pairs,
+                                    const fbk_count_stats* stats, uint64_t* id);
+/* Counts every submitted isolate that is not done yet; returns when all are done. */
+FBK_API fbk_status fbk_batch_run(fbk_batch* b);
+FBK_API fbk_status fbk_batch_get_result(const fbk_batch* b, uint64_t id, fbk_batch_result* out);
+/* Hands the isolate's solid table to the caller (release with fbk_table_release). */
+FBK_API fbk_status fbk_batch_take_table(fbk_batch* b, uint64_t id, fbk_table** out);
+/* Frees the isolate's device state (reads, sketch, table if not taken). */
+FBK_API fbk_status fbk_batch_drop(fbk_batch* b, uint64_t id);
+FBK_API fbk_status fbk_batch_get_stats(const fbk_batch* b, fbk_batch_stats* out);
+FBK_API fbk_status fbk_batch_release(fbk_batch* b);
+
 /* ---- host ingest (trim_merge.rs:17-417), CPU side ----------------------------- */
 FBK_API fbk_status fbk_ingest_fastq(const char* r1, const char* r2, double subsample_factor, uint64_t min_len, uint32_t min_qual,
                                     int enable_trim, int enable_merge, uint64_t seed, fbk_hbank** out, char* err, size_t errlen);

@@ -217,3 +217,35 @@ def test_ingest_subsample_matches_keep_rule(tmp_path):
 def test_tuning_rejects_out_of_range_without_device():
     # validation happens before any device work; a NULL context is rejected outright
     assert N.lib().fbk_ctx_set_tuning(None, b"sweep_bytes", 1e6) == 1
+
+
+def _estimate(cov, total_bases, confidence):
+    e = N.GenomeEstimate()
+    e.genome_size, e.total_bases, e.estimated_cov, e.confidence = 5_000_000, total_bases, cov, confidence
+    return api.GenomeEstimate.from_c(e)
+
+
+def test_subsample_policy_branches():  # src/main.rs:76-180
+    auto = dict(enable_auto_subsample=True, depth=110.0, threshold_ratio=150.0 / 110.0)
+    hi = _estimate(200.0, 1_000_000_000, 0)
+    cases = [
+        (dict(no_subsample=True, **auto), hi, 1.0, "EXPLICIT_NO_SUBSAMPLE_FLAG"),
+        (dict(), hi, 1.0, "DISABLED_BY_DEFAULT_SAFE_FALLBACK"),
+        (dict(genome_size=4_000_000), hi, 1.0, "GENOME_SIZE_PRIOR_PROVIDED_SUBSAMPLING_NOT_ENABLED"),
+        (auto, hi, 110.0 / 200.0, "AUTO_SUBSAMPLE_HIGH_CONFIDENCE"),
+        (auto, _estimate(140.0, 1, 0), 1.0, "AUTO_SUBSAMPLE_HIGH_CONFIDENCE_WITHIN_TARGET"),
+        (auto, _estimate(150.0, 1, 0), 1.0, "AUTO_SUBSAMPLE_HIGH_CONFIDENCE_WITHIN_TARGET"),
+        (auto, _estimate(400.0, 1, 1), 1.0, "AUTO_SUBSAMPLE_INTERCEPTED_LOW_COVERAGE_WARNING"),
+        (auto, _estimate(400.0, 1, 2), 1.0, "AUTO_SUBSAMPLE_INTERCEPTED_UNRELIABLE"),
+        (dict(genome_size=0, **auto), hi, 1.0, "EXPLICIT_GENOME_SIZE_ZERO_INVALID"),
+        (dict(genome_size=5_000_000, **auto), hi, 110.0 / 200.0, "AUTO_SUBSAMPLE_EXPLICIT_GENOME_SIZE"),
+        (dict(genome_size=8_000_000, **auto), hi, 1.0, "AUTO_SUBSAMPLE_EXPLICIT_GENOME_SIZE_WITHIN_TARGET"),
+        (auto, _estimate(1e6, 1, 0), 0.01, "AUTO_SUBSAMPLE_HIGH_CONFIDENCE"),   # clamp(0.01, 1.0)
+        (dict(enable_auto_subsample=True, depth=0.0), hi, 1.0, "AUTO_SUBSAMPLE_HIGH_CONFIDENCE_WITHIN_TARGET"),
+    ]
+    for kw, est, f, why in cases:
+        assert api.subsample_decide(api.subsample_policy(**kw), est) == (f, why), (kw, why)
+    with pytest.raises(N.FbkError):   # main.rs:76-81 rejects a ratio below 1 or not finite
+        api.subsample_decide(api.subsample_policy(threshold_ratio=0.5), hi)
+    with pytest.raises(N.FbkError):
+        api.subsample_decide(api.subsample_policy(threshold_ratio=float("nan")), hi)
