@@ -92,6 +92,22 @@ class BatchStats(C.Structure):
                 ("upsert_grid", C.c_int32), ("tuned", C.c_int32), ("_pad", C.c_int32), ("tune_ms", C.c_double)]
 
 
+class ServerParams(C.Structure):
+    _fields_ = [("batch", BatchParams), ("workers", C.c_uint32), ("_pad", C.c_uint32), ("budget_bytes", C.c_uint64)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("t_submit_ms", C.c_double), ("t_admit_ms", C.c_double),
+                ("t_done_ms", C.c_double), ("reserved_bytes", C.c_uint64), ("result", BatchResult)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("done", C.c_uint64), ("failed", C.c_uint64), ("waves_a", C.c_uint64),
+                ("waves_b", C.c_uint64), ("isolates_a", C.c_uint64), ("isolates_b", C.c_uint64),
+                ("reserved_bytes", C.c_uint64), ("peak_reserved_bytes", C.c_uint64), ("budget_bytes", C.c_uint64),
+                ("peak_in_flight", C.c_uint64), ("busy_ms", C.c_double)]
+
+
 class SynthParams(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("genome_len", C.c_uint64), ("gc", C.c_double), ("n_repeats", C.c_uint32),
                 ("repeat_len", C.c_uint32), ("repeat_identity", C.c_double), ("tandem_copies", C.c_uint32),
@@ -135,6 +151,7 @@ SIGNATURES = {
     "fbk_cms_add_contigs": (S, [vp, u8p, u64p, C.c_uint64, C.c_uint32, C.c_uint32]),
     "fbk_cms_nbytes": (S, [vp, u64p]),
     "fbk_cms_export": (S, [vp, u8p, C.c_uint64]),
+    "fbk_cms_import": (S, [vp, u8p, C.c_uint64]),
     "fbk_cms_merge": (S, [vp, vp]),
     "fbk_cms_release": (S, [vp]),
     "fbk_hll_create": (S, [vp, C.c_uint32, P(vp)]),
@@ -175,6 +192,15 @@ SIGNATURES = {
     "fbk_batch_drop": (S, [vp, C.c_uint64]),
     "fbk_batch_get_stats": (S, [vp, P(BatchStats)]),
     "fbk_batch_release": (S, [vp]),
+    "fbk_server_defaults": (None, [P(ServerParams)]),
+    "fbk_server_create": (S, [vp, P(ServerParams), P(vp)]),
+    "fbk_server_submit": (S, [vp, P(ArenaView), P(ArenaView), C.c_uint64, P(CountStats), u64p]),
+    "fbk_server_poll": (S, [vp, C.c_uint64, P(RequestInfo)]),
+    "fbk_server_wait": (S, [vp, C.c_uint64, C.c_double, P(RequestInfo)]),
+    "fbk_server_take_table": (S, [vp, C.c_uint64, P(vp)]),
+    "fbk_server_release_request": (S, [vp, C.c_uint64]),
+    "fbk_server_get_stats": (S, [vp, P(ServerStats)]),
+    "fbk_server_destroy": (S, [vp]),
     "fbk_ingest_fastq": (S, [C.c_char_p, C.c_char_p, C.c_double, C.c_uint64, C.c_uint32, C.c_int, C.c_int, C.c_uint64,
                              P(vp), C.c_char_p, C.c_size_t]),
     "fbk_hbank_arena": (S, [vp, C.c_int, P(ArenaView)]),

@@ -481,6 +481,11 @@ class CountMinSketch:
         check(N.lib().fbk_cms_export(self._h, ptr(out), n.value), self.ctx.handle, "cms export")
         return out
 
+    def load(self, raw: np.ndarray) -> None:
+        """Replaces the counters with bytes in the export layout."""
+        raw = np.ascontiguousarray(raw, dtype=np.uint8)
+        check(N.lib().fbk_cms_import(self._h, ptr(raw), raw.size), self.ctx.handle, "cms import")
+
     def merge(self, other: "CountMinSketch") -> None:
         check(N.lib().fbk_cms_merge(self._h, other._h), self.ctx.handle, "cms merge")
 
@@ -801,6 +806,87 @@ class Batch:
         if self._h and self.ctx.alive:
             N.lib().fbk_batch_release(self._h)
         self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+REQUEST_STATES = {0: "queued", 1: "admitted", 2: "estimated", 3: "counted", 4: "done", 5: "drained", -1: "failed"}
+
+
+def server_params(policy: N.SubsamplePolicy | None = None, workers: int = 2, budget_bytes: int = 0, **batch_kw) -> N.ServerParams:
+    p = N.ServerParams()
+    N.lib().fbk_server_defaults(C.byref(p))
+    if policy is not None:
+        p.batch.policy = policy
+    for k, v in batch_kw.items():
+        setattr(p.batch, k, v)
+    p.workers = workers
+    p.budget_bytes = budget_bytes
+    return p
+
+
+class Server:
+    """Request loop with continuous batching (fbk_server_*).  submit() queues an
+    isolate and returns its id; the host arrays passed in are kept referenced until
+    the request has been uploaded."""
+
+    def __init__(self, ctx: Context, params: N.ServerParams | None = None, **kw):
+        self.ctx = ctx
+        self.params = params if params is not None else server_params(**kw)
+        self._h = C.c_void_p()
+        self._pending: dict[int, tuple] = {}
+        check(N.lib().fbk_server_create(ctx.handle, C.byref(self.params), C.byref(self._h)), ctx.handle, "server create")
+        ctx.adopt(self)
+
+    def submit(self, bank: ReadBank, sample: BitSeqArena, sample_pairs: int, stats: ExactCountStats) -> int:
+        views = bank.views()
+        sv = sample.view()
+        cs = stats.to_c()
+        i = C.c_uint64()
+        check(N.lib().fbk_server_submit(self._h, views, C.byref(sv), sample_pairs, C.byref(cs), C.byref(i)),
+              self.ctx.handle, "server submit")
+        self._pending[i.value] = (bank, sample, views, sv)   # alive until uploaded
+        return i.value
+
+    def _settle(self, i: int, info: N.RequestInfo) -> None:
+        if info.state >= 2 or info.state < 0:
+            self._pending.pop(i, None)
+
+    def poll(self, i: int) -> N.RequestInfo:
+        info = N.RequestInfo()
+        check(N.lib().fbk_server_poll(self._h, i, C.byref(info)), self.ctx.handle, "server poll")
+        self._settle(i, info)
+        return info
+
+    def wait(self, i: int, timeout_ms: float = 600_000.0) -> N.RequestInfo:
+        info = N.RequestInfo()
+        st = N.lib().fbk_server_wait(self._h, i, timeout_ms, C.byref(info))
+        self._settle(i, info)
+        check(st, self.ctx.handle, f"server wait (request {i})")
+        return info
+
+    def take_table(self, i: int) -> SolidTable:
+        h = C.c_void_p()
+        check(N.lib().fbk_server_take_table(self._h, i, C.byref(h)), self.ctx.handle, "server take table")
+        return SolidTable(self.ctx, h, self.params.batch.k, self.params.batch.key_bits)
+
+    def release_request(self, i: int) -> None:
+        check(N.lib().fbk_server_release_request(self._h, i), self.ctx.handle, "server release request")
+
+    def stats(self) -> N.ServerStats:
+        s = N.ServerStats()
+        check(N.lib().fbk_server_get_stats(self._h, C.byref(s)), self.ctx.handle, "server stats")
+        return s
+
+    def release(self):
+        if self._h and self.ctx.alive:
+            N.lib().fbk_server_destroy(self._h)
+        self._h = C.c_void_p()
+        self._pending.clear()
 
     def __del__(self):
         try:

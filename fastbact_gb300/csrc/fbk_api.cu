@@ -803,6 +803,25 @@ FBK_API fbk_status fbk_cms_export(fbk_cms* c, uint8_t* out, uint64_t nbytes) {
     return FBK_OK;
 }
 
+FBK_API fbk_status fbk_cms_import(fbk_cms* c, const uint8_t* in, uint64_t nbytes) {
+    uint64_t want = 0;
+    if (!c || !in || fbk_cms_nbytes(c, &want) != FBK_OK || nbytes != want) return FBK_ERR_INVALID;
+    fbk_ctx* ctx = c->ctx;
+    uint8_t* d = (uint8_t*)dev_alloc(ctx, nbytes);
+    if (!d) return set_err(ctx, FBK_ERR_OOM, "cms import buffer");
+    cudaError_t e = cudaMemcpyAsync(d, in, nbytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) {
+        TimedLaunch tl;
+        time_begin(ctx, "cms_import", tl);
+        e = launch_cms_import((int)c->cbits, launch_cfg(ctx, 256, 0), c->cnt, c->n, d);
+        time_end(ctx, tl);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, d);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cms import");
+    return FBK_OK;
+}
+
 FBK_API fbk_status fbk_cms_merge(fbk_cms* dst, const fbk_cms* src) {
     if (!dst || !src || dst->cbits != src->cbits || dst->log2w != src->log2w) return FBK_ERR_INVALID;
     fbk_ctx* ctx = dst->ctx;

@@ -17,8 +17,13 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <map>
 #include <memory>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "fbk_device.cuh"
@@ -602,9 +607,13 @@ fbk_status drain_b(fbk_batch* B, const std::vector<BatchIso*>& W) {
             if (!V.empty() && bytes + q.bytes + (64ULL << 20) > free_b) break;
             st = alloc_b(B, W[j], q);
             if (st) {
+                // the pool is full or fragmented: run what fits, retry this isolate next
                 release_b(B, W[j]);
                 ctx->err.clear();
-                if (!V.empty()) break;
+                if (!V.empty()) {
+                    st = FBK_OK;
+                    break;
+                }
                 st = fallback(B, W[j]);
                 if (st) break;
                 finish_iso(B, W[j]);
@@ -874,6 +883,447 @@ FBK_API fbk_status fbk_batch_release(fbk_batch* B) {
         if (e) cudaEventDestroy(e);
     if (B->h_stage) cudaFreeHost(B->h_stage);
     delete B;
+    return FBK_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Serving: a request loop with continuous batching (see include/fbk.h)
+// ===========================================================================
+namespace {
+
+struct Req {
+    std::unique_ptr<BatchIso> iso;
+    fbk_arena_view bank[3]{};
+    fbk_arena_view sample{};
+    uint64_t n_bases = 0, n_reads = 0, sample_bases = 0;
+    int32_t state = 0;
+    fbk_status status = FBK_OK;
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    uint64_t reserved = 0;
+};
+
+// Device bytes a request may need before its pass 1 tells the exact table and
+// bucket sizes: reads, sketch, bitmap, and records/table/rows from the k-mer
+// occurrences (records <= windows; table keys taken as a quarter of the windows).
+uint64_t request_estimate(const fbk_batch_params& p, int nw, uint64_t n_bases, uint64_t n_reads, uint64_t sample_bases) {
+    const uint64_t reads = n_bases / 4 + n_reads * 16 + 8192;
+    const uint64_t sample = sample_bases / 4 + 65536;
+    const uint64_t a = (4ULL << p.cms_log2_width) * 4 + 4096 * 4 + n_bases / 8 + n_reads / 8 + 8192;
+    const double w = (double)n_bases;
+    const double b = w * (0.9 * 1.15 * 8.0 * (nw + 1) + 0.25 / 0.62 * (double)slot_bytes_of(nw) + 0.275 * (8.0 * nw + 3));
+    return reads + sample + a + (uint64_t)b + (16ULL << 20);
+}
+
+uint64_t bank_bytes(const fbk_bank* b) { return b ? b->n_words * 8 + b->n_reads * 16 + 4096 : 0; }
+
+void bank_free_done(fbk_ctx* ctx, fbk_bank*& b) {
+    if (!b) return;
+    dev_free(ctx, b->data);
+    dev_free(ctx, b->off);
+    dev_free(ctx, b->len);
+    dev_free(ctx, b->pair_idx);
+    delete b;
+    b = nullptr;
+}
+
+// Frees a finished request's device state without waiting on any stream (its work
+// has completed; the memory goes back to the shared pool).
+void free_iso_done(fbk_ctx* ctx, BatchIso* it) {
+    for (void** q : {(void**)&it->recs, (void**)&it->fill, (void**)&it->cnt, (void**)&it->hll12, (void**)&it->bm,
+                     (void**)&it->keep}) {
+        dev_free(ctx, *q);
+        *q = nullptr;
+    }
+    if (it->table) {
+        tbl_free_storage(it->table);
+        tbl_free_out(it->table);
+        delete it->table;
+        it->table = nullptr;
+    }
+    bank_free_done(ctx, it->bank);
+    bank_free_done(ctx, it->sample);
+}
+
+}  // namespace
+
+struct fbk_server {
+    fbk_ctx* ctx = nullptr;
+    fbk_server_params p{};
+    int nw = 1;
+    std::vector<fbk_ctx*> wctx;
+    std::vector<fbk_batch*> wb;
+    std::vector<std::thread> th;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<uint64_t> queued;
+    std::deque<uint64_t> counted;
+    std::map<uint64_t, std::unique_ptr<Req>> reqs;
+    uint64_t next_id = 0, budget = 0, reserved = 0, in_flight = 0;
+    bool stop = false;
+    double t0 = 0;
+    fbk_server_stats stats{};
+    Shape pass1{256, 0, 4}, solid{256, 0, 4};
+    bool tuned = false, tuning = false;
+};
+
+namespace {
+
+double srv_ms(const fbk_server* S) { return now_ms() - S->t0; }
+
+void reserve_set(fbk_server* S, Req* r, uint64_t bytes) {  // caller holds the lock
+    S->reserved = S->reserved - r->reserved + bytes;
+    r->reserved = bytes;
+    S->stats.peak_reserved_bytes = std::max(S->stats.peak_reserved_bytes, S->reserved);
+}
+
+void fail_req(fbk_server* S, Req* r, fbk_status st) {  // caller holds the lock
+    r->state = -1;
+    r->status = st;
+    r->t_done = srv_ms(S);
+    S->stats.failed++;
+    if (S->in_flight) S->in_flight--;
+    reserve_set(S, r, 0);
+}
+
+// Uploads, estimates and phase A of a wave of newly admitted requests.
+void job_admit(fbk_server* S, int w, const std::vector<Req*>& job) {
+    fbk_batch* B = S->wb[w];
+    fbk_ctx* ctx = B->ctx;
+    std::vector<Req*> ok;
+    for (Req* r : job) {
+        BatchIso* it = r->iso.get();
+        fbk_status st = bank_upload_impl(ctx, r->bank, 3, &it->bank);
+        if (st == FBK_OK) {
+            fbk_arena_view v = r->sample;
+            v.n_seqs = 2 * it->sample_pairs;
+            v.pair_idx = nullptr;
+            st = bank_upload_impl(ctx, &v, 1, &it->sample);
+        }
+        if (st == FBK_OK) {
+            std::lock_guard<std::mutex> lk(S->mu);
+            r->state = 2;  // the host buffers are no longer read
+            S->cv.notify_all();
+        }
+        if (st == FBK_OK) st = estimate_one(B, it);
+        if (st) {
+            free_iso(B, it);
+            std::lock_guard<std::mutex> lk(S->mu);
+            fail_req(S, r, st);
+            continue;
+        }
+        ok.push_back(r);
+    }
+    if (ok.empty()) return;
+    std::vector<BatchIso*> W;
+    for (Req* r : ok) W.push_back(r->iso.get());
+    bool tune_here = false;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (B->p.autotune && !S->tuned && !S->tuning) {
+            S->tuning = true;
+            tune_here = true;
+            B->tuned = false;
+        } else {
+            B->pass1 = S->pass1;
+            B->solid = S->solid;
+            B->tuned = true;  // tuned already, or another worker is tuning
+        }
+    }
+    const double a0 = now_ms();
+    fbk_status st = phase_a(B, W);
+    const double a1 = now_ms();
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (tune_here) {
+        S->tuning = false;
+        if (B->tuned) {
+            S->pass1 = B->pass1;
+            S->solid = B->solid;
+            S->tuned = true;
+        }
+    }
+    S->stats.busy_ms += a1 - a0;
+    if (st) {
+        for (Req* r : ok) {
+            free_iso(B, r->iso.get());
+            fail_req(S, r, st);
+        }
+        S->cv.notify_all();
+        return;
+    }
+    S->stats.waves_a++;
+    S->stats.isolates_a += ok.size();
+    for (Req* r : ok) {
+        BatchIso* it = r->iso.get();
+        r->state = 3;
+        reserve_set(S, r, bank_bytes(it->bank) + phase_a_bytes(B, it) + plan_b(B, it).bytes);
+        S->counted.push_back(r->iso->id);
+    }
+    S->cv.notify_all();
+}
+
+// Phase B of a wave of counted requests; their tables stay on the device.
+void job_tables(fbk_server* S, int w, const std::vector<Req*>& job) {
+    fbk_batch* B = S->wb[w];
+    std::vector<BatchIso*> W;
+    for (Req* r : job) W.push_back(r->iso.get());
+    const double b0 = now_ms();
+    fbk_status st = drain_b(B, W);
+    const double b1 = now_ms();
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stats.busy_ms += b1 - b0;
+    S->stats.waves_b++;
+    S->stats.isolates_b += job.size();
+    for (Req* r : job) {
+        BatchIso* it = r->iso.get();
+        if (it->res.state != 3) {
+            free_iso(B, it);
+            fail_req(S, r, st ? st : it->res.status);
+            continue;
+        }
+        bank_free_done(B->ctx, it->bank);  // the reads are consumed (the wave has completed)
+        uint64_t keep = it->table ? it->table->out_cap * (8ULL * S->nw + 3) : 0;
+        if (it->cnt) keep += (4ULL << B->p.cms_log2_width) * 4;
+        reserve_set(S, r, keep);
+        r->state = 4;
+        r->t_done = srv_ms(S);
+        S->stats.done++;
+        if (S->in_flight) S->in_flight--;
+    }
+    S->cv.notify_all();
+}
+
+void worker_main(fbk_server* S, int w) {
+    cudaSetDevice(S->ctx->device);
+    const uint32_t max_wave = std::max<uint32_t>(1, std::min<uint32_t>(BATCH_MAX_ISO, S->p.batch.max_wave ? S->p.batch.max_wave : 64));
+    std::unique_lock<std::mutex> lk(S->mu);
+    for (;;) {
+        std::vector<Req*> job;
+        int kind = 0;
+        if (!S->counted.empty()) {
+            kind = 2;
+            while (!S->counted.empty() && job.size() < max_wave) {
+                job.push_back(S->reqs[S->counted.front()].get());
+                S->counted.pop_front();
+            }
+        } else if (!S->queued.empty() && !S->stop) {
+            kind = 1;
+            while (!S->queued.empty() && job.size() < max_wave) {
+                Req* r = S->reqs[S->queued.front()].get();
+                const uint64_t est = r->reserved;  // the estimate, reserved on admission
+                const bool fits = S->reserved + est <= S->budget;
+                // first come, first served; a request alone always runs
+                if (!fits && !(S->in_flight == 0 && job.empty())) break;
+                S->queued.pop_front();
+                r->state = 1;
+                r->t_admit = srv_ms(S);
+                S->reserved += est;
+                S->stats.peak_reserved_bytes = std::max(S->stats.peak_reserved_bytes, S->reserved);
+                S->in_flight++;
+                S->stats.peak_in_flight = std::max<uint64_t>(S->stats.peak_in_flight, S->in_flight);
+                job.push_back(r);
+            }
+        }
+        if (job.empty()) {
+            if (S->stop && S->counted.empty()) break;
+            S->cv.wait_for(lk, std::chrono::milliseconds(20));
+            continue;
+        }
+        lk.unlock();
+        if (kind == 1) job_admit(S, w, job);
+        else job_tables(S, w, job);
+        lk.lock();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+FBK_API void fbk_server_defaults(fbk_server_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    fbk_batch_defaults(&p->batch);
+    p->batch.policy.enable_auto_subsample = 1;
+    p->batch.policy.depth = 110.0;
+    p->batch.policy.threshold_ratio = 150.0 / 110.0;
+    p->workers = 2;
+}
+
+FBK_API fbk_status fbk_server_create(fbk_ctx* ctx, const fbk_server_params* p, fbk_server** out) {
+    if (!ctx || !p || !out) return FBK_ERR_INVALID;
+    *out = nullptr;
+    if (p->workers < 1 || p->workers > 8) return set_err(ctx, FBK_ERR_INVALID, "server: 1 to 8 workers");
+    fbk_server* S = new fbk_server();
+    S->ctx = ctx;
+    S->p = *p;
+    S->nw = key_words(p->batch.key_bits);
+    S->t0 = now_ms();
+    fbk_status st = FBK_OK;
+    for (uint32_t w = 0; w < p->workers && st == FBK_OK; ++w) {
+        fbk_ctx* c = nullptr;
+        st = fbk_ctx_fork(ctx, &c);
+        if (st) break;
+        S->wctx.push_back(c);
+        fbk_batch* B = nullptr;
+        st = fbk_batch_create(c, &p->batch, &B);
+        if (st) {
+            ctx->err = c->err;
+            break;
+        }
+        S->wb.push_back(B);
+    }
+    if (st) {
+        fbk_server_destroy(S);
+        return st;
+    }
+    S->pass1 = S->wb[0]->pass1;
+    S->solid = S->wb[0]->solid;
+    uint64_t budget = p->budget_bytes;
+    if (!budget) {
+        uint64_t used = 0, size = 0, free_b = 0, largest = 0;
+        fbk_ctx_mem_info(ctx, &used, &size);
+        fbk_ctx_pool_free(ctx, &free_b, &largest);
+        budget = (uint64_t)(0.9 * (double)(size ? size : free_b));
+    }
+    // each worker keeps room for the estimator's scratch and its wave descriptors
+    const uint64_t scratch = (uint64_t)p->workers * (512ULL << 20);
+    S->budget = budget > scratch ? budget - scratch : budget / 2;
+    S->stats.budget_bytes = S->budget;
+    for (uint32_t w = 0; w < p->workers; ++w) S->th.emplace_back(worker_main, S, (int)w);
+    *out = S;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_server_submit(fbk_server* S, const fbk_arena_view bank[3], const fbk_arena_view* sample,
+                                     uint64_t sample_pairs, const fbk_count_stats* stats, uint64_t* id) {
+    if (!S || !bank || !sample || !stats) return FBK_ERR_INVALID;
+    if (sample->n_seqs < 2 * sample_pairs) return FBK_ERR_INVALID;
+    auto r = std::make_unique<Req>();
+    r->iso = std::make_unique<BatchIso>();
+    r->iso->stats = *stats;
+    r->iso->sample_pairs = sample_pairs;
+    r->iso->sample_len.assign(sample->lengths, sample->lengths + 2 * sample_pairs);
+    for (int a = 0; a < 3; ++a) {
+        r->bank[a] = bank[a];
+        for (uint64_t i = 0; i < bank[a].n_seqs; ++i) r->n_bases += bank[a].lengths[i];
+        r->n_reads += bank[a].n_seqs;
+    }
+    if (r->n_bases >= (1ULL << 31)) return FBK_ERR_INVALID;
+    r->sample = *sample;
+    for (uint64_t i = 0; i < 2 * sample_pairs; ++i) r->sample_bases += sample->lengths[i];
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->stop) return FBK_ERR_BUSY;
+    const uint64_t i = S->next_id++;
+    r->iso->id = i;
+    r->t_submit = srv_ms(S);
+    r->reserved = request_estimate(S->p.batch, S->nw, r->n_bases, r->n_reads, r->sample_bases);
+    S->reqs[i] = std::move(r);
+    S->queued.push_back(i);
+    S->stats.submitted++;
+    if (id) *id = i;
+    S->cv.notify_all();
+    return FBK_OK;
+}
+
+static void request_info(const fbk_server* S, const Req* r, fbk_request_info* out) {
+    out->state = r->state;
+    out->status = r->status;
+    out->t_submit_ms = r->t_submit;
+    out->t_admit_ms = r->t_admit;
+    out->t_done_ms = r->t_done;
+    out->reserved_bytes = r->state == 0 ? 0 : r->reserved;
+    out->result = r->iso->res;
+    (void)S;
+}
+
+FBK_API fbk_status fbk_server_poll(fbk_server* S, uint64_t id, fbk_request_info* out) {
+    if (!S || !out) return FBK_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto f = S->reqs.find(id);
+    if (f == S->reqs.end()) return FBK_ERR_INVALID;
+    request_info(S, f->second.get(), out);
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_server_wait(fbk_server* S, uint64_t id, double timeout_ms, fbk_request_info* out) {
+    if (!S) return FBK_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto f = S->reqs.find(id);
+    if (f == S->reqs.end()) return FBK_ERR_INVALID;
+    Req* r = f->second.get();
+    const auto until = std::chrono::steady_clock::now() + std::chrono::microseconds((int64_t)(timeout_ms * 1000.0));
+    while (r->state >= 0 && r->state < 4) {
+        if (S->cv.wait_until(lk, until) == std::cv_status::timeout && r->state >= 0 && r->state < 4) {
+            if (out) request_info(S, r, out);
+            return FBK_ERR_NOT_READY;
+        }
+    }
+    if (out) request_info(S, r, out);
+    return r->state < 0 ? (fbk_status)r->status : FBK_OK;
+}
+
+FBK_API fbk_status fbk_server_take_table(fbk_server* S, uint64_t id, fbk_table** out) {
+    if (!S || !out) return FBK_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto f = S->reqs.find(id);
+    if (f == S->reqs.end() || f->second->state != 4) return set_err(S->ctx, FBK_ERR_INVALID, "server: request has no table to take");
+    Req* r = f->second.get();
+    BatchIso* it = r->iso.get();
+    fbk_table* t = it->table;
+    it->table = nullptr;
+    t->ctx = S->ctx;  // the table lives in the shared pool; the caller's context releases it
+    free_iso_done(S->ctx, it);
+    reserve_set(S, r, 0);
+    r->state = 5;
+    *out = t;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_server_release_request(fbk_server* S, uint64_t id) {
+    if (!S) return FBK_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto f = S->reqs.find(id);
+    if (f == S->reqs.end()) return FBK_ERR_INVALID;
+    Req* r = f->second.get();
+    if (r->state != 4 && r->state != -1 && r->state != 5) return set_err(S->ctx, FBK_ERR_BUSY, "server: request still in flight");
+    free_iso_done(S->ctx, r->iso.get());
+    reserve_set(S, r, 0);
+    S->reqs.erase(f);
+    S->cv.notify_all();
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_server_get_stats(fbk_server* S, fbk_server_stats* out) {
+    if (!S || !out) return FBK_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(S->mu);
+    *out = S->stats;
+    out->reserved_bytes = S->reserved;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_server_destroy(fbk_server* S) {
+    if (!S) return FBK_OK;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop = true;
+        while (!S->queued.empty()) {
+            Req* r = S->reqs[S->queued.front()].get();
+            S->queued.pop_front();
+            r->state = -1;
+            r->status = FBK_ERR_BUSY;
+            S->stats.failed++;
+        }
+        S->cv.notify_all();
+    }
+    for (auto& t : S->th) t.join();
+    for (auto& kv : S->reqs)
+        if (!S->wb.empty()) free_iso(S->wb[0], kv.second->iso.get());
+    S->reqs.clear();
+    for (fbk_batch* B : S->wb) fbk_batch_release(B);
+    for (fbk_ctx* c : S->wctx) fbk_ctx_destroy(c);
+    delete S;
     return FBK_OK;
 }
 

@@ -183,6 +183,17 @@ __global__ void k_cms_export_u16(const uint32_t* __restrict__ cnt, uint64_t n, u
     }
 }
 
+// Inverse of the exports: counters from reference-layout bytes.
+__global__ void k_cms_import_nib(uint32_t* __restrict__ cnt, uint64_t n_bytes, const uint8_t* __restrict__ in) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_bytes; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = in[i];
+        reinterpret_cast<uint2*>(cnt)[i] = make_uint2(v & 15u, v >> 4);
+    }
+}
+__global__ void k_cms_import_u16(uint32_t* __restrict__ cnt, uint64_t n, const uint16_t* __restrict__ in) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) cnt[i] = in[i];
+}
+
 __global__ void __launch_bounds__(256) k_nthash_arena(BankDev b, const uint64_t* __restrict__ kbase, uint32_t k, uint64_t* out) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -269,6 +280,11 @@ cudaError_t launch_cms_merge(const Launch& L, uint32_t* dst, const uint32_t* src
 cudaError_t launch_cms_export(int cb, const Launch& L, const uint32_t* cnt, uint64_t n, uint8_t* out) {
     if (cb == 4) k_cms_export_nib<<<L.grid, L.block, 0, L.stream>>>(cnt, n / 2, out);
     else k_cms_export_u16<<<L.grid, L.block, 0, L.stream>>>(cnt, n, reinterpret_cast<uint16_t*>(out));
+    return cudaGetLastError();
+}
+cudaError_t launch_cms_import(int cb, const Launch& L, uint32_t* cnt, uint64_t n, const uint8_t* in) {
+    if (cb == 4) k_cms_import_nib<<<L.grid, L.block, 0, L.stream>>>(cnt, n / 2, in);
+    else k_cms_import_u16<<<L.grid, L.block, 0, L.stream>>>(cnt, n, reinterpret_cast<const uint16_t*>(in));
     return cudaGetLastError();
 }
 cudaError_t launch_nthash_arena(const Launch& L, const BankDev& b, const uint64_t* kbase, uint32_t k, uint64_t* out) {

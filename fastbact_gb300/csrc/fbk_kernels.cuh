@@ -151,6 +151,7 @@ cudaError_t launch_cms_merge(const Launch& L, uint32_t* dst, const uint32_t* src
 // Reference byte layout: counter_bits 4 = nibbles (byte c>>1, high nibble for odd c),
 // 16 = little-endian u16; values min(cap, count).
 cudaError_t launch_cms_export(int cb, const Launch& L, const uint32_t* cnt, uint64_t n, uint8_t* out);
+cudaError_t launch_cms_import(int cb, const Launch& L, uint32_t* cnt, uint64_t n, const uint8_t* in);
 cudaError_t launch_nthash_arena(const Launch& L, const BankDev& b, const uint64_t* kbase, uint32_t k, uint64_t* out);
 cudaError_t launch_canon_arena(int nw, const Launch& L, const BankDev& b, const uint64_t* kbase, uint32_t k,
                                uint64_t* out_words, uint8_t* out_rc);

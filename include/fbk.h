@@ -192,6 +192,9 @@ FBK_API fbk_status fbk_cms_nbytes(const fbk_cms* c, uint64_t* nbytes);
 FBK_API fbk_status fbk_cms_export(fbk_cms* c, uint8_t* out, uint64_t nbytes);
 /* dst = min(cap, dst + src) counter by counter: merging sketches of disjoint read
  * sets equals the sketch of their union. */
+/* Replaces the counters with bytes in the fbk_cms_export layout, e.g. the merged
+ * sketch of reads counted on several ranks (no counterpart in the reference). */
+FBK_API fbk_status fbk_cms_import(fbk_cms* c, const uint8_t* in, uint64_t nbytes);
 FBK_API fbk_status fbk_cms_merge(fbk_cms* dst, const fbk_cms* src);
 FBK_API fbk_status fbk_cms_release(fbk_cms* c);
 
@@ -372,6 +375,59 @@ FBK_API fbk_status fbk_batch_take_table(fbk_batch* b, uint64_t id, fbk_table** o
 FBK_API fbk_status fbk_batch_drop(fbk_batch* b, uint64_t id);
 FBK_API fbk_status fbk_batch_get_stats(const fbk_batch* b, fbk_batch_stats* out);
 FBK_API fbk_status fbk_batch_release(fbk_batch* b);
+
+/* ---- serving: a request loop with continuous batching ----------------------------
+ * No counterpart in the reference (one isolate per process).  A request is one
+ * isolate (reads, raw sample pairs, count statistics); the server computes for it
+ * exactly what a batch does.  Admission: a request enters when the reserved device
+ * bytes of all admitted requests plus its own estimate (reads, sketch, bitmap,
+ * solid table and record buckets; replaced by the exact sizes after pass 1) fit
+ * the budget.  Continuous batching: each worker (its own stream on the shared pool)
+ * takes every admitted request waiting for the same stage as one wave, so requests
+ * that arrive while others run join the next wave and waves of different stages
+ * overlap on the device.  Finished tables stay on the device (their bytes stay
+ * reserved) until the caller takes or releases them.  Calls may come from any
+ * host thread. */
+typedef struct fbk_server fbk_server;
+typedef struct {
+    fbk_batch_params batch;   /* counting parameters of every request */
+    uint32_t workers;         /* concurrent waves, one stream each: 2 */
+    uint32_t _pad;
+    uint64_t budget_bytes;    /* admission budget; 0: 90% of the pool (of free memory without a pool) */
+} fbk_server_params;
+/* Request states: 0 queued, 1 admitted (reads being uploaded), 2 estimated (reads on
+ * the device, host buffers no longer used), 3 counted (pass 1 done), 4 done (table
+ * ready), 5 drained (table taken or released), -1 failed. */
+typedef struct {
+    int32_t state;
+    int32_t status;           /* fbk_status of a failed request */
+    double t_submit_ms, t_admit_ms, t_done_ms;   /* server clock: ms since fbk_server_create */
+    uint64_t reserved_bytes;
+    fbk_batch_result result;
+} fbk_request_info;
+typedef struct {
+    uint64_t submitted, done, failed, waves_a, waves_b, isolates_a, isolates_b;
+    uint64_t reserved_bytes, peak_reserved_bytes, budget_bytes;
+    uint64_t peak_in_flight;  /* most requests admitted and not yet done */
+    double busy_ms;           /* summed worker time inside waves */
+} fbk_server_stats;
+
+FBK_API void fbk_server_defaults(fbk_server_params* p);
+FBK_API fbk_status fbk_server_create(fbk_ctx* ctx, const fbk_server_params* p, fbk_server** out);
+/* Queues one isolate.  The host buffers must stay valid until the request's state is
+ * 2 or more (or -1). */
+FBK_API fbk_status fbk_server_submit(fbk_server* s, const fbk_arena_view bank[3], const fbk_arena_view* sample,
+                                     uint64_t sample_pairs, const fbk_count_stats* stats, uint64_t* id);
+FBK_API fbk_status fbk_server_poll(fbk_server* s, uint64_t id, fbk_request_info* out);
+/* Waits until the request is done or failed; FBK_ERR_NOT_READY after timeout_ms. */
+FBK_API fbk_status fbk_server_wait(fbk_server* s, uint64_t id, double timeout_ms, fbk_request_info* out);
+/* Hands a done request's table to the caller (release it with fbk_table_release before
+ * destroying the context) and frees the request's remaining device state. */
+FBK_API fbk_status fbk_server_take_table(fbk_server* s, uint64_t id, fbk_table** out);
+FBK_API fbk_status fbk_server_release_request(fbk_server* s, uint64_t id);
+FBK_API fbk_status fbk_server_get_stats(fbk_server* s, fbk_server_stats* out);
+/* Finishes in-flight waves, fails queued requests, frees all request state. */
+FBK_API fbk_status fbk_server_destroy(fbk_server* s);
 
 /* ---- host ingest (trim_merge.rs:17-417), CPU side ----------------------------- */
 FBK_API fbk_status fbk_ingest_fastq(const char* r1, const char* r2, double subsample_factor, uint64_t min_len, uint32_t min_qual,

@@ -885,6 +885,17 @@ ORC_API uint64_t orc_cms_nbytes(const void* c) {
     const CMS* x = (const CMS*)c;
     return x->bits == 4 ? 4 * x->width / 2 : 4 * x->width * 2;
 }
+// Loads raw table bytes in the export layout (test plumbing for merged sketches of
+// sharded counts; the reference has no counterpart).
+ORC_API void orc_cms_import(void* c, const uint8_t* in) {
+    CMS* x = (CMS*)c;
+    if (x->bits == 4) {
+        for (size_t i = 0; i < x->nib.size(); ++i) x->nib[i].store(in[i], std::memory_order_relaxed);
+    } else {
+        for (size_t i = 0; i < x->c16.size(); ++i)
+            x->c16[i].store((uint16_t)(in[2 * i] | (in[2 * i + 1] << 8)), std::memory_order_relaxed);
+    }
+}
 ORC_API void orc_cms_export(const void* c, uint8_t* out) {
     const CMS* x = (const CMS*)c;
     if (x->bits == 4) {

@@ -69,6 +69,7 @@ _SIG = {
     "orc_cms_add_and_estimate": (C.c_uint32, [vp, C.c_uint64]),
     "orc_cms_nbytes": (C.c_uint64, [vp]),
     "orc_cms_export": (None, [vp, u8p]),
+    "orc_cms_import": (None, [vp, u8p]),
     "orc_build_pass1": (C.c_int, [C.POINTER(OrcArena), C.c_uint, C.c_int, vp, C.c_int, u64p, C.POINTER(u32p)]),
     "orc_build_pass1_contigs": (C.c_int, [u8p, u64p, C.c_uint64, C.c_uint, C.c_int, vp]),
     "orc_build_pass2": (vp, [C.POINTER(OrcArena), C.c_uint, C.c_int, vp, C.c_uint, C.c_int, u64p, C.POINTER(u32p), u8p,
@@ -150,6 +151,12 @@ class Cms:
         out = np.zeros(lib().orc_cms_nbytes(self.h), np.uint8)
         lib().orc_cms_export(self.h, p(out))
         return out
+
+    def load(self, raw: np.ndarray) -> None:
+        """Replaces the counters with raw bytes in the export layout."""
+        raw = np.ascontiguousarray(raw, dtype=np.uint8)
+        assert raw.size == lib().orc_cms_nbytes(self.h)
+        lib().orc_cms_import(self.h, p(raw))
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -1,0 +1,119 @@
+"""Counting one isolate across ranks (fastbact_gb300.shard) gives the single-process
+result: world-size-2 process groups over gloo on the CPU, with the oracle as each
+rank's counting engine (the device engine runs the same exchange code).  Checked:
+the merged pass-1 sketch bytes, the SolidKmerNode rows (union of the owners' rows)
+and the table digest, against the oracle counting every read in one process."""
+import os
+import socket
+
+import numpy as np
+import pytest
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+from fastbact_gb300 import api, shard
+from oracle import orc
+
+
+class OracleEngine:
+    """The oracle as a rank's counting engine (build.rs:84-289 restated on the CPU)."""
+
+    def pass1(self, bank, k, key_bits, log2w, counter_bits):
+        self.cms = orc.Cms(1 << log2w, counter_bits)
+        ar = orc.arenas3(bank)
+        assert orc.lib().orc_build_pass1(ar, k, key_bits, self.cms.h, 2, None, None) == 0
+        return self.cms.export()
+
+    def load(self, raw):
+        self.cms.load(raw)
+
+    def pass2(self, bank, k, key_bits, target_solid_cov):
+        ar = orc.arenas3(bank)
+        t_solid = 2 if target_solid_cov is None else target_solid_cov
+        h = orc.lib().orc_build_pass2(ar, k, key_bits, self.cms.h, t_solid, 2, None, None, None, None, 0)
+        assert h
+        keys, cov, edges = orc.Table(h, key_bits).export_acc()
+        return keys, edges
+
+
+CASES = [(31, 64, 16, 16, None), (21, 64, 4, 14, None), (45, 128, 16, 15, 4), (77, 256, 4, 14, None)]
+
+
+def isolate():
+    p = api.synth_params(seed=77, genome_len=20_000, coverage=25.0, gc=0.55, n_repeats=2, repeat_len=1000)
+    return api.synth_isolate(p, threads=1, sample_pairs=0)[0]
+
+
+def _rank_main(rank, world, port, q):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        bank = isolate()
+        out = []
+        for k, kb, cb, log2w, tsc in CASES:
+            rows, merged, d = shard.sharded_build(OracleEngine(), bank, k, kb, log2w, cb, tsc, rank, world)
+            gathered = [None] * world
+            dist.all_gather_object(gathered, rows)
+            out.append((gathered, merged, d))
+        if rank == 0:
+            q.put(out)
+    finally:
+        dist.destroy_process_group()
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+@pytest.mark.parametrize("world", [2])
+def test_sharded_count_equals_single_process(world):
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    try:
+        out = q.get(timeout=300)  # read before joining: a child cannot exit while its result fills the pipe
+    finally:
+        for p in procs:
+            if p.is_alive():
+                p.join(timeout=60)
+    for p in procs:
+        p.join(timeout=300)
+        assert p.exitcode == 0
+    bank = isolate()
+    for (k, kb, cb, log2w, tsc), (gathered, merged, d) in zip(CASES, out):
+        o_cms, o_tab, _, mtc = orc.build_front(bank, k, kb, log2w, cb, tsc, threads=2)
+        assert np.array_equal(merged, o_cms.export()), (k, "merged sketch differs")
+        keys = np.concatenate([g[0] for g in gathered])
+        cov = np.concatenate([g[1] for g in gathered])
+        mask = np.concatenate([g[2] for g in gathered])
+        sk, sc, sm = api.sort_rows(keys, cov, mask)
+        ok, oc, om = api.sort_rows(*o_tab.export_solid(mtc))
+        assert len(sk) > 100
+        assert np.array_equal(sk, ok) and np.array_equal(sc, oc) and np.array_equal(sm, om), k
+        # every key has exactly one owner
+        assert len(np.unique(sk, axis=0)) == len(sk)
+        assert d == o_tab.digest(mtc)[0]
+
+
+
+def test_owner_partition_is_balanced():
+    keys = np.arange(1, 200_001, dtype=np.uint64).reshape(-1, 1) * np.uint64(0x9E3779B97F4A7C15)
+    for world in (2, 3, 8):
+        counts = np.bincount(shard.owner(keys, world), minlength=world)
+        assert counts.min() > 0.9 * len(keys) / world
+
+
+def test_capped_sum_identity():
+    # min(cap, min(cap, a) + min(cap, b)) == min(cap, a + b) for positive counts
+    rng = np.random.default_rng(3)
+    a, b = rng.integers(0, 70000, 10000), rng.integers(0, 70000, 10000)
+    for cap in (15, 65535):
+        assert np.array_equal(np.minimum(cap, np.minimum(cap, a) + np.minimum(cap, b)), np.minimum(cap, a + b))
