@@ -345,8 +345,10 @@ def run_ours(args, rank, world, local):
                 "generation_s": round(gen_s, 1), "tuning": tune,
             },
             "kernel_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in kernel_ms.items()},
-            "roofline": {"kernel": {"pass1": "pass 1 (k_pass1_sweep: 4 row-slice sweeps)",
-                                    "pass2": "pass 2 (k_solid_sweep + k_emit + k_upsert)"}[dom],
+            "roofline": {"kernel": ({"pass1": "pass 1 (k_pass1_sweep: 4 row-slice sweeps)",
+                                     "pass2": "pass 2 (k_solid_sweep + k_emit + k_upsert)"} if kernel_ms["solid"][0] > 0 else
+                                    {"pass1": "pass 1 (k_ladder_pass1: one sweep, t_solid-level gate ladder)",
+                                     "pass2": "pass 2 (k_emit_ladder + k_upsert)"})[dom],
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
                          "alg_bytes_per_pass": per_pass_bytes, "ms_per_pass": per_pass_ms,
@@ -456,6 +458,37 @@ def run_batch_mode(args):
     mismatches = sum(1 for a, c in zip(digests, plain) if a != c)
     st = b.stats()
     b.release()
+
+    # ---- diagnostics: per-kernel device time of both paths (stream launches, events) --
+    fams = ("batch_pass1", "batch_solid", "batch_count", "batch_emit", "batch_prefix", "batch_upsert", "pass1", "solid",
+            "pass2_emit", "pass2_upsert", "pass2_direct", "table_init", "convert", "est_", "subsample", "clamp")
+
+    def timed_families(fn):
+        ctx.sync()
+        ctx.timing_reset()
+        ctx.set_timing(True)
+        fn()
+        ctx.sync()
+        out = {f: round(ctx.timing(f)[0], 2) for f in fams}
+        ctx.set_timing(False)
+        return {f: v for f, v in out.items() if v > 0}
+
+    def diag_batch():
+        bd = api.Batch(ctx, api.batch_params(policy=cohort.policy(), k=BATCH_K, cms_log2_width=BATCH_LOG2W, counter_bits=16,
+                                             use_graphs=0, autotune=0))
+        ids_d = [bd.submit(m.bank, m.sample, m.sample_pairs, m.stats) for m in members]
+        bd.run()
+        bd.release()
+
+    def diag_plain():
+        for m in members:
+            db, ds = api.DeviceBank(ctx, m.bank), api.DeviceBank(ctx, m.sample)
+            _, _, t = plain_isolate(api, ctx, db, ds, m)
+            t.release()
+            db.release()
+            ds.release()
+
+    diag = {"batch_ms": timed_families(diag_batch), "plain_ms": timed_families(diag_plain)}
     line = {
         "metric": "isolates/h (batched k=31 counting front end: estimator + subsampling policy + passes 1-2)",
         "value": args.isolates / batch_s * 3600.0, "unit": "isolates/h", "n_gpus": 1, "steps": 1, "warmup": 1,
@@ -480,6 +513,7 @@ def run_batch_mode(args):
                              "solid": [st.solid_block, st.solid_grid, st.solid_rows],
                              "emit": [st.emit_block, st.emit_grid], "upsert": [st.upsert_block, st.upsert_grid]}},
         "gpu_launches": s1.kernel_launches - launches0 if s1.kernel_launches >= launches0 else None,
+        "kernel_ms": diag,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)

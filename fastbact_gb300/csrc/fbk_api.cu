@@ -391,6 +391,7 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "load_factor" && v >= 0.1 && v <= 0.9) ctx->load_factor = v;
     else if (n == "pass2_mode" && (v == 0 || v == 1)) ctx->pass2_mode = (int)v;
     else if (n == "record_factor" && v > 0 && v <= 16) ctx->record_factor = v;
+    else if (n == "sketch_mode" && (v == 0 || v == 1)) ctx->sketch_mode = (int)v;
     // the pass kernels are compiled for blocks of at most 256 threads
     else if (n == "block_pass1" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_pass1 = (int)v;
     else if (n == "grid_pass1" && v >= 0) ctx->grid_pass1 = (int)v;
@@ -409,6 +410,7 @@ FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, doub
     else if (n == "load_factor") *v = ctx->load_factor;
     else if (n == "pass2_mode") *v = ctx->pass2_mode;
     else if (n == "record_factor") *v = ctx->record_factor;
+    else if (n == "sketch_mode") *v = ctx->sketch_mode;
     else if (n == "block_pass1") *v = ctx->block_pass1;
     else if (n == "grid_pass1") *v = ctx->grid_pass1;
     else if (n == "block_pass2") *v = ctx->block_pass2;
@@ -1017,16 +1019,27 @@ static uint64_t next_pow2(uint64_t x) {
     return t;
 }
 
+// The pass-1 gate kept as a threshold ladder instead of counts (fbk_k_ladder.cu).
+struct Ladder {
+    uint32_t* bits = nullptr;
+    uint32_t log2w = 0;
+};
+
 // Solidity bitmap of a bank (bit = first base of a window, 1 = passes the CMS gate):
 // starts all ones, one sweep per row slice clears the failing windows.
 static fbk_status solidity_bitmap(fbk_ctx* ctx, const fbk_bank* b, const fbk_cms* cms, const fbk_build_params* p, int nw,
-                                  const uint64_t* keep_bits, uint32_t** bm_out) {
+                                  const uint64_t* keep_bits, uint32_t** bm_out, const Ladder* lad) {
     const uint64_t n_bm = b->n_words + 9;
     uint32_t* bm = (uint32_t*)dev_alloc(ctx, n_bm * 4);
     if (!bm) return set_err(ctx, FBK_ERR_OOM, "solidity bitmap");
     *bm_out = bm;
     CK(ctx, cudaMemsetAsync(bm, 0xFF, n_bm * 4, ctx->stream));
     Launch L = launch_cfg_persistent(ctx, ctx->block_pass2, ctx->grid_pass2);
+    if (lad) {
+        TIMED(ctx, "solid", launch_ladder_solid(nw, L, bank_view(b, 0, b->n_reads, keep_bits), p->k, lad->bits, lad->log2w,
+                                                p->t_solid, bm));
+        return FBK_OK;
+    }
     const uint64_t w = 1ULL << cms->log2w;
     const SweepPlan sp = sweep_plan(ctx, cms->log2w);
     const BankDev bv = bank_view(b, 0, b->n_reads, keep_bits);
@@ -1080,7 +1093,7 @@ static fbk_status buckets_alloc(fbk_ctx* ctx, uint64_t cap, uint64_t slot_bytes,
 // bucket stripe overflows, the chunk is redone by the direct sweep.
 static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cms* cms, const fbk_build_params* p,
                                    const uint64_t* keep_bits, const fbk_bank* contigs, uint64_t distinct_hint,
-                                   fbk_table** out) {
+                                   fbk_table** out, const Ladder* lad = nullptr) {
     const int nw = nw_of(p->key_bits);
     if (!nw || p->k < 1 || p->k > max_k_of(p->key_bits)) return set_err(ctx, FBK_ERR_INVALID, "k out of range for key_bits");
     if (p->t_solid > 0xFFFF || p->min_trans_cov > 0xFFFF) return set_err(ctx, FBK_ERR_INVALID, "thresholds must fit u16");
@@ -1093,20 +1106,29 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
     } else {
         cap = std::max<uint64_t>(1024, (uint64_t)((double)distinct_hint / ctx->load_factor) + 1024);
     }
+    // With a ladder gate and record buckets, the emit kernel evaluates the gate
+    // itself; the bitmap is built only if a direct sweep is needed.
     uint32_t* bm = nullptr;
-    fbk_status st = solidity_bitmap(ctx, b, cms, p, nw, keep_bits, &bm);
-    if (st) {
-        dev_free(ctx, bm);
-        return st;
-    }
     struct BmGuard {
         fbk_ctx* c;
-        uint32_t* p;
+        uint32_t** p;
         ~BmGuard() {
             cudaStreamSynchronize(c->stream);
-            dev_free(c, p);
+            dev_free(c, *p);
         }
-    } bmg{ctx, bm};
+    } bmg{ctx, &bm};
+    const bool inline_gate = lad && ctx->pass2_mode == 1;
+    auto need_bitmap = [&]() -> fbk_status {
+        if (bm) return FBK_OK;
+        fbk_status s2 = solidity_bitmap(ctx, b, cms, p, nw, keep_bits, &bm, lad);
+        if (s2) {
+            dev_free(ctx, bm);
+            bm = nullptr;
+        }
+        return s2;
+    };
+    fbk_status st = inline_gate ? FBK_OK : need_bitmap();
+    if (st) return st;
     fbk_table* t = new fbk_table();
     t->ctx = ctx;
     t->nw = (uint32_t)nw;
@@ -1155,7 +1177,10 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
             first_launch = false;
             const BankDev bv = bank_view(b, b->chunk_starts[c], b->chunk_starts[c + 1], keep_bits);
             CK(ctx, cudaMemsetAsync(bk.d.fill, 0, (uint64_t)bk.d.n_buckets * bk.d.stripes * 8, ctx->stream));
-            TIMED(ctx, "pass2_emit", launch_emit(nw, L, bv, p->k, bm, 1, td, bk.d));
+            if (inline_gate)
+                TIMED(ctx, "pass2_emit", launch_emit_ladder(nw, L, bv, p->k, lad->bits, lad->log2w, p->t_solid, td, bk.d));
+            else
+                TIMED(ctx, "pass2_emit", launch_emit(nw, L, bv, p->k, bm, 1, td, bk.d));
             for (uint32_t bu = 0; bu < bk.d.n_buckets; ++bu)
                 TIMED(ctx, "pass2_upsert", launch_upsert(nw, L, bk.d, bu, 1, 1, td, ctx->d_status));
         }
@@ -1166,6 +1191,13 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
             ovf = *(uint32_t*)ctx->h_pinned;
         }
         if (ovf && max_records) {
+            st = need_bitmap();
+            if (st) {
+                table_free_storage(t);
+                table_free_out(t);
+                delete t;
+                return st;
+            }
             if (use_buckets) {
                 // A stripe ran out of room: recount every chunk with the direct sweep.
                 table_free_storage(t);
@@ -1251,6 +1283,52 @@ FBK_API fbk_status fbk_solid_build(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
     return st;
 }
 
+// Build front end when the caller does not ask for the sketch: pass 1 keeps only
+// the gate pass 2 reads (a t_solid-level ladder, fbk_k_ladder.cu) in one sweep per read
+// chunk, the solidity bitmap takes one sweep, pass 2 and the conversion are unchanged.
+static fbk_status build_front_ladder(fbk_ctx* ctx, const fbk_bank* b, const fbk_build_params* p, const fbk_subsample* ss,
+                                     uint32_t log2w, fbk_table** out) {
+    const int nw = nw_of(p->key_bits);
+    if (!nw || p->k < 1 || p->k > max_k_of(p->key_bits)) return set_err(ctx, FBK_ERR_INVALID, "k out of range for key_bits");
+    if (log2w < 1 || log2w > 30) return set_err(ctx, FBK_ERR_INVALID, "cms_log2_width out of range");
+    Ladder lad;
+    lad.log2w = log2w;
+    const uint64_t lad_bytes = (uint64_t)p->t_solid * (4ULL << log2w) / 8 + 256;
+    lad.bits = (uint32_t*)dev_alloc(ctx, lad_bytes);
+    uint32_t* hll = (uint32_t*)dev_alloc(ctx, 4096 * 4);
+    uint64_t* keep = nullptr;
+    fbk_status st = (!lad.bits || !hll) ? set_err(ctx, FBK_ERR_OOM, "sketch gate") : FBK_OK;
+    if (st == FBK_OK) st = make_keep_bits(ctx, b, ss, &keep);
+    if (st == FBK_OK) {
+        cudaError_t e = cudaMemsetAsync(lad.bits, 0, lad_bytes, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(hll, 0, 4096 * 4, ctx->stream);
+        if (e != cudaSuccess) st = cuda_err(ctx, e, "sketch gate clear");
+    }
+    Launch L = launch_cfg_persistent(ctx, ctx->block_pass1, ctx->grid_pass1);
+    for (size_t c = 0; st == FBK_OK && c + 1 < b->chunk_starts.size(); ++c) {
+        TimedLaunch tl;
+        time_begin(ctx, "pass1", tl);
+        cudaError_t e = launch_ladder_pass1(nw, L, bank_view(b, b->chunk_starts[c], b->chunk_starts[c + 1], keep), p->k, lad.bits,
+                                            log2w, p->t_solid, hll);
+        time_end(ctx, tl);
+        if (e != cudaSuccess) st = cuda_err(ctx, e, "pass1 ladder");
+    }
+    uint64_t distinct = 0;
+    if (st == FBK_OK && !p->table_log2_cap) {
+        fbk_cms view;
+        view.ctx = ctx;
+        view.hll12 = hll;
+        st = cms_distinct(&view, &distinct);
+        view.hll12 = nullptr;
+    }
+    if (st == FBK_OK) st = solid_build_impl(ctx, b, nullptr, p, keep, nullptr, distinct, out, &lad);
+    cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, keep);
+    dev_free(ctx, hll);
+    dev_free(ctx, lad.bits);
+    return st;
+}
+
 FBK_API fbk_status fbk_build_front(fbk_ctx* ctx, const fbk_bank* b, const fbk_build_params* p, const fbk_subsample* ss,
                                    const uint8_t* contig_ascii, const uint64_t* contig_offs, uint64_t n_contigs,
                                    fbk_table** out, fbk_cms** cms_out) {
@@ -1264,6 +1342,10 @@ FBK_API fbk_status fbk_build_front(fbk_ctx* ctx, const fbk_bank* b, const fbk_bu
         log2w = 0;
         while ((1ULL << log2w) < w) ++log2w;
     }
+    const uint32_t cap = p->counter_bits == 4 ? 15u : 0xFFFFu;
+    if (!cms_out && n_contigs == 0 && ctx->sketch_mode == 1 && p->t_solid >= 1 && p->t_solid <= LADDER_MAX_LEVELS &&
+        p->t_solid <= cap && p->counter_bits != 0 && (p->counter_bits == 4 || p->counter_bits == 16))
+        return build_front_ladder(ctx, b, p, ss, log2w, out);
     fbk_cms* cms = nullptr;
     fbk_status st = fbk_cms_create(ctx, log2w, p->counter_bits, &cms);
     if (st) return st;
@@ -1488,5 +1570,12 @@ fbk_status tbl_convert(fbk_table* t) { return table_convert(t, nullptr, nullptr,
 fbk_status solid_build(fbk_ctx* ctx, const fbk_bank* b, const fbk_cms* cms, const fbk_build_params* p, const uint64_t* keep_bits,
                        uint64_t distinct_hint, fbk_table** out) {
     return solid_build_impl(ctx, b, cms, p, keep_bits, nullptr, distinct_hint, out);
+}
+fbk_status solid_build_ladder(fbk_ctx* ctx, const fbk_bank* b, uint32_t* ladder, uint32_t log2w, const fbk_build_params* p,
+                              const uint64_t* keep_bits, uint64_t distinct_hint, fbk_table** out) {
+    Ladder lad;
+    lad.bits = ladder;
+    lad.log2w = log2w;
+    return solid_build_impl(ctx, b, nullptr, p, keep_bits, nullptr, distinct_hint, out, &lad);
 }
 }  // namespace fbk

@@ -42,7 +42,8 @@ struct BatchIso {
     fbk_count_stats stats{};
     fbk_batch_result res{};
     uint64_t* keep = nullptr;
-    uint32_t* cnt = nullptr;
+    uint32_t* cnt = nullptr;   // exact sketch (keep_sketch), or
+    uint32_t* lad = nullptr;   // the gate ladder
     uint32_t* hll12 = nullptr;
     uint32_t* bm = nullptr;
     uint64_t distinct = 0, records = 0;
@@ -67,6 +68,7 @@ struct fbk_batch {
     fbk_ctx* ctx = nullptr;
     fbk_batch_params p{};
     int nw = 1;
+    bool ladder = false;  // the gate is a t_solid-level ladder (no sketch kept)
     std::vector<std::unique_ptr<BatchIso>> isos;
     fbk_batch_stats stats{};
     Shape pass1{256, 0, 4}, solid{256, 0, 4}, emit{256, 0, 0}, upsert{256, 0, 0};
@@ -88,8 +90,10 @@ void free_counting(fbk_batch* B, BatchIso* it, bool keep_sketch) {
         dev_free(ctx, it->cnt);
         it->cnt = nullptr;
     }
+    dev_free(ctx, it->lad);
     dev_free(ctx, it->hll12);
     dev_free(ctx, it->bm);
+    it->lad = nullptr;
     it->hll12 = nullptr;
     it->bm = nullptr;
 }
@@ -194,6 +198,7 @@ IsoDev iso_dev(const fbk_batch* B, const BatchIso* it, unsigned long long* nrec,
     IsoDev d{};
     d.b = bank_view(it->bank, 0, it->bank->n_reads, it->keep);
     d.cnt = it->cnt;
+    d.lad = it->lad;
     d.hll12 = it->hll12;
     d.bm = it->bm;
     d.n_records = nrec;
@@ -263,8 +268,12 @@ fbk_status upload_wave(fbk_batch* B, const std::vector<BatchIso*>& W, WaveBufs& 
     return FBK_OK;
 }
 
+uint64_t gate_bytes(const fbk_batch* B) {
+    return B->ladder ? (uint64_t)B->p.t_solid * (4ULL << B->p.cms_log2_width) / 8 + 256 : (4ULL << B->p.cms_log2_width) * 4;
+}
+
 uint64_t phase_a_bytes(const fbk_batch* B, const BatchIso* it) {
-    return (4ULL << B->p.cms_log2_width) * 4 + 4096 * 4 + (it->bank->n_words + 9) * 4 + 4096;
+    return gate_bytes(B) + 4096 * 4 + (it->bank->n_words + 9) * 4 + 4096;
 }
 
 // Autotuner: times candidate launch shapes of the pass-1 and solidity kernels on one
@@ -278,10 +287,14 @@ fbk_status autotune(fbk_batch* B, BatchIso* it) {
     std::vector<BatchIso*> one{it};
     st = upload_wave(B, one, w);
     if (st) return st;
-    const uint64_t cms_bytes = (4ULL << B->p.cms_log2_width) * 4;
+    const uint64_t cms_bytes = gate_bytes(B);
     const int blocks[] = {128, 256};
     const int per_sm[] = {0, 2, 4};
-    const int rows[] = {4, 2, 1};
+    const int rows_all[] = {4, 2, 1};
+    const int rows_one[] = {4};
+    // a ladder serves all rows in one sweep: only block and grid are tuned
+    const std::vector<int> rows = B->ladder ? std::vector<int>(rows_one, rows_one + 1) : std::vector<int>(rows_all, rows_all + 3);
+    uint32_t* gate = B->ladder ? it->lad : it->cnt;
     auto timed = [&](auto&& launch, float* ms) -> fbk_status {
         CK(ctx, cudaEventRecord(B->ev[0], ctx->stream));
         fbk_status s2 = launch();
@@ -297,9 +310,13 @@ fbk_status autotune(fbk_batch* B, BatchIso* it) {
         for (int bl : blocks)
             for (int ps : per_sm) {
                 Shape s{bl, ps ? ps * ctx->num_sms : 0, rp};
-                CK(ctx, cudaMemsetAsync(it->cnt, 0, cms_bytes, ctx->stream));
+                CK(ctx, cudaMemsetAsync(gate, 0, cms_bytes, ctx->stream));
                 float ms = 0;
                 st = timed([&]() -> fbk_status {
+                    if (B->ladder) {
+                        TIMED(ctx, "tune_pass1", launch_batch_lpass1(B->nw, shape_launch(ctx, s), w.iso, w.rb, 1, B->p.k));
+                        return FBK_OK;
+                    }
                     for (uint32_t r = 0; r < 4; r += (uint32_t)rp)
                         TIMED(ctx, "tune_pass1", launch_batch_pass1(B->nw, shape_launch(ctx, s), w.iso, w.rb, 1, B->p.k, r, r + rp, 0));
                     return FBK_OK;
@@ -321,6 +338,10 @@ fbk_status autotune(fbk_batch* B, BatchIso* it) {
                 CK(ctx, cudaMemsetAsync(it->bm, 0xFF, bm_bytes, ctx->stream));
                 float ms = 0;
                 st = timed([&]() -> fbk_status {
+                    if (B->ladder) {
+                        TIMED(ctx, "tune_solid", launch_batch_lsolid(B->nw, shape_launch(ctx, s), w.iso, w.rb, 1, B->p.k));
+                        return FBK_OK;
+                    }
                     for (uint32_t r = 0; r < 4; r += (uint32_t)rp)
                         TIMED(ctx, "tune_solid", launch_batch_solid(B->nw, shape_launch(ctx, s), w.iso, w.rb, 1, B->p.k, r, r + rp));
                     return FBK_OK;
@@ -344,12 +365,13 @@ fbk_status autotune(fbk_batch* B, BatchIso* it) {
 fbk_status phase_a(fbk_batch* B, const std::vector<BatchIso*>& W) {
     fbk_ctx* ctx = B->ctx;
     const uint32_t n = (uint32_t)W.size();
-    const uint64_t cms_bytes = (4ULL << B->p.cms_log2_width) * 4;
+    const uint64_t cms_bytes = gate_bytes(B);
     for (BatchIso* it : W) {
-        it->cnt = (uint32_t*)dev_alloc(ctx, cms_bytes);
+        if (B->ladder) it->lad = (uint32_t*)dev_alloc(ctx, cms_bytes);
+        else it->cnt = (uint32_t*)dev_alloc(ctx, cms_bytes);
         it->hll12 = (uint32_t*)dev_alloc(ctx, 4096 * 4);
         it->bm = (uint32_t*)dev_alloc(ctx, (it->bank->n_words + 9) * 4);
-        if (!it->cnt || !it->hll12 || !it->bm) return set_err(ctx, FBK_ERR_OOM, "batch sketches");
+        if (!(it->cnt || it->lad) || !it->hll12 || !it->bm) return set_err(ctx, FBK_ERR_OOM, "batch sketches");
     }
     if (B->p.autotune && !B->tuned) {
         BatchIso* big = *std::max_element(W.begin(), W.end(), [](const BatchIso* a, const BatchIso* b) {
@@ -366,12 +388,18 @@ fbk_status phase_a(fbk_batch* B, const std::vector<BatchIso*>& W) {
     const uint32_t k = B->p.k;
     st = run_phase(B, &B->stats.ms_phase_a, [&]() -> fbk_status {
         for (BatchIso* it : W) {
-            CK(ctx, cudaMemsetAsync(it->cnt, 0, cms_bytes, ctx->stream));
+            CK(ctx, cudaMemsetAsync(B->ladder ? it->lad : it->cnt, 0, cms_bytes, ctx->stream));
             CK(ctx, cudaMemsetAsync(it->hll12, 0, 4096 * 4, ctx->stream));
             CK(ctx, cudaMemsetAsync(it->bm, 0xFF, (it->bank->n_words + 9) * 4, ctx->stream));
         }
         CK(ctx, cudaMemsetAsync(w.cnt, 0, (uint64_t)n * 64, ctx->stream));
         CK(ctx, cudaMemsetAsync(w.status, 0, (uint64_t)n * 8, ctx->stream));
+        if (B->ladder) {
+            TIMED(ctx, "batch_pass1", launch_batch_lpass1(B->nw, shape_launch(ctx, B->pass1), w.iso, w.rb, n, k));
+            TIMED(ctx, "batch_solid", launch_batch_lsolid(B->nw, shape_launch(ctx, B->solid), w.iso, w.rb, n, k));
+            TIMED(ctx, "batch_count", launch_batch_count(shape_launch(ctx, B->solid), w.iso, w.rb, n, k));
+            return FBK_OK;
+        }
         for (uint32_t r = 0; r < 4; r += (uint32_t)B->pass1.rows)
             TIMED(ctx, "batch_pass1", launch_batch_pass1(B->nw, shape_launch(ctx, B->pass1), w.iso, w.rb, n, k, r,
                                                          r + (uint32_t)B->pass1.rows, r == 0));
@@ -491,7 +519,8 @@ fbk_status fallback(fbk_batch* B, BatchIso* it) {
     bp.counter_bits = B->p.counter_bits;
     bp.t_solid = B->p.t_solid;
     bp.min_trans_cov = B->p.min_trans_cov;
-    fbk_status st = solid_build(ctx, it->bank, &view, &bp, it->keep, it->distinct * 2, &it->table);
+    fbk_status st = B->ladder ? solid_build_ladder(ctx, it->bank, it->lad, B->p.cms_log2_width, &bp, it->keep, it->distinct * 2, &it->table)
+                              : solid_build(ctx, it->bank, &view, &bp, it->keep, it->distinct * 2, &it->table);
     view.cnt = nullptr;
     if (st) return st;
     it->res.fallback = 1;
@@ -786,6 +815,8 @@ FBK_API fbk_status fbk_batch_create(fbk_ctx* ctx, const fbk_batch_params* p, fbk
     B->ctx = ctx;
     B->p = *p;
     B->nw = nw;
+    B->ladder = !p->keep_sketch && ctx->sketch_mode == 1 && p->t_solid >= 1 && p->t_solid <= LADDER_MAX_LEVELS &&
+                p->t_solid <= cms_cap_of(p->counter_bits);
     B->pass1 = {ctx->block_pass1, ctx->grid_pass1, 4};
     B->solid = {ctx->block_pass2, ctx->grid_pass2, 4};
     B->emit = {ctx->block_pass2, ctx->grid_pass2, 0};
@@ -931,8 +962,8 @@ void bank_free_done(fbk_ctx* ctx, fbk_bank*& b) {
 // Frees a finished request's device state without waiting on any stream (its work
 // has completed; the memory goes back to the shared pool).
 void free_iso_done(fbk_ctx* ctx, BatchIso* it) {
-    for (void** q : {(void**)&it->recs, (void**)&it->fill, (void**)&it->cnt, (void**)&it->hll12, (void**)&it->bm,
-                     (void**)&it->keep}) {
+    for (void** q : {(void**)&it->recs, (void**)&it->fill, (void**)&it->cnt, (void**)&it->lad, (void**)&it->hll12,
+                     (void**)&it->bm, (void**)&it->keep}) {
         dev_free(ctx, *q);
         *q = nullptr;
     }

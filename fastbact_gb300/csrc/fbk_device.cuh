@@ -112,13 +112,18 @@ __device__ __forceinline__ void window_canonical(const uint64_t* __restrict__ d,
     Key<NW> fwd, rc;
 #pragma unroll
     for (int j = 0; j < NW; ++j) {
-        const int src = j - (int)ws;
-        uint64_t v = 0;
-        if (src >= 0) {
-            v = R[src] >> bs;
-            if (bs && src >= 1) v |= R[src - 1] << (64 - bs);
+        // word j takes R[j - ws] >> bs and the low bits of R[j - ws - 1]; the word
+        // shift is selected among its NW possible values so every R index is a
+        // compile-time constant (the array stays in registers)
+        uint64_t hi = 0, lo = 0;
+#pragma unroll
+        for (int c = 0; c < NW; ++c) {
+            if (ws == (uint32_t)c) {
+                hi = (j - c >= 0) ? R[j - c >= 0 ? j - c : 0] : 0ULL;
+                lo = (j - c - 1 >= 0) ? R[j - c - 1 >= 0 ? j - c - 1 : 0] : 0ULL;
+            }
         }
-        fwd.w[j] = v;
+        fwd.w[j] = (hi >> bs) | (bs ? (lo << (64 - bs)) : 0ULL);
     }
     // rc: ~W masked to 2k bits; LSB-first word i is big-endian word NW-1-i.
 #pragma unroll

@@ -70,6 +70,7 @@ struct fbk_ctx {
     double load_factor = 0.62;            // solid table keys / slots when sized from the estimate
     int pass2_mode = 1;                   // 1 = record buckets, 0 = direct sweep
     double record_factor = 1.25;          // bucket capacity / expected records per stripe
+    int sketch_mode = 1;                  // 1: a build that does not return its sketch keeps only the gate ladder
     bool capturing = false;               // launches are being captured into a CUDA graph
 };
 
@@ -159,6 +160,9 @@ void tbl_free_out(fbk_table* t);
 fbk_status tbl_convert(fbk_table* t);  // conversion, growing the output when it was too small
 fbk_status solid_build(fbk_ctx* ctx, const fbk_bank* b, const fbk_cms* cms, const fbk_build_params* p, const uint64_t* keep_bits,
                        uint64_t distinct_hint, fbk_table** out);
+// The same with the pass-1 gate as a t_solid-level ladder (fbk_k_ladder.cu).
+fbk_status solid_build_ladder(fbk_ctx* ctx, const fbk_bank* b, uint32_t* ladder, uint32_t log2w, const fbk_build_params* p,
+                              const uint64_t* keep_bits, uint64_t distinct_hint, fbk_table** out);
 
 // host f64 HyperLogLog::estimate from the register sum and zero count (sketch.rs:83-114)
 double hll_estimate_from_sum(double sum, uint64_t zeros, uint32_t p);

@@ -26,8 +26,11 @@ __device__ __forceinline__ uint32_t load_bases(const unsigned long long* read_ba
 }
 
 // Pass 1 (build.rs:90-116) for rows [r0, r1) of every isolate's sketch, plus the
-// p=12 HyperLogLog of its keys when do_hll (registers are only raised, so a stale
-// cached read merely costs an extra atomicMax).
+// p=12 HyperLogLog of its keys when do_hll.  The registers (16 KB per isolate) are
+// read through L2, where the atomics land, so an atomicMax is issued only when it
+// raises a register: after the first few million keys that is rare.  (A read
+// through the non-coherent cache would keep returning zeros and turn every key
+// into an atomic on 4096 hot words.)
 template <int NW>
 __global__ void __launch_bounds__(256) k_batch_pass1(const IsoDev* __restrict__ iso, const unsigned long long* __restrict__ read_base,
                                                      uint32_t n_iso, uint32_t k, uint32_t r0, uint32_t r1, int do_hll) {
@@ -71,7 +74,7 @@ __global__ void __launch_bounds__(256) k_batch_pass1(const IsoDev* __restrict__ 
             if (hll) {
                 uint32_t idx, rho;
                 hll_idx_rho(smix(key ^ cms_seed(0)), 12, idx, rho);
-                if (__ldg(&hll[idx]) < rho) atomicMax(&hll[idx], rho);
+                if (__ldcg(&hll[idx]) < rho) atomicMax(&hll[idx], rho);
             }
         }
     }
@@ -125,6 +128,122 @@ __global__ void __launch_bounds__(256) k_batch_solid(const IsoDev* __restrict__ 
                     uint32_t c = __ldg(cnt + ((uint64_t)row << log2w) + col);
                     c = c < cap ? c : cap;
                     clr |= c < t_solid;
+                }
+            }
+            const uint32_t m = __ballot_sync(0xffffffffu, clr);
+            if (lane == 0 && m) {
+                const uint64_t g0 = off + ((uint64_t)it << 5);
+                const uint32_t sh = (uint32_t)(g0 & 31);
+                atomicAnd(&bm[g0 >> 5], ~(m << sh));
+                if (sh) atomicAnd(&bm[(g0 >> 5) + 1], ~(m >> (32 - sh)));
+            }
+        }
+    }
+}
+
+// Ladder forms (fbk_k_ladder.cu has the single-isolate kernels and the argument):
+// level j of (row, col) is set once the count reached j + 1; the top level is t_solid.
+template <int NW>
+__global__ void __launch_bounds__(256) k_batch_lpass1(const IsoDev* __restrict__ iso, const unsigned long long* __restrict__ read_base,
+                                                      uint32_t n_iso, uint32_t k) {
+    __shared__ unsigned long long s_base[BATCH_MAX_ISO + 1];
+    load_bases(read_base, n_iso, s_base);
+    const uint64_t total = s_base[n_iso];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    uint32_t ci = 0, cur = 0xFFFFFFFFu;
+    BankDev b{};
+    uint32_t* lad = nullptr;
+    uint32_t* top = nullptr;
+    uint32_t* hll = nullptr;
+    uint64_t wmask = 0, base = 0, level_words = 0;
+    uint32_t log2w = 0, t = 1;
+    for (uint64_t R = gw; R < total; R += nwarps) {
+        ci = iso_walk(s_base, n_iso, ci, R);
+        if (ci != cur) {
+            cur = ci;
+            b = iso[ci].b;
+            lad = iso[ci].lad;
+            log2w = iso[ci].log2w;
+            t = iso[ci].t_solid;
+            wmask = (1ULL << log2w) - 1;
+            level_words = (4ULL << log2w) >> 5;
+            top = lad + (uint64_t)(t - 1) * level_words;
+            hll = iso[ci].hll12;
+            base = s_base[ci];
+        }
+        const uint64_t r = R - base;
+        const uint32_t len = b.len[r];
+        if (len < k || !bank_keep(b, r)) continue;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        for (uint32_t i = lane; i < nk; i += 32) {
+            Key<NW> can;
+            bool rc;
+            window_canonical<NW>(b.data, off + i, k, can, rc);
+            const uint64_t key = key_fold<NW>(can);
+            const uint64_t h0 = smix(key ^ cms_seed(0));
+#pragma unroll
+            for (int row = 0; row < 4; ++row) {
+                const uint64_t h = row == 0 ? h0 : smix(key ^ cms_seed(row));
+                const uint64_t bit = ((uint64_t)row << log2w) + (h & wmask);
+                const uint64_t w = bit >> 5;
+                const uint32_t m = 1u << (bit & 31);
+                if (__ldcg(top + w) & m) continue;
+                for (uint32_t j = 0; j < t; ++j)
+                    if (!(atomicOr(lad + (uint64_t)j * level_words + w, m) & m)) break;
+            }
+            uint32_t idx, rho;
+            hll_idx_rho(h0, 12, idx, rho);
+            if (__ldcg(&hll[idx]) < rho) atomicMax(&hll[idx], rho);
+        }
+    }
+}
+
+template <int NW>
+__global__ void __launch_bounds__(256) k_batch_lsolid(const IsoDev* __restrict__ iso, const unsigned long long* __restrict__ read_base,
+                                                      uint32_t n_iso, uint32_t k) {
+    __shared__ unsigned long long s_base[BATCH_MAX_ISO + 1];
+    load_bases(read_base, n_iso, s_base);
+    const uint64_t total = s_base[n_iso];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    uint32_t ci = 0, cur = 0xFFFFFFFFu;
+    BankDev b{};
+    const uint32_t* top = nullptr;
+    uint32_t* bm = nullptr;
+    uint64_t wmask = 0, base = 0;
+    uint32_t log2w = 0;
+    for (uint64_t R = gw; R < total; R += nwarps) {
+        ci = iso_walk(s_base, n_iso, ci, R);
+        if (ci != cur) {
+            cur = ci;
+            b = iso[ci].b;
+            log2w = iso[ci].log2w;
+            wmask = (1ULL << log2w) - 1;
+            top = iso[ci].lad + (uint64_t)(iso[ci].t_solid - 1) * ((4ULL << log2w) >> 5);
+            bm = iso[ci].bm;
+            base = s_base[ci];
+        }
+        const uint64_t r = R - base;
+        const uint32_t len = b.len[r];
+        if (len < k + 1 || !bank_keep(b, r)) continue;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        for (uint32_t it = 0; it < ((nk + 31) >> 5); ++it) {
+            const uint32_t q = (it << 5) + lane;
+            bool clr = false;
+            if (q < nk) {
+                Key<NW> can;
+                bool rc;
+                window_canonical<NW>(b.data, off + q, k, can, rc);
+                const uint64_t key = key_fold<NW>(can);
+#pragma unroll
+                for (int row = 0; row < 4; ++row) {
+                    const uint64_t bit = ((uint64_t)row << log2w) + (smix(key ^ cms_seed(row)) & wmask);
+                    clr |= !((__ldg(top + (bit >> 5)) >> (bit & 31)) & 1u);
                 }
             }
             const uint32_t m = __ballot_sync(0xffffffffu, clr);
@@ -407,6 +526,31 @@ cudaError_t launch_batch_solid(int nw, const Launch& L, const IsoDev* iso, const
     if (nw == 1) return bsolid<1>(L, iso, read_base, n_iso, k, r0, r1);
     if (nw == 2) return bsolid<2>(L, iso, read_base, n_iso, k, r0, r1);
     return bsolid<4>(L, iso, read_base, n_iso, k, r0, r1);
+}
+
+template <int NW>
+static cudaError_t blp1(const Launch& L, const IsoDev* iso, const unsigned long long* rb, uint32_t n, uint32_t k) {
+    k_batch_lpass1<NW><<<grid_of(k_batch_lpass1<NW>, L, 0), L.block, 0, L.stream>>>(iso, rb, n, k);
+    return cudaGetLastError();
+}
+cudaError_t launch_batch_lpass1(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
+                                uint32_t k) {
+    if (n_iso > BATCH_MAX_ISO) return cudaErrorInvalidValue;
+    if (nw == 1) return blp1<1>(L, iso, read_base, n_iso, k);
+    if (nw == 2) return blp1<2>(L, iso, read_base, n_iso, k);
+    return blp1<4>(L, iso, read_base, n_iso, k);
+}
+template <int NW>
+static cudaError_t bls(const Launch& L, const IsoDev* iso, const unsigned long long* rb, uint32_t n, uint32_t k) {
+    k_batch_lsolid<NW><<<grid_of(k_batch_lsolid<NW>, L, 0), L.block, 0, L.stream>>>(iso, rb, n, k);
+    return cudaGetLastError();
+}
+cudaError_t launch_batch_lsolid(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
+                                uint32_t k) {
+    if (n_iso > BATCH_MAX_ISO) return cudaErrorInvalidValue;
+    if (nw == 1) return bls<1>(L, iso, read_base, n_iso, k);
+    if (nw == 2) return bls<2>(L, iso, read_base, n_iso, k);
+    return bls<4>(L, iso, read_base, n_iso, k);
 }
 
 cudaError_t launch_batch_count(const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso, uint32_t k) {

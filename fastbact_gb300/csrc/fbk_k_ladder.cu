@@ -1,0 +1,148 @@
+// fbk_k_ladder.cu — the CMS gate of the build front end as threshold ladders.
+//
+// Pass 2 reads the pass-1 sketch only through one predicate (build.rs:259-267):
+//   solid(x)  <=>  min over rows r of min(cap, count_r(col_r(x))) >= t_solid.
+// With 1 <= t_solid <= cap that is "every row's count reached t_solid".  A ladder
+// keeps t_solid bits per (row, column); level j (0-based) is set by the (j+1)-th
+// increment.  An increment climbs: atomicOr on level 0; if that bit was already set,
+// level 1; and so on.  Each level is claimed by exactly one increment, and a level is
+// tried only when the one below it is already set, so the claimed levels are always
+// {0 .. m-1} with m = min(t_solid, increments): the top level is set iff the count
+// reached t_solid.  The top level is read first, so a saturated counter costs one L2
+// load and no atomic.
+//
+// Size: t_solid x 4 x 2^log2w bits — 16 MB for t = 2 and 2^24 columns — so the whole
+// gate stays in L2 and one sweep serves all four rows (the exact u32 sketch needs one
+// 64 MB sweep per row).  Layout: bit ((level * 4 + row) << log2w) + col.
+#include "fbk_device.cuh"
+#include "fbk_kernels.cuh"
+
+namespace fbk {
+
+template <int NW>
+__global__ void __launch_bounds__(256) k_ladder_pass1(BankDev b, uint32_t k, uint32_t* __restrict__ lad, uint32_t log2w,
+                                                      uint32_t t, uint32_t* __restrict__ hll12) {
+    __shared__ uint32_t s_hll[4096];
+    const bool do_hll = hll12 != nullptr;
+    if (do_hll) {
+        for (int i = threadIdx.x; i < 4096; i += blockDim.x) s_hll[i] = 0;
+        __syncthreads();
+    }
+    const uint64_t wmask = (1ULL << log2w) - 1;
+    const uint64_t level_words = (4ULL << log2w) >> 5;
+    uint32_t* top = lad + (uint64_t)(t - 1) * level_words;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t r = b.r_begin + gw; r < b.r_end; r += nwarps) {
+        const uint32_t len = b.len[r];
+        if (len < k || !bank_keep(b, r)) continue;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        for (uint32_t i = lane; i < nk; i += 32) {
+            Key<NW> can;
+            bool rc;
+            window_canonical<NW>(b.data, off + i, k, can, rc);
+            const uint64_t key = key_fold<NW>(can);
+            const uint64_t h0 = smix(key ^ cms_seed(0));
+#pragma unroll
+            for (int row = 0; row < 4; ++row) {
+                const uint64_t h = row == 0 ? h0 : smix(key ^ cms_seed(row));
+                const uint64_t bit = ((uint64_t)row << log2w) + (h & wmask);
+                const uint64_t w = bit >> 5;
+                const uint32_t m = 1u << (bit & 31);
+                if (__ldcg(top + w) & m) continue;  // count already >= t
+                for (uint32_t j = 0; j < t; ++j)
+                    if (!(atomicOr(lad + (uint64_t)j * level_words + w, m) & m)) break;
+            }
+            if (do_hll) {
+                uint32_t idx, rho;
+                hll_idx_rho(h0, 12, idx, rho);
+                if (s_hll[idx] < rho) atomicMax(&s_hll[idx], rho);
+            }
+        }
+    }
+    if (do_hll) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < 4096; i += blockDim.x) {
+            const uint32_t v = s_hll[i];
+            if (v) atomicMax(&hll12[i], v);
+        }
+    }
+}
+
+// Solidity bitmap from a ladder: a window's bit is cleared unless the top level is
+// set in all four rows (one sweep).
+template <int NW>
+__global__ void __launch_bounds__(256) k_ladder_solid(BankDev b, uint32_t k, const uint32_t* __restrict__ lad, uint32_t log2w,
+                                                      uint32_t t, uint32_t* __restrict__ bm) {
+    const uint64_t wmask = (1ULL << log2w) - 1;
+    const uint32_t* top = lad + (uint64_t)(t - 1) * ((4ULL << log2w) >> 5);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t r = b.r_begin + gw; r < b.r_end; r += nwarps) {
+        const uint32_t len = b.len[r];
+        if (len < k + 1 || !bank_keep(b, r)) continue;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        for (uint32_t it = 0; it < ((nk + 31) >> 5); ++it) {
+            const uint32_t q = (it << 5) + lane;
+            bool clr = false;
+            if (q < nk) {
+                Key<NW> can;
+                bool rc;
+                window_canonical<NW>(b.data, off + q, k, can, rc);
+                const uint64_t key = key_fold<NW>(can);
+#pragma unroll
+                for (int row = 0; row < 4; ++row) {
+                    const uint64_t bit = ((uint64_t)row << log2w) + (smix(key ^ cms_seed(row)) & wmask);
+                    clr |= !((__ldg(top + (bit >> 5)) >> (bit & 31)) & 1u);
+                }
+            }
+            const uint32_t m = __ballot_sync(0xffffffffu, clr);
+            if (lane == 0 && m) {
+                const uint64_t g0 = off + ((uint64_t)it << 5);
+                const uint32_t sh = (uint32_t)(g0 & 31);
+                atomicAnd(&bm[g0 >> 5], ~(m << sh));
+                if (sh) atomicAnd(&bm[(g0 >> 5) + 1], ~(m >> (32 - sh)));
+            }
+        }
+    }
+}
+
+template <class K>
+static int grid_l(K kernel, const Launch& L) {
+    if (L.grid > 0) return L.grid;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, L.block, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+    return per_sm * (L.sms > 0 ? L.sms : 1);
+}
+
+template <int NW>
+static cudaError_t lp1(const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t, uint32_t* hll) {
+    k_ladder_pass1<NW><<<grid_l(k_ladder_pass1<NW>, L), L.block, 0, L.stream>>>(b, k, lad, log2w, t, hll);
+    return cudaGetLastError();
+}
+cudaError_t launch_ladder_pass1(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t,
+                                uint32_t* hll12) {
+    if (t < 1 || t > LADDER_MAX_LEVELS) return cudaErrorInvalidValue;
+    if (nw == 1) return lp1<1>(L, b, k, lad, log2w, t, hll12);
+    if (nw == 2) return lp1<2>(L, b, k, lad, log2w, t, hll12);
+    return lp1<4>(L, b, k, lad, log2w, t, hll12);
+}
+
+template <int NW>
+static cudaError_t lsol(const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w, uint32_t t, uint32_t* bm) {
+    k_ladder_solid<NW><<<grid_l(k_ladder_solid<NW>, L), L.block, 0, L.stream>>>(b, k, lad, log2w, t, bm);
+    return cudaGetLastError();
+}
+cudaError_t launch_ladder_solid(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
+                                uint32_t t, uint32_t* bm) {
+    if (t < 1 || t > LADDER_MAX_LEVELS) return cudaErrorInvalidValue;
+    if (nw == 1) return lsol<1>(L, b, k, lad, log2w, t, bm);
+    if (nw == 2) return lsol<2>(L, b, k, lad, log2w, t, bm);
+    return lsol<4>(L, b, k, lad, log2w, t, bm);
+}
+
+}  // namespace fbk

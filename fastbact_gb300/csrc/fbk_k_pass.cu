@@ -263,6 +263,99 @@ __global__ void __launch_bounds__(256) k_emit(BankDev b, uint32_t k, const uint3
     if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
 }
 
+// Record emit with the gate read inline from a threshold ladder (fbk_k_ladder.cu):
+// every lane decides its own window's solidity (the top ladder level set in all
+// four rows), and a warp walks its read one chunk of 32 windows ahead, so the
+// solidity of both neighbours of every window comes from the ballots of the
+// previous, current and next chunks.  No solidity bitmap is built or read.
+template <int NW>
+__device__ __forceinline__ bool ladder_gate(const uint32_t* __restrict__ top, uint32_t log2w, uint64_t key) {
+    const uint64_t wmask = (1ULL << log2w) - 1;
+    bool ok = true;
+#pragma unroll
+    for (int row = 0; row < 4; ++row) {
+        const uint64_t bit = ((uint64_t)row << log2w) + (smix(key ^ cms_seed(row)) & wmask);
+        ok &= (__ldg(top + (bit >> 5)) >> (bit & 31)) & 1u;
+    }
+    return ok;
+}
+
+template <int NW>
+__global__ void __launch_bounds__(256) k_emit_ladder(BankDev b, uint32_t k, const uint32_t* __restrict__ lad, uint32_t log2w,
+                                                     uint32_t t_solid, TableDev t, BucketDev bk) {
+    extern __shared__ uint64_t emit_smem[];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint64_t* buf = emit_smem + (uint64_t)wib * EMIT_WARP_WORDS(NW);
+    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + EMIT_BUF * (NW + 1));
+    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + EMIT_BUF);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + EMIT_BUF);
+    unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
+    const uint32_t* top = lad + (uint64_t)(t_solid - 1) * ((4ULL << log2w) >> 5);
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t stripe = (uint32_t)(gw % bk.stripes);
+    uint32_t n_buf = 0;  // warp-uniform
+    for (uint64_t r = b.r_begin + gw; r < b.r_end; r += nwarps) {
+        const uint32_t len = b.len[r];
+        if (len < k + 1 || !bank_keep(b, r)) continue;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        const uint32_t n_it = (nk + 31) >> 5;
+        Key<NW> kc;
+        bool rcc = false, sc = false;
+        if (lane < nk) {
+            window_canonical<NW>(b.data, off + lane, k, kc, rcc);
+            sc = ladder_gate<NW>(top, log2w, key_fold<NW>(kc));
+        }
+        uint32_t mprev = 0, mcur = __ballot_sync(0xffffffffu, sc);
+        for (uint32_t it = 0; it < n_it; ++it) {
+            Key<NW> kn;
+            bool rcn = false, sn = false;
+            const uint32_t qn = ((it + 1) << 5) + lane;
+            if (qn < nk) {
+                window_canonical<NW>(b.data, off + qn, k, kn, rcn);
+                sn = ladder_gate<NW>(top, log2w, key_fold<NW>(kn));
+            }
+            const uint32_t mnext = __ballot_sync(0xffffffffu, sn);
+            const uint32_t q = (it << 5) + lane;
+            bool emit = false;
+            uint32_t info = 0, bucket = 0;
+            if (q < nk) {
+                const bool sq = (mcur >> lane) & 1u;
+                const bool sl = q > 0 && (lane ? ((mcur >> (lane - 1)) & 1u) : (mprev >> 31));
+                const bool sr = q + 1 < nk && (lane < 31 ? ((mcur >> (lane + 1)) & 1u) : (mnext & 1u));
+                emit = sq && (sl || sr);
+                if (emit) {
+                    const uint64_t g = off + q;
+                    if (sr) info |= 8u | (base_at(b.data, g + k) + (rcc ? 4u : 0u));
+                    if (sl) info |= (8u | ((3u - base_at(b.data, g - 1)) + (rcc ? 0u : 4u))) << 4;
+                    bucket = (uint32_t)(home_slot(key_fold<NW>(kc), t.cap) >> bk.shift);
+                }
+            }
+            const uint32_t active = __ballot_sync(0xffffffffu, emit);
+            if (emit) {
+                const uint32_t pos = n_buf + __popc(active & ((1u << lane) - 1));
+#pragma unroll
+                for (int i = 0; i < NW; ++i) buf[pos * (NW + 1) + i] = kc.w[i];
+                buf[pos * (NW + 1) + NW] = info;
+                bbuf[pos] = (uint8_t)bucket;
+            }
+            n_buf += __popc(active);
+            if (n_buf > EMIT_BUF - 32) {
+                __syncwarp();
+                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+                n_buf = 0;
+            }
+            mprev = mcur;
+            mcur = mnext;
+            kc = kn;
+            rcc = rcn;
+        }
+    }
+    __syncwarp();
+    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+}
+
 template <int NW>
 __global__ void __launch_bounds__(256) k_upsert(BucketDev bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov, TableDev t,
                                                 uint32_t* status) {
@@ -528,6 +621,32 @@ static cudaError_t emit_nw(const Launch& L, const BankDev& b, uint32_t k, const 
     k_emit<NW><<<grid, L.block, smem, L.stream>>>(b, k, bm, gate, t, bk);
     return cudaGetLastError();
 }
+template <int NW>
+static cudaError_t emitl_nw(const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w, uint32_t ts,
+                            const TableDev& t, const BucketDev& bk) {
+    const size_t smem = (size_t)(L.block / 32) * EMIT_WARP_WORDS(NW) * 8;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_emit_ladder<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    int grid = L.grid;
+    if (grid <= 0) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_ladder<NW>, L.block, smem) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        grid = per_sm * (L.sms > 0 ? L.sms : 1);
+    }
+    k_emit_ladder<NW><<<grid, L.block, smem, L.stream>>>(b, k, lad, log2w, ts, t, bk);
+    return cudaGetLastError();
+}
+cudaError_t launch_emit_ladder(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
+                               uint32_t t_solid, const TableDev& t, const BucketDev& bk) {
+    if (t_solid < 1 || t_solid > LADDER_MAX_LEVELS) return cudaErrorInvalidValue;
+    if (nw == 1) return emitl_nw<1>(L, b, k, lad, log2w, t_solid, t, bk);
+    if (nw == 2) return emitl_nw<2>(L, b, k, lad, log2w, t_solid, t, bk);
+    return emitl_nw<4>(L, b, k, lad, log2w, t_solid, t, bk);
+}
+
 cudaError_t launch_emit(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* bm, int gate, const TableDev& t,
                         const BucketDev& bk) {
     if (nw == 1) return emit_nw<1>(L, b, k, bm, gate, t, bk);

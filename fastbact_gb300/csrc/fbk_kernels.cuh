@@ -74,7 +74,8 @@ struct ConvOut {
 constexpr uint32_t BATCH_MAX_ISO = 256;
 struct IsoDev {
     BankDev b;                      // r_begin = 0, r_end = the isolate's reads
-    uint32_t* cnt;                  // exact u32 sketch, 4 rows of 2^log2w
+    uint32_t* cnt;                  // exact u32 sketch, 4 rows of 2^log2w (or null with a ladder)
+    uint32_t* lad;                  // t_solid-level gate ladder (or null with a sketch)
     uint32_t* hll12;                // p=12 registers of the keys (table sizing)
     uint32_t* bm;                   // solidity bitmap
     unsigned long long* n_records;  // [0] pass-2 records, [1] pass-1 and [2] pass-2 k-mer occurrences
@@ -118,6 +119,18 @@ cudaError_t launch_convert(int nw, const Launch& L, const TableDev& t, uint32_t 
 cudaError_t launch_clamp_counters(const Launch& L, uint32_t* cnt, uint64_t n);
 cudaError_t launch_table_init(int nw, const Launch& L, const TableDev& t);
 
+// ---- threshold ladders (fbk_k_ladder.cu) -----------------------------------------
+// The CMS gate of pass 2 without counts: t levels x 4 rows x 2^log2w bits, level j of
+// (row, col) set once the count reached j + 1.  1 <= t <= LADDER_MAX_LEVELS.
+constexpr uint32_t LADDER_MAX_LEVELS = 8;
+cudaError_t launch_ladder_pass1(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t,
+                                uint32_t* hll12);
+cudaError_t launch_ladder_solid(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
+                                uint32_t t, uint32_t* bm);
+// Record emit of pass 2 with the ladder gate evaluated inline (no solidity bitmap).
+cudaError_t launch_emit_ladder(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
+                               uint32_t t_solid, const TableDev& t, const BucketDev& bk);
+
 // ---- multi-isolate waves (fbk_k_batch.cu) ----------------------------------------
 // read_base: n_iso + 1 global read indices (isolate i owns [read_base[i], read_base[i+1])).
 cudaError_t launch_batch_pass1(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
@@ -125,6 +138,11 @@ cudaError_t launch_batch_pass1(int nw, const Launch& L, const IsoDev* iso, const
 cudaError_t launch_batch_solid(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
                                uint32_t k, uint32_t r0, uint32_t r1);
 cudaError_t launch_batch_count(const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso, uint32_t k);
+// Ladder forms (every isolate's gate is a t_solid-level ladder): one sweep each.
+cudaError_t launch_batch_lpass1(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
+                                uint32_t k);
+cudaError_t launch_batch_lsolid(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
+                                uint32_t k);
 cudaError_t launch_batch_emit(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
                               uint32_t k, uint32_t stripes);
 // unit_pre: n_iso * 64 + 1 entries; stripe_pre: n_iso * 64 * (stripes + 1) entries.

@@ -168,6 +168,56 @@ def compare_build(ctx, bank, k, kb, cb, tsc, log2w, contigs=None, subsample=None
     return table, len(sk)
 
 
+def compare_gate_only(ctx, bank, k, kb, cb, tsc, log2w, subsample=None, keep_mask=None):
+    """A build that does not return its sketch (pass 1 keeps only the gate, as a
+    threshold ladder when 1 <= t_solid <= 8) against the oracle's full build."""
+    table = api.build_cdbg_with_contigs_ext(bank, [], k, tsc, None, ctx=ctx, key_bits=kb, counter_bits=cb,
+                                            cms_log2_width=log2w, subsample=subsample)
+    _, o_tab, _, mtc = orc.build_front(bank, k, kb, log2w, cb, tsc, threads=4, keep_mask=keep_mask)
+    gk, gc, ge = table.export_acc(sort=True)
+    ok, oc, oe = api.sort_rows(*o_tab.export_acc())
+    assert gk.shape == ok.shape, (gk.shape, ok.shape)
+    assert np.array_equal(gk, ok) and np.array_equal(gc, oc) and np.array_equal(ge, oe)
+    sk, sc, sm = table.export(sort=True)
+    xk, xc, xm = api.sort_rows(*o_tab.export_solid(mtc))
+    assert np.array_equal(sk, xk) and np.array_equal(sc, xc) and np.array_equal(sm, xm)
+    assert table.digest() == o_tab.digest(mtc)
+    return len(sk)
+
+
+@pytest.mark.parametrize("k,kb", [(21, 64), (31, 64), (33, 128), (55, 128), (77, 256), (127, 256)])
+@pytest.mark.parametrize("cb", [4, 16])
+def test_gate_only_build_matches_oracle(ctx, small_isolate, k, kb, cb):
+    assert compare_gate_only(ctx, small_isolate[0], k, kb, cb, None, 16) > 1000
+
+
+@pytest.mark.parametrize("tsc", [None, 1, 3, 5, 8, 9, 15])
+def test_gate_only_thresholds_and_saturation(ctx, repeat_isolate, tsc):
+    # t <= 8: ladder levels; 9 and 15: the exact sketch; 2^12 columns: heavy collisions
+    for cb in (4, 16):
+        for log2w in (12, 16):
+            compare_gate_only(ctx, repeat_isolate[0], 31, 64, cb, tsc, log2w)
+    compare_gate_only(ctx, repeat_isolate[0], 45, 128, 16, tsc, 14)
+    compare_gate_only(ctx, repeat_isolate[0], 99, 256, 4, tsc, 14)
+
+
+def test_gate_only_with_subsampling(ctx, repeat_isolate):
+    bank = repeat_isolate[0]
+    n_pairs = int(max(int(a.pair_idx.max()) for a in bank.arenas if len(a))) + 1
+    keep = api.subsample_mask(ctx, n_pairs, 0.35, 1234)
+    compare_gate_only(ctx, bank, 31, 64, 16, None, 16, subsample=(0.35, 1234), keep_mask=keep)
+
+
+def test_sketch_mode_off_matches(repeat_isolate):
+    c = api.Context(0)
+    try:
+        c.set_tuning(sketch_mode=0)
+        assert c.get_tuning("sketch_mode") == 0
+        compare_gate_only(c, repeat_isolate[0], 31, 64, 16, None, 14)
+    finally:
+        c.close()
+
+
 @pytest.mark.parametrize("k,kb", [(21, 64), (31, 64), (33, 128), (55, 128), (77, 256), (127, 256)])
 @pytest.mark.parametrize("cb", [4, 16])
 def test_build_front_matches_oracle(ctx, small_isolate, k, kb, cb):
@@ -322,5 +372,6 @@ def test_build_tuning_variants(repeat_isolate, tune):
         c.set_tuning(**tune)
         for k, kb, cb in [(31, 64, 4), (45, 128, 16), (99, 256, 4)]:
             compare_build(c, repeat_isolate[0], k, kb, cb, None, 14)
+            compare_gate_only(c, repeat_isolate[0], k, kb, cb, None, 14)
     finally:
         c.close()
