@@ -178,10 +178,12 @@ __global__ void __launch_bounds__(256) k_batch_lpass1(const IsoDev* __restrict__
         if (len < k || !bank_keep(b, r)) continue;
         const uint64_t off = b.off[r];
         const uint32_t nk = len - k + 1;
-        for (uint32_t i = lane; i < nk; i += 32) {
+        for (uint32_t it = 0; it < ((nk + 31) >> 5); ++it) {
+            const uint32_t q = (it << 5) + lane;
+            if (q >= nk) continue;
             Key<NW> can;
             bool rc;
-            window_canonical<NW>(b.data, off + i, k, can, rc);
+            window_canonical<NW>(b.data, off + q, k, can, rc);
             const uint64_t key = key_fold<NW>(can);
             const uint64_t h0 = smix(key ^ cms_seed(0));
 #pragma unroll
@@ -190,9 +192,9 @@ __global__ void __launch_bounds__(256) k_batch_lpass1(const IsoDev* __restrict__
                 const uint64_t bit = ((uint64_t)row << log2w) + (h & wmask);
                 const uint64_t w = bit >> 5;
                 const uint32_t m = 1u << (bit & 31);
-                if (__ldcg(top + w) & m) continue;
+                bool climb = !(__ldcg(top + w) & m);
                 for (uint32_t j = 0; j < t; ++j)
-                    if (!(atomicOr(lad + (uint64_t)j * level_words + w, m) & m)) break;
+                    if (climb) climb = (atomicOr(lad + (uint64_t)j * level_words + w, m) & m) != 0;
             }
             uint32_t idx, rho;
             hll_idx_rho(h0, 12, idx, rho);
@@ -427,42 +429,38 @@ __global__ void k_batch_prefix(const IsoDev* __restrict__ iso, uint32_t n_iso, u
 }
 
 // Upsert of every record of every unit, units in order (isolate-major, then
-// bucket): resident blocks work on consecutive records, i.e. on one bucket's table
-// range at a time.  Each block takes tiles of blockDim records; the tile's units are
-// found once per tile.
+// bucket): resident warps work on consecutive records, i.e. on one bucket's table
+// range at a time.  A warp takes 32 consecutive records: lane 0 finds the unit of
+// the first one, the lanes step forward from there (a warp's records rarely cross a
+// unit boundary), and no block barrier holds warps back from issuing their probes.
 template <int NW>
 __global__ void __launch_bounds__(256) k_batch_upsert(const IsoDev* __restrict__ iso, uint32_t n_iso, uint32_t stripes,
                                                       const unsigned long long* __restrict__ unit_pre,
                                                       const unsigned long long* __restrict__ stripe_pre) {
-    __shared__ uint32_t s_u[2];
     const uint32_t n_units = n_iso * EMIT_MAX_BUCKETS, S = stripes;
     const uint64_t total = unit_pre[n_units];
-    const uint64_t tile = blockDim.x;
-    for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < total; t0 += (uint64_t)gridDim.x * tile) {
-        if (threadIdx.x < 2) {
-            const uint64_t x = threadIdx.x == 0 ? t0 : (t0 + tile - 1 < total ? t0 + tile - 1 : total - 1);
-            uint32_t lo = 0, hi = n_units;  // last u with unit_pre[u] <= x
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t base = gw * 32; base < total; base += nwarps * 32) {
+        uint32_t u0 = 0;
+        if (lane == 0) {
+            uint32_t lo = 0, hi = n_units;  // last u with unit_pre[u] <= base
             while (hi - lo > 1) {
                 const uint32_t mid = (lo + hi) >> 1;
-                if (unit_pre[mid] <= x) lo = mid;
+                if (unit_pre[mid] <= base) lo = mid;
                 else hi = mid;
             }
-            s_u[threadIdx.x] = lo;
+            u0 = lo;
         }
-        __syncthreads();
-        const uint64_t i = t0 + threadIdx.x;
-        uint32_t ulo = s_u[0], uhi = s_u[1] + 1;
-        __syncthreads();
+        u0 = __shfl_sync(0xffffffffu, u0, 0);
+        const uint64_t i = base + lane;
         if (i >= total) continue;
-        while (uhi - ulo > 1) {
-            const uint32_t mid = (ulo + uhi) >> 1;
-            if (unit_pre[mid] <= i) ulo = mid;
-            else uhi = mid;
-        }
-        const uint32_t u = ulo;
+        uint32_t u = u0;
+        while (u + 1 < n_units && unit_pre[u + 1] <= i) ++u;
         const uint64_t j = i - unit_pre[u];
         const unsigned long long* sp = stripe_pre + (uint64_t)u * (S + 1);
-        uint32_t lo = 0, hi = S;
+        uint32_t lo = 0, hi = S;  // last stripe s with sp[s] <= j
         while (hi - lo > 1) {
             const uint32_t mid = (lo + hi) >> 1;
             if (sp[mid] <= j) lo = mid;

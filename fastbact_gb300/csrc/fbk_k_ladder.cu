@@ -39,10 +39,14 @@ __global__ void __launch_bounds__(256) k_ladder_pass1(BankDev b, uint32_t k, uin
         if (len < k || !bank_keep(b, r)) continue;
         const uint64_t off = b.off[r];
         const uint32_t nk = len - k + 1;
-        for (uint32_t i = lane; i < nk; i += 32) {
+        // Warp-uniform trip counts throughout (chunks of 32 windows, all t levels):
+        // the climb is a predicated atomic per level, so the warp never splits.
+        for (uint32_t it = 0; it < ((nk + 31) >> 5); ++it) {
+            const uint32_t q = (it << 5) + lane;
+            if (q >= nk) continue;
             Key<NW> can;
             bool rc;
-            window_canonical<NW>(b.data, off + i, k, can, rc);
+            window_canonical<NW>(b.data, off + q, k, can, rc);
             const uint64_t key = key_fold<NW>(can);
             const uint64_t h0 = smix(key ^ cms_seed(0));
 #pragma unroll
@@ -51,9 +55,9 @@ __global__ void __launch_bounds__(256) k_ladder_pass1(BankDev b, uint32_t k, uin
                 const uint64_t bit = ((uint64_t)row << log2w) + (h & wmask);
                 const uint64_t w = bit >> 5;
                 const uint32_t m = 1u << (bit & 31);
-                if (__ldcg(top + w) & m) continue;  // count already >= t
+                bool climb = !(__ldcg(top + w) & m);  // false once the count reached t
                 for (uint32_t j = 0; j < t; ++j)
-                    if (!(atomicOr(lad + (uint64_t)j * level_words + w, m) & m)) break;
+                    if (climb) climb = (atomicOr(lad + (uint64_t)j * level_words + w, m) & m) != 0;
             }
             if (do_hll) {
                 uint32_t idx, rho;
