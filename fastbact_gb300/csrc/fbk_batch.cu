@@ -218,8 +218,6 @@ struct WaveBufs {
     unsigned long long* rb = nullptr;
     unsigned long long* cnt = nullptr;   // 8 per isolate: [0..2] record/k-mer counts, [3..7] conversion counts
     uint32_t* status = nullptr;          // 2 per isolate: status bits, bucket overflow
-    unsigned long long* unit_pre = nullptr;
-    unsigned long long* stripe_pre = nullptr;
     ~WaveBufs() {
         if (!ctx) return;
         cudaStreamSynchronize(ctx->stream);
@@ -227,8 +225,6 @@ struct WaveBufs {
         dev_free(ctx, rb);
         dev_free(ctx, cnt);
         dev_free(ctx, status);
-        dev_free(ctx, unit_pre);
-        dev_free(ctx, stripe_pre);
     }
 };
 
@@ -239,11 +235,8 @@ fbk_status wave_bufs(fbk_batch* B, uint32_t n, bool phase_b, WaveBufs& w) {
     w.rb = (unsigned long long*)dev_alloc(ctx, (n + 1) * 8);
     w.cnt = (unsigned long long*)dev_alloc(ctx, (uint64_t)n * 8 * 8);
     w.status = (uint32_t*)dev_alloc(ctx, (uint64_t)n * 2 * 4);
-    if (phase_b) {
-        w.unit_pre = (unsigned long long*)dev_alloc(ctx, ((uint64_t)n * 64 + 1) * 8);
-        w.stripe_pre = (unsigned long long*)dev_alloc(ctx, (uint64_t)n * 64 * (BATCH_STRIPES + 1) * 8);
-    }
-    if (!w.iso || !w.rb || !w.cnt || !w.status || (phase_b && (!w.unit_pre || !w.stripe_pre)))
+    (void)phase_b;
+    if (!w.iso || !w.rb || !w.cnt || !w.status)
         return set_err(ctx, FBK_ERR_OOM, "batch wave descriptors");
     return FBK_OK;
 }
@@ -273,7 +266,7 @@ uint64_t gate_bytes(const fbk_batch* B) {
 }
 
 uint64_t phase_a_bytes(const fbk_batch* B, const BatchIso* it) {
-    return gate_bytes(B) + 4096 * 4 + (it->bank->n_words + 9) * 4 + 4096;
+    return gate_bytes(B) + 4096 * 4 + (B->ladder ? 0 : (it->bank->n_words + 9) * 4) + 4096;
 }
 
 // Autotuner: times candidate launch shapes of the pass-1 and solidity kernels on one
@@ -328,20 +321,17 @@ fbk_status autotune(fbk_batch* B, BatchIso* it) {
                 }
             }
     // the sketch now holds the isolate's full counts: tune the solidity sweep on it
+    // (a ladder gate has no solidity sweep: the emit evaluates it)
     const uint64_t bm_bytes = (it->bank->n_words + 9) * 4;
     best = 1e30f;
     Shape best2 = B->solid;
-    for (int rp : rows)
+    for (int rp : (B->ladder ? std::vector<int>() : rows))
         for (int bl : blocks)
             for (int ps : per_sm) {
                 Shape s{bl, ps ? ps * ctx->num_sms : 0, rp};
                 CK(ctx, cudaMemsetAsync(it->bm, 0xFF, bm_bytes, ctx->stream));
                 float ms = 0;
                 st = timed([&]() -> fbk_status {
-                    if (B->ladder) {
-                        TIMED(ctx, "tune_solid", launch_batch_lsolid(B->nw, shape_launch(ctx, s), w.iso, w.rb, 1, B->p.k));
-                        return FBK_OK;
-                    }
                     for (uint32_t r = 0; r < 4; r += (uint32_t)rp)
                         TIMED(ctx, "tune_solid", launch_batch_solid(B->nw, shape_launch(ctx, s), w.iso, w.rb, 1, B->p.k, r, r + rp));
                     return FBK_OK;
@@ -370,8 +360,8 @@ fbk_status phase_a(fbk_batch* B, const std::vector<BatchIso*>& W) {
         if (B->ladder) it->lad = (uint32_t*)dev_alloc(ctx, cms_bytes);
         else it->cnt = (uint32_t*)dev_alloc(ctx, cms_bytes);
         it->hll12 = (uint32_t*)dev_alloc(ctx, 4096 * 4);
-        it->bm = (uint32_t*)dev_alloc(ctx, (it->bank->n_words + 9) * 4);
-        if (!(it->cnt || it->lad) || !it->hll12 || !it->bm) return set_err(ctx, FBK_ERR_OOM, "batch sketches");
+        if (!B->ladder) it->bm = (uint32_t*)dev_alloc(ctx, (it->bank->n_words + 9) * 4);
+        if (!(it->cnt || it->lad) || !it->hll12 || (!B->ladder && !it->bm)) return set_err(ctx, FBK_ERR_OOM, "batch sketches");
     }
     if (B->p.autotune && !B->tuned) {
         BatchIso* big = *std::max_element(W.begin(), W.end(), [](const BatchIso* a, const BatchIso* b) {
@@ -390,13 +380,14 @@ fbk_status phase_a(fbk_batch* B, const std::vector<BatchIso*>& W) {
         for (BatchIso* it : W) {
             CK(ctx, cudaMemsetAsync(B->ladder ? it->lad : it->cnt, 0, cms_bytes, ctx->stream));
             CK(ctx, cudaMemsetAsync(it->hll12, 0, 4096 * 4, ctx->stream));
-            CK(ctx, cudaMemsetAsync(it->bm, 0xFF, (it->bank->n_words + 9) * 4, ctx->stream));
+            if (it->bm) CK(ctx, cudaMemsetAsync(it->bm, 0xFF, (it->bank->n_words + 9) * 4, ctx->stream));
         }
         CK(ctx, cudaMemsetAsync(w.cnt, 0, (uint64_t)n * 64, ctx->stream));
         CK(ctx, cudaMemsetAsync(w.status, 0, (uint64_t)n * 8, ctx->stream));
         if (B->ladder) {
+            // the gate is evaluated inside the record emit: no bitmap, and the
+            // records are bounded by the windows the count kernel tallies
             TIMED(ctx, "batch_pass1", launch_batch_lpass1(B->nw, shape_launch(ctx, B->pass1), w.iso, w.rb, n, k));
-            TIMED(ctx, "batch_solid", launch_batch_lsolid(B->nw, shape_launch(ctx, B->solid), w.iso, w.rb, n, k));
             TIMED(ctx, "batch_count", launch_batch_count(shape_launch(ctx, B->solid), w.iso, w.rb, n, k));
             return FBK_OK;
         }
@@ -429,8 +420,9 @@ fbk_status phase_a(fbk_batch* B, const std::vector<BatchIso*>& W) {
             sum += std::ldexp(1.0, -(int)v);
             zeros += v == 0;
         }
-        it->distinct = (uint64_t)(hll_estimate_from_sum(sum, zeros, 12) * 1.05) + 1024;
-        it->records = hc[8 * i];
+        // the registers saw 1 in BATCH_HLL_SAMPLE keys (by hash)
+        it->distinct = (uint64_t)(hll_estimate_from_sum(sum, zeros, 12) * BATCH_HLL_SAMPLE * 1.08) + 4096;
+        it->records = B->ladder ? hc[8 * i + 2] : hc[8 * i];
         it->res.kmers = hc[8 * i + 1] + hc[8 * i + 2];
         it->res.state = 2;
     }
@@ -547,10 +539,27 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
             CK(ctx, cudaMemsetAsync(it->table->cnt, 0, it->table->cap * 32, ctx->stream));
             CK(ctx, cudaMemsetAsync(it->fill, 0, (uint64_t)it->bk.n_buckets * BATCH_STRIPES * 8, ctx->stream));
         }
-        TIMED(ctx, "batch_emit", launch_batch_emit(B->nw, shape_launch(ctx, B->emit), w.iso, w.rb, n, k, BATCH_STRIPES));
-        TIMED(ctx, "batch_prefix", launch_batch_prefix(launch_cfg(ctx, 1024, 1), w.iso, n, BATCH_STRIPES, w.unit_pre, w.stripe_pre));
-        TIMED(ctx, "batch_upsert", launch_batch_upsert(B->nw, shape_launch(ctx, B->upsert), w.iso, n, BATCH_STRIPES, w.unit_pre,
-                                                       w.stripe_pre));
+        if (B->ladder) {
+            for (uint32_t i = 0; i < n; ++i) {
+                BatchIso* it = V[i];
+                BucketDev bk = it->bk;
+                bk.overflow = w.status + 2 * i + 1;
+                TIMED(ctx, "batch_emit", launch_emit_ladder(B->nw, shape_launch(ctx, B->emit),
+                                                            bank_view(it->bank, 0, it->bank->n_reads, it->keep), k, it->lad,
+                                                            B->p.cms_log2_width, B->p.t_solid, tbl_dev(it->table), bk));
+            }
+        } else {
+            TIMED(ctx, "batch_emit", launch_batch_emit(B->nw, shape_launch(ctx, B->emit), w.iso, w.rb, n, k, BATCH_STRIPES));
+        }
+        // upserts bucket by bucket, so each launch's table range stays in L2
+        for (uint32_t i = 0; i < n; ++i) {
+            BatchIso* it = V[i];
+            BucketDev bk = it->bk;
+            bk.overflow = w.status + 2 * i + 1;
+            for (uint32_t bu = 0; bu < bk.n_buckets; ++bu)
+                TIMED(ctx, "batch_upsert", launch_upsert(B->nw, shape_launch(ctx, B->upsert), bk, bu, 1, 1, tbl_dev(it->table),
+                                                         w.status + 2 * i));
+        }
         for (uint32_t i = 0; i < n; ++i) {
             fbk_table* t = V[i]->table;
             ConvOut o{};

@@ -26,11 +26,12 @@ __device__ __forceinline__ uint32_t load_bases(const unsigned long long* read_ba
 }
 
 // Pass 1 (build.rs:90-116) for rows [r0, r1) of every isolate's sketch, plus the
-// p=12 HyperLogLog of its keys when do_hll.  The registers (16 KB per isolate) are
-// read through L2, where the atomics land, so an atomicMax is issued only when it
-// raises a register: after the first few million keys that is rare.  (A read
-// through the non-coherent cache would keep returning zeros and turn every key
-// into an atomic on 4096 hot words.)
+// p=12 HyperLogLog of its keys when do_hll.  Only keys whose hash has its low
+// log2(BATCH_HLL_SAMPLE) bits zero enter the registers (the host scales the estimate
+// back; it only sizes the table).  The registers (16 KB per isolate) are read
+// through L2, where the atomics land, so an atomicMax is issued only when it raises
+// a register.  (A read through the non-coherent cache would keep returning zeros and
+// turn every sampled key into an atomic on 4096 hot words.)
 template <int NW>
 __global__ void __launch_bounds__(256) k_batch_pass1(const IsoDev* __restrict__ iso, const unsigned long long* __restrict__ read_base,
                                                      uint32_t n_iso, uint32_t k, uint32_t r0, uint32_t r1, int do_hll) {
@@ -71,9 +72,10 @@ __global__ void __launch_bounds__(256) k_batch_pass1(const IsoDev* __restrict__ 
                 const uint64_t col = smix(key ^ cms_seed((int)row)) & wmask;
                 atomicAdd(cnt + ((uint64_t)row << log2w) + col, 1u);
             }
-            if (hll) {
+            const uint64_t h0 = smix(key ^ cms_seed(0));
+            if (hll && (h0 & (BATCH_HLL_SAMPLE - 1)) == 0) {
                 uint32_t idx, rho;
-                hll_idx_rho(smix(key ^ cms_seed(0)), 12, idx, rho);
+                hll_idx_rho(h0, 12, idx, rho);
                 if (__ldcg(&hll[idx]) < rho) atomicMax(&hll[idx], rho);
             }
         }
@@ -196,64 +198,10 @@ __global__ void __launch_bounds__(256) k_batch_lpass1(const IsoDev* __restrict__
                 for (uint32_t j = 0; j < t; ++j)
                     if (climb) climb = (atomicOr(lad + (uint64_t)j * level_words + w, m) & m) != 0;
             }
-            uint32_t idx, rho;
-            hll_idx_rho(h0, 12, idx, rho);
-            if (__ldcg(&hll[idx]) < rho) atomicMax(&hll[idx], rho);
-        }
-    }
-}
-
-template <int NW>
-__global__ void __launch_bounds__(256) k_batch_lsolid(const IsoDev* __restrict__ iso, const unsigned long long* __restrict__ read_base,
-                                                      uint32_t n_iso, uint32_t k) {
-    __shared__ unsigned long long s_base[BATCH_MAX_ISO + 1];
-    load_bases(read_base, n_iso, s_base);
-    const uint64_t total = s_base[n_iso];
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    uint32_t ci = 0, cur = 0xFFFFFFFFu;
-    BankDev b{};
-    const uint32_t* top = nullptr;
-    uint32_t* bm = nullptr;
-    uint64_t wmask = 0, base = 0;
-    uint32_t log2w = 0;
-    for (uint64_t R = gw; R < total; R += nwarps) {
-        ci = iso_walk(s_base, n_iso, ci, R);
-        if (ci != cur) {
-            cur = ci;
-            b = iso[ci].b;
-            log2w = iso[ci].log2w;
-            wmask = (1ULL << log2w) - 1;
-            top = iso[ci].lad + (uint64_t)(iso[ci].t_solid - 1) * ((4ULL << log2w) >> 5);
-            bm = iso[ci].bm;
-            base = s_base[ci];
-        }
-        const uint64_t r = R - base;
-        const uint32_t len = b.len[r];
-        if (len < k + 1 || !bank_keep(b, r)) continue;
-        const uint64_t off = b.off[r];
-        const uint32_t nk = len - k + 1;
-        for (uint32_t it = 0; it < ((nk + 31) >> 5); ++it) {
-            const uint32_t q = (it << 5) + lane;
-            bool clr = false;
-            if (q < nk) {
-                Key<NW> can;
-                bool rc;
-                window_canonical<NW>(b.data, off + q, k, can, rc);
-                const uint64_t key = key_fold<NW>(can);
-#pragma unroll
-                for (int row = 0; row < 4; ++row) {
-                    const uint64_t bit = ((uint64_t)row << log2w) + (smix(key ^ cms_seed(row)) & wmask);
-                    clr |= !((__ldg(top + (bit >> 5)) >> (bit & 31)) & 1u);
-                }
-            }
-            const uint32_t m = __ballot_sync(0xffffffffu, clr);
-            if (lane == 0 && m) {
-                const uint64_t g0 = off + ((uint64_t)it << 5);
-                const uint32_t sh = (uint32_t)(g0 & 31);
-                atomicAnd(&bm[g0 >> 5], ~(m << sh));
-                if (sh) atomicAnd(&bm[(g0 >> 5) + 1], ~(m >> (32 - sh)));
+            if ((h0 & (BATCH_HLL_SAMPLE - 1)) == 0) {
+                uint32_t idx, rho;
+                hll_idx_rho(h0, 12, idx, rho);
+                if (__ldcg(&hll[idx]) < rho) atomicMax(&hll[idx], rho);
             }
         }
     }
@@ -296,6 +244,7 @@ __global__ void __launch_bounds__(256) k_batch_count(const IsoDev* __restrict__ 
         w1 += len - k + 1;
         if (len < k + 1) continue;
         w2 += len - k + 1;
+        if (!bm) continue;  // a ladder gate: the records are bounded by the windows
         const uint64_t off = b.off[r];
         const uint32_t nk = len - k + 1;
         for (uint32_t q = lane; q < ((nk + 31) & ~31u); q += 32) {
@@ -397,96 +346,6 @@ __global__ void __launch_bounds__(256) k_batch_emit(const IsoDev* __restrict__ i
     if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
 }
 
-// Record totals of every (isolate, bucket) unit: stripe_pre[u * (S + 1) + s] is the
-// number of records in stripes < s of unit u (fills capped at the stripe size), and
-// unit_pre[u] the records of all units before u.  One block.
-__global__ void k_batch_prefix(const IsoDev* __restrict__ iso, uint32_t n_iso, uint32_t stripes,
-                               unsigned long long* __restrict__ unit_pre, unsigned long long* __restrict__ stripe_pre) {
-    const uint32_t n_units = n_iso * EMIT_MAX_BUCKETS, S = stripes;
-    for (uint32_t u = threadIdx.x; u < n_units; u += blockDim.x) {
-        const IsoDev& d = iso[u / EMIT_MAX_BUCKETS];
-        const uint32_t bu = u % EMIT_MAX_BUCKETS;
-        unsigned long long acc = 0;
-        unsigned long long* sp = stripe_pre + (uint64_t)u * (S + 1);
-        for (uint32_t s = 0; s < S; ++s) {
-            sp[s] = acc;
-            if (bu < d.bk.n_buckets) {
-                const unsigned long long f = d.bk.fill[(uint64_t)bu * S + s];
-                acc += f < d.bk.stripe_cap ? f : d.bk.stripe_cap;
-            }
-        }
-        sp[S] = acc;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long acc = 0;
-        for (uint32_t u = 0; u < n_units; ++u) {
-            unit_pre[u] = acc;
-            acc += stripe_pre[(uint64_t)u * (S + 1) + S];
-        }
-        unit_pre[n_units] = acc;
-    }
-}
-
-// Upsert of every record of every unit, units in order (isolate-major, then
-// bucket): resident warps work on consecutive records, i.e. on one bucket's table
-// range at a time.  A warp takes 32 consecutive records: lane 0 finds the unit of
-// the first one, the lanes step forward from there (a warp's records rarely cross a
-// unit boundary), and no block barrier holds warps back from issuing their probes.
-template <int NW>
-__global__ void __launch_bounds__(256) k_batch_upsert(const IsoDev* __restrict__ iso, uint32_t n_iso, uint32_t stripes,
-                                                      const unsigned long long* __restrict__ unit_pre,
-                                                      const unsigned long long* __restrict__ stripe_pre) {
-    const uint32_t n_units = n_iso * EMIT_MAX_BUCKETS, S = stripes;
-    const uint64_t total = unit_pre[n_units];
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t base = gw * 32; base < total; base += nwarps * 32) {
-        uint32_t u0 = 0;
-        if (lane == 0) {
-            uint32_t lo = 0, hi = n_units;  // last u with unit_pre[u] <= base
-            while (hi - lo > 1) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (unit_pre[mid] <= base) lo = mid;
-                else hi = mid;
-            }
-            u0 = lo;
-        }
-        u0 = __shfl_sync(0xffffffffu, u0, 0);
-        const uint64_t i = base + lane;
-        if (i >= total) continue;
-        uint32_t u = u0;
-        while (u + 1 < n_units && unit_pre[u + 1] <= i) ++u;
-        const uint64_t j = i - unit_pre[u];
-        const unsigned long long* sp = stripe_pre + (uint64_t)u * (S + 1);
-        uint32_t lo = 0, hi = S;  // last stripe s with sp[s] <= j
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (sp[mid] <= j) lo = mid;
-            else hi = mid;
-        }
-        const IsoDev& d = iso[u / EMIT_MAX_BUCKETS];
-        const uint32_t bucket = u % EMIT_MAX_BUCKETS;
-        const uint64_t* rec = d.bk.recs + (((uint64_t)bucket * S + lo) * d.bk.stripe_cap + (j - sp[lo])) * (NW + 1);
-        Key<NW> key;
-#pragma unroll
-        for (int w = 0; w < NW; ++w) key.w[w] = __ldcs(rec + w);
-        const uint32_t info = (uint32_t)__ldcs(rec + NW);
-        const TableDev t = d.t;
-        const uint64_t f = key_fold<NW>(key);
-        const uint64_t home = home_slot(f, t.cap);
-        int64_t s;
-        if constexpr (NW == 1) s = table_slot1(t, key.w[0], home, d.status);
-        else if constexpr (NW == 2) s = table_slot2(t, key, home, d.status);
-        else s = table_slotw<NW>(t, key, f, home, d.status);
-        if (s < 0) continue;
-        uint32_t* c = t.cnt + (uint64_t)s * 8;
-        if ((info >> 3) & 1u) atomicAdd(&c[info & 7u], 1u);
-        if ((info >> 7) & 1u) atomicAdd(&c[(info >> 4) & 7u], 1u);
-    }
-}
-
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -538,19 +397,6 @@ cudaError_t launch_batch_lpass1(int nw, const Launch& L, const IsoDev* iso, cons
     if (nw == 2) return blp1<2>(L, iso, read_base, n_iso, k);
     return blp1<4>(L, iso, read_base, n_iso, k);
 }
-template <int NW>
-static cudaError_t bls(const Launch& L, const IsoDev* iso, const unsigned long long* rb, uint32_t n, uint32_t k) {
-    k_batch_lsolid<NW><<<grid_of(k_batch_lsolid<NW>, L, 0), L.block, 0, L.stream>>>(iso, rb, n, k);
-    return cudaGetLastError();
-}
-cudaError_t launch_batch_lsolid(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
-                                uint32_t k) {
-    if (n_iso > BATCH_MAX_ISO) return cudaErrorInvalidValue;
-    if (nw == 1) return bls<1>(L, iso, read_base, n_iso, k);
-    if (nw == 2) return bls<2>(L, iso, read_base, n_iso, k);
-    return bls<4>(L, iso, read_base, n_iso, k);
-}
-
 cudaError_t launch_batch_count(const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso, uint32_t k) {
     if (n_iso > BATCH_MAX_ISO) return cudaErrorInvalidValue;
     k_batch_count<<<grid_of(k_batch_count, L, 0), L.block, 0, L.stream>>>(iso, read_base, n_iso, k);
@@ -573,27 +419,6 @@ cudaError_t launch_batch_emit(int nw, const Launch& L, const IsoDev* iso, const 
     if (nw == 1) return bemit<1>(L, iso, read_base, n_iso, k, stripes);
     if (nw == 2) return bemit<2>(L, iso, read_base, n_iso, k, stripes);
     return bemit<4>(L, iso, read_base, n_iso, k, stripes);
-}
-
-cudaError_t launch_batch_prefix(const Launch& L, const IsoDev* iso, uint32_t n_iso, uint32_t stripes, unsigned long long* unit_pre,
-                                unsigned long long* stripe_pre) {
-    if (n_iso > BATCH_MAX_ISO || stripes == 0 || stripes > 256) return cudaErrorInvalidValue;
-    k_batch_prefix<<<1, 1024, 0, L.stream>>>(iso, n_iso, stripes, unit_pre, stripe_pre);
-    return cudaGetLastError();
-}
-
-template <int NW>
-static cudaError_t bupsert(const Launch& L, const IsoDev* iso, uint32_t n, uint32_t S, const unsigned long long* up,
-                           const unsigned long long* sp) {
-    k_batch_upsert<NW><<<grid_of(k_batch_upsert<NW>, L, 0), L.block, 0, L.stream>>>(iso, n, S, up, sp);
-    return cudaGetLastError();
-}
-cudaError_t launch_batch_upsert(int nw, const Launch& L, const IsoDev* iso, uint32_t n_iso, uint32_t stripes,
-                                const unsigned long long* unit_pre, const unsigned long long* stripe_pre) {
-    if (n_iso > BATCH_MAX_ISO || stripes == 0 || stripes > 256) return cudaErrorInvalidValue;
-    if (nw == 1) return bupsert<1>(L, iso, n_iso, stripes, unit_pre, stripe_pre);
-    if (nw == 2) return bupsert<2>(L, iso, n_iso, stripes, unit_pre, stripe_pre);
-    return bupsert<4>(L, iso, n_iso, stripes, unit_pre, stripe_pre);
 }
 
 }  // namespace fbk

@@ -72,6 +72,7 @@ struct ConvOut {
 
 // One isolate of a multi-isolate wave (fbk_k_batch.cu).
 constexpr uint32_t BATCH_MAX_ISO = 256;
+constexpr uint32_t BATCH_HLL_SAMPLE = 16;  // 1 in 16 keys (by hash) feeds the table-sizing HyperLogLog
 struct IsoDev {
     BankDev b;                      // r_begin = 0, r_end = the isolate's reads
     uint32_t* cnt;                  // exact u32 sketch, 4 rows of 2^log2w (or null with a ladder)
@@ -138,18 +139,13 @@ cudaError_t launch_batch_pass1(int nw, const Launch& L, const IsoDev* iso, const
 cudaError_t launch_batch_solid(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
                                uint32_t k, uint32_t r0, uint32_t r1);
 cudaError_t launch_batch_count(const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso, uint32_t k);
-// Ladder forms (every isolate's gate is a t_solid-level ladder): one sweep each.
+// Ladder form of pass 1 (every isolate's gate is a t_solid-level ladder): one sweep.
 cudaError_t launch_batch_lpass1(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
                                 uint32_t k);
-cudaError_t launch_batch_lsolid(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
-                                uint32_t k);
+
 cudaError_t launch_batch_emit(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,
                               uint32_t k, uint32_t stripes);
-// unit_pre: n_iso * 64 + 1 entries; stripe_pre: n_iso * 64 * (stripes + 1) entries.
-cudaError_t launch_batch_prefix(const Launch& L, const IsoDev* iso, uint32_t n_iso, uint32_t stripes, unsigned long long* unit_pre,
-                                unsigned long long* stripe_pre);
-cudaError_t launch_batch_upsert(int nw, const Launch& L, const IsoDev* iso, uint32_t n_iso, uint32_t stripes,
-                                const unsigned long long* unit_pre, const unsigned long long* stripe_pre);
+
 
 // ---- estimator and utilities (fbk_k_est.cu) -----------------------------------
 cudaError_t launch_est_firstpos(const Launch& L, const BankDev& b, const uint64_t* kbase, uint32_t k, uint32_t* first,
