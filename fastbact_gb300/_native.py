@@ -181,6 +181,11 @@ SIGNATURES = {
     "fbk_estimate_genome": (S, [vp, C.c_char_p, C.c_char_p, C.c_uint64, C.c_double, P(GenomeEstimate)]),
     "fbk_compute_dynamic_kmers": (C.c_int, [C.c_uint64, C.c_int64, u64p, C.c_int]),
     "fbk_subsample_mask": (S, [vp, C.c_uint64, P(Subsample), u64p]),
+    "fbk_compact": (S, [vp, P(vp)]),
+    "fbk_unitigs_info": (S, [vp, u64p, u64p, u64p]),
+    "fbk_unitigs_export": (S, [vp, u8p, u64p, P(C.c_float), u8p]),
+    "fbk_unitigs_edges": (S, [vp, u32p, C.c_uint64, u64p]),
+    "fbk_unitigs_release": (S, [vp]),
     "fbk_subsample_policy_defaults": (None, [P(SubsamplePolicy)]),
     "fbk_subsample_decide": (S, [P(SubsamplePolicy), P(GenomeEstimate), P(C.c_double), P(C.c_int32)]),
     "fbk_batch_defaults": (None, [P(BatchParams)]),

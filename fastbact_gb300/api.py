@@ -555,6 +555,10 @@ class SolidTable:
         self.nw = key_bits // 64
         ctx.adopt(self)
 
+    @property
+    def handle(self):
+        return self._h
+
     def info(self) -> tuple[int, int, int]:
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
         check(N.lib().fbk_table_info(self._h, C.byref(a), C.byref(b), C.byref(c)))
@@ -605,6 +609,29 @@ class SolidTable:
             self.release()
         except Exception:
             pass
+
+
+def compact(table: "SolidTable"):
+    """Unitig compaction of a solid table (build.rs:330-594): returns (sequences
+    list[bytes], cov f32[n], circular bool[n], edges u32[m, 6] = from unitig, from side,
+    to unitig, to reverse, overlap, support)."""
+    h = C.c_void_p()
+    check(N.lib().fbk_compact(table.handle, C.byref(h)), table.ctx.handle, "compact")
+    try:
+        n, nb, ne = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        check(N.lib().fbk_unitigs_info(h, C.byref(n), C.byref(nb), C.byref(ne)))
+        seqs = np.zeros(max(nb.value, 1), np.uint8)
+        offs = np.zeros(n.value + 1, np.uint64)
+        cov = np.zeros(max(n.value, 1), np.float32)
+        circ = np.zeros(max(n.value, 1), np.uint8)
+        check(N.lib().fbk_unitigs_export(h, ptr(seqs), ptr(offs), cov.ctypes.data_as(C.POINTER(C.c_float)), ptr(circ)))
+        edges = np.zeros((max(ne.value, 1), 6), np.uint32)
+        m = C.c_uint64()
+        check(N.lib().fbk_unitigs_edges(h, ptr(edges.reshape(-1)), ne.value, C.byref(m)))
+    finally:
+        N.lib().fbk_unitigs_release(h)
+    out = [seqs[offs[i]:offs[i + 1]].tobytes() for i in range(n.value)]
+    return out, cov[:n.value], circ[:n.value].astype(bool), edges[:ne.value]
 
 
 def sort_rows(keys: np.ndarray, *cols):

@@ -286,6 +286,26 @@ FBK_API int fbk_compute_dynamic_kmers(uint64_t median_len, int64_t target_max_k,
 /* Bit i of keep_bits (host, ceil(n_pairs/64) words) = input pair i (0-based) kept. */
 FBK_API fbk_status fbk_subsample_mask(fbk_ctx* ctx, uint64_t n_pairs, const fbk_subsample* ss, uint64_t* keep_bits);
 
+/* ---- unitig compaction (build.rs:330-594) ------------------------------------------
+ * Compacts a converted solid table into unitigs: boundary walks on the device (one
+ * thread per boundary out-edge; a unitig reachable from both ends is kept from the end
+ * with the smaller (row, direction, edge), the set the reference's visited marks
+ * keep), isolated cycles and the k / k-1 overlap edges on the host.  Sequences are
+ * min(seq, reverse complement) for linear unitigs; a cycle starts at one of its
+ * k-mers (the reference starts at the first one its map order meets).  Coverage =
+ * mean node coverage of the walk without its last node, as build.rs:379-435 computes
+ * it. */
+typedef struct fbk_unitigs fbk_unitigs;
+FBK_API fbk_status fbk_compact(fbk_table* t, fbk_unitigs** out);
+FBK_API fbk_status fbk_unitigs_info(const fbk_unitigs* u, uint64_t* n_unitigs, uint64_t* total_bases, uint64_t* n_edges);
+/* ascii: total_bases bytes (may be NULL), offsets: n_unitigs + 1, cov and circular:
+ * n_unitigs each (may be NULL). */
+FBK_API fbk_status fbk_unitigs_export(const fbk_unitigs* u, uint8_t* ascii, uint64_t* offsets, float* cov, uint8_t* circular);
+/* 6 u32 per edge: from unitig, from side (0 forward strand, 1 reverse), to unitig, to
+ * reverse (0/1), overlap, support (cdbg.rs:113-122 merges repeats). */
+FBK_API fbk_status fbk_unitigs_edges(const fbk_unitigs* u, uint32_t* edges, uint64_t cap, uint64_t* n_out);
+FBK_API fbk_status fbk_unitigs_release(fbk_unitigs* u);
+
 /* Subsampling policy of the pipeline driver (src/main.rs:76-180): decides the
  * subsample factor from an estimate.  reason: 0 EXPLICIT_NO_SUBSAMPLE_FLAG,
  * 1 EXPLICIT_GENOME_SIZE_ZERO_INVALID, 2 AUTO_SUBSAMPLE_EXPLICIT_GENOME_SIZE,

@@ -19,6 +19,8 @@
 // estimator math must round exactly like Rust's f64, which calls the same libm).
 
 #include <algorithm>
+#include <array>
+#include <type_traits>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -1255,3 +1257,304 @@ ORC_API int orc_estimate_genome(const char* r1, const char* r2, uint64_t max_pai
     if (rc != 0 && err && errlen > 0) snprintf(err, errlen, "Input FASTQ files contain 0 valid read pairs");
     return rc;
 }
+
+// ===========================================================================
+// Unitig compaction — build.rs:330-594 (boundary walks, circular components,
+// overlap edges) over SolidKmerNode rows.  The reference keeps the nodes in 64
+// hashbrown shards (shard = splitmix64(to_u64) & 63, build.rs:152-153) and walks
+// them in map order; here std::unordered_map stands in, so the emission order (and,
+// for circular components, the start of the rotation) may differ — results are
+// compared as multisets.
+// ===========================================================================
+#include <unordered_map>
+
+namespace {
+
+template <class K>
+struct KHash {
+    size_t operator()(const K& x) const { return (size_t)splitmix64(x.to_u64()); }
+};
+template <class K>
+struct KEq {
+    bool operator()(const K& a, const K& b) const { return !(a < b) && !(b < a); }
+};
+
+struct SNode {
+    uint16_t cov;
+    uint8_t mask;
+    uint8_t visited;
+};
+
+template <class K>
+static std::string kmer_ascii(const K& x, unsigned k) {  // KmerInt::to_ascii (kmer.rs:83-90)
+    constexpr int NW = sizeof(K) / 8 > 4 ? 4 : (int)(sizeof(K) / 8);
+    uint64_t w[4] = {0, 0, 0, 0};
+    x.words(w);
+    const int nw = std::is_same<K, K64>::value ? 1 : std::is_same<K, K128>::value ? 2 : 4;
+    (void)NW;
+    std::string s(k, 'A');
+    for (unsigned i = 0; i < k; ++i) {  // base i from the 3' end
+        const unsigned bit = 2 * i;
+        const uint64_t word = w[nw - 1 - bit / 64];
+        const unsigned code = (unsigned)(word >> (bit % 64)) & 3u;
+        s[k - 1 - i] = "ACGT"[code];
+    }
+    return s;
+}
+
+static std::string rc_ascii(const std::string& s) {  // reverse_complement_ascii (bitseq.rs:90-98)
+    std::string r(s.size(), 'A');
+    for (size_t i = 0; i < s.size(); ++i) r[s.size() - 1 - i] = "TGCA"[A2B.t[(uint8_t)s[i]]];
+    return r;
+}
+
+struct OUnitig {
+    std::string seq;
+    float cov;
+    bool circular;
+    // (target id, target rc, overlap, support) per side
+    std::vector<std::array<uint32_t, 4>> edges[2];
+    void add_edge(bool rc_side, uint32_t tid, bool trc, uint32_t ov, uint32_t support) {  // cdbg.rs:113-122
+        for (auto& e : edges[rc_side]) {
+            if (e[0] == tid && e[1] == (uint32_t)trc && e[2] == ov) {
+                e[3] = std::min<uint32_t>(65535, e[3] + support);
+                return;
+            }
+        }
+        edges[rc_side].push_back({tid, (uint32_t)trc, ov, support});
+    }
+};
+
+template <class K>
+static std::vector<OUnitig> compact_impl(unsigned k, const uint64_t* keys, const uint16_t* cov, const uint8_t* mask, uint64_t n) {
+    constexpr int NWK = std::is_same<K, K64>::value ? 1 : std::is_same<K, K128>::value ? 2 : 4;
+    using Map = std::unordered_map<K, SNode, KHash<K>, KEq<K>>;
+    std::vector<Map> shards(64);
+    auto shard_of = [](const K& x) { return (size_t)(splitmix64(x.to_u64()) & 63); };
+    for (uint64_t i = 0; i < n; ++i) {
+        K x = from_words<K>(keys + i * NWK);
+        shards[shard_of(x)][x] = SNode{cov[i], mask[i], 0};
+    }
+    auto find = [&](const K& x) -> SNode* {
+        auto& m = shards[shard_of(x)];
+        auto it = m.find(x);
+        return it == m.end() ? nullptr : &it->second;
+    };
+    std::vector<OUnitig> out;
+    auto pc = [](uint8_t v) { return __builtin_popcount(v); };
+    // 4. boundary directed k-mers (in_deg != 1 || out_deg != 1), build.rs:332-347
+    std::vector<std::pair<K, bool>> boundary;
+    for (auto& sh : shards)
+        for (auto& kv : sh) {
+            const uint8_t m = kv.second.mask;
+            if (pc(m >> 4 & 0xF) != 1 || pc(m & 0xF) != 1) boundary.push_back({kv.first, false});
+            if (pc(m & 0xF) != 1 || pc(m >> 4 & 0xF) != 1) boundary.push_back({kv.first, true});
+        }
+    auto next_dir = [&](const K& fwd, const K& rev, uint8_t b, K& can, bool& is_rc) {
+        K nf = fwd, nr = rev;
+        K::roll_next(nf, nr, b, k);
+        is_rc = nr < nf;
+        can = is_rc ? nr : nf;
+    };
+    auto oriented = [&](const K& kmer, bool is_rc, K& f, K& r) {
+        if (!is_rc) {
+            f = kmer;
+            r = kmer.rev_comp(k);
+        } else {
+            f = kmer.rev_comp(k);
+            r = kmer;
+        }
+    };
+    // build.rs:349-445
+    for (auto& u : boundary) {
+        for (uint8_t b = 0; b < 4; ++b) {
+            SNode* nu = find(u.first);
+            if (!nu) break;
+            const uint8_t u_out = !u.second ? (nu->mask & 0x0F) : ((nu->mask >> 4) & 0x0F);
+            const uint8_t u_vis = !u.second ? (nu->visited & 0x0F) : ((nu->visited >> 4) & 0x0F);
+            if (!((u_out >> b) & 1) || ((u_vis >> b) & 1)) continue;
+            nu->visited |= (uint8_t)(1u << (!u.second ? b : b + 4));
+            std::string path = kmer_ascii(u.first, k);
+            if (u.second) path = rc_ascii(path);
+            K fwd, rev;
+            oriented(u.first, u.second, fwd, rev);
+            const uint8_t rc_first = 3 - A2B.t[(uint8_t)kmer_ascii(fwd, k)[0]];
+            K cur;
+            bool cur_rc;
+            next_dir(fwd, rev, b, cur, cur_rc);
+            if (SNode* nc = find(cur)) nc->visited |= (uint8_t)(1u << (!cur_rc ? rc_first + 4 : rc_first));
+            path.push_back("ACGT"[b]);
+            uint64_t total_cov = nu->cov, points = 1;
+            for (;;) {
+                SNode* ncp = find(cur);
+                if (!ncp) break;
+                const SNode nc = *ncp;
+                const uint8_t c_out = !cur_rc ? (nc.mask & 0x0F) : ((nc.mask >> 4) & 0x0F);
+                const uint8_t c_in = !cur_rc ? ((nc.mask >> 4) & 0x0F) : (nc.mask & 0x0F);
+                if (pc(c_in) != 1 || pc(c_out) != 1) break;
+                const uint8_t nb = (uint8_t)__builtin_ctz(c_out);
+                const uint8_t ebit = !cur_rc ? nb : nb + 4;
+                if ((nc.visited >> ebit) & 1) break;
+                ncp->visited |= (uint8_t)(1u << ebit);
+                K cf, cr;
+                oriented(cur, cur_rc, cf, cr);
+                const uint8_t rc_p = 3 - A2B.t[(uint8_t)kmer_ascii(cf, k)[0]];
+                K nxt;
+                bool nxt_rc;
+                next_dir(cf, cr, nb, nxt, nxt_rc);
+                if (SNode* nn = find(nxt)) nn->visited |= (uint8_t)(1u << (!nxt_rc ? rc_p + 4 : rc_p));
+                path.push_back("ACGT"[nb]);
+                total_cov += nc.cov;
+                points++;
+                cur = nxt;
+                cur_rc = nxt_rc;
+            }
+            const std::string rcs = rc_ascii(path);
+            OUnitig t;
+            t.seq = rcs < path ? rcs : path;
+            t.cov = std::max(1.0f, (float)total_cov / (float)points);
+            t.circular = false;
+            out.push_back(std::move(t));
+        }
+    }
+    // 5. isolated circular components, build.rs:450-555
+    for (size_t s = 0; s < 64; ++s) {
+        std::vector<K> ks;
+        for (auto& kv : shards[s]) ks.push_back(kv.first);
+        for (const K& kmer : ks) {
+            SNode* np = find(kmer);
+            if (!np) continue;
+            const SNode n0 = *np;
+            const uint8_t fo = n0.mask & 0x0F, fi = (n0.mask >> 4) & 0x0F;
+            if (pc(fo) != 1 || pc(fi) != 1) continue;
+            const uint8_t b = (uint8_t)__builtin_ctz(fo);
+            if ((n0.visited >> b) & 1) continue;
+            np->visited |= (uint8_t)(1u << b);
+            std::string path = kmer_ascii(kmer, k);
+            const K fwd = kmer, rev = kmer.rev_comp(k);
+            K cur;
+            bool cur_rc;
+            next_dir(fwd, rev, b, cur, cur_rc);
+            const uint8_t rc_first = 3 - A2B.t[(uint8_t)kmer_ascii(fwd, k)[0]];
+            if (SNode* nc = find(cur)) nc->visited |= (uint8_t)(1u << (!cur_rc ? rc_first + 4 : rc_first));
+            path.push_back("ACGT"[b]);
+            uint64_t total_cov = n0.cov, points = 1;
+            while (!KEq<K>()(cur, kmer)) {
+                SNode* ncp = find(cur);
+                if (!ncp) break;
+                const SNode nc = *ncp;
+                const uint8_t c_out = !cur_rc ? (nc.mask & 0x0F) : ((nc.mask >> 4) & 0x0F);
+                const uint8_t c_in = !cur_rc ? ((nc.mask >> 4) & 0x0F) : (nc.mask & 0x0F);
+                if (pc(c_in) != 1 || pc(c_out) != 1) break;
+                const uint8_t nb = (uint8_t)__builtin_ctz(c_out);
+                const uint8_t ebit = !cur_rc ? nb : nb + 4;
+                if ((nc.visited >> ebit) & 1) break;
+                ncp->visited |= (uint8_t)(1u << ebit);
+                K cf, cr;
+                oriented(cur, cur_rc, cf, cr);
+                const uint8_t rc_p = 3 - A2B.t[(uint8_t)kmer_ascii(cf, k)[0]];
+                K nxt;
+                bool nxt_rc;
+                next_dir(cf, cr, nb, nxt, nxt_rc);
+                if (SNode* nn = find(nxt)) nn->visited |= (uint8_t)(1u << (!nxt_rc ? rc_p + 4 : rc_p));
+                path.push_back("ACGT"[nb]);
+                total_cov += nc.cov;
+                points++;
+                cur = nxt;
+                cur_rc = nxt_rc;
+            }
+            if (KEq<K>()(cur, kmer) && path.size() > k) {
+                if (path.size() > k && path.compare(path.size() - k, k, path, 0, k) == 0) path.resize(path.size() - k);
+                else if (path.size() > k - 1 && path.compare(path.size() - (k - 1), k - 1, path, 0, k - 1) == 0)
+                    path.resize(path.size() - (k - 1));
+                OUnitig t;
+                t.seq = path;
+                t.cov = std::max(1.0f, (float)total_cov / (float)points);
+                t.circular = true;
+                const uint32_t id = (uint32_t)out.size();
+                t.add_edge(false, id, false, k - 1, 10);
+                out.push_back(std::move(t));
+            }
+        }
+    }
+    // 6. overlap edges of k and k-1 bases, build.rs:558-594
+    for (unsigned ov : {k, k - 1}) {
+        if (ov == 0) continue;
+        std::unordered_map<std::string, std::vector<std::pair<uint32_t, bool>>> prefix;
+        for (uint32_t id = 0; id < out.size(); ++id) {
+            const std::string& f = out[id].seq;
+            if (f.size() >= ov) {
+                prefix[f.substr(0, ov)].push_back({id, false});
+                prefix[rc_ascii(f).substr(0, ov)].push_back({id, true});
+            }
+        }
+        for (uint32_t id = 0; id < out.size(); ++id) {
+            const std::string f = out[id].seq, r = rc_ascii(f);
+            if (f.size() < ov) continue;
+            auto a = prefix.find(f.substr(f.size() - ov));
+            if (a != prefix.end())
+                for (auto& t : a->second)
+                    if (t.first != id || out[id].circular) out[id].add_edge(false, t.first, t.second, ov, 10);
+            auto c = prefix.find(r.substr(r.size() - ov));
+            if (c != prefix.end())
+                for (auto& t : c->second)
+                    if (t.first != id || out[id].circular) out[id].add_edge(true, t.first, t.second, ov, 10);
+        }
+    }
+    return out;
+}
+
+struct OCompacted {
+    std::vector<OUnitig> u;
+};
+
+}  // namespace
+
+// Compaction oracle: SolidKmerNode rows in, unitigs out (an opaque handle).
+ORC_API void* orc_compact(int key_bits, unsigned k, const uint64_t* keys, const uint16_t* cov, const uint8_t* mask, uint64_t n) {
+    auto* c = new OCompacted();
+    if (key_bits == 64) c->u = compact_impl<K64>(k, keys, cov, mask, n);
+    else if (key_bits == 128) c->u = compact_impl<K128>(k, keys, cov, mask, n);
+    else if (key_bits == 256) c->u = compact_impl<K256>(k, keys, cov, mask, n);
+    else {
+        delete c;
+        return nullptr;
+    }
+    return c;
+}
+ORC_API uint64_t orc_compact_count(const void* h) { return ((const OCompacted*)h)->u.size(); }
+ORC_API uint64_t orc_compact_bases(const void* h) {
+    uint64_t t = 0;
+    for (auto& u : ((const OCompacted*)h)->u) t += u.seq.size();
+    return t;
+}
+ORC_API uint64_t orc_compact_n_edges(const void* h) {
+    uint64_t t = 0;
+    for (auto& u : ((const OCompacted*)h)->u) t += u.edges[0].size() + u.edges[1].size();
+    return t;
+}
+// seqs: concatenated ASCII; offs: n+1; cov; circular; edges: 6 u32 per edge
+// (from id, from side, to id, to rc, overlap, support)
+ORC_API void orc_compact_export(const void* h, uint8_t* seqs, uint64_t* offs, float* cov, uint8_t* circular, uint32_t* edges) {
+    const auto& U = ((const OCompacted*)h)->u;
+    uint64_t p = 0, e = 0;
+    offs[0] = 0;
+    for (size_t i = 0; i < U.size(); ++i) {
+        memcpy(seqs + p, U[i].seq.data(), U[i].seq.size());
+        p += U[i].seq.size();
+        offs[i + 1] = p;
+        cov[i] = U[i].cov;
+        circular[i] = U[i].circular;
+        for (int side = 0; side < 2; ++side)
+            for (auto& ed : U[i].edges[side]) {
+                uint32_t* o = edges + 6 * e++;
+                o[0] = (uint32_t)i;
+                o[1] = (uint32_t)side;
+                o[2] = ed[0];
+                o[3] = ed[1];
+                o[4] = ed[2];
+                o[5] = ed[3];
+            }
+    }
+}
+ORC_API void orc_compact_free(void* h) { delete (OCompacted*)h; }

@@ -70,6 +70,12 @@ _SIG = {
     "orc_cms_nbytes": (C.c_uint64, [vp]),
     "orc_cms_export": (None, [vp, u8p]),
     "orc_cms_import": (None, [vp, u8p]),
+    "orc_compact": (vp, [C.c_int, C.c_uint, u64p, u16p, u8p, C.c_uint64]),
+    "orc_compact_count": (C.c_uint64, [vp]),
+    "orc_compact_bases": (C.c_uint64, [vp]),
+    "orc_compact_n_edges": (C.c_uint64, [vp]),
+    "orc_compact_export": (None, [vp, u8p, u64p, C.POINTER(C.c_float), u8p, u32p]),
+    "orc_compact_free": (None, [vp]),
     "orc_build_pass1": (C.c_int, [C.POINTER(OrcArena), C.c_uint, C.c_int, vp, C.c_int, u64p, C.POINTER(u32p)]),
     "orc_build_pass1_contigs": (C.c_int, [u8p, u64p, C.c_uint64, C.c_uint, C.c_int, vp]),
     "orc_build_pass2": (vp, [C.POINTER(OrcArena), C.c_uint, C.c_int, vp, C.c_uint, C.c_int, u64p, C.POINTER(u32p), u8p,
@@ -272,3 +278,27 @@ def count_stats(**kw) -> OrcCountStats:
     for k, v in kw.items():
         setattr(s, k, v)
     return s
+
+
+def compact(keys: np.ndarray, cov: np.ndarray, mask: np.ndarray, k: int, key_bits: int):
+    """Oracle of build.rs:330-594: SolidKmerNode rows -> (seqs list[bytes], cov f32[n],
+    circular bool[n], edges u32[m, 6] = from id, from side, to id, to rc, overlap, support)."""
+    keys = np.ascontiguousarray(keys, np.uint64).reshape(-1)
+    cov = np.ascontiguousarray(cov, np.uint16)
+    mask = np.ascontiguousarray(mask, np.uint8)
+    h = lib().orc_compact(key_bits, k, p(keys), p(cov), p(mask), len(cov))
+    assert h
+    try:
+        n = lib().orc_compact_count(h)
+        nb = lib().orc_compact_bases(h)
+        ne = lib().orc_compact_n_edges(h)
+        seqs = np.zeros(max(nb, 1), np.uint8)
+        offs = np.zeros(n + 1, np.uint64)
+        cv = np.zeros(max(n, 1), np.float32)
+        circ = np.zeros(max(n, 1), np.uint8)
+        edges = np.zeros((max(ne, 1), 6), np.uint32)
+        lib().orc_compact_export(h, p(seqs), p(offs), cv.ctypes.data_as(C.POINTER(C.c_float)), p(circ), p(edges.reshape(-1)))
+    finally:
+        lib().orc_compact_free(h)
+    out = [seqs[offs[i]:offs[i + 1]].tobytes() for i in range(n)]
+    return out, cv[:n], circ[:n].astype(bool), edges[:ne]

@@ -375,3 +375,86 @@ def test_build_tuning_variants(repeat_isolate, tune):
             compare_gate_only(c, repeat_isolate[0], k, kb, cb, None, 14)
     finally:
         c.close()
+
+
+# ---------------------------------------------------------------------------
+# unitig compaction (build.rs:330-594)
+# ---------------------------------------------------------------------------
+def _canon_cycle(s: bytes) -> bytes:
+    """Rotation- and strand-independent form of a circular sequence."""
+    rc = s[::-1].translate(bytes.maketrans(b"ACGT", b"TGCA"))
+    return min(min(x[i:] + x[:i] for i in range(len(x))) for x in (s, rc))
+
+
+def _cov_choices(seq: bytes, rows: dict, k: int, kb: int):
+    """Both coverages a linear unitig can get (walked from either end): mean node
+    coverage of its k-mers without the last one of the walk."""
+    nw = kb // 64
+    covs = []
+    for i in range(len(seq) - k + 1):
+        w = seq[i:i + k]
+        key = np.zeros(nw, np.uint64)
+        assert orc.lib().orc_kmer_from_ascii(kb, orc.p(np.frombuffer(w, np.uint8).copy()), k, orc.p(key)) == 0
+        rk = np.zeros(nw, np.uint64)
+        orc.lib().orc_kmer_rev_comp(kb, orc.p(key), k, orc.p(rk))
+        can = min(tuple(int(x) for x in key), tuple(int(x) for x in rk))
+        covs.append(rows.get(can, 0))
+    a = np.float32(max(1.0, np.float32(sum(covs[:-1])) / np.float32(len(covs) - 1))) if len(covs) > 1 else None
+    b = np.float32(max(1.0, np.float32(sum(covs[1:])) / np.float32(len(covs) - 1))) if len(covs) > 1 else None
+    return {a, b}
+
+
+def compare_compaction(ctx, bank, k, kb, cb, tsc, log2w):
+    table = api.build_cdbg_with_contigs_ext(bank, [], k, tsc, None, ctx=ctx, key_bits=kb, counter_bits=cb,
+                                            cms_log2_width=log2w)
+    keys, cov, mask = table.export()
+    gseq, gcov, gcirc, gedges = api.compact(table)
+    oseq, ocov, ocirc, oedges = orc.compact(keys, cov, mask, k, kb)
+    # linear unitigs: the same canonical sequences; circular ones up to rotation
+    assert sorted(s for s, c in zip(gseq, gcirc) if not c) == sorted(s for s, c in zip(oseq, ocirc) if not c)
+    assert sorted(_canon_cycle(s) for s, c in zip(gseq, gcirc) if c) == sorted(_canon_cycle(s) for s, c in zip(oseq, ocirc) if c)
+    # coverage: one of the two ends' values, as the reference's map order picks one
+    rows = {tuple(int(x) for x in kk): int(c) for kk, c in zip(keys.reshape(len(cov), -1), cov)}
+    for s, c, circ in zip(gseq, gcov, gcirc):
+        if not circ:
+            assert np.float32(c) in _cov_choices(s, rows, k, kb), s[:40]
+    # edges between linear unitigs: same (from seq, side, to seq, strand, overlap, support) multiset
+    def edge_set(seqs, circ, edges):
+        out = []
+        for f, side, t, trc, ov, sup in edges:
+            if circ[f] or circ[t]:
+                continue
+            out.append((seqs[f], int(side), seqs[t], int(trc), int(ov), int(sup)))
+        return sorted(out)
+    assert edge_set(gseq, gcirc, gedges) == edge_set(oseq, ocirc, oedges)
+    return gseq, gcirc
+
+
+@pytest.mark.parametrize("k,kb", [(21, 64), (31, 64), (45, 128), (77, 256)])
+def test_compaction_matches_oracle(ctx, repeat_isolate, k, kb):
+    seqs, circ = compare_compaction(ctx, repeat_isolate[0], k, kb, 16, None, 16)
+    assert len(seqs) > 10
+
+
+def test_compaction_three_unitig_gate(ctx):
+    # build.rs:604-687: 10 kb circular genome with a 200 bp repeat, 1% errors, solidity 5
+    from test_compact_oracle import gate_reads, gate_width
+    reads = gate_reads()
+    bank = api.ReadBank(merged_reads=api.BitSeqArena.from_seqs(reads))
+    log2w = gate_width(sum(map(len, reads))).bit_length() - 1
+    table = api.build_cdbg(bank, 31, 5, ctx=ctx, key_bits=64, counter_bits=4, cms_log2_width=log2w)
+    seqs, cov, circ, edges = api.compact(table)
+    assert len(seqs) == 3 and not circ.any()
+    compare_compaction(ctx, bank, 31, 64, 4, 5, log2w)
+
+
+def test_compaction_circular_plasmid(ctx):
+    # an error-free circular sequence with no repeat compacts to one circular unitig
+    rng = np.random.default_rng(5)
+    plasmid = bytes(np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, 3000)])
+    ring = plasmid + plasmid[:200]
+    reads = [ring[i:i + 150] for i in range(0, 3000, 7)] * 8
+    bank = api.ReadBank(merged_reads=api.BitSeqArena.from_seqs(reads))
+    seqs, circ = compare_compaction(ctx, bank, 31, 64, 16, None, 16)
+    assert list(circ) == [True] and len(seqs[0]) == 3000
+    assert _canon_cycle(seqs[0]) == _canon_cycle(plasmid)
