@@ -392,6 +392,7 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "pass2_mode" && (v == 0 || v == 1)) ctx->pass2_mode = (int)v;
     else if (n == "record_factor" && v > 0 && v <= 16) ctx->record_factor = v;
     else if (n == "sketch_mode" && (v == 0 || v == 1)) ctx->sketch_mode = (int)v;
+    else if (n == "ladder_ilp" && (v == 1 || v == 2)) ctx->ladder_ilp = (int)v;
     // the pass kernels are compiled for blocks of at most 256 threads
     else if (n == "block_pass1" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_pass1 = (int)v;
     else if (n == "grid_pass1" && v >= 0) ctx->grid_pass1 = (int)v;
@@ -411,6 +412,7 @@ FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, doub
     else if (n == "pass2_mode") *v = ctx->pass2_mode;
     else if (n == "record_factor") *v = ctx->record_factor;
     else if (n == "sketch_mode") *v = ctx->sketch_mode;
+    else if (n == "ladder_ilp") *v = ctx->ladder_ilp;
     else if (n == "block_pass1") *v = ctx->block_pass1;
     else if (n == "grid_pass1") *v = ctx->grid_pass1;
     else if (n == "block_pass2") *v = ctx->block_pass2;
@@ -1309,7 +1311,7 @@ static fbk_status build_front_ladder(fbk_ctx* ctx, const fbk_bank* b, const fbk_
         TimedLaunch tl;
         time_begin(ctx, "pass1", tl);
         cudaError_t e = launch_ladder_pass1(nw, L, bank_view(b, b->chunk_starts[c], b->chunk_starts[c + 1], keep), p->k, lad.bits,
-                                            log2w, p->t_solid, hll);
+                                            log2w, p->t_solid, hll, ctx->ladder_ilp);
         time_end(ctx, tl);
         if (e != cudaSuccess) st = cuda_err(ctx, e, "pass1 ladder");
     }

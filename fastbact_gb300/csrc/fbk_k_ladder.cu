@@ -19,9 +19,9 @@
 
 namespace fbk {
 
-template <int NW>
-__global__ void __launch_bounds__(256) k_ladder_pass1(BankDev b, uint32_t k, uint32_t* __restrict__ lad, uint32_t log2w,
-                                                      uint32_t t, uint32_t* __restrict__ hll12) {
+template <int NW, int ILP>
+__global__ void __launch_bounds__(256, ILP == 1 ? 4 : 2) k_ladder_pass1(BankDev b, uint32_t k, uint32_t* __restrict__ lad,
+                                                                        uint32_t log2w, uint32_t t, uint32_t* __restrict__ hll12) {
     __shared__ uint32_t s_hll[4096];
     const bool do_hll = hll12 != nullptr;
     if (do_hll) {
@@ -39,30 +39,51 @@ __global__ void __launch_bounds__(256) k_ladder_pass1(BankDev b, uint32_t k, uin
         if (len < k || !bank_keep(b, r)) continue;
         const uint64_t off = b.off[r];
         const uint32_t nk = len - k + 1;
-        // Warp-uniform trip counts throughout (chunks of 32 windows, all t levels):
-        // the climb is a predicated atomic per level, so the warp never splits.
-        for (uint32_t it = 0; it < ((nk + 31) >> 5); ++it) {
-            const uint32_t q = (it << 5) + lane;
-            if (q >= nk) continue;
-            Key<NW> can;
-            bool rc;
-            window_canonical<NW>(b.data, off + q, k, can, rc);
-            const uint64_t key = key_fold<NW>(can);
-            const uint64_t h0 = smix(key ^ cms_seed(0));
+        // Warp-uniform trip counts throughout (ILP chunks of 32 windows at a time, all t
+        // levels): the climb is a predicated atomic per level, so the warp never splits.
+        // With ILP = 2 each lane takes two windows and issues the eight top-level loads
+        // together (the kernel is bound by their L2 latency) at half the resident warps.
+        for (uint32_t it = 0; it < ((nk + 31) >> 5); it += ILP) {
+            uint32_t wd[ILP][4], mk[ILP][4];
+            bool live[ILP];
+            uint64_t h0[ILP];
 #pragma unroll
-            for (int row = 0; row < 4; ++row) {
-                const uint64_t h = row == 0 ? h0 : smix(key ^ cms_seed(row));
-                const uint64_t bit = ((uint64_t)row << log2w) + (h & wmask);
-                const uint64_t w = bit >> 5;
-                const uint32_t m = 1u << (bit & 31);
-                bool climb = !(__ldcg(top + w) & m);  // false once the count reached t
-                for (uint32_t j = 0; j < t; ++j)
-                    if (climb) climb = (atomicOr(lad + (uint64_t)j * level_words + w, m) & m) != 0;
+            for (int p = 0; p < ILP; ++p) {
+                const uint32_t q = ((it + p) << 5) + lane;
+                live[p] = q < nk;
+                h0[p] = 0;
+                if (!live[p]) continue;
+                Key<NW> can;
+                bool rc;
+                window_canonical<NW>(b.data, off + q, k, can, rc);
+                const uint64_t key = key_fold<NW>(can);
+                h0[p] = smix(key ^ cms_seed(0));
+#pragma unroll
+                for (int row = 0; row < 4; ++row) {
+                    const uint64_t h = row == 0 ? h0[p] : smix(key ^ cms_seed(row));
+                    const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
+                    wd[p][row] = bit >> 5;
+                    mk[p][row] = 1u << (bit & 31);
+                }
             }
-            if (do_hll) {
-                uint32_t idx, rho;
-                hll_idx_rho(h0, 12, idx, rho);
-                if (s_hll[idx] < rho) atomicMax(&s_hll[idx], rho);
+            uint32_t topw[ILP][4];
+#pragma unroll
+            for (int p = 0; p < ILP; ++p)
+#pragma unroll
+                for (int row = 0; row < 4; ++row) topw[p][row] = live[p] ? __ldcg(top + wd[p][row]) : ~0u;
+#pragma unroll
+            for (int p = 0; p < ILP; ++p) {
+#pragma unroll
+                for (int row = 0; row < 4; ++row) {
+                    bool climb = !(topw[p][row] & mk[p][row]);  // false once the count reached t
+                    for (uint32_t j = 0; j < t; ++j)
+                        if (climb) climb = (atomicOr(lad + (uint64_t)j * level_words + wd[p][row], mk[p][row]) & mk[p][row]) != 0;
+                }
+                if (do_hll && live[p]) {
+                    uint32_t idx, rho;
+                    hll_idx_rho(h0[p], 12, idx, rho);
+                    if (s_hll[idx] < rho) atomicMax(&s_hll[idx], rho);
+                }
             }
         }
     }
@@ -123,17 +144,22 @@ static int grid_l(K kernel, const Launch& L) {
     return per_sm * (L.sms > 0 ? L.sms : 1);
 }
 
-template <int NW>
+template <int NW, int ILP>
 static cudaError_t lp1(const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t, uint32_t* hll) {
-    k_ladder_pass1<NW><<<grid_l(k_ladder_pass1<NW>, L), L.block, 0, L.stream>>>(b, k, lad, log2w, t, hll);
+    k_ladder_pass1<NW, ILP><<<grid_l(k_ladder_pass1<NW, ILP>, L), L.block, 0, L.stream>>>(b, k, lad, log2w, t, hll);
     return cudaGetLastError();
 }
 cudaError_t launch_ladder_pass1(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t,
-                                uint32_t* hll12) {
-    if (t < 1 || t > LADDER_MAX_LEVELS) return cudaErrorInvalidValue;
-    if (nw == 1) return lp1<1>(L, b, k, lad, log2w, t, hll12);
-    if (nw == 2) return lp1<2>(L, b, k, lad, log2w, t, hll12);
-    return lp1<4>(L, b, k, lad, log2w, t, hll12);
+                                uint32_t* hll12, int ilp) {
+    if (t < 1 || t > LADDER_MAX_LEVELS || log2w > 29) return cudaErrorInvalidValue;  // bit indices fit 32 bits
+    if (ilp == 2) {
+        if (nw == 1) return lp1<1, 2>(L, b, k, lad, log2w, t, hll12);
+        if (nw == 2) return lp1<2, 2>(L, b, k, lad, log2w, t, hll12);
+        return lp1<4, 2>(L, b, k, lad, log2w, t, hll12);
+    }
+    if (nw == 1) return lp1<1, 1>(L, b, k, lad, log2w, t, hll12);
+    if (nw == 2) return lp1<2, 1>(L, b, k, lad, log2w, t, hll12);
+    return lp1<4, 1>(L, b, k, lad, log2w, t, hll12);
 }
 
 template <int NW>

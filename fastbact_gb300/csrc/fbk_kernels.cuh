@@ -124,8 +124,9 @@ cudaError_t launch_table_init(int nw, const Launch& L, const TableDev& t);
 // The CMS gate of pass 2 without counts: t levels x 4 rows x 2^log2w bits, level j of
 // (row, col) set once the count reached j + 1.  1 <= t <= LADDER_MAX_LEVELS.
 constexpr uint32_t LADDER_MAX_LEVELS = 8;
+// ilp: windows per lane per step (1 or 2).
 cudaError_t launch_ladder_pass1(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t,
-                                uint32_t* hll12);
+                                uint32_t* hll12, int ilp);
 cudaError_t launch_ladder_solid(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
                                 uint32_t t, uint32_t* bm);
 // Record emit of pass 2 with the ladder gate evaluated inline (no solidity bitmap).

@@ -362,6 +362,7 @@ TUNINGS = [
     dict(sweep_bytes=1 << 31, bucket_bytes=1 << 30),      # one sweep over all rows, one bucket
     dict(stripes=1, record_factor=0.05),                  # stripes overflow -> direct fallback
     dict(load_factor=0.85, block_pass1=128, block_pass2=64, grid_pass1=37, grid_pass2=91),
+    dict(ladder_ilp=2, block_pass1=128),                 # two windows per lane in the ladder pass 1
 ]
 
 
