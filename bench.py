@@ -539,7 +539,9 @@ def run_serve_mode(args):
     gen_s = time.time() - t0
     n_req = max(8, 3 * args.isolates // 2)
     ctx = api.Context(0, pool_bytes=int(os.environ.get("FBK_POOL_BYTES", str(200 << 30))))
-    sp = api.server_params(policy=cohort.policy(), k=BATCH_K, cms_log2_width=BATCH_LOG2W, counter_bits=16, workers=2)
+    sp = api.server_params(policy=cohort.policy(), k=BATCH_K, cms_log2_width=BATCH_LOG2W, counter_bits=16,
+                           workers=int(os.environ.get("FBK_SERVE_WORKERS", "2")),
+                           use_graphs=int(os.environ.get("FBK_SERVE_GRAPHS", "1")))
     srv = api.Server(ctx, sp)
 
     def consume(i):
@@ -648,7 +650,9 @@ def run_serve_mode(args):
                           "rate = FIFO replay of these measured service times on the same arrivals"},
         "server": {"waves_a": st.waves_a, "waves_b": st.waves_b, "peak_in_flight": st.peak_in_flight,
                    "peak_reserved_gb": st.peak_reserved_bytes / 1e9, "budget_gb": st.budget_bytes / 1e9,
-                   "failed": st.failed},
+                   "failed": st.failed, "busy_ms": st.busy_ms, "device_ms": {"estimate": st.ms_estimate,
+                   "phase_a": st.ms_phase_a, "phase_b": st.ms_phase_b}, "requests": st.submitted,
+                   "graphs": sp.batch.use_graphs, "workers": sp.workers},
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)

@@ -105,7 +105,8 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("done", C.c_uint64), ("failed", C.c_uint64), ("waves_a", C.c_uint64),
                 ("waves_b", C.c_uint64), ("isolates_a", C.c_uint64), ("isolates_b", C.c_uint64),
                 ("reserved_bytes", C.c_uint64), ("peak_reserved_bytes", C.c_uint64), ("budget_bytes", C.c_uint64),
-                ("peak_in_flight", C.c_uint64), ("busy_ms", C.c_double)]
+                ("peak_in_flight", C.c_uint64), ("busy_ms", C.c_double), ("ms_estimate", C.c_double),
+                ("ms_phase_a", C.c_double), ("ms_phase_b", C.c_double)]
 
 
 class SynthParams(C.Structure):

@@ -1046,7 +1046,17 @@ void job_admit(fbk_server* S, int w, const std::vector<Req*>& job) {
             r->state = 2;  // the host buffers are no longer read
             S->cv.notify_all();
         }
-        if (st == FBK_OK) st = estimate_one(B, it);
+        if (st == FBK_OK) {
+            cudaEventRecord(B->ev[0], ctx->stream);
+            st = estimate_one(B, it);
+            if (st == FBK_OK) {
+                float t_est = 0.f;
+                cudaEventRecord(B->ev[1], ctx->stream);
+                cudaEventSynchronize(B->ev[1]);
+                cudaEventElapsedTime(&t_est, B->ev[0], B->ev[1]);
+                B->stats.ms_estimate += t_est;
+            }
+        }
         if (st) {
             free_iso(B, it);
             std::lock_guard<std::mutex> lk(S->mu);
@@ -1340,6 +1350,12 @@ FBK_API fbk_status fbk_server_get_stats(fbk_server* S, fbk_server_stats* out) {
     std::lock_guard<std::mutex> lk(S->mu);
     *out = S->stats;
     out->reserved_bytes = S->reserved;
+    out->ms_estimate = out->ms_phase_a = out->ms_phase_b = 0.0;
+    for (const fbk_batch* B : S->wb) {
+        out->ms_estimate += B->stats.ms_estimate;
+        out->ms_phase_a += B->stats.ms_phase_a;
+        out->ms_phase_b += B->stats.ms_phase_b;
+    }
     return FBK_OK;
 }
 

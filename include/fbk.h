@@ -430,6 +430,7 @@ typedef struct {
     uint64_t reserved_bytes, peak_reserved_bytes, budget_bytes;
     uint64_t peak_in_flight;  /* most requests admitted and not yet done */
     double busy_ms;           /* summed worker time inside waves */
+    double ms_estimate, ms_phase_a, ms_phase_b;  /* summed device time of the workers' stages */
 } fbk_server_stats;
 
 FBK_API void fbk_server_defaults(fbk_server_params* p);
