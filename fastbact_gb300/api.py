@@ -405,6 +405,7 @@ class DeviceBank:
         check(N.lib().fbk_bank_upload(ctx.handle, self._views, C.byref(self._h)), ctx.handle, "bank upload")
         ctx.adopt(self)
         self.n_bases = bank.total_bases()
+        self.n_reads = bank.total_reads()
 
     @property
     def handle(self):
@@ -632,6 +633,47 @@ def compact(table: "SolidTable"):
         N.lib().fbk_unitigs_release(h)
     out = [seqs[offs[i]:offs[i + 1]].tobytes() for i in range(n.value)]
     return out, cov[:n.value], circ[:n.value].astype(bool), edges[:ne.value]
+
+
+def filter_active_reads(ctx: Context, bank, seqs: list, circular, edges, graph_k: int):
+    """filter_active_reads (local_multik.rs:259-333) on the device: the keep byte of every
+    read in bank order (merged, pe_forward, pe_reverse) and the kept count.  seqs,
+    circular and edges are compact()'s unitigs."""
+    dbank = bank if isinstance(bank, DeviceBank) else DeviceBank(ctx, bank)
+    n = len(seqs)
+    useq = np.frombuffer(b"".join(seqs), np.uint8).copy() if n else np.zeros(1, np.uint8)
+    uoff = np.zeros(n + 1, np.uint64)
+    if n:
+        uoff[1:] = np.cumsum([len(x) for x in seqs])
+    circ = np.ascontiguousarray(np.asarray(circular, np.uint8)) if n else np.zeros(1, np.uint8)
+    e = np.asarray(edges).reshape(-1, 6)
+    fwd = np.bincount(e[e[:, 1] == 0, 0].astype(np.int64), minlength=n)[:n].astype(np.uint32)
+    rev = np.bincount(e[e[:, 1] == 1, 0].astype(np.int64), minlength=n)[:n].astype(np.uint32)
+    if not n:
+        fwd = rev = np.zeros(1, np.uint32)
+    total = int(sum(dbank_reads for dbank_reads in _bank_reads(bank)))
+    keep = np.zeros(max(total, 1), np.uint8)
+    kept = C.c_uint64()
+    check(N.lib().fbk_filter_active_reads(ctx.handle, dbank.handle, ptr(useq), ptr(uoff), ptr(circ), ptr(fwd), ptr(rev), n,
+                                          graph_k, ptr(keep), C.byref(kept)), ctx.handle, "filter_active_reads")
+    return keep[:total], kept.value
+
+
+def _bank_reads(bank):
+    if isinstance(bank, DeviceBank):
+        return [bank.n_reads]
+    return [len(a) for a in bank.arenas]
+
+
+def select_reads(bank: "ReadBank", keep: np.ndarray) -> "ReadBank":
+    """The ReadBank of the reads whose keep byte is set (packed words shared)."""
+    out, pos = [], 0
+    for a in bank.arenas:
+        m = keep[pos:pos + len(a)].astype(bool)
+        pos += len(a)
+        out.append(BitSeqArena(a.data, np.ascontiguousarray(a.offsets[m]), np.ascontiguousarray(a.lengths[m]),
+                               np.ascontiguousarray(a.pair_idx[m]) if a.pair_idx is not None else None))
+    return ReadBank(*out)
 
 
 def sort_rows(keys: np.ndarray, *cols):

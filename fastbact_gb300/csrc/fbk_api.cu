@@ -499,6 +499,7 @@ fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_ar
         }
         wbase += v.n_words;
         rbase += v.n_seqs;
+        b->arena_reads.push_back(v.n_seqs);
     }
     cudaError_t e = cudaMemsetAsync(b->data + n_words, 0, 8 * 8, ctx->stream);
     if (e != cudaSuccess) {

@@ -84,6 +84,7 @@ struct fbk_bank {
     uint64_t n_reads = 0, n_words = 0, n_bases = 0, n_pairs = 0;
     uint32_t max_len = 0;
     std::vector<uint64_t> chunk_starts;  // read-range boundaries (see bank_upload_impl)
+    std::vector<uint64_t> arena_reads;   // reads of each uploaded arena, in bank order
     uint64_t max_chunk = 0;              // most bases in one range
     uint64_t max_chunk_bases() const { return max_chunk; }
     std::vector<uint64_t> len_hist;      // read-length histogram (last bin: all longer reads)

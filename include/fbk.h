@@ -306,6 +306,17 @@ FBK_API fbk_status fbk_unitigs_export(const fbk_unitigs* u, uint8_t* ascii, uint
 FBK_API fbk_status fbk_unitigs_edges(const fbk_unitigs* u, uint32_t* edges, uint64_t cap, uint64_t* n_out);
 FBK_API fbk_status fbk_unitigs_release(fbk_unitigs* u);
 
+/* filter_active_reads (src/graph/local_multik.rs:259-333), the multi-k upgrade's input
+ * filter: keep_out gets one byte per read of the bank, in bank order (merged,
+ * pe_forward, pe_reverse): merged reads are kept when active, a pair (pe_forward[i],
+ * pe_reverse[i], i < min of the two arena sizes) when either read is.  The unitigs are
+ * the graph's sequences (ASCII, offsets: n_unitigs + 1), circular flags and the number
+ * of edges on each side (edges_fwd.len(), edges_rev.len()); graph_k is the graph's k. */
+FBK_API fbk_status fbk_filter_active_reads(fbk_ctx* ctx, const fbk_bank* bank, const uint8_t* unitig_ascii,
+                                           const uint64_t* unitig_offsets, const uint8_t* circular, const uint32_t* edges_fwd,
+                                           const uint32_t* edges_rev, uint64_t n_unitigs, uint32_t graph_k, uint8_t* keep_out,
+                                           uint64_t* n_kept);
+
 /* Subsampling policy of the pipeline driver (src/main.rs:76-180): decides the
  * subsample factor from an estimate.  reason: 0 EXPLICIT_NO_SUBSAMPLE_FLAG,
  * 1 EXPLICIT_GENOME_SIZE_ZERO_INVALID, 2 AUTO_SUBSAMPLE_EXPLICIT_GENOME_SIZE,

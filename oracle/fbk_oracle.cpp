@@ -1558,3 +1558,58 @@ ORC_API void orc_compact_export(const void* h, uint8_t* seqs, uint64_t* offs, fl
     }
 }
 ORC_API void orc_compact_free(void* h) { delete (OCompacted*)h; }
+
+// ===========================================================================
+// filter_active_reads — local_multik.rs:259-333.  unitigs: ASCII + offsets, circular
+// flags, edge counts per side; arenas: merged, pe_forward, pe_reverse.  keep: one byte
+// per read in that order.
+// ===========================================================================
+#include <unordered_set>
+
+static std::string arena_read(const orc_arena& a, uint64_t i) {  // BitSeqArena::extract_ascii_into
+    std::string s(a.lengths[i], 'A');
+    for (uint32_t j = 0; j < a.lengths[i]; ++j) {
+        const uint64_t p = a.offsets[i] + j;
+        s[j] = "ACGT"[(a.data[p >> 5] >> ((p & 31) * 2)) & 3];
+    }
+    return s;
+}
+
+ORC_API uint64_t orc_filter_active_reads(const orc_arena* arenas, const uint8_t* useq, const uint64_t* uoff, const uint8_t* circular,
+                                         const uint32_t* efwd, const uint32_t* erev, uint64_t n_unitigs, unsigned graph_k,
+                                         uint8_t* keep) {
+    const unsigned k = std::min(graph_k, 31u);
+    const uint64_t W = 350;
+    std::unordered_set<uint64_t> boundary;
+    auto h = [&](const char* s) { return orc_nthash_canonical((const uint8_t*)s, k); };
+    for (uint64_t u = 0; u < n_unitigs; ++u) {
+        const std::string seq((const char*)useq + uoff[u], uoff[u + 1] - uoff[u]);
+        if (seq.size() < k) continue;
+        if (seq.size() < 2000 || circular[u] || efwd[u] > 1 || erev[u] > 1) {
+            for (size_t i = 0; i + k <= seq.size(); ++i) boundary.insert(h(seq.data() + i));
+        } else {
+            const size_t left = std::min<size_t>(W, seq.size() - k + 1);
+            for (size_t i = 0; i < left; ++i) boundary.insert(h(seq.data() + i));
+            const size_t right = std::min<size_t>(seq.size() > W ? seq.size() - W : 0, seq.size() - k);
+            for (size_t i = right; i <= seq.size() - k; ++i) boundary.insert(h(seq.data() + i));
+        }
+    }
+    auto active = [&](const std::string& s) {
+        if (s.size() < k) return false;
+        const size_t offs[3] = {0, (s.size() - k) / 2, s.size() - k};
+        for (size_t o : offs)
+            if (boundary.count(h(s.data() + o))) return true;
+        return false;
+    };
+    uint64_t kept = 0, r = 0;
+    const uint64_t M = arenas[0].n_seqs, F = arenas[1].n_seqs, R = arenas[2].n_seqs;
+    for (uint64_t i = 0; i < M; ++i, ++r) kept += keep[r] = active(arena_read(arenas[0], i));
+    for (uint64_t i = 0; i < F + R; ++i) keep[M + i] = 0;
+    const uint64_t pe = std::min(F, R);
+    for (uint64_t i = 0; i < pe; ++i) {
+        const uint8_t kp = active(arena_read(arenas[1], i)) || active(arena_read(arenas[2], i));
+        keep[M + i] = keep[M + F + i] = kp;
+        kept += 2 * kp;
+    }
+    return kept;
+}

@@ -76,6 +76,7 @@ _SIG = {
     "orc_compact_n_edges": (C.c_uint64, [vp]),
     "orc_compact_export": (None, [vp, u8p, u64p, C.POINTER(C.c_float), u8p, u32p]),
     "orc_compact_free": (None, [vp]),
+    "orc_filter_active_reads": (C.c_uint64, [C.POINTER(OrcArena), u8p, u64p, u8p, u32p, u32p, C.c_uint64, C.c_uint, u8p]),
     "orc_build_pass1": (C.c_int, [C.POINTER(OrcArena), C.c_uint, C.c_int, vp, C.c_int, u64p, C.POINTER(u32p)]),
     "orc_build_pass1_contigs": (C.c_int, [u8p, u64p, C.c_uint64, C.c_uint, C.c_int, vp]),
     "orc_build_pass2": (vp, [C.POINTER(OrcArena), C.c_uint, C.c_int, vp, C.c_uint, C.c_int, u64p, C.POINTER(u32p), u8p,
@@ -302,3 +303,27 @@ def compact(keys: np.ndarray, cov: np.ndarray, mask: np.ndarray, k: int, key_bit
         lib().orc_compact_free(h)
     out = [seqs[offs[i]:offs[i + 1]].tobytes() for i in range(n)]
     return out, cv[:n], circ[:n].astype(bool), edges[:ne]
+
+
+def edge_counts(n: int, edges: np.ndarray):
+    """Edges per unitig side (edges_fwd.len(), edges_rev.len()) from the export layout."""
+    e = np.asarray(edges).reshape(-1, 6)
+    fwd = np.bincount(e[e[:, 1] == 0, 0].astype(np.int64), minlength=n)[:n].astype(np.uint32)
+    rev = np.bincount(e[e[:, 1] == 1, 0].astype(np.int64), minlength=n)[:n].astype(np.uint32)
+    return fwd, rev
+
+
+def filter_active_reads(bank, seqs: list, circular, edges, graph_k: int):
+    """Oracle of local_multik.rs:259-333: keep byte per read (merged, pe_fwd, pe_rev)."""
+    n = len(seqs)
+    useq = np.frombuffer(b"".join(seqs), np.uint8).copy() if seqs else np.zeros(1, np.uint8)
+    uoff = np.zeros(n + 1, np.uint64)
+    uoff[1:] = np.cumsum([len(x) for x in seqs]) if n else []
+    circ = np.ascontiguousarray(np.asarray(circular, np.uint8)) if n else np.zeros(1, np.uint8)
+    fwd, rev = edge_counts(n, edges)
+    ar = arenas3(bank)
+    total = sum(len(a) for a in bank.arenas)
+    keep = np.zeros(max(total, 1), np.uint8)
+    lib().orc_filter_active_reads(ar, p(useq), p(uoff), p(circ), p(np.ascontiguousarray(fwd)), p(np.ascontiguousarray(rev)),
+                                  n, graph_k, p(keep))
+    return keep[:total]

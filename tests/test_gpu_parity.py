@@ -459,3 +459,21 @@ def test_compaction_circular_plasmid(ctx):
     seqs, circ = compare_compaction(ctx, bank, 31, 64, 16, None, 16)
     assert list(circ) == [True] and len(seqs[0]) == 3000
     assert _canon_cycle(seqs[0]) == _canon_cycle(plasmid)
+
+
+# ---------------------------------------------------------------------------
+# multi-k input filter (local_multik.rs:259-333)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("k,graph_k", [(31, 31), (45, 45), (21, 21)])
+def test_filter_active_reads_matches_oracle(ctx, repeat_isolate, k, graph_k):
+    bank = repeat_isolate[0]
+    kb = api.key_bits_for_k(k)
+    table = api.build_cdbg_ext(bank, k, None, ctx=ctx, key_bits=kb, counter_bits=16, cms_log2_width=16)
+    seqs, cov, circ, edges = api.compact(table)
+    keep, kept = api.filter_active_reads(ctx, bank, seqs, circ, edges, graph_k)
+    okeep = orc.filter_active_reads(bank, seqs, circ, edges, graph_k)
+    assert np.array_equal(keep, okeep)
+    assert kept == int(okeep.sum()) and 0 < kept < len(keep)
+    assert any(len(s) >= 2000 for s in seqs)  # the long-unitig branch ran
+    sub = api.select_reads(bank, keep)
+    assert sub.total_reads() == kept
