@@ -52,6 +52,8 @@ __global__ void __launch_bounds__(256, ILP == 1 ? 4 : 2) k_ladder_pass1(BankDev 
                 const uint32_t q = ((it + p) << 5) + lane;
                 live[p] = q < nk;
                 h0[p] = 0;
+#pragma unroll
+                for (int row = 0; row < 4; ++row) wd[p][row] = mk[p][row] = 0;
                 if (!live[p]) continue;
                 Key<NW> can;
                 bool rc;
@@ -75,7 +77,8 @@ __global__ void __launch_bounds__(256, ILP == 1 ? 4 : 2) k_ladder_pass1(BankDev 
             for (int p = 0; p < ILP; ++p) {
 #pragma unroll
                 for (int row = 0; row < 4; ++row) {
-                    bool climb = !(topw[p][row] & mk[p][row]);  // false once the count reached t
+                    // false once the count reached t, and for lanes past the read's last window
+                    bool climb = live[p] && !(topw[p][row] & mk[p][row]);
                     for (uint32_t j = 0; j < t; ++j)
                         if (climb) climb = (atomicOr(lad + (uint64_t)j * level_words + wd[p][row], mk[p][row]) & mk[p][row]) != 0;
                 }
