@@ -473,7 +473,9 @@ def test_filter_active_reads_matches_oracle(ctx, repeat_isolate, k, graph_k):
     keep, kept = api.filter_active_reads(ctx, bank, seqs, circ, edges, graph_k)
     okeep = orc.filter_active_reads(bank, seqs, circ, edges, graph_k)
     assert np.array_equal(keep, okeep)
-    assert kept == int(okeep.sum()) and 0 < kept < len(keep)
-    assert any(len(s) >= 2000 for s in seqs)  # the long-unitig branch ran
+    assert kept == int(okeep.sum()) and 0 < kept <= len(keep)
+    if k == 31:
+        # long unitigs exist, so only reads near their ends and junctions stay
+        assert any(len(s) >= 2000 for s in seqs) and kept < len(keep)
     sub = api.select_reads(bank, keep)
     assert sub.total_reads() == kept
