@@ -188,6 +188,7 @@ SIGNATURES = {
     "fbk_unitigs_edges": (S, [vp, u32p, C.c_uint64, u64p]),
     "fbk_unitigs_release": (S, [vp]),
     "fbk_filter_active_reads": (S, [vp, vp, u8p, u64p, u8p, u32p, u32p, C.c_uint64, C.c_uint32, u8p, u64p]),
+    "fbk_index_terminal_kmers": (S, [vp, u8p, u64p, C.c_uint64, C.c_uint32, C.c_uint32, u64p, u32p, u8p, u32p, C.c_uint64, u64p]),
     "fbk_subsample_policy_defaults": (None, [P(SubsamplePolicy)]),
     "fbk_subsample_decide": (S, [P(SubsamplePolicy), P(GenomeEstimate), P(C.c_double), P(C.c_int32)]),
     "fbk_batch_defaults": (None, [P(BatchParams)]),

@@ -659,6 +659,26 @@ def filter_active_reads(ctx: Context, bank, seqs: list, circular, edges, graph_k
     return keep[:total], kept.value
 
 
+def index_terminal_kmers(ctx: Context, seqs: list, k: int, key_bits: int | None = None):
+    """index_terminal_kmers (mapper.rs:89-136) on the device: unique canonical terminal
+    k-mers (folded to u64) of the unitigs with (unitig, is_rc, position), sorted by key."""
+    key_bits = key_bits or key_bits_for_k(k)
+    n = len(seqs)
+    useq = np.frombuffer(b"".join(seqs), np.uint8).copy() if n else np.zeros(1, np.uint8)
+    uoff = np.zeros(n + 1, np.uint64)
+    if n:
+        uoff[1:] = np.cumsum([len(x) for x in seqs])
+    m = C.c_uint64()
+    check(N.lib().fbk_index_terminal_kmers(ctx.handle, ptr(useq), ptr(uoff), n, k, key_bits, None, None, None, None, 0,
+                                           C.byref(m)), ctx.handle, "index_terminal_kmers")
+    cap = m.value
+    keys, uni = np.zeros(max(cap, 1), np.uint64), np.zeros(max(cap, 1), np.uint32)
+    rc, pos = np.zeros(max(cap, 1), np.uint8), np.zeros(max(cap, 1), np.uint32)
+    check(N.lib().fbk_index_terminal_kmers(ctx.handle, ptr(useq), ptr(uoff), n, k, key_bits, ptr(keys), ptr(uni), ptr(rc),
+                                           ptr(pos), cap, C.byref(m)), ctx.handle, "index_terminal_kmers")
+    return keys[:cap], uni[:cap], rc[:cap], pos[:cap]
+
+
 def _bank_reads(bank):
     if isinstance(bank, DeviceBank):
         return [bank.n_reads]

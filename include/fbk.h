@@ -317,6 +317,15 @@ FBK_API fbk_status fbk_filter_active_reads(fbk_ctx* ctx, const fbk_bank* bank, c
                                            const uint32_t* edges_rev, uint64_t n_unitigs, uint32_t graph_k, uint8_t* keep_out,
                                            uint64_t* n_kept);
 
+/* index_terminal_kmers (src/resolve/mapper.rs:89-136): canonical k-mers folded to u64
+ * (KmerInt::to_u64) of the first and last 1000 k-mers of every unitig (all of them when
+ * it has at most 2000), those occurring exactly once, with their unitig, strand
+ * (DirUnitigId is_rc) and k-mer position; sorted by key.  Fills up to cap entries and
+ * returns the total in n_out (call with cap 0 to size the outputs). */
+FBK_API fbk_status fbk_index_terminal_kmers(fbk_ctx* ctx, const uint8_t* unitig_ascii, const uint64_t* unitig_offsets,
+                                            uint64_t n_unitigs, uint32_t k, uint32_t key_bits, uint64_t* keys, uint32_t* unitig,
+                                            uint8_t* is_rc, uint32_t* pos, uint64_t cap, uint64_t* n_out);
+
 /* Subsampling policy of the pipeline driver (src/main.rs:76-180): decides the
  * subsample factor from an estimate.  reason: 0 EXPLICIT_NO_SUBSAMPLE_FLAG,
  * 1 EXPLICIT_GENOME_SIZE_ZERO_INVALID, 2 AUTO_SUBSAMPLE_EXPLICIT_GENOME_SIZE,

@@ -1613,3 +1613,50 @@ ORC_API uint64_t orc_filter_active_reads(const orc_arena* arenas, const uint8_t*
     }
     return kept;
 }
+
+// ===========================================================================
+// index_terminal_kmers — src/resolve/mapper.rs:89-136 (sorted by key for comparison)
+// ===========================================================================
+template <class K>
+static uint64_t term_index_impl(unsigned k, const uint8_t* useq, const uint64_t* uoff, uint64_t n, uint64_t* keys, uint32_t* unitig,
+                                uint8_t* is_rc, uint32_t* pos, uint64_t cap) {
+    std::unordered_map<uint64_t, uint32_t> counts;
+    std::unordered_map<uint64_t, std::pair<uint32_t, uint32_t>> where;  // (id << 1 | is_rc, i)
+    for (uint64_t id = 0; id < n; ++id) {
+        const uint8_t* seq = useq + uoff[id];
+        const uint64_t len = uoff[id + 1] - uoff[id];
+        if (len < k) continue;
+        const uint64_t total = len - k + 1;
+        auto index_kmer = [&](uint64_t i) {
+            const K f = K::from_ascii(seq + i, k), r = f.rev_comp(k);
+            const bool rc = r < f;
+            const uint64_t h = (rc ? r : f).to_u64();
+            counts[h] += 1;
+            where[h] = {(uint32_t)(id << 1 | (rc ? 1 : 0)), (uint32_t)i};
+        };
+        if (total <= 2000) {
+            for (uint64_t i = 0; i < total; ++i) index_kmer(i);
+        } else {
+            for (uint64_t i = 0; i < 1000; ++i) index_kmer(i);
+            for (uint64_t i = total - 1000; i < total; ++i) index_kmer(i);
+        }
+    }
+    std::vector<std::pair<uint64_t, std::pair<uint32_t, uint32_t>>> out;
+    for (auto& kv : where)
+        if (counts[kv.first] == 1) out.push_back(kv);
+    std::sort(out.begin(), out.end());
+    for (uint64_t i = 0; i < out.size() && i < cap; ++i) {
+        keys[i] = out[i].first;
+        unitig[i] = out[i].second.first >> 1;
+        is_rc[i] = out[i].second.first & 1;
+        pos[i] = out[i].second.second;
+    }
+    return out.size();
+}
+
+ORC_API uint64_t orc_index_terminal_kmers(int key_bits, unsigned k, const uint8_t* useq, const uint64_t* uoff, uint64_t n,
+                                          uint64_t* keys, uint32_t* unitig, uint8_t* is_rc, uint32_t* pos, uint64_t cap) {
+    if (key_bits == 64) return term_index_impl<K64>(k, useq, uoff, n, keys, unitig, is_rc, pos, cap);
+    if (key_bits == 128) return term_index_impl<K128>(k, useq, uoff, n, keys, unitig, is_rc, pos, cap);
+    return term_index_impl<K256>(k, useq, uoff, n, keys, unitig, is_rc, pos, cap);
+}

@@ -76,6 +76,7 @@ _SIG = {
     "orc_compact_n_edges": (C.c_uint64, [vp]),
     "orc_compact_export": (None, [vp, u8p, u64p, C.POINTER(C.c_float), u8p, u32p]),
     "orc_compact_free": (None, [vp]),
+    "orc_index_terminal_kmers": (C.c_uint64, [C.c_int, C.c_uint, u8p, u64p, C.c_uint64, u64p, u32p, u8p, u32p, C.c_uint64]),
     "orc_filter_active_reads": (C.c_uint64, [C.POINTER(OrcArena), u8p, u64p, u8p, u32p, u32p, C.c_uint64, C.c_uint, u8p]),
     "orc_build_pass1": (C.c_int, [C.POINTER(OrcArena), C.c_uint, C.c_int, vp, C.c_int, u64p, C.POINTER(u32p)]),
     "orc_build_pass1_contigs": (C.c_int, [u8p, u64p, C.c_uint64, C.c_uint, C.c_int, vp]),
@@ -327,3 +328,17 @@ def filter_active_reads(bank, seqs: list, circular, edges, graph_k: int):
     lib().orc_filter_active_reads(ar, p(useq), p(uoff), p(circ), p(np.ascontiguousarray(fwd)), p(np.ascontiguousarray(rev)),
                                   n, graph_k, p(keep))
     return keep[:total]
+
+
+def index_terminal_kmers(seqs: list, k: int, key_bits: int):
+    """Oracle of mapper.rs:89-136: (keys u64, unitig u32, is_rc u8, pos u32) sorted by key."""
+    n = len(seqs)
+    useq = np.frombuffer(b"".join(seqs), np.uint8).copy() if n else np.zeros(1, np.uint8)
+    uoff = np.zeros(n + 1, np.uint64)
+    if n:
+        uoff[1:] = np.cumsum([len(x) for x in seqs])
+    cap = sum(max(0, len(x) - k + 1) for x in seqs) + 1
+    keys, uni = np.zeros(cap, np.uint64), np.zeros(cap, np.uint32)
+    rc, pos = np.zeros(cap, np.uint8), np.zeros(cap, np.uint32)
+    m = lib().orc_index_terminal_kmers(key_bits, k, p(useq), p(uoff), n, p(keys), p(uni), p(rc), p(pos), cap)
+    return keys[:m], uni[:m], rc[:m], pos[:m]

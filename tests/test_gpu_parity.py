@@ -479,3 +479,20 @@ def test_filter_active_reads_matches_oracle(ctx, repeat_isolate, k, graph_k):
         assert any(len(s) >= 2000 for s in seqs) and kept < len(keep)
     sub = api.select_reads(bank, keep)
     assert sub.total_reads() == kept
+
+
+# ---------------------------------------------------------------------------
+# PE mapper terminal k-mer index (mapper.rs:89-136)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("k,kb", [(31, 64), (45, 128), (77, 256)])
+def test_terminal_kmer_index_matches_oracle(ctx, repeat_isolate, k, kb):
+    table = api.build_cdbg_ext(repeat_isolate[0], k, None, ctx=ctx, key_bits=kb, counter_bits=16, cms_log2_width=16)
+    seqs, cov, circ, edges = api.compact(table)
+    got = api.index_terminal_kmers(ctx, seqs, k, kb)
+    exp = orc.index_terminal_kmers(seqs, k, kb)
+    for a, b in zip(got, exp):
+        assert np.array_equal(a, b)
+    assert len(got[0]) > 1000
+    # a repeat k-mer shared by two unitig ends is not unique and is dropped
+    total = sum(min(len(s) - k + 1, 2000) for s in seqs if len(s) >= k)
+    assert len(got[0]) <= total
