@@ -92,6 +92,12 @@ class BatchStats(C.Structure):
                 ("upsert_grid", C.c_int32), ("tuned", C.c_int32), ("_pad", C.c_int32), ("tune_ms", C.c_double)]
 
 
+class IngestStatsC(C.Structure):
+    _fields_ = [("input_read_pairs", C.c_uint64), ("retained_read_pairs", C.c_uint64), ("bases_before_trim", C.c_uint64),
+                ("bases_after_trim", C.c_uint64), ("merged_pairs_count", C.c_uint64), ("merged_bases", C.c_uint64),
+                ("unmerged_pairs_count", C.c_uint64)]
+
+
 class ServerParams(C.Structure):
     _fields_ = [("batch", BatchParams), ("workers", C.c_uint32), ("_pad", C.c_uint32), ("budget_bytes", C.c_uint64)]
 
@@ -189,6 +195,11 @@ SIGNATURES = {
     "fbk_unitigs_release": (S, [vp]),
     "fbk_filter_active_reads": (S, [vp, vp, u8p, u64p, u8p, u32p, u32p, C.c_uint64, C.c_uint32, u8p, u64p]),
     "fbk_index_terminal_kmers": (S, [vp, u8p, u64p, C.c_uint64, C.c_uint32, C.c_uint32, u64p, u32p, u8p, u32p, C.c_uint64, u64p]),
+    "fbk_ingest_fastq_device": (S, [vp, u8p, C.c_uint64, u8p, C.c_uint64, C.c_double, C.c_uint64, C.c_uint32, C.c_int, C.c_int,
+                                    C.c_uint64, P(vp), P(IngestStatsC)]),
+    "fbk_bank_export": (S, [vp, u64p, u64p, u32p, u32p]),
+    "fbk_bank_arena_counts": (S, [vp, u64p]),
+    "fbk_bank_words": (S, [vp, u64p]),
     "fbk_subsample_policy_defaults": (None, [P(SubsamplePolicy)]),
     "fbk_subsample_decide": (S, [P(SubsamplePolicy), P(GenomeEstimate), P(C.c_double), P(C.c_int32)]),
     "fbk_batch_defaults": (None, [P(BatchParams)]),

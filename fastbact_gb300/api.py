@@ -407,6 +407,31 @@ class DeviceBank:
         self.n_bases = bank.total_bases()
         self.n_reads = bank.total_reads()
 
+    @classmethod
+    def from_handle(cls, ctx: Context, h) -> "DeviceBank":
+        """Wraps a bank made on the device (e.g. by ingest_fastq_device)."""
+        self = cls.__new__(cls)
+        self.ctx, self._h, self._views = ctx, h, None
+        ctx.adopt(self)
+        nr, nb = C.c_uint64(), C.c_uint64()
+        check(N.lib().fbk_bank_info(h, C.byref(nr), C.byref(nb)))
+        self.n_reads, self.n_bases = nr.value, nb.value
+        return self
+
+    def export(self):
+        """(words, bank-global offsets, lengths, pair indices, reads per arena)."""
+        nw = C.c_uint64()
+        check(N.lib().fbk_bank_words(self._h, C.byref(nw)))
+        words = np.zeros(max(nw.value, 1), np.uint64)
+        offs = np.zeros(max(self.n_reads, 1), np.uint64)
+        lens = np.zeros(max(self.n_reads, 1), np.uint32)
+        pidx = np.zeros(max(self.n_reads, 1), np.uint32)
+        check(N.lib().fbk_bank_export(self._h, ptr(words), ptr(offs), ptr(lens), ptr(pidx)), self.ctx.handle, "bank export")
+        counts = np.zeros(3, np.uint64)
+        check(N.lib().fbk_bank_arena_counts(self._h, ptr(counts)))
+        n = self.n_reads
+        return words[:nw.value], offs[:n], lens[:n], pidx[:n], [int(c) for c in counts]
+
     @property
     def handle(self):
         return self._h
@@ -677,6 +702,22 @@ def index_terminal_kmers(ctx: Context, seqs: list, k: int, key_bits: int | None 
     check(N.lib().fbk_index_terminal_kmers(ctx.handle, ptr(useq), ptr(uoff), n, k, key_bits, ptr(keys), ptr(uni), ptr(rc),
                                            ptr(pos), cap, C.byref(m)), ctx.handle, "index_terminal_kmers")
     return keys[:cap], uni[:cap], rc[:cap], pos[:cap]
+
+
+def ingest_fastq_device(ctx: Context, r1: str, r2: str, subsample_factor: float = 1.0, min_len: int = 30, min_qual: int = 20,
+                        enable_trim: bool = True, enable_merge: bool = True, seed: int = 0):
+    """ingest_reads_ext_with_seed (trim_merge.rs:307-417) on the device: reads the two
+    files, uploads their bytes and returns (DeviceBank, IngestStats, merged_bases)."""
+    a = np.fromfile(str(r1), dtype=np.uint8)
+    b = np.fromfile(str(r2), dtype=np.uint8)
+    h = C.c_void_p()
+    st = N.IngestStatsC()
+    check(N.lib().fbk_ingest_fastq_device(ctx.handle, ptr(a) if a.size else None, a.size, ptr(b) if b.size else None, b.size,
+                                          subsample_factor, min_len, min_qual, int(enable_trim), int(enable_merge), seed,
+                                          C.byref(h), C.byref(st)), ctx.handle, "device ingest")
+    stats = IngestStats(st.input_read_pairs, st.retained_read_pairs, st.merged_pairs_count, st.unmerged_pairs_count,
+                        st.bases_before_trim, st.bases_after_trim)
+    return DeviceBank.from_handle(ctx, h), stats, st.merged_bases
 
 
 def _bank_reads(bank):

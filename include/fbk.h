@@ -470,6 +470,24 @@ FBK_API fbk_status fbk_server_get_stats(fbk_server* s, fbk_server_stats* out);
 /* Finishes in-flight waves, fails queued requests, frees all request state. */
 FBK_API fbk_status fbk_server_destroy(fbk_server* s);
 
+/* ---- device ingest: FASTQ text to a device bank (trim_merge.rs:307-417) ------------
+ * The same reads, trimming, merging, subsampling and arena layout as fbk_ingest_fastq,
+ * computed on the device from the two files' bytes (plain 4-line FASTQ records; a '\r'
+ * before a newline is dropped; blank lines between records are refused with
+ * FBK_ERR_FORMAT — the host ingest reads those).  IngestStats: trim_merge.rs:270-290. */
+typedef struct {
+    uint64_t input_read_pairs, retained_read_pairs, bases_before_trim, bases_after_trim;
+    uint64_t merged_pairs_count, merged_bases, unmerged_pairs_count;
+} fbk_ingest_stats;
+FBK_API fbk_status fbk_ingest_fastq_device(fbk_ctx* ctx, const uint8_t* r1, uint64_t r1_len, const uint8_t* r2, uint64_t r2_len,
+                                           double subsample_factor, uint64_t min_len, uint32_t min_qual, int enable_trim,
+                                           int enable_merge, uint64_t seed, fbk_bank** out, fbk_ingest_stats* stats);
+/* A device bank back on the host: words (fbk_bank_words of them), bank-global base offsets, lengths, pair indices (n_reads each; any pointer may be NULL). */
+FBK_API fbk_status fbk_bank_export(const fbk_bank* b, uint64_t* words, uint64_t* offsets, uint32_t* lengths, uint32_t* pair_idx);
+/* Reads per arena (merged, pe_forward, pe_reverse) and words of a bank. */
+FBK_API fbk_status fbk_bank_arena_counts(const fbk_bank* b, uint64_t* counts3);
+FBK_API fbk_status fbk_bank_words(const fbk_bank* b, uint64_t* n_words);
+
 /* ---- host ingest (trim_merge.rs:17-417), CPU side ----------------------------- */
 FBK_API fbk_status fbk_ingest_fastq(const char* r1, const char* r2, double subsample_factor, uint64_t min_len, uint32_t min_qual,
                                     int enable_trim, int enable_merge, uint64_t seed, fbk_hbank** out, char* err, size_t errlen);

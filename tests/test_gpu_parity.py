@@ -496,3 +496,55 @@ def test_terminal_kmer_index_matches_oracle(ctx, repeat_isolate, k, kb):
     # a repeat k-mer shared by two unitig ends is not unique and is dropped
     total = sum(min(len(s) - k + 1, 2000) for s in seqs if len(s) >= k)
     assert len(got[0]) <= total
+
+
+# ---------------------------------------------------------------------------
+# ingest on the device (trim_merge.rs:307-417) equals the host ingest
+# ---------------------------------------------------------------------------
+def _host_bank_concat(bank):
+    """The device bank layout of a host ReadBank: words of the three arenas back to
+    back, offsets rebased by the preceding arenas' words."""
+    words, offs, lens, pidx, wbase = [], [], [], [], 0
+    for a in bank.arenas:
+        words.append(a.data)
+        offs.append(a.offsets.astype(np.uint64) + np.uint64(wbase * 32))
+        lens.append(a.lengths)
+        pidx.append(a.pair_idx)
+        wbase += len(a.data)
+    return np.concatenate(words), np.concatenate(offs), np.concatenate(lens), np.concatenate(pidx)
+
+
+@pytest.mark.parametrize("opts", [dict(), dict(subsample_factor=0.4, seed=11), dict(enable_merge=False),
+                                  dict(enable_trim=False, min_len=100), dict(min_qual=35, min_len=60)])
+def test_device_ingest_matches_host(ctx, tmp_path, opts):
+    p = api.synth_params(seed=303, genome_len=30_000, coverage=20.0, gc=0.45, sub_rate=0.01)
+    r1, r2 = tmp_path / "d_1.fq", tmp_path / "d_2.fq"
+    api.synth_write_fastq(p, r1, r2)
+    kw = dict(subsample_factor=1.0, min_len=30, min_qual=20, enable_trim=True, enable_merge=True, seed=0)
+    kw.update(opts)
+    hbank, hst = api.ingest_reads_ext_with_seed(r1, r2, kw["subsample_factor"], kw["min_len"], kw["min_qual"], kw["enable_trim"],
+                                                kw["enable_merge"], kw["seed"])
+    dbank, dst, merged_bases = api.ingest_fastq_device(ctx, r1, r2, **kw)
+    assert dst == hst
+    words, offs, lens, pidx, counts = dbank.export()
+    hw, ho, hl, hp = _host_bank_concat(hbank)
+    assert counts == [len(a) for a in hbank.arenas]
+    assert np.array_equal(lens, hl) and np.array_equal(offs, ho) and np.array_equal(pidx, hp)
+    assert np.array_equal(words, hw)
+    if kw["enable_merge"]:
+        assert len(hbank.merged_reads) > 0 and merged_bases == hbank.merged_reads.total_bases()
+    # the device bank counts like the uploaded one
+    t1 = api.build_cdbg_ext(dbank, 31, None, ctx=ctx, key_bits=64, counter_bits=16, cms_log2_width=16)
+    t2 = api.build_cdbg_ext(hbank, 31, None, ctx=ctx, key_bits=64, counter_bits=16, cms_log2_width=16)
+    assert t1.digest() == t2.digest()
+
+
+def test_device_ingest_rejects_bad_records(ctx, tmp_path):
+    r1, r2 = tmp_path / "b_1.fq", tmp_path / "b_2.fq"
+    r1.write_text("@a/1\nACGT\n+\nIIII\n@b/1\nACGT\n+\nIII\n")
+    r2.write_text("@a/2\nACGT\n+\nIIII\n@b/2\nACGT\n+\nIIII\n")
+    with pytest.raises(Exception):
+        api.ingest_fastq_device(ctx, r1, r2)
+    r1.write_text("@a/1\nACGT\n+\nIIII\n")
+    with pytest.raises(Exception):
+        api.ingest_fastq_device(ctx, r1, r2)
