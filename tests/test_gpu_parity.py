@@ -531,8 +531,9 @@ def test_device_ingest_matches_host(ctx, tmp_path, opts):
     assert counts == [len(a) for a in hbank.arenas]
     assert np.array_equal(lens, hl) and np.array_equal(offs, ho) and np.array_equal(pidx, hp)
     assert np.array_equal(words, hw)
-    if kw["enable_merge"]:
-        assert len(hbank.merged_reads) > 0 and merged_bases == hbank.merged_reads.total_bases()
+    assert merged_bases == hbank.merged_reads.total_bases()
+    if not opts:
+        assert len(hbank.merged_reads) > 0  # the default settings merge overlapping pairs
     # the device bank counts like the uploaded one
     t1 = api.build_cdbg_ext(dbank, 31, None, ctx=ctx, key_bits=64, counter_bits=16, cms_log2_width=16)
     t2 = api.build_cdbg_ext(hbank, 31, None, ctx=ctx, key_bits=64, counter_bits=16, cms_log2_width=16)
