@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
-    ap.add_argument("--mode", choices=["plain", "batch", "serve"], default="plain",
+    ap.add_argument("--mode", choices=["plain", "batch", "serve", "stress"], default="plain",
                     help="plain: one isolate per step (the headline line); batch: a cohort in multi-isolate waves; "
                          "serve: Poisson arrivals through the request loop")
     ap.add_argument("--isolates", type=int, default=64, help="cohort size (batch and serve modes)")
@@ -521,6 +521,89 @@ def run_batch_mode(args):
 
 
 # ---------------------------------------------------------------------------
+# stress mode: 12 Mbp GC 0.66 genome, repeats and a tandem array, 300x, k = 127
+# ---------------------------------------------------------------------------
+STRESS = dict(seed=46, genome_len=12_000_000, gc=0.66, n_repeats=10, repeat_len=5000, repeat_identity=0.99,
+              tandem_copies=200, tandem_unit=60, coverage=300.0, sub_rate=0.01, indel_rate=0.0005)
+
+
+def run_stress_mode(args):
+    import torch
+
+    from fastbact_gb300 import api
+    from fastbact_gb300.build import build
+
+    build()
+    torch.cuda.set_device(0)
+    wl = dict(STRESS)
+    wl["coverage"] = STRESS["coverage"] * args.scale
+    t0 = time.time()
+    bank, ist, sample, n_sample, stats = api.synth_isolate(api.synth_params(**wl), threads=0, sample_pairs=150_000)
+    gen_s = time.time() - t0
+    ctx = api.Context(0, pool_bytes=int(os.environ.get("FBK_POOL_BYTES", str(200 << 30))))
+    dbank, dsample = api.DeviceBank(ctx, bank), api.DeviceBank(ctx, sample)
+    k, kb, log2w = 127, 256, 26
+    runs = {}
+
+    def timed(name, fn, kmers):
+        ctx.sync()
+        ctx.record(0)
+        out = fn()
+        ctx.record(1)
+        ms = ctx.elapsed_ms(0, 1)
+        runs[name] = {"ms": ms, "kmers": kmers, "kmers_per_s": kmers / (ms / 1e3)}
+        return out
+
+    # estimator with HLL p = 16 over the raw sample
+    ge, _, _ = api.estimate_bank(ctx, dsample, sample.lengths, n_sample, stats, max_pairs=250_000, target_cov=110.0, hll_p=16)
+    ge, _, _ = timed("estimator_p16", lambda: api.estimate_bank(ctx, dsample, sample.lengths, n_sample, stats, max_pairs=250_000,
+                                                                target_cov=110.0, hll_p=16), 0)
+    runs["estimator_p16"]["kmers"] = ge.m_sample
+    runs["estimator_p16"]["kmers_per_s"] = ge.m_sample / (runs["estimator_p16"]["ms"] / 1e3)
+    occ = kmers_in(bank, k, k) + kmers_in(bank, k, k + 1)
+    api.build_cdbg_ext(dbank, k, None, ctx=ctx, key_bits=kb, counter_bits=16, cms_log2_width=log2w).release()  # warm-up
+    t = timed("full_input", lambda: api.build_cdbg_ext(dbank, k, None, ctx=ctx, key_bits=kb, counter_bits=16,
+                                                        cms_log2_width=log2w), occ)
+    runs["full_input"].update(dict(zip(("table_keys", "solid", "capacity"), t.info())))
+    t.release()
+    # the counted sketch, to see its saturation
+    t, cms = timed("full_input_counted_sketch", lambda: api.build_cdbg_ext(dbank, k, None, ctx=ctx, key_bits=kb, counter_bits=16,
+                                                                            cms_log2_width=log2w, keep_cms=True), occ)
+    vals = cms.export().view(np.uint16)
+    runs["full_input_counted_sketch"]["saturated_counters"] = float((vals == 65535).mean())
+    runs["full_input_counted_sketch"]["max_counter"] = int(vals.max())
+    t.release()
+    cms.release()
+    # subsampled to 110x by the pipeline driver's policy
+    f, why = api.subsample_decide(api.subsample_policy(enable_auto_subsample=True, depth=110.0, threshold_ratio=150.0 / 110.0), ge)
+    n_pairs = int(stats.exact_read_pairs)
+    keep = api.subsample_mask(ctx, n_pairs, f, 0)
+    kept = np.unpackbits(keep.view(np.uint8), bitorder="little")[:n_pairs].astype(bool)
+    sub = api.select_reads(bank, np.concatenate([kept[a.pair_idx.astype(np.int64)].astype(np.uint8) for a in bank.arenas]))
+    occ_sub = kmers_in(sub, k, k) + kmers_in(sub, k, k + 1)
+    t = timed("subsampled_110x", lambda: api.build_cdbg_ext(dbank, k, None, ctx=ctx, key_bits=kb, counter_bits=16,
+                                                             cms_log2_width=log2w, subsample=(f, 0)), occ_sub)
+    runs["subsampled_110x"].update(dict(zip(("table_keys", "solid", "capacity"), t.info())))
+    runs["subsampled_110x"]["factor"] = f
+    runs["subsampled_110x"]["policy"] = why
+    t.release()
+    line = {
+        "metric": "k-mers/s at k = 127 (stress: 12 Mbp GC 0.66, repeats + tandem array, 300x, 1% subs, 0.05% indels)",
+        "value": runs["full_input"]["kmers_per_s"], "unit": "k-mers/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64x4 integer",
+        "data": "synthetic (seeded generator; no dataset)",
+        "config": {"workload": "stress: 12 Mbp GC 0.66, 10 x 5 kb repeats, 200 x 60 bp tandem array, PE150 at "
+                               f"{wl['coverage']:.0f}x, 1% substitutions, 0.05% indels; k = 127 (256-bit keys), "
+                               "CMS 4 x 2^26 u16, estimator HLL p = 16",
+                   "bank_reads": bank.total_reads(), "bank_bases": bank.total_bases(), "generation_s": round(gen_s, 1),
+                   "genome_size_est": ge.genome_size, "estimated_cov": ge.estimated_cov},
+        "runs": runs,
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+# ---------------------------------------------------------------------------
 # serve mode: Poisson arrivals through the request loop
 # ---------------------------------------------------------------------------
 SERVE_RATES = [20.0, 50.0, 100.0, 200.0]  # requests per minute
@@ -748,6 +831,8 @@ def main():
         run_batch_mode(args)
     elif args.mode == "serve":
         run_serve_mode(args)
+    elif args.mode == "stress":
+        run_stress_mode(args)
     else:
         run_ours(args, rank, world, local)
 

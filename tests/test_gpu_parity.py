@@ -549,3 +549,16 @@ def test_device_ingest_rejects_bad_records(ctx, tmp_path):
     r1.write_text("@a/1\nACGT\n+\nIIII\n")
     with pytest.raises(Exception):
         api.ingest_fastq_device(ctx, r1, r2)
+
+
+def test_u16_sketch_saturates_like_the_reference(ctx):
+    # 2^10 columns and ~50 M k-mer occurrences: most u16 counters pass 65535 and must
+    # stop there (sketch.rs:199-221), in the exported sketch and in the gate
+    p = api.synth_params(seed=404, genome_len=400_000, coverage=120.0, gc=0.66, n_repeats=3, repeat_len=3000,
+                         tandem_copies=50, tandem_unit=60, sub_rate=0.01, indel_rate=0.0005)
+    bank = api.synth_isolate(p, threads=0, sample_pairs=0)[0]
+    table, n_solid = compare_build(ctx, bank, 31, 64, 16, None, 10)
+    cms = api.build_cdbg_ext(bank, 31, None, ctx=ctx, key_bits=64, counter_bits=16, cms_log2_width=10, keep_cms=True)[1]
+    vals = cms.export().view(np.uint16)
+    assert (vals == 65535).mean() > 0.5
+    compare_gate_only(ctx, bank, 127, 256, 16, None, 10)
