@@ -705,6 +705,13 @@ def run_serve_mode(args):
             "mean_ms": float(lat.mean()), "throughput_iso_per_h": n_req / (span / 1e3) * 3600.0,
             "mean_wave_a": (s1.isolates_a - s0.isolates_a) / max(1, s1.waves_a - s0.waves_a),
             "plain_fifo_p50_ms": float(np.percentile(pl, 50)), "plain_fifo_p99_ms": float(np.percentile(pl, 99)),
+            "stage_median_ms": {
+                "queue": float(np.median([x.t_admit_ms - x.t_submit_ms for x in infos])),
+                "upload": float(np.median([x.t_uploaded_ms - x.t_admit_ms for x in infos])),
+                "estimate": float(np.median([x.t_estimated_ms - x.t_uploaded_ms for x in infos])),
+                "pass1": float(np.median([x.t_counted_ms - x.t_estimated_ms for x in infos])),
+                "pass2": float(np.median([x.t_done_ms - x.t_counted_ms for x in infos])),
+            },
         }
     # saturation: every request at once
     s0 = srv.stats()

@@ -104,7 +104,8 @@ class ServerParams(C.Structure):
 
 class RequestInfo(C.Structure):
     _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("t_submit_ms", C.c_double), ("t_admit_ms", C.c_double),
-                ("t_done_ms", C.c_double), ("reserved_bytes", C.c_uint64), ("result", BatchResult)]
+                ("t_done_ms", C.c_double), ("t_uploaded_ms", C.c_double), ("t_estimated_ms", C.c_double),
+                ("t_counted_ms", C.c_double), ("reserved_bytes", C.c_uint64), ("result", BatchResult)]
 
 
 class ServerStats(C.Structure):

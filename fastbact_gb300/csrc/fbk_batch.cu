@@ -941,6 +941,7 @@ struct Req {
     int32_t state = 0;
     fbk_status status = FBK_OK;
     double t_submit = 0, t_admit = 0, t_done = 0;
+    double t_uploaded = 0, t_estimated = 0, t_counted = 0;
     uint64_t reserved = 0;
 };
 
@@ -1044,6 +1045,7 @@ void job_admit(fbk_server* S, int w, const std::vector<Req*>& job) {
         if (st == FBK_OK) {
             std::lock_guard<std::mutex> lk(S->mu);
             r->state = 2;  // the host buffers are no longer read
+            r->t_uploaded = srv_ms(S);
             S->cv.notify_all();
         }
         if (st == FBK_OK) {
@@ -1055,6 +1057,7 @@ void job_admit(fbk_server* S, int w, const std::vector<Req*>& job) {
                 cudaEventSynchronize(B->ev[1]);
                 cudaEventElapsedTime(&t_est, B->ev[0], B->ev[1]);
                 B->stats.ms_estimate += t_est;
+                r->t_estimated = srv_ms(S);
             }
         }
         if (st) {
@@ -1107,6 +1110,7 @@ void job_admit(fbk_server* S, int w, const std::vector<Req*>& job) {
     for (Req* r : ok) {
         BatchIso* it = r->iso.get();
         r->state = 3;
+        r->t_counted = srv_ms(S);
         reserve_set(S, r, bank_bytes(it->bank) + phase_a_bytes(B, it) + plan_b(B, it).bytes);
         S->counted.push_back(r->iso->id);
     }
@@ -1283,6 +1287,9 @@ static void request_info(const fbk_server* S, const Req* r, fbk_request_info* ou
     out->t_submit_ms = r->t_submit;
     out->t_admit_ms = r->t_admit;
     out->t_done_ms = r->t_done;
+    out->t_uploaded_ms = r->t_uploaded;
+    out->t_estimated_ms = r->t_estimated;
+    out->t_counted_ms = r->t_counted;
     out->reserved_bytes = r->state == 0 ? 0 : r->reserved;
     out->result = r->iso->res;
     (void)S;

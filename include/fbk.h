@@ -442,6 +442,7 @@ typedef struct {
     int32_t state;
     int32_t status;           /* fbk_status of a failed request */
     double t_submit_ms, t_admit_ms, t_done_ms;   /* server clock: ms since fbk_server_create */
+    double t_uploaded_ms, t_estimated_ms, t_counted_ms;  /* stage ends: reads on the device, estimate, pass 1 */
     uint64_t reserved_bytes;
     fbk_batch_result result;
 } fbk_request_info;
