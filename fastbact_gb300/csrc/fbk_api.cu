@@ -393,6 +393,7 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "record_factor" && v > 0 && v <= 16) ctx->record_factor = v;
     else if (n == "sketch_mode" && (v == 0 || v == 1)) ctx->sketch_mode = (int)v;
     else if (n == "ladder_ilp" && (v == 1 || v == 2)) ctx->ladder_ilp = (int)v;
+    else if (n == "emit_lookahead" && (v == 1 || v == 2)) ctx->emit_lookahead = (int)v;
     // the pass kernels are compiled for blocks of at most 256 threads
     else if (n == "block_pass1" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_pass1 = (int)v;
     else if (n == "grid_pass1" && v >= 0) ctx->grid_pass1 = (int)v;
@@ -413,6 +414,7 @@ FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, doub
     else if (n == "record_factor") *v = ctx->record_factor;
     else if (n == "sketch_mode") *v = ctx->sketch_mode;
     else if (n == "ladder_ilp") *v = ctx->ladder_ilp;
+    else if (n == "emit_lookahead") *v = ctx->emit_lookahead;
     else if (n == "block_pass1") *v = ctx->block_pass1;
     else if (n == "grid_pass1") *v = ctx->grid_pass1;
     else if (n == "block_pass2") *v = ctx->block_pass2;
@@ -1181,7 +1183,8 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
             const BankDev bv = bank_view(b, b->chunk_starts[c], b->chunk_starts[c + 1], keep_bits);
             CK(ctx, cudaMemsetAsync(bk.d.fill, 0, (uint64_t)bk.d.n_buckets * bk.d.stripes * 8, ctx->stream));
             if (inline_gate)
-                TIMED(ctx, "pass2_emit", launch_emit_ladder(nw, L, bv, p->k, lad->bits, lad->log2w, p->t_solid, td, bk.d));
+                TIMED(ctx, "pass2_emit", launch_emit_ladder(nw, L, bv, p->k, lad->bits, lad->log2w, p->t_solid, td, bk.d,
+                                                                     ctx->emit_lookahead));
             else
                 TIMED(ctx, "pass2_emit", launch_emit(nw, L, bv, p->k, bm, 1, td, bk.d));
             for (uint32_t bu = 0; bu < bk.d.n_buckets; ++bu)

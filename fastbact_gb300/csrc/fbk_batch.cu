@@ -546,7 +546,8 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
                 bk.overflow = w.status + 2 * i + 1;
                 TIMED(ctx, "batch_emit", launch_emit_ladder(B->nw, shape_launch(ctx, B->emit),
                                                             bank_view(it->bank, 0, it->bank->n_reads, it->keep), k, it->lad,
-                                                            B->p.cms_log2_width, B->p.t_solid, tbl_dev(it->table), bk));
+                                                            B->p.cms_log2_width, B->p.t_solid, tbl_dev(it->table), bk,
+                                                            ctx->emit_lookahead));
             }
         } else {
             TIMED(ctx, "batch_emit", launch_batch_emit(B->nw, shape_launch(ctx, B->emit), w.iso, w.rb, n, k, BATCH_STRIPES));

@@ -356,6 +356,116 @@ __global__ void __launch_bounds__(256) k_emit_ladder(BankDev b, uint32_t k, cons
     if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
 }
 
+// The same emit with the gate loads of chunk it + 2 in flight while chunk it is
+// emitted: a lane holds three keys (chunks it, it + 1, it + 2), the loads of the
+// farthest one are issued before the emit work and resolved after it.
+struct GateLoads {
+    uint32_t w[4], m[4];
+};
+__device__ __forceinline__ void gate_issue(const uint32_t* __restrict__ top, uint32_t log2w, uint64_t key, bool live, GateLoads& g) {
+    const uint64_t wmask = (1ULL << log2w) - 1;
+#pragma unroll
+    for (int row = 0; row < 4; ++row) {
+        const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(smix(key ^ cms_seed(row)) & wmask);
+        g.m[row] = 1u << (bit & 31);
+        g.w[row] = live ? __ldg(top + (bit >> 5)) : 0u;
+    }
+}
+__device__ __forceinline__ bool gate_resolve(const GateLoads& g, bool live) {
+    bool ok = live;
+#pragma unroll
+    for (int row = 0; row < 4; ++row) ok &= (g.w[row] & g.m[row]) != 0;
+    return ok;
+}
+
+template <int NW>
+__global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, const uint32_t* __restrict__ lad, uint32_t log2w,
+                                                         uint32_t t_solid, TableDev t, BucketDev bk) {
+    extern __shared__ uint64_t emit_smem[];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint64_t* buf = emit_smem + (uint64_t)wib * EMIT_WARP_WORDS(NW);
+    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + EMIT_BUF * (NW + 1));
+    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + EMIT_BUF);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + EMIT_BUF);
+    unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
+    const uint32_t* top = lad + (uint64_t)(t_solid - 1) * ((4ULL << log2w) >> 5);
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t stripe = (uint32_t)(gw % bk.stripes);
+    uint32_t n_buf = 0;  // warp-uniform
+    for (uint64_t r = b.r_begin + gw; r < b.r_end; r += nwarps) {
+        const uint32_t len = b.len[r];
+        if (len < k + 1 || !bank_keep(b, r)) continue;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        const uint32_t n_it = (nk + 31) >> 5;
+        // chunks 0 and 1 resolved up front
+        Key<NW> k0, k1;
+        bool rc0 = false, rc1 = false;
+        const bool l0 = lane < nk, l1 = 32 + lane < nk;
+        if (l0) window_canonical<NW>(b.data, off + lane, k, k0, rc0);
+        if (l1) window_canonical<NW>(b.data, off + 32 + lane, k, k1, rc1);
+        GateLoads g0, g1;
+        gate_issue(top, log2w, l0 ? key_fold<NW>(k0) : 0, l0, g0);
+        gate_issue(top, log2w, l1 ? key_fold<NW>(k1) : 0, l1, g1);
+        uint32_t mprev = 0, mcur = __ballot_sync(0xffffffffu, gate_resolve(g0, l0));
+        uint32_t mnext = __ballot_sync(0xffffffffu, gate_resolve(g1, l1));
+        Key<NW> kc = k0, kn = k1;
+        bool rcc = rc0, rcn = rc1;
+        for (uint32_t it = 0; it < n_it; ++it) {
+            // issue chunk it + 2
+            Key<NW> kf;
+            bool rcf = false;
+            const uint32_t qf = ((it + 2) << 5) + lane;
+            const bool lf = qf < nk;
+            if (lf) window_canonical<NW>(b.data, off + qf, k, kf, rcf);
+            GateLoads gf;
+            gate_issue(top, log2w, lf ? key_fold<NW>(kf) : 0, lf, gf);
+            // emit chunk it
+            const uint32_t q = (it << 5) + lane;
+            bool emit = false;
+            uint32_t info = 0, bucket = 0;
+            if (q < nk) {
+                const bool sq = (mcur >> lane) & 1u;
+                const bool sl = q > 0 && (lane ? ((mcur >> (lane - 1)) & 1u) : (mprev >> 31));
+                const bool sr = q + 1 < nk && (lane < 31 ? ((mcur >> (lane + 1)) & 1u) : (mnext & 1u));
+                emit = sq && (sl || sr);
+                if (emit) {
+                    const uint64_t g = off + q;
+                    if (sr) info |= 8u | (base_at(b.data, g + k) + (rcc ? 4u : 0u));
+                    if (sl) info |= (8u | ((3u - base_at(b.data, g - 1)) + (rcc ? 0u : 4u))) << 4;
+                    bucket = (uint32_t)(home_slot(key_fold<NW>(kc), t.cap) >> bk.shift);
+                }
+            }
+            const uint32_t active = __ballot_sync(0xffffffffu, emit);
+            if (emit) {
+                const uint32_t pos = n_buf + __popc(active & ((1u << lane) - 1));
+#pragma unroll
+                for (int i = 0; i < NW; ++i) buf[pos * (NW + 1) + i] = kc.w[i];
+                buf[pos * (NW + 1) + NW] = info;
+                bbuf[pos] = (uint8_t)bucket;
+            }
+            n_buf += __popc(active);
+            if (n_buf > EMIT_BUF - 32) {
+                __syncwarp();
+                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+                n_buf = 0;
+            }
+            // resolve chunk it + 2 and rotate
+            const uint32_t mfar = __ballot_sync(0xffffffffu, gate_resolve(gf, lf));
+            mprev = mcur;
+            mcur = mnext;
+            mnext = mfar;
+            kc = kn;
+            rcc = rcn;
+            kn = kf;
+            rcn = rcf;
+        }
+    }
+    __syncwarp();
+    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+}
+
 // Upsert of one bucket's records: every thread resolves its record's key from its
 // home slot and adds the pushes.  (Taking two records per thread and issuing both
 // home-slot loads first measured 18% slower: register pressure cost more occupancy
@@ -625,30 +735,35 @@ static cudaError_t emit_nw(const Launch& L, const BankDev& b, uint32_t k, const 
     k_emit<NW><<<grid, L.block, smem, L.stream>>>(b, k, bm, gate, t, bk);
     return cudaGetLastError();
 }
-template <int NW>
-static cudaError_t emitl_nw(const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w, uint32_t ts,
-                            const TableDev& t, const BucketDev& bk) {
-    const size_t smem = (size_t)(L.block / 32) * EMIT_WARP_WORDS(NW) * 8;
+template <class Kern>
+static cudaError_t emit_launch(Kern kern, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
+                               uint32_t ts, const TableDev& t, const BucketDev& bk, size_t smem) {
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_emit_ladder<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     int grid = L.grid;
     if (grid <= 0) {
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_ladder<NW>, L.block, smem) != cudaSuccess || per_sm < 1)
-            per_sm = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, L.block, smem) != cudaSuccess || per_sm < 1) per_sm = 1;
         grid = per_sm * (L.sms > 0 ? L.sms : 1);
     }
-    k_emit_ladder<NW><<<grid, L.block, smem, L.stream>>>(b, k, lad, log2w, ts, t, bk);
+    kern<<<grid, L.block, smem, L.stream>>>(b, k, lad, log2w, ts, t, bk);
     return cudaGetLastError();
 }
+template <int NW>
+static cudaError_t emitl_nw(const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w, uint32_t ts,
+                            const TableDev& t, const BucketDev& bk, int lookahead) {
+    const size_t smem = (size_t)(L.block / 32) * EMIT_WARP_WORDS(NW) * 8;
+    if (lookahead == 2) return emit_launch(k_emit_ladder2<NW>, L, b, k, lad, log2w, ts, t, bk, smem);
+    return emit_launch(k_emit_ladder<NW>, L, b, k, lad, log2w, ts, t, bk, smem);
+}
 cudaError_t launch_emit_ladder(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
-                               uint32_t t_solid, const TableDev& t, const BucketDev& bk) {
-    if (t_solid < 1 || t_solid > LADDER_MAX_LEVELS) return cudaErrorInvalidValue;
-    if (nw == 1) return emitl_nw<1>(L, b, k, lad, log2w, t_solid, t, bk);
-    if (nw == 2) return emitl_nw<2>(L, b, k, lad, log2w, t_solid, t, bk);
-    return emitl_nw<4>(L, b, k, lad, log2w, t_solid, t, bk);
+                               uint32_t t_solid, const TableDev& t, const BucketDev& bk, int lookahead) {
+    if (t_solid < 1 || t_solid > LADDER_MAX_LEVELS || log2w > 29) return cudaErrorInvalidValue;
+    if (nw == 1) return emitl_nw<1>(L, b, k, lad, log2w, t_solid, t, bk, lookahead);
+    if (nw == 2) return emitl_nw<2>(L, b, k, lad, log2w, t_solid, t, bk, lookahead);
+    return emitl_nw<4>(L, b, k, lad, log2w, t_solid, t, bk, lookahead);
 }
 
 cudaError_t launch_emit(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* bm, int gate, const TableDev& t,

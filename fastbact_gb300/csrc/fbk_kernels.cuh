@@ -130,8 +130,10 @@ cudaError_t launch_ladder_pass1(int nw, const Launch& L, const BankDev& b, uint3
 cudaError_t launch_ladder_solid(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
                                 uint32_t t, uint32_t* bm);
 // Record emit of pass 2 with the ladder gate evaluated inline (no solidity bitmap).
+// lookahead 1: the gate of the next chunk is resolved before each chunk is emitted;
+// 2: the loads of the chunk after it are in flight while a chunk is emitted.
 cudaError_t launch_emit_ladder(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
-                               uint32_t t_solid, const TableDev& t, const BucketDev& bk);
+                               uint32_t t_solid, const TableDev& t, const BucketDev& bk, int lookahead);
 
 // ---- multi-isolate waves (fbk_k_batch.cu) ----------------------------------------
 // read_base: n_iso + 1 global read indices (isolate i owns [read_base[i], read_base[i+1])).
