@@ -553,9 +553,9 @@ def test_device_ingest_rejects_bad_records(ctx, tmp_path):
 
 
 def test_u16_sketch_saturates_like_the_reference(ctx):
-    # 2^10 columns and ~50 M k-mer occurrences: most u16 counters pass 65535 and must
+    # 2^10 columns and ~80 M k-mer occurrences: most u16 counters pass 65535 and must
     # stop there (sketch.rs:199-221), in the exported sketch and in the gate
-    p = api.synth_params(seed=404, genome_len=400_000, coverage=120.0, gc=0.66, n_repeats=3, repeat_len=3000,
+    p = api.synth_params(seed=404, genome_len=400_000, coverage=220.0, gc=0.66, n_repeats=3, repeat_len=3000,
                          tandem_copies=50, tandem_unit=60, sub_rate=0.01, indel_rate=0.0005)
     bank = api.synth_isolate(p, threads=0, sample_pairs=0)[0]
     table, n_solid = compare_build(ctx, bank, 31, 64, 16, None, 10)
