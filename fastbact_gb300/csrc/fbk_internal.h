@@ -72,7 +72,7 @@ struct fbk_ctx {
     double record_factor = 1.25;          // bucket capacity / expected records per stripe
     int sketch_mode = 1;                  // 1: a build that does not return its sketch keeps only the gate ladder
     int ladder_ilp = 1;                   // windows per lane per step in the ladder pass 1 (1 or 2)
-    int emit_lookahead = 1;               // chunks of gate loads ahead of the record emit (1 or 2)
+    int emit_lookahead = 2;               // chunks of gate loads ahead of the record emit (1 or 2)
     bool capturing = false;               // launches are being captured into a CUDA graph
 };
 
