@@ -183,6 +183,10 @@ SIGNATURES = {
     "fbk_estimator_defaults": (None, [P(EstimatorParams)]),
     "fbk_estimate_sample": (S, [vp, P(ArenaView), C.c_uint64, P(CountStats), P(EstimatorParams), P(GenomeEstimate), u8p, u8p]),
     "fbk_estimate_bank": (S, [vp, vp, u32p, C.c_uint64, P(CountStats), P(EstimatorParams), P(GenomeEstimate), u8p, u8p]),
+    "fbk_est_shard_plan": (S, [u32p, C.c_uint64, P(CountStats), P(EstimatorParams), u64p, u32p]),
+    "fbk_est_shard_firstpos": (S, [vp, vp, u32p, C.c_uint64, C.c_uint64, C.c_uint64, P(EstimatorParams), u32p]),
+    "fbk_est_shard_segments": (S, [vp, vp, u32p, C.c_uint64, C.c_uint64, C.c_uint64, P(EstimatorParams), u32p, u8p]),
+    "fbk_est_shard_finish": (S, [u32p, C.c_uint64, P(CountStats), P(EstimatorParams), u8p, P(GenomeEstimate), u8p, u8p]),
     "fbk_estimate_sample_noalloc": (S, [C.c_int, vp, P(ArenaView), C.c_uint64, P(CountStats), P(EstimatorParams),
                                         P(GenomeEstimate), u8p, u8p, C.c_char_p, C.c_size_t]),
     "fbk_count_fastx_exact": (S, [C.c_char_p, C.c_char_p, P(CountStats), C.c_char_p, C.c_size_t]),

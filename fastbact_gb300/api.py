@@ -390,6 +390,59 @@ def estimate_bank(ctx: Context, sample_bank: "DeviceBank", lengths: np.ndarray, 
     return GenomeEstimate.from_c(e), rt, rs
 
 
+def est_shard_plan(lengths: np.ndarray, n_pairs: int, stats: ExactCountStats, **params) -> tuple[int, int]:
+    """(n_use, n_segs) of the sharded estimator: the pairs the sample loop can read and
+    its checkpoint segments (host only)."""
+    p = estimator_params(**params)
+    lengths = np.ascontiguousarray(lengths, np.uint32)
+    cs = stats.to_c()
+    n_use, n_segs = C.c_uint64(), C.c_uint32()
+    check(N.lib().fbk_est_shard_plan(ptr(lengths), n_pairs, C.byref(cs), C.byref(p), C.byref(n_use), C.byref(n_segs)),
+          None, "est_shard_plan")
+    return n_use.value, n_segs.value
+
+
+def est_shard_firstpos(ctx: Context, sample_bank: "DeviceBank", lengths: np.ndarray, n_use: int, pair_begin: int,
+                       pair_end: int, **params) -> np.ndarray:
+    """Stage 1 of the sharded estimator on this rank's pairs: the first occurrence
+    index touching each sketch counter (uint32[4 << cms_log2_width])."""
+    p = estimator_params(**params)
+    lengths = np.ascontiguousarray(lengths, np.uint32)
+    first = np.zeros(4 << p.cms_log2_width, np.uint32)
+    check(N.lib().fbk_est_shard_firstpos(ctx.handle, sample_bank.handle, ptr(lengths), n_use, pair_begin, pair_end,
+                                         C.byref(p), ptr(first)), ctx.handle, "est_shard_firstpos")
+    return first
+
+
+def est_shard_segments(ctx: Context, sample_bank: "DeviceBank", lengths: np.ndarray, n_use: int, pair_begin: int,
+                       pair_end: int, first: np.ndarray, **params) -> np.ndarray:
+    """Stage 2 on this rank's pairs with the merged first-touch array: HLL register
+    maxima per checkpoint segment, uint8[2 * n_segs << hll_p] (total, then solid)."""
+    p = estimator_params(**params)
+    lengths = np.ascontiguousarray(lengths, np.uint32)
+    n_segs = 1 if n_use <= 6000 else 1 + (n_use - 6000 + 1999) // 2000
+    regs = np.zeros(2 * n_segs << p.hll_p, np.uint8)
+    first = np.ascontiguousarray(first, np.uint32)
+    check(N.lib().fbk_est_shard_segments(ctx.handle, sample_bank.handle, ptr(lengths), n_use, pair_begin, pair_end,
+                                         C.byref(p), ptr(first), ptr(regs)), ctx.handle, "est_shard_segments")
+    return regs
+
+
+def est_shard_finish(lengths: np.ndarray, n_use: int, stats: ExactCountStats, regs: np.ndarray, **params):
+    """Checkpoints and post-math from the merged segment registers (host only).
+    Returns (GenomeEstimate, regs_total, regs_solid)."""
+    p = estimator_params(**params)
+    lengths = np.ascontiguousarray(lengths, np.uint32)
+    regs = np.ascontiguousarray(regs, np.uint8)
+    m = 1 << p.hll_p
+    rt, rs = np.zeros(m, np.uint8), np.zeros(m, np.uint8)
+    cs = stats.to_c()
+    e = N.GenomeEstimate()
+    check(N.lib().fbk_est_shard_finish(ptr(lengths), n_use, C.byref(cs), C.byref(p), ptr(regs), C.byref(e), ptr(rt),
+                                       ptr(rs)), None, "est_shard_finish")
+    return GenomeEstimate.from_c(e), rt, rs
+
+
 # ---------------------------------------------------------------------------
 # device objects
 # ---------------------------------------------------------------------------

@@ -17,6 +17,12 @@ every read (src/graph/build.rs:84-328):
 * the table digest is a sum over rows, so the owners' digests add up (mod 2^64)
   to the single-process digest.
 
+The genome-size estimator's sample loop (estimator.rs:296-379) shards by pair range
+with two exchanges (sharded_estimate): the first occurrence touching each sketch
+counter (all-reduce MIN; occurrence t's estimate is >= 2 iff every row's counter was
+touched before t), then the HLL register maxima per checkpoint segment (all-reduce
+MAX); the checkpoints and the post-math run on the merged registers.
+
 The engine is what counts one rank's reads: DeviceEngine runs this library's
 kernels; any object with the same three methods (pass1, load, pass2) can stand
 in, which is how the exchange logic is tested on hosts without a GPU.
@@ -172,6 +178,56 @@ def sharded_build(engine, bank, k: int, key_bits: int, log2w: int, counter_bits:
     t = torch.tensor([d - (1 << 64) if d >= (1 << 63) else d], dtype=torch.int64)
     dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)  # wraps: the sum mod 2^64
     return (nkeys, ncov, nmask), merged, int(t.item()) & ((1 << 64) - 1)
+
+
+def pair_range(n_use: int, rank: int, world: int) -> tuple[int, int]:
+    """The contiguous pairs of the estimator sample that rank `rank` of `world` runs."""
+    return n_use * rank // world, n_use * (rank + 1) // world
+
+
+def sharded_estimate(engine, lengths: np.ndarray, n_pairs: int, stats, rank: int, world: int, group=None, **params):
+    """estimate_genome's sample loop over this rank's pairs and the two exchange steps.
+    Every rank holds the whole sample (R1,R2 interleaved; `lengths` are its read
+    lengths) and gets the same (GenomeEstimate, regs_total, regs_solid) as one process
+    running every pair.  `engine` runs the two stages on the rank's pairs:
+    firstpos(n_use, pair_begin, pair_end) and segments(n_use, pair_begin, pair_end, first)."""
+    import torch
+    import torch.distributed as dist
+
+    from . import api
+
+    n_use, _ = api.est_shard_plan(lengths, n_pairs, stats, **params)
+    lo, hi = pair_range(n_use, rank, world)
+    first = torch.from_numpy(engine.firstpos(n_use, lo, hi).astype(np.int64))
+    dist.all_reduce(first, op=dist.ReduceOp.MIN, group=group)
+    merged_first = first.numpy().astype(np.uint32)
+    regs = torch.from_numpy(engine.segments(n_use, lo, hi, merged_first).astype(np.int32))
+    dist.all_reduce(regs, op=dist.ReduceOp.MAX, group=group)
+    return api.est_shard_finish(lengths, n_use, stats, regs.numpy().astype(np.uint8), **params)
+
+
+class DeviceEstimatorEngine:
+    """Runs a rank's estimator stages on its GPU; the sample is uploaded once."""
+
+    def __init__(self, ctx, sample, lengths: np.ndarray, **params):
+        from . import api
+
+        self.ctx, self.params = ctx, params
+        self.lengths = np.ascontiguousarray(lengths, np.uint32)
+        self.bank = api.DeviceBank(ctx, sample)
+
+    def firstpos(self, n_use, lo, hi):
+        from . import api
+
+        return api.est_shard_firstpos(self.ctx, self.bank, self.lengths, n_use, lo, hi, **self.params)
+
+    def segments(self, n_use, lo, hi, first):
+        from . import api
+
+        return api.est_shard_segments(self.ctx, self.bank, self.lengths, n_use, lo, hi, first, **self.params)
+
+    def release(self):
+        self.bank.release()
 
 
 class DeviceEngine:

@@ -282,6 +282,34 @@ FBK_API fbk_status fbk_estimate_genome(fbk_ctx* ctx, const char* r1, const char*
                                        fbk_genome_estimate* out);
 FBK_API int fbk_compute_dynamic_kmers(uint64_t median_len, int64_t target_max_k, uint64_t* out, int cap); /* estimator.rs:104-161 */
 
+/* Sharded estimator: the sample loop of estimate_genome (estimator.rs:296-379) split
+ * over ranks, one process per GPU, with the single-process result bit for bit.
+ * Occurrence t (pairs in order, R1 then R2, windows in order) makes the estimate >= 2
+ * exactly when every row's counter was touched by some t' < t, so:
+ *   1. each rank runs fbk_est_shard_firstpos on its pair range [pair_begin, pair_end)
+ *      (global occurrence indices) -> first[4 << cms_log2_width], the smallest t that
+ *      touched each counter (0xFFFFFFFF if none); the caller all-reduces with MIN;
+ *   2. each rank runs fbk_est_shard_segments with the merged array -> its HLL register
+ *      maxima per checkpoint segment, regs[2][n_segs][1 << hll_p] (total, then solid;
+ *      segment 0 = pairs 1..6000, segment j = pairs 6000+2000(j-1)+1 .. 6000+2000j);
+ *      the caller all-reduces with MAX;
+ *   3. fbk_est_shard_finish (host only, no device) takes the merged registers, walks the
+ *      checkpoints (early stop at lambda >= 15) and runs the post-math.
+ * Every rank holds the whole sample (reads 0 .. 2*n_use-1 of `sample`, R1,R2
+ * interleaved) and its read lengths; fbk_est_shard_plan gives n_use (the pairs the
+ * sample loop can read) and n_segs. */
+FBK_API fbk_status fbk_est_shard_plan(const uint32_t* read_lengths, uint64_t n_pairs, const fbk_count_stats* stats,
+                                      const fbk_estimator_params* p, uint64_t* n_use, uint32_t* n_segs);
+FBK_API fbk_status fbk_est_shard_firstpos(fbk_ctx* ctx, const fbk_bank* sample, const uint32_t* read_lengths, uint64_t n_use,
+                                          uint64_t pair_begin, uint64_t pair_end, const fbk_estimator_params* p,
+                                          uint32_t* first);
+FBK_API fbk_status fbk_est_shard_segments(fbk_ctx* ctx, const fbk_bank* sample, const uint32_t* read_lengths, uint64_t n_use,
+                                          uint64_t pair_begin, uint64_t pair_end, const fbk_estimator_params* p,
+                                          const uint32_t* first, uint8_t* regs);
+FBK_API fbk_status fbk_est_shard_finish(const uint32_t* read_lengths, uint64_t n_use, const fbk_count_stats* stats,
+                                        const fbk_estimator_params* p, const uint8_t* regs, fbk_genome_estimate* out,
+                                        uint8_t* regs_total, uint8_t* regs_solid);
+
 /* ---- subsampler (trim_merge.rs:324-348) -------------------------------------- */
 /* Bit i of keep_bits (host, ceil(n_pairs/64) words) = input pair i (0-based) kept. */
 FBK_API fbk_status fbk_subsample_mask(fbk_ctx* ctx, uint64_t n_pairs, const fbk_subsample* ss, uint64_t* keep_bits);

@@ -1168,6 +1168,68 @@ ORC_API int orc_estimate_from_reads(const uint8_t* reads, const uint64_t* read_o
     return 0;
 }
 
+// The estimator sample loop split by pair range, for the sharded-estimator tests: a
+// rank's part of the first-touch form of estimator.rs:338-363 (the estimate after the
+// add at occurrence t is >= 2 iff every row's counter was touched before t).  Reads are
+// as in orc_estimate_from_reads over the first n_use pairs; t counts the k-mers of all
+// pairs before pair_begin.  orc_est_firstpos fills first[4*cms_width] with the smallest
+// t of [pair_begin, pair_end) touching each counter (0xFFFFFFFF if none);
+// orc_est_segments writes, from a merged first array, the HLL register maxima of the
+// range per checkpoint segment (segment 0 = pairs 1..6000, segment j = pairs
+// 6000+2000(j-1)+1 .. 6000+2000j), regs[2][n_segs][1 << hll_p]: total, then solid.
+template <class F>
+static void est_walk(const uint8_t* reads, const uint64_t* read_offs, uint64_t pair_begin, uint64_t pair_end, unsigned k,
+                     F&& f) {
+    uint64_t t = 0;
+    for (uint64_t r = 0; r < 2 * pair_begin; ++r) {
+        const uint64_t len = read_offs[r + 1] - read_offs[r];
+        if (len >= k) t += len - k + 1;
+    }
+    for (uint64_t p = pair_begin; p < pair_end; ++p)
+        for (int mate = 0; mate < 2; ++mate) {
+            const uint8_t* s = reads + read_offs[2 * p + mate];
+            const uint64_t len = read_offs[2 * p + mate + 1] - read_offs[2 * p + mate];
+            if (len < k) continue;
+            RollingNtHash rh(s, k);
+            f(p, t++, rh.canonical());
+            for (uint64_t i = k; i < len; ++i) f(p, t++, rh.roll(s[i - k], s[i]));
+        }
+}
+
+ORC_API void orc_est_firstpos(const uint8_t* reads, const uint64_t* read_offs, uint64_t pair_begin, uint64_t pair_end,
+                              unsigned k, uint64_t cms_width, uint32_t* first) {
+    std::fill(first, first + 4 * cms_width, 0xFFFFFFFFu);
+    est_walk(reads, read_offs, pair_begin, pair_end, k, [&](uint64_t, uint64_t t, uint64_t raw) {
+        for (int r = 0; r < 4; ++r) {
+            uint32_t& f = first[(uint64_t)r * cms_width + (splitmix64(raw ^ CMS_SEEDS[r]) & (cms_width - 1))];
+            if (t < f) f = (uint32_t)t;
+        }
+    });
+}
+
+ORC_API void orc_est_segments(const uint8_t* reads, const uint64_t* read_offs, uint64_t n_use, uint64_t pair_begin,
+                              uint64_t pair_end, unsigned k, uint64_t cms_width, unsigned hll_p, const uint32_t* first,
+                              uint8_t* regs) {
+    const uint32_t n_segs = n_use <= 6000 ? 1u : (uint32_t)(1 + (n_use - 6000 + 1999) / 2000);
+    const uint64_t m = 1ULL << hll_p;
+    std::fill(regs, regs + 2 * n_segs * m, 0);
+    est_walk(reads, read_offs, pair_begin, pair_end, k, [&](uint64_t p, uint64_t t, uint64_t raw) {
+        const uint64_t pc = p + 1;
+        uint32_t seg = pc <= 6000 ? 0u : (uint32_t)(1 + (pc - 6001) / 2000);
+        if (seg >= n_segs) seg = n_segs - 1;
+        bool solid = true;
+        for (int r = 0; r < 4; ++r)
+            solid = solid && first[(uint64_t)r * cms_width + (splitmix64(raw ^ CMS_SEEDS[r]) & (cms_width - 1))] < t;
+        const uint64_t h = splitmix64(raw);
+        const uint64_t idx = h >> (64 - hll_p), w = h & ((1ULL << (64 - hll_p)) - 1);
+        const uint8_t rho = w == 0 ? (uint8_t)(64 - hll_p + 1) : (uint8_t)(__builtin_clzll(w) - hll_p + 1);
+        uint8_t* tot = regs + (uint64_t)seg * m;
+        uint8_t* sol = regs + ((uint64_t)n_segs + seg) * m;
+        if (rho > tot[idx]) tot[idx] = rho;
+        if (solid && rho > sol[idx]) sol[idx] = rho;
+    });
+}
+
 // count_fastx_exact — estimator.rs:167-283.  Returns 0, or -1 with the reference's
 // error message text in err.
 ORC_API int orc_count_fastx_exact(const char* r1, const char* r2, orc_count_stats* out, char* err, int errlen) {

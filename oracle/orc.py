@@ -91,6 +91,8 @@ _SIG = {
     "orc_subsample_keep": (C.c_int, [C.c_uint64, C.c_double, C.c_uint64]),
     "orc_estimate_from_reads": (C.c_int, [u8p, u64p, C.c_uint64, C.POINTER(OrcCountStats), C.c_uint64, C.c_double, C.c_uint,
                                           C.c_uint64, C.c_uint, C.POINTER(OrcEstimate), u8p, u8p]),
+    "orc_est_firstpos": (None, [u8p, u64p, C.c_uint64, C.c_uint64, C.c_uint, C.c_uint64, u32p]),
+    "orc_est_segments": (None, [u8p, u64p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint, C.c_uint64, C.c_uint, u32p, u8p]),
     "orc_count_fastx_exact": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(OrcCountStats), C.c_char_p, C.c_int]),
     "orc_estimate_genome": (C.c_int, [C.c_char_p, C.c_char_p, C.c_uint64, C.c_double, C.POINTER(OrcEstimate), u8p, u8p,
                                       C.c_char_p, C.c_int]),
@@ -273,6 +275,33 @@ def estimate_from_reads(seqs_r1r2: list[bytes], stats: OrcCountStats, max_pairs:
     rc = lib().orc_estimate_from_reads(p(buf), p(offs), len(seqs_r1r2) // 2, C.byref(stats), max_pairs, target_cov, k,
                                        cms_width, hll_p, C.byref(e), p(rt), p(rs))
     return rc, e, rt, rs
+
+
+def _reads_buf(seqs_r1r2: list[bytes]):
+    buf = np.frombuffer(b"".join(seqs_r1r2), np.uint8).copy() if seqs_r1r2 else np.zeros(1, np.uint8)
+    offs = np.zeros(len(seqs_r1r2) + 1, np.uint64)
+    if seqs_r1r2:
+        offs[1:] = np.cumsum([len(s) for s in seqs_r1r2])
+    return buf, offs
+
+
+def est_firstpos(seqs_r1r2: list[bytes], pair_begin: int, pair_end: int, k: int, cms_width: int) -> np.ndarray:
+    """A rank's first-touch array of the sharded estimator (pairs [pair_begin, pair_end))."""
+    buf, offs = _reads_buf(seqs_r1r2)
+    first = np.zeros(4 * cms_width, np.uint32)
+    lib().orc_est_firstpos(p(buf), p(offs), pair_begin, pair_end, k, cms_width, p(first))
+    return first
+
+
+def est_segments(seqs_r1r2: list[bytes], n_use: int, pair_begin: int, pair_end: int, k: int, cms_width: int, hll_p: int,
+                 first: np.ndarray) -> np.ndarray:
+    """A rank's per-segment HLL register maxima of the sharded estimator."""
+    buf, offs = _reads_buf(seqs_r1r2)
+    n_segs = 1 if n_use <= 6000 else 1 + (n_use - 6000 + 1999) // 2000
+    regs = np.zeros(2 * n_segs << hll_p, np.uint8)
+    first = np.ascontiguousarray(first, np.uint32)
+    lib().orc_est_segments(p(buf), p(offs), n_use, pair_begin, pair_end, k, cms_width, hll_p, p(first), p(regs))
+    return regs
 
 
 def count_stats(**kw) -> OrcCountStats:

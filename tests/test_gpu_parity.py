@@ -353,6 +353,35 @@ def test_estimator_reads_with_n_and_short(ctx):
     assert (ge.genome_size, ge.u_ge_2, ge.pairs_sampled) == (oe.genome_size, oe.u_ge_2, oe.pairs_sampled)
 
 
+@pytest.mark.parametrize("world,max_pairs,hll_p", [(1, 250000, 14), (3, 250000, 14), (4, 9000, 16), (2, 5000, 14)])
+def test_sharded_estimator_stages_on_device(ctx, repeat_isolate, world, max_pairs, hll_p):
+    """The device stages of the sharded estimator, run per pair range and merged (MIN,
+    then MAX) as the ranks' all-reduces would, give the one-process device estimate
+    and the oracle's sequential sample loop."""
+    from fastbact_gb300 import shard
+
+    bank, st, sample, n_sample, cs = repeat_isolate
+    params = dict(max_pairs=max_pairs, hll_p=hll_p, target_cov=110.0)
+    lengths = np.ascontiguousarray(sample.lengths[:2 * n_sample])
+    eng = shard.DeviceEstimatorEngine(ctx, sample, lengths, **params)
+    try:
+        n_use, n_segs = api.est_shard_plan(lengths, n_sample, cs, **params)
+        ranges = [shard.pair_range(n_use, r, world) for r in range(world)]
+        first = np.minimum.reduce([eng.firstpos(n_use, lo, hi) for lo, hi in ranges])
+        regs = np.maximum.reduce([eng.segments(n_use, lo, hi, first) for lo, hi in ranges])
+        ge, rt, rs = api.est_shard_finish(lengths, n_use, cs, regs, **params)
+        one, ort1, ors1 = api.estimate_bank(ctx, eng.bank, lengths, n_sample, cs, want_registers=True, **params)
+    finally:
+        eng.release()
+    assert ge == one
+    assert np.array_equal(rt, ort1) and np.array_equal(rs, ors1)
+    rc, oe, ort, ors = orc.estimate_from_reads(sample_reads(sample, n_sample), orc.count_stats(**cs.__dict__), max_pairs,
+                                               110.0, hll_p=hll_p)
+    assert (ge.genome_size, ge.u_ge_1, ge.u_ge_2, ge.pairs_sampled, ge.m_sample) == \
+        (oe.genome_size, oe.u_ge_1, oe.u_ge_2, oe.pairs_sampled, oe.m_sample)
+    assert np.array_equal(rt, ort) and np.array_equal(rs, ors)
+
+
 # ---------------------------------------------------------------------------
 # launch / sizing variants must not change any result
 # ---------------------------------------------------------------------------
