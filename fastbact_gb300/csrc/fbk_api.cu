@@ -296,6 +296,10 @@ FBK_API fbk_status fbk_ctx_fork(fbk_ctx* parent, fbk_ctx** out) {
     c->grid_pass1 = parent->grid_pass1;
     c->block_pass2 = parent->block_pass2;
     c->grid_pass2 = parent->grid_pass2;
+    c->block_misc = parent->block_misc;
+    c->sketch_mode = parent->sketch_mode;
+    c->ladder_ilp = parent->ladder_ilp;
+    c->emit_lookahead = parent->emit_lookahead;
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_status, 64);
