@@ -157,7 +157,7 @@ def pinned_copy(a: np.ndarray) -> np.ndarray:
 
     t = torch.empty(max(a.nbytes, 8), dtype=torch.uint8, pin_memory=True)
     _PINNED.append(t)
-    out = t.numpy().view(a.dtype)[: a.size]
+    out = t.numpy().view(a.dtype)[: a.size].reshape(a.shape)
     out[...] = a
     return out
 
@@ -199,7 +199,7 @@ def run_ours(args, rank, world, local):
     ctx.sync()
     cb = args.counter_bits
 
-    def step(ctx, dbank, dsample, sample_lengths, export=False):
+    def step(ctx, dbank, dsample, sample_lengths, export=False, outs=None):
         ge, _, _ = api.estimate_bank(ctx, dsample, sample_lengths, n_sample, stats, max_pairs=250_000, target_cov=110.0)
         res = []
         for k in KS:
@@ -207,7 +207,7 @@ def run_ours(args, rank, world, local):
             info = t.info()
             res.append((k, info[0], info[1], t.pushes()))
             if export:
-                t.export()
+                t.export(out=outs.get(k) if outs else None)
             t.release()
         return ge, res
 
@@ -292,14 +292,23 @@ def run_ours(args, rank, world, local):
         h2d = sum(a.data.nbytes + a.offsets.nbytes + a.lengths.nbytes + (a.pair_idx.nbytes if a.pair_idx is not None else 0)
                   for a in pb.arenas) + ps.data.nbytes + ps.offsets.nbytes + ps.lengths.nbytes
 
+        # the solid rows land in pinned host buffers that a caller keeps from step to
+        # step (sized from the warm-up step; a larger table gets fresh arrays)
+        outs = {}
+
         def e2e_step():
             db = api.DeviceBank(ctx, pb)
             ds = api.DeviceBank(ctx, ps)
-            ge2, res2 = step(ctx, db, ds, ps.lengths, export=True)
+            ge2, res2 = step(ctx, db, ds, ps.lengths, export=True, outs=outs)
             db.release()
             ds.release()
             return ge2, res2
 
+        _, res0 = e2e_step()
+        for (k, _, n_solid, _) in res0:
+            nw = key_bytes[k] // 8
+            outs[k] = (pinned_copy(np.zeros((n_solid, nw), np.uint64)), pinned_copy(np.zeros(n_solid, np.uint16)),
+                       pinned_copy(np.zeros(n_solid, np.uint8)))
         e2e_step()
         if world > 1:
             torch.distributed.barrier()

@@ -646,12 +646,20 @@ class SolidTable:
     def __len__(self):
         return self.info()[1]
 
-    def export(self, sort: bool = False):
-        """(keys[n, nw] big-endian words, cov u16, mask u8)."""
+    def export(self, sort: bool = False, out=None):
+        """(keys[n, nw] big-endian words, cov u16, mask u8).  `out` = (keys, cov, mask)
+        arrays with room for at least n rows (e.g. reused pinned buffers) receive the
+        rows; the returned arrays are views of their first n rows."""
         n_solid = self.info()[1]
-        keys = np.zeros((n_solid, self.nw), np.uint64)
-        cov = np.zeros(n_solid, np.uint16)
-        mask = np.zeros(n_solid, np.uint8)
+        if out is not None and len(out[1]) >= n_solid and len(out[2]) >= n_solid and len(out[0]) >= n_solid:
+            keys, cov, mask = out[0][:n_solid], out[1][:n_solid], out[2][:n_solid]
+            if keys.dtype != np.uint64 or keys.shape[1:] != (self.nw,) or not keys.flags.c_contiguous \
+                    or cov.dtype != np.uint16 or mask.dtype != np.uint8:
+                raise ValueError("export: out must be (uint64[n, nw], uint16[n], uint8[n]) C-contiguous arrays")
+        else:
+            keys = np.zeros((n_solid, self.nw), np.uint64)
+            cov = np.zeros(n_solid, np.uint16)
+            mask = np.zeros(n_solid, np.uint8)
         n = C.c_uint64()
         check(N.lib().fbk_table_export(self._h, ptr(keys.reshape(-1)), ptr(cov), ptr(mask), n_solid, C.byref(n)),
               self.ctx.handle, "table export")

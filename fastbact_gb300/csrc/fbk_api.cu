@@ -1,6 +1,8 @@
 // fbk_api.cu — host side of the C ABI: contexts, device pool, bank upload, and the
 // CountMinSketch / HyperLogLog / solid-table objects with their build passes.
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -447,27 +449,75 @@ FBK_API fbk_status fbk_ctx_mem_info(const fbk_ctx* ctx, uint64_t* used, uint64_t
 // ===========================================================================
 namespace fbk {
 
+void scan_arenas(const fbk_arena_view* arenas, int n_arenas, ArenaScan& sc) {
+    struct Job { int a; uint64_t lo, hi; };
+    std::vector<Job> jobs;
+    for (int a = 0; a < n_arenas; ++a)
+        for (uint64_t lo = 0; lo < arenas[a].n_seqs; lo += ArenaScan::BLOCK)
+            jobs.push_back({a, lo, std::min(arenas[a].n_seqs, lo + ArenaScan::BLOCK)});
+    sc.block_bases.assign(jobs.size(), 0);
+    struct Part {
+        uint64_t bases = 0, max_pair = 0, long_bases = 0;
+        uint32_t max_len = 0;
+        bool bad = false;
+        std::vector<uint64_t> hist;
+    };
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned T = (unsigned)std::min<uint64_t>(std::min(16u, hw), std::max<uint64_t>(1, jobs.size() / 4));
+    std::vector<Part> parts(T);
+    std::atomic<uint64_t> next{0};
+    auto work = [&](unsigned t) {
+        Part& P = parts[t];
+        P.hist.assign(ArenaScan::BINS, 0);
+        for (uint64_t j; (j = next.fetch_add(1)) < jobs.size();) {
+            const fbk_arena_view& v = arenas[jobs[j].a];
+            const uint64_t cap = v.n_words * 32;
+            uint64_t bases = 0;
+            for (uint64_t i = jobs[j].lo; i < jobs[j].hi; ++i) {
+                const uint32_t L = v.lengths[i];
+                // every sequence must lie inside its arena's words: the kernels read only there
+                P.bad |= L && v.offsets[i] + (uint64_t)L > cap;
+                bases += L;
+                P.max_len = std::max(P.max_len, L);
+                if (v.pair_idx) P.max_pair = std::max<uint64_t>(P.max_pair, v.pair_idx[i]);
+                if (L < ArenaScan::BINS - 1) P.hist[L]++;
+                else P.long_bases += L;
+            }
+            sc.block_bases[j] = bases;
+            P.bases += bases;
+        }
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < T; ++t) th.emplace_back(work, t);
+    work(0);
+    for (auto& x : th) x.join();
+    sc.hist.assign(ArenaScan::BINS, 0);
+    for (const Part& P : parts) {
+        sc.n_bases += P.bases;
+        sc.max_pair = std::max(sc.max_pair, P.max_pair);
+        sc.max_len = std::max(sc.max_len, P.max_len);
+        sc.long_bases += P.long_bases;
+        sc.bad |= P.bad;
+        for (uint64_t L = 0; L <= std::min<uint64_t>(P.max_len, ArenaScan::BINS - 1); ++L) sc.hist[L] += P.hist[L];
+    }
+    for (int a = 0; a < n_arenas; ++a) sc.n_reads += arenas[a].n_seqs;
+}
+
 fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_arenas, fbk_bank** out, uint64_t chunk_bases) {
-    uint64_t n_words = 0, n_reads = 0, n_bases = 0;
+    uint64_t n_words = 0;
     bool all_pairs = true;
-    uint32_t max_len = 0;
-    uint64_t max_pair = 0;
     for (int a = 0; a < n_arenas; ++a) {
         const fbk_arena_view& v = arenas[a];
         if (v.n_seqs && (!v.offsets || !v.lengths)) return set_err(ctx, FBK_ERR_INVALID, "arena has sequences but no offsets/lengths");
         if (v.n_words && !v.data) return set_err(ctx, FBK_ERR_INVALID, "arena has words but no data pointer");
-        // Every sequence must lie inside its arena's words: the kernels read only there.
-        for (uint64_t i = 0; i < v.n_seqs; ++i) {
-            const uint64_t end = v.offsets[i] + (uint64_t)v.lengths[i];
-            if (v.lengths[i] && end > v.n_words * 32) return set_err(ctx, FBK_ERR_INVALID, "sequence extends past the arena data");
-            n_bases += v.lengths[i];
-            max_len = std::max(max_len, v.lengths[i]);
-            if (v.pair_idx) max_pair = std::max<uint64_t>(max_pair, v.pair_idx[i]);
-        }
         if (v.n_seqs && !v.pair_idx) all_pairs = false;
         n_words += v.n_words;
-        n_reads += v.n_seqs;
     }
+    ArenaScan sc;
+    scan_arenas(arenas, n_arenas, sc);
+    if (sc.bad) return set_err(ctx, FBK_ERR_INVALID, "sequence extends past the arena data");
+    const uint64_t n_reads = sc.n_reads, n_bases = sc.n_bases, max_pair = sc.max_pair;
+    const uint32_t max_len = sc.max_len;
     fbk_bank* b = new fbk_bank();
     b->ctx = ctx;
     b->n_reads = n_reads;
@@ -514,28 +564,36 @@ fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_ar
     }
     // Read ranges with fewer than chunk_bases bases: one launch over a range adds
     // at most (bases x weight) to any 32-bit counter, which the callers keep below
-    // 2^32 - 2^17 (counters start each launch at <= 65535).
+    // 2^32 - 2^17 (counters start each launch at <= 65535).  Greedy walk: a range
+    // ends before the read that would bring it to chunk_bases; a block whose bases
+    // cannot reach that is skipped whole.
     b->chunk_starts.push_back(0);
-    uint64_t acc = 0, r = 0;
+    uint64_t acc = 0, r = 0, j = 0;
     for (int a = 0; a < n_arenas; ++a)
-        for (uint64_t i = 0; i < arenas[a].n_seqs; ++i, ++r) {
-            if (acc && acc + arenas[a].lengths[i] >= chunk_bases) {
-                b->chunk_starts.push_back(r);
-                b->max_chunk = std::max(b->max_chunk, acc);
-                acc = 0;
+        for (uint64_t lo = 0; lo < arenas[a].n_seqs; lo += ArenaScan::BLOCK, ++j) {
+            const uint64_t hi = std::min(arenas[a].n_seqs, lo + ArenaScan::BLOCK);
+            if (acc + sc.block_bases[j] < chunk_bases) {
+                acc += sc.block_bases[j];
+                r += hi - lo;
+                continue;
             }
-            acc += arenas[a].lengths[i];
+            for (uint64_t i = lo; i < hi; ++i, ++r) {
+                if (acc && acc + arenas[a].lengths[i] >= chunk_bases) {
+                    b->chunk_starts.push_back(r);
+                    b->max_chunk = std::max(b->max_chunk, acc);
+                    acc = 0;
+                }
+                acc += arenas[a].lengths[i];
+            }
         }
     b->max_chunk = std::max(b->max_chunk, acc);
     b->chunk_starts.push_back(n_reads);
-    const uint64_t bins = std::min<uint64_t>((uint64_t)max_len + 2, 1ULL << 16);
-    b->len_hist.assign(bins, 0);
-    for (int a = 0; a < n_arenas; ++a)
-        for (uint64_t i = 0; i < arenas[a].n_seqs; ++i) {
-            const uint64_t L = arenas[a].lengths[i];
-            if (L < bins - 1) b->len_hist[L]++;
-            else b->long_bases += L;
-        }
+    // length histogram with bins 0 .. max_len (+1 spare); longer reads (>= 2^16 - 1)
+    // are counted by their bases only
+    const uint64_t bins = std::min<uint64_t>((uint64_t)max_len + 2, ArenaScan::BINS);
+    b->len_hist.assign(sc.hist.begin(), sc.hist.begin() + bins);
+    b->long_bases = sc.long_bases;
+    for (uint64_t L = bins - 1; L < ArenaScan::BINS; ++L) b->long_bases += L * sc.hist[L];
     *out = b;
     return FBK_OK;
 }

@@ -1260,10 +1260,12 @@ FBK_API fbk_status fbk_server_submit(fbk_server* S, const fbk_arena_view bank[3]
     r->iso->stats = *stats;
     r->iso->sample_pairs = sample_pairs;
     r->iso->sample_len.assign(sample->lengths, sample->lengths + 2 * sample_pairs);
-    for (int a = 0; a < 3; ++a) {
-        r->bank[a] = bank[a];
-        for (uint64_t i = 0; i < bank[a].n_seqs; ++i) r->n_bases += bank[a].lengths[i];
-        r->n_reads += bank[a].n_seqs;
+    for (int a = 0; a < 3; ++a) r->bank[a] = bank[a];
+    {
+        ArenaScan sc;
+        scan_arenas(bank, 3, sc);
+        r->n_bases = sc.n_bases;
+        r->n_reads = sc.n_reads;
     }
     if (r->n_bases >= (1ULL << 31)) return FBK_ERR_INVALID;
     r->sample = *sample;

@@ -145,6 +145,22 @@ void time_begin(fbk_ctx* ctx, const char* name, TimedLaunch& t);
 void time_end(fbk_ctx* ctx, TimedLaunch& t);
 fbk_status ctx_check_status(fbk_ctx* ctx, uint32_t* bits);
 
+// One host pass over the sequences of a set of arenas: bounds check, totals, the
+// read-length histogram and the sums of fixed read blocks (for the chunk walk).
+// Blocks of BLOCK reads are scanned by up to 16 threads; the results do not depend on
+// the thread count.
+struct ArenaScan {
+    static constexpr uint64_t BLOCK = 1 << 16;
+    static constexpr uint64_t BINS = 1 << 16;
+    uint64_t n_reads = 0, n_bases = 0, max_pair = 0;
+    uint32_t max_len = 0;
+    bool bad = false;
+    std::vector<uint64_t> hist, block_bases;  // hist over lengths < BINS - 1 (capped index)
+    uint64_t long_bases = 0;                  // bases of reads of length >= BINS - 1
+};
+
+void scan_arenas(const fbk_arena_view* arenas, int n_arenas, ArenaScan& sc);
+
 // Upload of a packed arena set into a device bank (used by the estimator for its
 // sample and by prior-contig handling).
 // chunk_bases: read ranges are cut so that each holds fewer bases than this.

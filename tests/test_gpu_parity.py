@@ -581,6 +581,30 @@ def test_device_ingest_rejects_bad_records(ctx, tmp_path):
         api.ingest_fastq_device(ctx, r1, r2)
 
 
+def test_bank_upload_checks_every_sequence(ctx):
+    """The upload scans all reads (in blocks, on several threads): a bad sequence in
+    any block is refused, and the bank's totals match the host arenas."""
+    from fastbact_gb300 import _native as N
+
+    rng = np.random.default_rng(8)
+    n = 300_000  # several scan blocks
+    lengths = rng.integers(0, 300, n).astype(np.uint32)
+    offsets = np.zeros(n, np.uint64)
+    offsets[1:] = np.cumsum(lengths[:-1], dtype=np.uint64)
+    words = rng.integers(0, 2**63, (int(lengths.sum()) + 31) // 32 + 1, dtype=np.uint64)
+    good = api.BitSeqArena(words, offsets, lengths)
+    db = api.DeviceBank(ctx, good)
+    assert (db.n_reads, db.n_bases) == (n, int(lengths.sum()))
+    db.release()
+    for bad_at in (0, 70_000, n - 1):  # first, middle and last scan block
+        offs = offsets.copy()
+        lens = lengths.copy()
+        lens[bad_at] = 100
+        offs[bad_at] = len(words) * 32 - 50
+        with pytest.raises(N.FbkError, match="extends past"):
+            api.DeviceBank(ctx, api.BitSeqArena(words, offs, lens))
+
+
 def test_u16_sketch_saturates_like_the_reference(ctx):
     # 2^10 columns and ~80 M k-mer occurrences: most u16 counters pass 65535 and must
     # stop there (sketch.rs:199-221), in the exported sketch and in the gate
