@@ -138,6 +138,29 @@ __device__ __forceinline__ uint64_t cms_index(uint64_t key, int r, uint32_t log2
     return ((uint64_t)r << log2w) + col;
 }
 
+// One increment of N (row, column) counters kept as threshold ladders (t levels of
+// bits, level j set by the (j+1)-th increment; see fbk_k_ladder.cu).  climb[i] is
+// false for a counter whose top level is already set.  The N atomics of a level are
+// issued together and waited on once, so a warp pays one L2 round trip per level
+// below the top, not one per (counter, level); the top level's old value is not
+// needed (a reduction with no return).
+template <int N>
+__device__ __forceinline__ void ladder_climb(uint32_t* __restrict__ lad, uint64_t level_words, uint32_t t,
+                                             const uint32_t (&wd)[N], const uint32_t (&mk)[N], bool (&climb)[N]) {
+    for (uint32_t j = 0; j + 1 < t; ++j) {
+        uint32_t* lv = lad + (uint64_t)j * level_words;
+        uint32_t old[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) old[i] = climb[i] ? atomicOr(lv + wd[i], mk[i]) : 0u;
+#pragma unroll
+        for (int i = 0; i < N; ++i) climb[i] = (old[i] & mk[i]) != 0;
+    }
+    uint32_t* lv = lad + (uint64_t)(t - 1) * level_words;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+        if (climb[i]) atomicOr(lv + wd[i], mk[i]);
+}
+
 // HyperLogLog register index and rank — sketch.rs:49-63 (p = 14 there).
 __device__ __forceinline__ void hll_idx_rho(uint64_t h, uint32_t p, uint32_t& idx, uint32_t& rho) {
     idx = (uint32_t)(h >> (64 - p));

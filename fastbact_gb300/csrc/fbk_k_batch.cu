@@ -146,8 +146,8 @@ __global__ void __launch_bounds__(256) k_batch_solid(const IsoDev* __restrict__ 
 // Ladder forms (fbk_k_ladder.cu has the single-isolate kernels and the argument):
 // level j of (row, col) is set once the count reached j + 1; the top level is t_solid.
 template <int NW>
-__global__ void __launch_bounds__(256) k_batch_lpass1(const IsoDev* __restrict__ iso, const unsigned long long* __restrict__ read_base,
-                                                      uint32_t n_iso, uint32_t k) {
+__global__ void __launch_bounds__(256, 4) k_batch_lpass1(const IsoDev* __restrict__ iso, const unsigned long long* __restrict__ read_base,
+                                                         uint32_t n_iso, uint32_t k) {
     __shared__ unsigned long long s_base[BATCH_MAX_ISO + 1];
     load_bases(read_base, n_iso, s_base);
     const uint64_t total = s_base[n_iso];
@@ -188,16 +188,18 @@ __global__ void __launch_bounds__(256) k_batch_lpass1(const IsoDev* __restrict__
             window_canonical<NW>(b.data, off + q, k, can, rc);
             const uint64_t key = key_fold<NW>(can);
             const uint64_t h0 = smix(key ^ cms_seed(0));
+            uint32_t wd[4], mk[4];
+            bool climb[4];
 #pragma unroll
             for (int row = 0; row < 4; ++row) {
                 const uint64_t h = row == 0 ? h0 : smix(key ^ cms_seed(row));
-                const uint64_t bit = ((uint64_t)row << log2w) + (h & wmask);
-                const uint64_t w = bit >> 5;
-                const uint32_t m = 1u << (bit & 31);
-                bool climb = !(__ldcg(top + w) & m);
-                for (uint32_t j = 0; j < t; ++j)
-                    if (climb) climb = (atomicOr(lad + (uint64_t)j * level_words + w, m) & m) != 0;
+                const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
+                wd[row] = bit >> 5;
+                mk[row] = 1u << (bit & 31);
             }
+#pragma unroll
+            for (int row = 0; row < 4; ++row) climb[row] = !(__ldcg(top + wd[row]) & mk[row]);
+            ladder_climb<4>(lad, level_words, t, wd, mk, climb);
             if ((h0 & (BATCH_HLL_SAMPLE - 1)) == 0) {
                 uint32_t idx, rho;
                 hll_idx_rho(h0, 12, idx, rho);

@@ -43,9 +43,10 @@ __global__ void __launch_bounds__(256, ILP == 1 ? 4 : 2) k_ladder_pass1(BankDev 
         // levels): the climb is a predicated atomic per level, so the warp never splits.
         // With ILP = 2 each lane takes two windows and issues the eight top-level loads
         // together (the kernel is bound by their L2 latency) at half the resident warps.
+        // Lanes past the read's last window keep word 0 / mask 0 and never climb.
         for (uint32_t it = 0; it < ((nk + 31) >> 5); it += ILP) {
-            uint32_t wd[ILP][4], mk[ILP][4];
-            bool live[ILP];
+            uint32_t wd[4 * ILP], mk[4 * ILP];
+            bool live[ILP], climb[4 * ILP];
             uint64_t h0[ILP];
 #pragma unroll
             for (int p = 0; p < ILP; ++p) {
@@ -53,7 +54,7 @@ __global__ void __launch_bounds__(256, ILP == 1 ? 4 : 2) k_ladder_pass1(BankDev 
                 live[p] = q < nk;
                 h0[p] = 0;
 #pragma unroll
-                for (int row = 0; row < 4; ++row) wd[p][row] = mk[p][row] = 0;
+                for (int row = 0; row < 4; ++row) wd[4 * p + row] = mk[4 * p + row] = 0;
                 if (!live[p]) continue;
                 Key<NW> can;
                 bool rc;
@@ -64,29 +65,22 @@ __global__ void __launch_bounds__(256, ILP == 1 ? 4 : 2) k_ladder_pass1(BankDev 
                 for (int row = 0; row < 4; ++row) {
                     const uint64_t h = row == 0 ? h0[p] : smix(key ^ cms_seed(row));
                     const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
-                    wd[p][row] = bit >> 5;
-                    mk[p][row] = 1u << (bit & 31);
+                    wd[4 * p + row] = bit >> 5;
+                    mk[4 * p + row] = 1u << (bit & 31);
                 }
             }
-            uint32_t topw[ILP][4];
+            // false once the count reached t, and for lanes past the read's last window
 #pragma unroll
-            for (int p = 0; p < ILP; ++p)
+            for (int i = 0; i < 4 * ILP; ++i) climb[i] = live[i / 4] && !(__ldcg(top + wd[i]) & mk[i]);
+            ladder_climb<4 * ILP>(lad, level_words, t, wd, mk, climb);
+            if (do_hll) {
 #pragma unroll
-                for (int row = 0; row < 4; ++row) topw[p][row] = live[p] ? __ldcg(top + wd[p][row]) : ~0u;
-#pragma unroll
-            for (int p = 0; p < ILP; ++p) {
-#pragma unroll
-                for (int row = 0; row < 4; ++row) {
-                    // false once the count reached t, and for lanes past the read's last window
-                    bool climb = live[p] && !(topw[p][row] & mk[p][row]);
-                    for (uint32_t j = 0; j < t; ++j)
-                        if (climb) climb = (atomicOr(lad + (uint64_t)j * level_words + wd[p][row], mk[p][row]) & mk[p][row]) != 0;
-                }
-                if (do_hll && live[p]) {
-                    uint32_t idx, rho;
-                    hll_idx_rho(h0[p], 12, idx, rho);
-                    if (s_hll[idx] < rho) atomicMax(&s_hll[idx], rho);
-                }
+                for (int p = 0; p < ILP; ++p)
+                    if (live[p]) {
+                        uint32_t idx, rho;
+                        hll_idx_rho(h0[p], 12, idx, rho);
+                        if (s_hll[idx] < rho) atomicMax(&s_hll[idx], rho);
+                    }
             }
         }
     }
