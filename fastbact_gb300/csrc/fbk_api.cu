@@ -10,6 +10,7 @@
 
 #include "fbk_device.cuh"
 #include "fbk_internal.h"
+#include "host/fbk_workers.h"
 
 using namespace fbk;
 
@@ -276,6 +277,10 @@ FBK_API fbk_status fbk_ctx_destroy(fbk_ctx* c) {
     if (c->d_status) cudaFree(c->d_status);
     if (c->d_counts) cudaFree(c->d_counts);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    for (int i = 0; i < 2; ++i) {
+        if (c->h_stage[i]) cudaFreeHost(c->h_stage[i]);
+        if (c->stage_ev[i]) cudaEventDestroy(c->stage_ev[i]);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FBK_OK;
@@ -449,6 +454,80 @@ FBK_API fbk_status fbk_ctx_mem_info(const fbk_ctx* ctx, uint64_t* used, uint64_t
 // ===========================================================================
 namespace fbk {
 
+static constexpr size_t STAGE_BYTES = 16u << 20;  // one staging slot
+static constexpr size_t STAGE_MIN = 4u << 20;     // smaller pageable copies go direct
+static constexpr size_t STAGE_PIECE = 1u << 20;   // host copy unit of the worker pool
+
+static bool host_page_locked(const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+static cudaError_t stage_ready(fbk_ctx* ctx) {
+    if (ctx->h_stage[0]) return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        e = cudaMallocHost(&ctx->h_stage[i], STAGE_BYTES);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->stage_ev[i], cudaEventDisableTiming);
+    }
+    return e;
+}
+
+static void pool_copy(void* dst, const void* src, size_t n) {
+    host_parallel_for((n + STAGE_PIECE - 1) / STAGE_PIECE, [&](uint64_t i, unsigned) {
+        const size_t o = i * STAGE_PIECE;
+        std::memcpy((char*)dst + o, (const char*)src + o, std::min(STAGE_PIECE, n - o));
+    });
+}
+
+cudaError_t copy_h2d(fbk_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return cudaSuccess;
+    if (bytes < STAGE_MIN || host_page_locked(src))
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    cudaError_t e = stage_ready(ctx);
+    for (size_t done = 0; e == cudaSuccess && done < bytes;) {
+        const int slot = (int)((done / STAGE_BYTES) & 1);
+        const size_t n = std::min(STAGE_BYTES, bytes - done);
+        e = cudaEventSynchronize(ctx->stage_ev[slot]);  // the slot's previous DMA has finished
+        if (e != cudaSuccess) break;
+        pool_copy(ctx->h_stage[slot], (const char*)src + done, n);
+        e = cudaMemcpyAsync((char*)dst + done, ctx->h_stage[slot], n, cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->stage_ev[slot], ctx->stream);
+        done += n;
+    }
+    return e;
+}
+
+cudaError_t copy_d2h(fbk_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return cudaSuccess;
+    if (bytes < STAGE_MIN || host_page_locked(dst)) {
+        cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+        return e == cudaSuccess ? cudaStreamSynchronize(ctx->stream) : e;
+    }
+    cudaError_t e = stage_ready(ctx);
+    const size_t nc = (bytes + STAGE_BYTES - 1) / STAGE_BYTES;
+    auto issue = [&](size_t c) {
+        const size_t o = c * STAGE_BYTES, n = std::min(STAGE_BYTES, bytes - o);
+        cudaError_t x = cudaMemcpyAsync(ctx->h_stage[c & 1], (const char*)src + o, n, cudaMemcpyDeviceToHost, ctx->stream);
+        return x == cudaSuccess ? cudaEventRecord(ctx->stage_ev[c & 1], ctx->stream) : x;
+    };
+    if (e == cudaSuccess) e = issue(0);
+    for (size_t c = 0; e == cudaSuccess && c < nc; ++c) {
+        // chunk c + 1 lands in the other slot, whose previous contents were copied out
+        // in the last iteration, while chunk c is copied out of this one
+        if (c + 1 < nc) e = issue(c + 1);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ctx->stage_ev[c & 1]);
+        if (e != cudaSuccess) break;
+        const size_t o = c * STAGE_BYTES;
+        pool_copy((char*)dst + o, ctx->h_stage[c & 1], std::min(STAGE_BYTES, bytes - o));
+    }
+    return e;
+}
+
 void scan_arenas(const fbk_arena_view* arenas, int n_arenas, ArenaScan& sc) {
     struct Job { int a; uint64_t lo, hi; };
     std::vector<Job> jobs;
@@ -462,37 +541,29 @@ void scan_arenas(const fbk_arena_view* arenas, int n_arenas, ArenaScan& sc) {
         bool bad = false;
         std::vector<uint64_t> hist;
     };
-    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const unsigned T = (unsigned)std::min<uint64_t>(std::min(16u, hw), std::max<uint64_t>(1, jobs.size() / 4));
-    std::vector<Part> parts(T);
-    std::atomic<uint64_t> next{0};
-    auto work = [&](unsigned t) {
+    std::vector<Part> parts(host_threads());
+    host_parallel_for(jobs.size(), [&](uint64_t j, unsigned t) {
         Part& P = parts[t];
-        P.hist.assign(ArenaScan::BINS, 0);
-        for (uint64_t j; (j = next.fetch_add(1)) < jobs.size();) {
-            const fbk_arena_view& v = arenas[jobs[j].a];
-            const uint64_t cap = v.n_words * 32;
-            uint64_t bases = 0;
-            for (uint64_t i = jobs[j].lo; i < jobs[j].hi; ++i) {
-                const uint32_t L = v.lengths[i];
-                // every sequence must lie inside its arena's words: the kernels read only there
-                P.bad |= L && v.offsets[i] + (uint64_t)L > cap;
-                bases += L;
-                P.max_len = std::max(P.max_len, L);
-                if (v.pair_idx) P.max_pair = std::max<uint64_t>(P.max_pair, v.pair_idx[i]);
-                if (L < ArenaScan::BINS - 1) P.hist[L]++;
-                else P.long_bases += L;
-            }
-            sc.block_bases[j] = bases;
-            P.bases += bases;
+        if (P.hist.empty()) P.hist.assign(ArenaScan::BINS, 0);
+        const fbk_arena_view& v = arenas[jobs[j].a];
+        const uint64_t cap = v.n_words * 32;
+        uint64_t bases = 0;
+        for (uint64_t i = jobs[j].lo; i < jobs[j].hi; ++i) {
+            const uint32_t L = v.lengths[i];
+            // every sequence must lie inside its arena's words: the kernels read only there
+            P.bad |= L && v.offsets[i] + (uint64_t)L > cap;
+            bases += L;
+            P.max_len = std::max(P.max_len, L);
+            if (v.pair_idx) P.max_pair = std::max<uint64_t>(P.max_pair, v.pair_idx[i]);
+            if (L < ArenaScan::BINS - 1) P.hist[L]++;
+            else P.long_bases += L;
         }
-    };
-    std::vector<std::thread> th;
-    for (unsigned t = 1; t < T; ++t) th.emplace_back(work, t);
-    work(0);
-    for (auto& x : th) x.join();
+        sc.block_bases[j] = bases;
+        P.bases += bases;
+    });
     sc.hist.assign(ArenaScan::BINS, 0);
     for (const Part& P : parts) {
+        if (P.hist.empty()) continue;
         sc.n_bases += P.bases;
         sc.max_pair = std::max(sc.max_pair, P.max_pair);
         sc.max_len = std::max(sc.max_len, P.max_len);
@@ -538,11 +609,10 @@ fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_ar
     for (int a = 0; a < n_arenas; ++a) {
         const fbk_arena_view& v = arenas[a];
         cudaError_t e = cudaSuccess;
-        if (v.n_words) e = cudaMemcpyAsync(b->data + wbase, v.data, v.n_words * 8, cudaMemcpyHostToDevice, ctx->stream);
-        if (e == cudaSuccess && v.n_seqs) e = cudaMemcpyAsync(b->off + rbase, v.offsets, v.n_seqs * 8, cudaMemcpyHostToDevice, ctx->stream);
-        if (e == cudaSuccess && v.n_seqs) e = cudaMemcpyAsync(b->len + rbase, v.lengths, v.n_seqs * 4, cudaMemcpyHostToDevice, ctx->stream);
-        if (e == cudaSuccess && v.n_seqs && b->pair_idx)
-            e = cudaMemcpyAsync(b->pair_idx + rbase, v.pair_idx, v.n_seqs * 4, cudaMemcpyHostToDevice, ctx->stream);
+        if (v.n_words) e = copy_h2d(ctx, b->data + wbase, v.data, v.n_words * 8);
+        if (e == cudaSuccess && v.n_seqs) e = copy_h2d(ctx, b->off + rbase, v.offsets, v.n_seqs * 8);
+        if (e == cudaSuccess && v.n_seqs) e = copy_h2d(ctx, b->len + rbase, v.lengths, v.n_seqs * 4);
+        if (e == cudaSuccess && v.n_seqs && b->pair_idx) e = copy_h2d(ctx, b->pair_idx + rbase, v.pair_idx, v.n_seqs * 4);
         if (e == cudaSuccess && wbase && v.n_seqs) {
             TimedLaunch tl;
             time_begin(ctx, "bank_rebase", tl);
@@ -865,8 +935,7 @@ FBK_API fbk_status fbk_cms_export(fbk_cms* c, uint8_t* out, uint64_t nbytes) {
         e = launch_cms_export((int)c->cbits, launch_cfg(ctx, 256, 0), c->cnt, c->n, d);
         time_end(ctx, tl);
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, nbytes, cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) e = copy_d2h(ctx, out, d, nbytes);
     dev_free(ctx, d);
     if (e != cudaSuccess) return cuda_err(ctx, e, "cms export");
     return FBK_OK;
@@ -878,7 +947,7 @@ FBK_API fbk_status fbk_cms_import(fbk_cms* c, const uint8_t* in, uint64_t nbytes
     fbk_ctx* ctx = c->ctx;
     uint8_t* d = (uint8_t*)dev_alloc(ctx, nbytes);
     if (!d) return set_err(ctx, FBK_ERR_OOM, "cms import buffer");
-    cudaError_t e = cudaMemcpyAsync(d, in, nbytes, cudaMemcpyHostToDevice, ctx->stream);
+    cudaError_t e = copy_h2d(ctx, d, in, nbytes);
     if (e == cudaSuccess) {
         TimedLaunch tl;
         time_begin(ctx, "cms_import", tl);
@@ -1448,10 +1517,9 @@ FBK_API fbk_status fbk_table_export(fbk_table* t, uint64_t* keys, uint16_t* cov,
     uint64_t n = std::min(cap, t->n_solid);
     if (n && (!keys || !cov || !mask)) return FBK_ERR_INVALID;
     if (n) {
-        CK(ctx, cudaMemcpyAsync(keys, t->out_keys, n * 8 * t->nw, cudaMemcpyDeviceToHost, ctx->stream));
-        CK(ctx, cudaMemcpyAsync(cov, t->out_cov, n * 2, cudaMemcpyDeviceToHost, ctx->stream));
-        CK(ctx, cudaMemcpyAsync(mask, t->out_mask, n, cudaMemcpyDeviceToHost, ctx->stream));
-        CK(ctx, cudaStreamSynchronize(ctx->stream));
+        CK(ctx, copy_d2h(ctx, keys, t->out_keys, n * 8 * t->nw));
+        CK(ctx, copy_d2h(ctx, cov, t->out_cov, n * 2));
+        CK(ctx, copy_d2h(ctx, mask, t->out_mask, n));
     }
     *n_out = t->n_solid;
     return FBK_OK;
@@ -1478,10 +1546,9 @@ FBK_API fbk_status fbk_table_export_acc(fbk_table* t, uint64_t* keys, uint16_t* 
     }
     fbk_status st = table_convert(t, dk, dc, de, n);
     if (st == FBK_OK && n) {
-        cudaError_t e = cudaMemcpyAsync(keys, dk, n * 8 * t->nw, cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(cov, dc, n * 2, cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(edges, de, n * 16, cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        cudaError_t e = copy_d2h(ctx, keys, dk, n * 8 * t->nw);
+        if (e == cudaSuccess) e = copy_d2h(ctx, cov, dc, n * 2);
+        if (e == cudaSuccess) e = copy_d2h(ctx, edges, de, n * 16);
         if (e != cudaSuccess) st = cuda_err(ctx, e, "accumulator export");
     }
     dev_free(ctx, dk);

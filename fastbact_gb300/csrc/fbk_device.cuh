@@ -95,41 +95,60 @@ __device__ __forceinline__ uint64_t field_mask(uint32_t k, int i) {
 }
 
 // Canonical k-mer (min(fwd, rc), rc chosen iff rc < fwd — build.rs:102,258) of the
-// window starting at base g.  k <= 32*NW - 1.
-template <int NW>
-__device__ __forceinline__ void window_canonical(const uint64_t* __restrict__ d, uint64_t g, uint32_t k, Key<NW>& can,
-                                                 bool& is_rc) {
-    uint64_t W[NW];
+// window starting at base g, for a word shift WS = (64*NW - 2k) / 64 known at compile
+// time: the 2k-bit field covers NK = NW - WS words, so only NK + 1 packed words are
+// read and reversed, and every register index is a constant.
+template <int NW, int WS>
+__device__ __forceinline__ void canonical_ws(const uint64_t* __restrict__ d, uint64_t g, uint32_t k, Key<NW>& can,
+                                             bool& is_rc) {
+    constexpr int NK = NW - WS;
+    const uint64_t wi = g >> 5;
+    const uint32_t sh = (uint32_t)(g & 31) << 1;
+    // bases g .. g + 32 NK - 1 (the bank carries 8 zero words of padding)
+    uint64_t D[NK + 1], W[NK], R[NK];
 #pragma unroll
-    for (int i = 0; i < NW; ++i) W[i] = bits_at(d, g + 32ull * i);
-    // fwd: full group reversal of the NW*64-bit field (R.w[i] = rev2(W[i])), then a
-    // right shift by s = 64*NW - 2k bits (big-endian words).
-    uint64_t R[NW];
+    for (int i = 0; i <= NK; ++i) D[i] = d[wi + i];
 #pragma unroll
-    for (int i = 0; i < NW; ++i) R[i] = rev2(W[i]);
-    const uint32_t s = 64u * NW - 2u * k;
-    const uint32_t ws = s >> 6, bs = s & 63;
+    for (int i = 0; i < NK; ++i) {
+        W[i] = (D[i] >> sh) | ((D[i + 1] << (63 - sh)) << 1);
+        R[i] = rev2(W[i]);
+    }
+    // fwd: full group reversal of the field (R), then a right shift by
+    // s = 64*NW - 2k bits across big-endian words: word j takes R[j - WS] >> bs and
+    // the low bits of R[j - WS - 1]
+    const uint32_t bs = (64u * NW - 2u * k) & 63;
     Key<NW> fwd, rc;
 #pragma unroll
     for (int j = 0; j < NW; ++j) {
-        // word j takes R[j - ws] >> bs and the low bits of R[j - ws - 1]; the word
-        // shift is selected among its NW possible values so every R index is a
-        // compile-time constant (the array stays in registers)
-        uint64_t hi = 0, lo = 0;
-#pragma unroll
-        for (int c = 0; c < NW; ++c) {
-            if (ws == (uint32_t)c) {
-                hi = (j - c >= 0) ? R[j - c >= 0 ? j - c : 0] : 0ULL;
-                lo = (j - c - 1 >= 0) ? R[j - c - 1 >= 0 ? j - c - 1 : 0] : 0ULL;
-            }
-        }
+        const uint64_t hi = j - WS >= 0 ? R[j - WS >= 0 ? j - WS : 0] : 0ULL;
+        const uint64_t lo = j - WS - 1 >= 0 ? R[j - WS - 1 >= 0 ? j - WS - 1 : 0] : 0ULL;
         fwd.w[j] = (hi >> bs) | (bs ? (lo << (64 - bs)) : 0ULL);
     }
     // rc: ~W masked to 2k bits; LSB-first word i is big-endian word NW-1-i.
 #pragma unroll
-    for (int i = 0; i < NW; ++i) rc.w[NW - 1 - i] = (~W[i]) & field_mask(k, i);
+    for (int i = 0; i < NW; ++i) rc.w[NW - 1 - i] = i < NK ? (~W[i < NK ? i : 0]) & field_mask(k, i) : 0ULL;
     is_rc = key_less<NW>(rc, fwd);
     can = is_rc ? rc : fwd;
+}
+
+// Canonical k-mer of the window at g for any k <= 32*NW - 1: the word shift is the
+// same for every window of a launch, so the branch below never diverges.
+template <int NW>
+__device__ __forceinline__ void window_canonical(const uint64_t* __restrict__ d, uint64_t g, uint32_t k, Key<NW>& can,
+                                                 bool& is_rc) {
+    const uint32_t ws = (64u * NW - 2u * k) >> 6;
+    if constexpr (NW == 1) {
+        canonical_ws<1, 0>(d, g, k, can, is_rc);
+    } else if constexpr (NW == 2) {
+        if (ws == 0) canonical_ws<2, 0>(d, g, k, can, is_rc);
+        else canonical_ws<2, 1>(d, g, k, can, is_rc);
+    } else {
+        static_assert(NW == 4, "keys are 1, 2 or 4 words");
+        if (ws == 0) canonical_ws<4, 0>(d, g, k, can, is_rc);
+        else if (ws == 1) canonical_ws<4, 1>(d, g, k, can, is_rc);
+        else if (ws == 2) canonical_ws<4, 2>(d, g, k, can, is_rc);
+        else canonical_ws<4, 3>(d, g, k, can, is_rc);
+    }
 }
 
 // Counter index of row r for key in a 4 x 2^log2w Count-Min Sketch (sketch.rs:193-195).

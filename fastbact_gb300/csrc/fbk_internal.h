@@ -51,6 +51,8 @@ struct fbk_ctx {
     uint32_t* d_status = nullptr;            // device status bits (4 words)
     unsigned long long* d_counts = nullptr;  // conversion counters (4)
     void* h_pinned = nullptr;                // 64 KiB pinned host scratch
+    void* h_stage[2] = {};                   // pinned staging slots for pageable copies (lazy)
+    cudaEvent_t stage_ev[2] = {};            // last DMA that used each slot
     std::string err;
     bool timing = false;
     std::vector<fbk::TimedLaunch> pending;
@@ -160,6 +162,15 @@ struct ArenaScan {
 };
 
 void scan_arenas(const fbk_arena_view* arenas, int n_arenas, ArenaScan& sc);
+
+// Host<->device copies on the context's stream.  Page-locked host memory and small
+// copies go straight to the DMA engines; larger pageable buffers move through two
+// pinned staging slots, the host side copied by the worker pool while the other
+// slot's DMA runs (a GPU reading pageable memory that it has not mapped recently
+// runs far below the copy engines' rate).  copy_h2d returns with the last DMA in
+// flight (src may be reused at once); copy_d2h returns when dst holds the data.
+cudaError_t copy_h2d(fbk_ctx* ctx, void* dst, const void* src, size_t bytes);
+cudaError_t copy_d2h(fbk_ctx* ctx, void* dst, const void* src, size_t bytes);
 
 // Upload of a packed arena set into a device bank (used by the estimator for its
 // sample and by prior-contig handling).

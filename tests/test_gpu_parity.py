@@ -57,8 +57,8 @@ def repeat_isolate():
 # ---------------------------------------------------------------------------
 # k-mer extraction and ntHash
 # ---------------------------------------------------------------------------
-KS = [(1, 64), (5, 64), (21, 64), (31, 64), (21, 128), (33, 128), (55, 128), (63, 128), (31, 256), (65, 256),
-      (77, 256), (99, 256), (127, 256)]
+KS = [(1, 64), (5, 64), (21, 64), (31, 64), (21, 128), (33, 128), (55, 128), (63, 128), (31, 256), (45, 256),
+      (65, 256), (77, 256), (96, 256), (97, 256), (99, 256), (127, 256)]
 
 
 @pytest.mark.parametrize("k,kb", KS)
@@ -603,6 +603,31 @@ def test_bank_upload_checks_every_sequence(ctx):
         offs[bad_at] = len(words) * 32 - 50
         with pytest.raises(N.FbkError, match="extends past"):
             api.DeviceBank(ctx, api.BitSeqArena(words, offs, lens))
+
+
+@pytest.mark.parametrize("cb,log2w", [(16, 22), (4, 24)])
+def test_large_sketch_export_import_round_trip(ctx, small_isolate, cb, log2w):
+    """Sketches of 32 MB go through the pinned staging slots both ways (several
+    16 MB chunks); the bytes equal the oracle's pass-1 sketch."""
+    bank = small_isolate[0]
+    t, cms = api.build_cdbg_ext(bank, 31, None, ctx=ctx, key_bits=64, counter_bits=cb, cms_log2_width=log2w,
+                                keep_cms=True)
+    t.release()
+    raw = cms.export()
+    assert raw.nbytes == 32 << 20
+    o_cms = orc.build_front(bank, 31, 64, log2w, cb, None, threads=4)[0]
+    assert np.array_equal(raw, o_cms.export())
+    other = api.CountMinSketch(1 << log2w, ctx, counter_bits=cb)
+    other.load(raw)
+    assert np.array_equal(other.export(), raw)
+    # a page-locked destination takes the direct path and gives the same bytes
+    import torch
+
+    from fastbact_gb300 import _native as N
+
+    pinned = torch.empty(raw.nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+    assert N.lib().fbk_cms_export(other._h, N.ptr(pinned), raw.nbytes) == 0
+    assert np.array_equal(pinned, raw)
 
 
 def test_u16_sketch_saturates_like_the_reference(ctx):
