@@ -404,7 +404,7 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "record_factor" && v > 0 && v <= 16) ctx->record_factor = v;
     else if (n == "sketch_mode" && (v == 0 || v == 1)) ctx->sketch_mode = (int)v;
     else if (n == "ladder_ilp" && (v == 1 || v == 2)) ctx->ladder_ilp = (int)v;
-    else if (n == "emit_lookahead" && (v == 1 || v == 2)) ctx->emit_lookahead = (int)v;
+    else if (n == "emit_lookahead" && v >= 1 && v <= 3) ctx->emit_lookahead = (int)v;
     // the pass kernels are compiled for blocks of at most 256 threads
     else if (n == "block_pass1" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_pass1 = (int)v;
     else if (n == "grid_pass1" && v >= 0) ctx->grid_pass1 = (int)v;
@@ -1065,8 +1065,8 @@ FBK_API fbk_status fbk_hll_release(fbk_hll* h) {
 // ===========================================================================
 static void table_free_storage(fbk_table* t) {
     fbk_ctx* ctx = t->ctx;
+    if (t->tags != t->keys) dev_free(ctx, t->tags);
     dev_free(ctx, t->keys);
-    dev_free(ctx, t->tags);
     dev_free(ctx, t->cnt);
     dev_free(ctx, t->cov);
     t->keys = t->tags = nullptr;
@@ -1086,6 +1086,7 @@ static TableDev table_dev(const fbk_table* t) {
     TableDev d;
     d.keys = t->keys;
     d.tags = t->tags;
+    d.tag_stride = t->tags && t->tags == t->keys ? 4u : 1u;
     d.cnt = t->cnt;
     d.cov = t->cov;
     d.cap = t->cap;
@@ -1098,7 +1099,7 @@ static fbk_status table_alloc(fbk_table* t, uint64_t cap, bool with_cov) {
     fbk_ctx* ctx = t->ctx;
     t->cap = cap;
     t->keys = (uint64_t*)dev_alloc(ctx, cap * 8 * t->nw);
-    if (t->nw > 2) t->tags = (uint64_t*)dev_alloc(ctx, cap * 8);
+    if (t->nw > 2) t->tags = tag_in_key(t->nw, t->k) ? t->keys : (uint64_t*)dev_alloc(ctx, cap * 8);
     t->cnt = (uint32_t*)dev_alloc(ctx, cap * 32);
     if (with_cov) t->cov = (uint32_t*)dev_alloc(ctx, cap * 4);
     if (!t->keys || (t->nw > 2 && !t->tags) || !t->cnt || (with_cov && !t->cov)) {

@@ -466,7 +466,7 @@ fbk_status alloc_b(fbk_batch* B, BatchIso* it, const PlanB& q) {
     it->table = t;
     t->cap = q.cap;
     t->keys = (uint64_t*)dev_alloc(ctx, q.cap * 8 * t->nw);
-    if (t->nw > 2) t->tags = (uint64_t*)dev_alloc(ctx, q.cap * 8);
+    if (t->nw > 2) t->tags = tag_in_key(t->nw, t->k) ? t->keys : (uint64_t*)dev_alloc(ctx, q.cap * 8);
     t->cnt = (uint32_t*)dev_alloc(ctx, q.cap * 32);
     t->out_keys = (uint64_t*)dev_alloc(ctx, q.out_cap * 8 * t->nw);
     t->out_cov = (uint16_t*)dev_alloc(ctx, q.out_cap * 2);

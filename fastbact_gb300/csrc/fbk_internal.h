@@ -74,7 +74,7 @@ struct fbk_ctx {
     double record_factor = 1.25;          // bucket capacity / expected records per stripe
     int sketch_mode = 1;                  // 1: a build that does not return its sketch keeps only the gate ladder
     int ladder_ilp = 1;                   // windows per lane per step in the ladder pass 1 (1 or 2)
-    int emit_lookahead = 2;               // chunks of gate loads ahead of the record emit (1 or 2)
+    int emit_lookahead = 2;               // record emit: gate loads 1 or 2 chunks ahead; 3 = 2 ahead over a flattened window stream
     bool capturing = false;               // launches are being captured into a CUDA graph
 };
 
@@ -122,7 +122,7 @@ struct fbk_table {
     uint32_t nw = 1, k = 0, min_trans_cov = 3;
     uint64_t cap = 0;
     uint64_t* keys = nullptr;
-    uint64_t* tags = nullptr;
+    uint64_t* tags = nullptr;  // == keys when the tags live in word 0 of the keys
     uint32_t* cnt = nullptr;
     uint32_t* cov = nullptr;
     // converted SolidKmerNode rows
@@ -178,6 +178,10 @@ cudaError_t copy_d2h(fbk_ctx* ctx, void* dst, const void* src, size_t bytes);
 fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_arenas, fbk_bank** out,
                             uint64_t chunk_bases = 1ull << 30);
 BankDev bank_view(const fbk_bank* b, uint64_t r_begin, uint64_t r_end, const uint64_t* keep_bits);
+
+// 256-bit keys of k <= 96 have a zero most significant word, which then holds the
+// slot's tag (no separate tag array).
+inline bool tag_in_key(uint32_t nw, uint32_t k) { return nw == 4 && k <= 96; }
 
 // Single-isolate pieces reused by the multi-isolate host code (fbk_api.cu).
 int key_words(uint32_t key_bits);     // 64 -> 1, 128 -> 2, 256 -> 4, else 0

@@ -466,6 +466,135 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
     if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
 }
 
+// The same emit over a flattened window stream: a warp takes a run of EMIT_RUN
+// consecutive reads and walks the concatenation of their windows 32 at a time, so a
+// chunk may hold the end of one read and the start of the next and no lane idles at
+// the end of each read (a 146-base read has 70 windows of 77 bases: three chunks of
+// 32 per read, 27% of the lanes idle, when walked read by read).  Window q of a read
+// has its left neighbour at the previous stream position iff q > 0 and its right
+// neighbour at the next iff q + 1 < nk, so the ballot logic is unchanged.  Gate
+// loads run two chunks ahead as in k_emit_ladder2.
+constexpr uint32_t EMIT_RUN = 32;
+
+struct StreamCursor {
+    uint64_t r, r_end;  // current read, end of the run
+    uint64_t off;       // first base of read r
+    uint32_t q, nk;     // window within read r, windows of read r (0 if skipped)
+};
+
+__device__ __forceinline__ uint32_t stream_nk(const BankDev& b, uint64_t r, uint32_t k) {
+    const uint32_t len = b.len[r];
+    return len >= k + 1 && bank_keep(b, r) ? len - k + 1 : 0u;
+}
+// Moves the cursor `step` windows forward; r == r_end afterwards means past the run.
+__device__ __forceinline__ void stream_advance(const BankDev& b, uint32_t k, StreamCursor& c, uint32_t step) {
+    c.q += step;
+    while (c.r < c.r_end && c.q >= c.nk) {
+        c.q -= c.nk;
+        if (++c.r < c.r_end) {
+            c.nk = stream_nk(b, c.r, k);
+            c.off = b.off[c.r];
+        }
+    }
+}
+
+template <int NW>
+struct StreamWindow {
+    Key<NW> key;
+    uint64_t g;     // first base
+    bool live, rc;
+    bool has_l, has_r;  // neighbours inside the read
+};
+template <int NW>
+__device__ __forceinline__ void stream_window(const BankDev& b, uint32_t k, const StreamCursor& c, StreamWindow<NW>& w) {
+    w.live = c.r < c.r_end;
+    w.rc = false;
+    w.g = c.off + c.q;
+    w.has_l = c.q > 0;
+    w.has_r = c.q + 1 < c.nk;
+    if (w.live) window_canonical<NW>(b.data, w.g, k, w.key, w.rc);
+}
+
+template <int NW>
+__global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, const uint32_t* __restrict__ lad, uint32_t log2w,
+                                                      uint32_t t_solid, TableDev t, BucketDev bk) {
+    extern __shared__ uint64_t emit_smem[];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint64_t* buf = emit_smem + (uint64_t)wib * EMIT_WARP_WORDS(NW);
+    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + EMIT_BUF * (NW + 1));
+    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + EMIT_BUF);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + EMIT_BUF);
+    unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
+    const uint32_t* top = lad + (uint64_t)(t_solid - 1) * ((4ULL << log2w) >> 5);
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t stripe = (uint32_t)(gw % bk.stripes);
+    uint32_t n_buf = 0;  // warp-uniform
+    for (uint64_t r0 = b.r_begin + gw * EMIT_RUN; r0 < b.r_end; r0 += nwarps * EMIT_RUN) {
+        StreamCursor cur;
+        cur.r = r0;
+        cur.r_end = r0 + EMIT_RUN < b.r_end ? r0 + EMIT_RUN : b.r_end;
+        cur.nk = stream_nk(b, r0, k);
+        cur.off = b.off[r0];
+        cur.q = 0;
+        stream_advance(b, k, cur, lane);
+        // chunks 0 and 1 resolved up front
+        StreamWindow<NW> wc, wn;
+        stream_window<NW>(b, k, cur, wc);
+        stream_advance(b, k, cur, 32);
+        stream_window<NW>(b, k, cur, wn);
+        stream_advance(b, k, cur, 32);
+        GateLoads g0, g1;
+        gate_issue(top, log2w, wc.live ? key_fold<NW>(wc.key) : 0, wc.live, g0);
+        gate_issue(top, log2w, wn.live ? key_fold<NW>(wn.key) : 0, wn.live, g1);
+        uint32_t mprev = 0, mcur = __ballot_sync(0xffffffffu, gate_resolve(g0, wc.live));
+        uint32_t mnext = __ballot_sync(0xffffffffu, gate_resolve(g1, wn.live));
+        // the stream of a run is contiguous: once a chunk has no live lane, none has
+        while (__any_sync(0xffffffffu, wc.live)) {
+            StreamWindow<NW> wf;
+            stream_window<NW>(b, k, cur, wf);
+            stream_advance(b, k, cur, 32);
+            GateLoads gf;
+            gate_issue(top, log2w, wf.live ? key_fold<NW>(wf.key) : 0, wf.live, gf);
+            bool emit = false;
+            uint32_t info = 0, bucket = 0;
+            if (wc.live) {
+                const bool sq = (mcur >> lane) & 1u;
+                const bool sl = wc.has_l && (lane ? ((mcur >> (lane - 1)) & 1u) : (mprev >> 31));
+                const bool sr = wc.has_r && (lane < 31 ? ((mcur >> (lane + 1)) & 1u) : (mnext & 1u));
+                emit = sq && (sl || sr);
+                if (emit) {
+                    if (sr) info |= 8u | (base_at(b.data, wc.g + k) + (wc.rc ? 4u : 0u));
+                    if (sl) info |= (8u | ((3u - base_at(b.data, wc.g - 1)) + (wc.rc ? 0u : 4u))) << 4;
+                    bucket = (uint32_t)(home_slot(key_fold<NW>(wc.key), t.cap) >> bk.shift);
+                }
+            }
+            const uint32_t active = __ballot_sync(0xffffffffu, emit);
+            if (emit) {
+                const uint32_t pos = n_buf + __popc(active & ((1u << lane) - 1));
+#pragma unroll
+                for (int i = 0; i < NW; ++i) buf[pos * (NW + 1) + i] = wc.key.w[i];
+                buf[pos * (NW + 1) + NW] = info;
+                bbuf[pos] = (uint8_t)bucket;
+            }
+            n_buf += __popc(active);
+            if (n_buf > EMIT_BUF - 32) {
+                __syncwarp();
+                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+                n_buf = 0;
+            }
+            const uint32_t mfar = __ballot_sync(0xffffffffu, gate_resolve(gf, wf.live));
+            mprev = mcur;
+            mcur = mnext;
+            mnext = mfar;
+            wc = wn;
+            wn = wf;
+        }
+    }
+    __syncwarp();
+    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+}
+
 // Upsert of one bucket's records: every thread resolves its record's key from its
 // home slot and adds the pushes.  (Taking two records per thread and issuing both
 // home-slot loads first measured 18% slower: register pressure cost more occupancy
@@ -566,7 +695,7 @@ __global__ void __launch_bounds__(256) k_convert(TableDev t, uint32_t min_trans_
         for (int j = 0; j < CONV_SLOTS; ++j) {
             const uint64_t s = s0 + j;
             if (s >= cap) break;
-            const bool occ = NW <= 2 ? (t.keys[s * NW] != KEY_EMPTY) : (t.tags[s] != 0);
+            const bool occ = NW <= 2 ? (t.keys[s * NW] != KEY_EMPTY) : (t.tags[s * t.tag_stride] != 0);
             occ_bits |= (uint32_t)occ << j;
         }
         // mask per occupied slot (needs the counters)
@@ -615,6 +744,7 @@ __global__ void __launch_bounds__(256) k_convert(TableDev t, uint32_t min_trans_
             Key<NW> key;
 #pragma unroll
             for (int i = 0; i < NW; ++i) key.w[i] = t.keys[s * NW + i];
+            if (NW == 4 && t.tag_stride == NW) key.w[0] = 0;  // word 0 holds the tag
             if (o.acc_keys) {
                 if (wa < o.cap_acc) {
 #pragma unroll
@@ -755,6 +885,7 @@ template <int NW>
 static cudaError_t emitl_nw(const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w, uint32_t ts,
                             const TableDev& t, const BucketDev& bk, int lookahead) {
     const size_t smem = (size_t)(L.block / 32) * EMIT_WARP_WORDS(NW) * 8;
+    if (lookahead == 3) return emit_launch(k_emit_flat<NW>, L, b, k, lad, log2w, ts, t, bk, smem);
     if (lookahead == 2) return emit_launch(k_emit_ladder2<NW>, L, b, k, lad, log2w, ts, t, bk, smem);
     return emit_launch(k_emit_ladder<NW>, L, b, k, lad, log2w, ts, t, bk, smem);
 }
@@ -804,7 +935,9 @@ cudaError_t launch_table_init(int nw, const Launch& L, const TableDev& t) {
         k_table_init<<<L.grid, L.block, 0, L.stream>>>(t.keys, cap * nw, KEY_EMPTY);
         return cudaGetLastError();
     }
-    return cudaMemsetAsync(t.tags, 0, cap * sizeof(uint64_t), L.stream);
+    // tags: their own array, or word 0 of every key (the other words are written
+    // when the slot is claimed)
+    return cudaMemsetAsync(t.tags, 0, cap * sizeof(uint64_t) * t.tag_stride, L.stream);
 }
 
 }  // namespace fbk

@@ -31,12 +31,16 @@ __host__ __device__ inline bool bank_keep(const BankDev& b, uint64_t r) {
 
 // Open-addressing solid table.  NW == 1: keys[] holds the key itself (EMPTY = ~0;
 // a k <= 31 key uses 62 bits).  NW == 2: keys[] holds the two words, claimed with one
-// 16-byte CAS (EMPTY = all ones).  NW == 4: tags[] claims slots (0 empty,
+// 16-byte CAS (EMPTY = all ones).  NW == 4: a tag claims the slot (0 empty,
 // fingerprint, fingerprint|READY once the key words are published) and keys[] holds
-// the four words.  cnt[] holds 8 edge counters (u32) per slot, 32-byte aligned.
+// the four words.  The tag of slot s is tags[s * tag_stride]: for k <= 96 the key's
+// most significant word is always zero, so the tag lives there (tags == keys, stride
+// 4) and one 32-byte sector holds tag and key; for k > 96 tags[] is its own array
+// (stride 1).  cnt[] holds 8 edge counters (u32) per slot, 32-byte aligned.
 struct TableDev {
     uint64_t* keys;
     uint64_t* tags;
+    uint32_t tag_stride;
     uint32_t* cnt;
     uint32_t* cov;       // separate cov counters, only when prior contigs are used
     uint64_t cap;        // slots (any size: home slot = high 64 bits of hash * cap)

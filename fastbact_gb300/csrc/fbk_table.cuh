@@ -70,14 +70,18 @@ __device__ __forceinline__ int64_t table_slot2(const TableDev& t, const Key<2>& 
 template <int NW>
 __device__ __forceinline__ int64_t table_slotw(const TableDev& t, const Key<NW>& key, uint64_t f, uint64_t s, uint32_t* status) {
     const uint64_t fp = (smix(f ^ FP_SALT) | 1ULL) & ~TAG_READY;
+    // with the tag in word 0 (tag_stride == NW) the key's word 0 is zero and not stored
+    const int w0 = t.tag_stride == NW ? 1 : 0;
     for (uint32_t probe = 0; probe < t.max_probe; ++probe) {
-        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> tag_ref(*(unsigned long long*)&t.tags[s]);
+        unsigned long long* tp = (unsigned long long*)&t.tags[s * t.tag_stride];
+        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> tag_ref(*tp);
         uint64_t tag = tag_ref.load(cuda::memory_order_acquire);
         if (tag == 0) {
-            const uint64_t old = atomicCAS((unsigned long long*)&t.tags[s], 0ULL, fp);
+            const uint64_t old = atomicCAS(tp, 0ULL, fp);
             if (old == 0) {
 #pragma unroll
-                for (int i = 0; i < NW; ++i) __stcg(&t.keys[s * NW + i], key.w[i]);
+                for (int i = 0; i < NW; ++i)
+                    if (i >= w0) __stcg(&t.keys[s * NW + i], key.w[i]);
                 tag_ref.fetch_or(TAG_READY, cuda::memory_order_release);
                 return (int64_t)s;
             }
@@ -97,7 +101,8 @@ __device__ __forceinline__ int64_t table_slotw(const TableDev& t, const Key<NW>&
             }
             bool eq = true;
 #pragma unroll
-            for (int i = 0; i < NW; ++i) eq &= (__ldcg(&t.keys[s * NW + i]) == key.w[i]);
+            for (int i = 0; i < NW; ++i)
+                if (i >= w0) eq &= (__ldcg(&t.keys[s * NW + i]) == key.w[i]);
             if (eq) return (int64_t)s;
         }
         s = s + 1 == t.cap ? 0 : s + 1;

@@ -208,6 +208,24 @@ def test_gate_only_with_subsampling(ctx, repeat_isolate):
     compare_gate_only(ctx, bank, 31, 64, 16, None, 16, subsample=(0.35, 1234), keep_mask=keep)
 
 
+@pytest.mark.parametrize("lookahead", [1, 2, 3])
+def test_emit_variants_with_subsampling_and_256_bit_keys(repeat_isolate, lookahead):
+    """Every record-emit form (gate one or two chunks ahead, read by read or over the
+    flattened window stream) with skipped reads and keys of every width, including
+    256-bit keys whose slot tag lives in the key (k <= 96) or apart (k > 96)."""
+    bank = repeat_isolate[0]
+    c = api.Context(0)
+    try:
+        c.set_tuning(emit_lookahead=lookahead)
+        n_pairs = int(max(int(a.pair_idx.max()) for a in bank.arenas if len(a))) + 1
+        keep = api.subsample_mask(c, n_pairs, 0.5, 77)
+        for k, kb in [(21, 64), (33, 128), (77, 256), (101, 256)]:
+            compare_gate_only(c, bank, k, kb, 16, None, 14, subsample=(0.5, 77), keep_mask=keep)
+        compare_gate_only(c, bank, 77, 256, 16, None, 16)
+    finally:
+        c.close()
+
+
 def test_sketch_mode_off_matches(repeat_isolate):
     c = api.Context(0)
     try:
@@ -393,6 +411,7 @@ TUNINGS = [
     dict(load_factor=0.85, block_pass1=128, block_pass2=64, grid_pass1=37, grid_pass2=91),
     dict(ladder_ilp=2, block_pass1=128),                 # two windows per lane in the ladder pass 1
     dict(emit_lookahead=1),                               # gate loads one chunk ahead of the emit
+    dict(emit_lookahead=3),                               # emit over a flattened window stream
 ]
 
 
