@@ -19,8 +19,10 @@
 
 namespace fbk {
 
-template <int NW, int ILP>
-__global__ void __launch_bounds__(256, ILP == 1 ? 4 : 2) k_ladder_pass1(BankDev b, uint32_t k, uint32_t* __restrict__ lad,
+// WS = (64*NW - 2k) / 64 is a template parameter (key words below it are constant
+// zeros).
+template <int NW, int ILP, int WS>
+__global__ void __launch_bounds__(256, ILP == 1 ? 6 : 2) k_ladder_pass1(BankDev b, uint32_t k, uint32_t* __restrict__ lad,
                                                                         uint32_t log2w, uint32_t t, uint32_t* __restrict__ hll12) {
     __shared__ uint32_t s_hll[4096];
     const bool do_hll = hll12 != nullptr;
@@ -56,9 +58,9 @@ __global__ void __launch_bounds__(256, ILP == 1 ? 4 : 2) k_ladder_pass1(BankDev 
 #pragma unroll
                 for (int row = 0; row < 4; ++row) wd[4 * p + row] = mk[4 * p + row] = 0;
                 if (!live[p]) continue;
-                Key<NW> can;
+                Key<NW> can{};
                 bool rc;
-                window_canonical<NW>(b.data, off + q, k, can, rc);
+                canonical_ws<NW, WS>(b.data, off + q, k, can, rc);
                 const uint64_t key = key_fold<NW>(can);
                 h0[p] = smix(key ^ cms_seed(0));
 #pragma unroll
@@ -141,22 +143,36 @@ static int grid_l(K kernel, const Launch& L) {
     return per_sm * (L.sms > 0 ? L.sms : 1);
 }
 
-template <int NW, int ILP>
+template <int NW, int ILP, int WS>
 static cudaError_t lp1(const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t, uint32_t* hll) {
-    k_ladder_pass1<NW, ILP><<<grid_l(k_ladder_pass1<NW, ILP>, L), L.block, 0, L.stream>>>(b, k, lad, log2w, t, hll);
+    k_ladder_pass1<NW, ILP, WS><<<grid_l(k_ladder_pass1<NW, ILP, WS>, L), L.block, 0, L.stream>>>(b, k, lad, log2w, t, hll);
     return cudaGetLastError();
+}
+template <int NW, int ILP>
+static cudaError_t lp1_ws(const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t, uint32_t* hll) {
+    const uint32_t ws = (64u * NW - 2u * k) >> 6;
+    if constexpr (NW == 1) {
+        return lp1<1, ILP, 0>(L, b, k, lad, log2w, t, hll);
+    } else if constexpr (NW == 2) {
+        return ws == 0 ? lp1<2, ILP, 0>(L, b, k, lad, log2w, t, hll) : lp1<2, ILP, 1>(L, b, k, lad, log2w, t, hll);
+    } else {
+        if (ws == 0) return lp1<4, ILP, 0>(L, b, k, lad, log2w, t, hll);
+        if (ws == 1) return lp1<4, ILP, 1>(L, b, k, lad, log2w, t, hll);
+        if (ws == 2) return lp1<4, ILP, 2>(L, b, k, lad, log2w, t, hll);
+        return lp1<4, ILP, 3>(L, b, k, lad, log2w, t, hll);
+    }
 }
 cudaError_t launch_ladder_pass1(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t,
                                 uint32_t* hll12, int ilp) {
     if (t < 1 || t > LADDER_MAX_LEVELS || log2w > 29) return cudaErrorInvalidValue;  // bit indices fit 32 bits
     if (ilp == 2) {
-        if (nw == 1) return lp1<1, 2>(L, b, k, lad, log2w, t, hll12);
-        if (nw == 2) return lp1<2, 2>(L, b, k, lad, log2w, t, hll12);
-        return lp1<4, 2>(L, b, k, lad, log2w, t, hll12);
+        if (nw == 1) return lp1_ws<1, 2>(L, b, k, lad, log2w, t, hll12);
+        if (nw == 2) return lp1_ws<2, 2>(L, b, k, lad, log2w, t, hll12);
+        return lp1_ws<4, 2>(L, b, k, lad, log2w, t, hll12);
     }
-    if (nw == 1) return lp1<1, 1>(L, b, k, lad, log2w, t, hll12);
-    if (nw == 2) return lp1<2, 1>(L, b, k, lad, log2w, t, hll12);
-    return lp1<4, 1>(L, b, k, lad, log2w, t, hll12);
+    if (nw == 1) return lp1_ws<1, 1>(L, b, k, lad, log2w, t, hll12);
+    if (nw == 2) return lp1_ws<2, 1>(L, b, k, lad, log2w, t, hll12);
+    return lp1_ws<4, 1>(L, b, k, lad, log2w, t, hll12);
 }
 
 template <int NW>

@@ -378,8 +378,11 @@ __device__ __forceinline__ bool gate_resolve(const GateLoads& g, bool live) {
     return ok;
 }
 
-template <int NW>
-__global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, const uint32_t* __restrict__ lad, uint32_t log2w,
+// WS = (64*NW - 2k) / 64 is a template parameter: key words below WS are constant
+// zeros, which saves their registers and instructions (k = 77 in 256-bit keys: one
+// word of four).
+template <int NW, int WS>
+__global__ void __launch_bounds__(256, NW == 4 ? 4 : 5) k_emit_ladder2(BankDev b, uint32_t k, const uint32_t* __restrict__ lad, uint32_t log2w,
                                                          uint32_t t_solid, TableDev t, BucketDev bk) {
     extern __shared__ uint64_t emit_smem[];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -400,11 +403,11 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
         const uint32_t nk = len - k + 1;
         const uint32_t n_it = (nk + 31) >> 5;
         // chunks 0 and 1 resolved up front
-        Key<NW> k0, k1;
+        Key<NW> k0{}, k1{};
         bool rc0 = false, rc1 = false;
         const bool l0 = lane < nk, l1 = 32 + lane < nk;
-        if (l0) window_canonical<NW>(b.data, off + lane, k, k0, rc0);
-        if (l1) window_canonical<NW>(b.data, off + 32 + lane, k, k1, rc1);
+        if (l0) canonical_ws<NW, WS>(b.data, off + lane, k, k0, rc0);
+        if (l1) canonical_ws<NW, WS>(b.data, off + 32 + lane, k, k1, rc1);
         GateLoads g0, g1;
         gate_issue(top, log2w, l0 ? key_fold<NW>(k0) : 0, l0, g0);
         gate_issue(top, log2w, l1 ? key_fold<NW>(k1) : 0, l1, g1);
@@ -414,11 +417,11 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
         bool rcc = rc0, rcn = rc1;
         for (uint32_t it = 0; it < n_it; ++it) {
             // issue chunk it + 2
-            Key<NW> kf;
+            Key<NW> kf{};
             bool rcf = false;
             const uint32_t qf = ((it + 2) << 5) + lane;
             const bool lf = qf < nk;
-            if (lf) window_canonical<NW>(b.data, off + qf, k, kf, rcf);
+            if (lf) canonical_ws<NW, WS>(b.data, off + qf, k, kf, rcf);
             GateLoads gf;
             gate_issue(top, log2w, lf ? key_fold<NW>(kf) : 0, lf, gf);
             // emit chunk it
@@ -886,7 +889,20 @@ static cudaError_t emitl_nw(const Launch& L, const BankDev& b, uint32_t k, const
                             const TableDev& t, const BucketDev& bk, int lookahead) {
     const size_t smem = (size_t)(L.block / 32) * EMIT_WARP_WORDS(NW) * 8;
     if (lookahead == 3) return emit_launch(k_emit_flat<NW>, L, b, k, lad, log2w, ts, t, bk, smem);
-    if (lookahead == 2) return emit_launch(k_emit_ladder2<NW>, L, b, k, lad, log2w, ts, t, bk, smem);
+    if (lookahead == 2) {
+        const uint32_t ws = (64u * NW - 2u * k) >> 6;
+        if constexpr (NW == 1) {
+            return emit_launch(k_emit_ladder2<1, 0>, L, b, k, lad, log2w, ts, t, bk, smem);
+        } else if constexpr (NW == 2) {
+            if (ws == 0) return emit_launch(k_emit_ladder2<2, 0>, L, b, k, lad, log2w, ts, t, bk, smem);
+            return emit_launch(k_emit_ladder2<2, 1>, L, b, k, lad, log2w, ts, t, bk, smem);
+        } else {
+            if (ws == 0) return emit_launch(k_emit_ladder2<4, 0>, L, b, k, lad, log2w, ts, t, bk, smem);
+            if (ws == 1) return emit_launch(k_emit_ladder2<4, 1>, L, b, k, lad, log2w, ts, t, bk, smem);
+            if (ws == 2) return emit_launch(k_emit_ladder2<4, 2>, L, b, k, lad, log2w, ts, t, bk, smem);
+            return emit_launch(k_emit_ladder2<4, 3>, L, b, k, lad, log2w, ts, t, bk, smem);
+        }
+    }
     return emit_launch(k_emit_ladder<NW>, L, b, k, lad, log2w, ts, t, bk, smem);
 }
 cudaError_t launch_emit_ladder(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
