@@ -382,7 +382,7 @@ __device__ __forceinline__ bool gate_resolve(const GateLoads& g, bool live) {
 // zeros, which saves their registers and instructions (k = 77 in 256-bit keys: one
 // word of four).
 template <int NW, int WS>
-__global__ void __launch_bounds__(256, NW == 4 ? 4 : 5) k_emit_ladder2(BankDev b, uint32_t k, const uint32_t* __restrict__ lad, uint32_t log2w,
+__global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, const uint32_t* __restrict__ lad, uint32_t log2w,
                                                          uint32_t t_solid, TableDev t, BucketDev bk) {
     extern __shared__ uint64_t emit_smem[];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
