@@ -199,6 +199,31 @@ __device__ __forceinline__ uint64_t nthash_canonical_at(const uint64_t* __restri
     return hf < hr ? hf : hr;
 }
 
+// Canonical ntHash of windows lo .. hi-1 of the read at base off, handed to f(i, h):
+// the first computed as above, each next one rolled from it (kmer.rs:447-464) —
+//   fwd(i+1) = rotl(fwd(i) ^ rotl(F[c_i], k-1), 1) ^ F[c_{i+k}]
+//   rev(i+1) = rotr(rev(i) ^ R[c_i] ^ rotl(R[c_{i+k}], k), 1),   R[c] = F[3-c]
+// exact identities of the XOR-of-rotations definition, so every value equals
+// nthash_canonical_at's.
+template <class Fn>
+__device__ __forceinline__ void nthash_run(const uint64_t* __restrict__ d, uint64_t off, uint32_t k, uint32_t lo, uint32_t hi,
+                                           Fn&& f) {
+    if (lo >= hi) return;
+    uint64_t hf = 0, hr = 0;
+    for (uint32_t j = 0; j < k; ++j) {
+        const uint32_t c = base_at(d, off + lo + j);
+        hf ^= rotl64(nt_fwd(c), (k - 1 - j) & 63);
+        hr ^= rotl64(nt_fwd(3 - c), j & 63);
+    }
+    f(lo, hf < hr ? hf : hr);
+    for (uint32_t i = lo + 1; i < hi; ++i) {
+        const uint32_t co = base_at(d, off + i - 1), ci = base_at(d, off + i - 1 + k);
+        hf = rotl64(hf ^ rotl64(nt_fwd(co), k - 1), 1) ^ nt_fwd(ci);
+        hr = rotr64(hr ^ nt_fwd(3 - co) ^ rotl64(nt_fwd(3 - ci), k), 1);
+        f(i, hf < hr ? hf : hr);
+    }
+}
+
 // Device status bits, read by the host after each phase.
 enum : uint32_t {
     ST_TABLE_FULL = 1u,

@@ -35,15 +35,17 @@ __global__ void __launch_bounds__(256) k_est_firstpos(BankDev b, const uint64_t*
         const uint32_t len = b.len[r];
         if (len < k) continue;
         const uint64_t off = b.off[r], t0 = kbase[r];
-        for (uint32_t i = lane; i < len - k + 1; i += 32) {
-            const uint64_t raw = nthash_canonical_at(b.data, off + i, k);
+        // lane takes a run of consecutive windows and rolls the hash along it
+        const uint32_t nk = len - k + 1, run = (nk + 31) >> 5;
+        const uint32_t lo = lane * run < nk ? lane * run : nk, hi = lo + run < nk ? lo + run : nk;
+        nthash_run(b.data, off, k, lo, hi, [&](uint32_t i, uint64_t raw) {
             const uint32_t t = (uint32_t)(t0 + i);
 #pragma unroll
             for (int rr = 0; rr < 4; ++rr) {
                 uint32_t* p = first + cms_index(raw, rr, log2w);
                 if (*(volatile uint32_t*)p > t) atomicMin(p, t);
             }
-        }
+        });
     }
 }
 
@@ -63,8 +65,9 @@ __global__ void __launch_bounds__(256) k_est_hll(BankDev b, const uint64_t* __re
         if (seg >= n_segs) seg = n_segs - 1;
         uint32_t* rt = regs_total + (uint64_t)seg * m;
         uint32_t* rs = regs_solid + (uint64_t)seg * m;
-        for (uint32_t i = lane; i < len - k + 1; i += 32) {
-            const uint64_t raw = nthash_canonical_at(b.data, off + i, k);
+        const uint32_t nk = len - k + 1, run = (nk + 31) >> 5;
+        const uint32_t lo = lane * run < nk ? lane * run : nk, hi = lo + run < nk ? lo + run : nk;
+        nthash_run(b.data, off, k, lo, hi, [&](uint32_t i, uint64_t raw) {
             const uint32_t t = (uint32_t)(t0 + i);
             bool solid = true;
 #pragma unroll
@@ -74,7 +77,7 @@ __global__ void __launch_bounds__(256) k_est_hll(BankDev b, const uint64_t* __re
             // Registers only grow, so a stale read that is already >= rho is safe to skip.
             if (*(volatile uint32_t*)&rt[idx] < rho) atomicMax(&rt[idx], rho);
             if (solid && *(volatile uint32_t*)&rs[idx] < rho) atomicMax(&rs[idx], rho);
-        }
+        });
     }
 }
 
@@ -201,7 +204,10 @@ __global__ void __launch_bounds__(256) k_nthash_arena(BankDev b, const uint64_t*
     for (uint64_t r = b.r_begin + gw; r < b.r_end; r += nwarps) {
         const uint32_t len = b.len[r];
         if (len < k) continue;
-        for (uint32_t i = lane; i < len - k + 1; i += 32) out[kbase[r] + i] = nthash_canonical_at(b.data, b.off[r] + i, k);
+        const uint32_t nk = len - k + 1, run = (nk + 31) >> 5;
+        const uint32_t lo = lane * run < nk ? lane * run : nk, hi = lo + run < nk ? lo + run : nk;
+        const uint64_t o = kbase[r];
+        nthash_run(b.data, b.off[r], k, lo, hi, [&](uint32_t i, uint64_t h) { out[o + i] = h; });
     }
 }
 
