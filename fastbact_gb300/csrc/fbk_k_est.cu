@@ -93,22 +93,58 @@ __global__ void k_est_prefix(uint32_t* regs, uint64_t m, uint32_t n_segs) {
     }
 }
 
-// One thread per (sketch, segment end): f64 sum of 2^-reg in register order and the
-// number of zero registers (sketch.rs:88-96).  2^-v is built exactly from its bits.
-__global__ void k_est_sums(const uint32_t* regs_total, const uint32_t* regs_solid, uint64_t m, uint32_t n_segs,
-                           double* sums, unsigned long long* zeros) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+// One block per (sketch, segment end): the f64 sum of 2^-reg in register order and
+// the number of zero registers (sketch.rs:88-96).  With m = 2^p registers all <= V =
+// 53 - p, every partial sum of the sequence is a multiple of 2^-V no larger than 2^p,
+// i.e. fits 53 bits: the sequential f64 sum is then exact and equals the integer sum
+// of 2^(V - reg) (taken by the block in any order, at most 2^53) times 2^-V.  A sketch
+// holding a larger register (V = 39 for p = 14: a hash with 39 or more leading zeros
+// after its index bits) is summed sequentially by one thread, in register order, with
+// 2^-v built exactly from its bits.
+__global__ void __launch_bounds__(256) k_est_sums(const uint32_t* regs_total, const uint32_t* regs_solid, uint32_t p,
+                                                  uint32_t n_segs, double* sums, unsigned long long* zeros) {
+    const uint64_t m = 1ULL << p;
+    const uint32_t V = 53 - p;
+    __shared__ unsigned long long s_sum[8], s_zero[8];
+    __shared__ uint32_t s_big;
+    const uint32_t i = blockIdx.x;
     if (i >= 2 * n_segs) return;
     const uint32_t* r = (i < n_segs ? regs_total : regs_solid) + (uint64_t)(i % n_segs) * m;
-    double s = 0.0;
-    unsigned long long z = 0;
-    for (uint64_t j = 0; j < m; ++j) {
+    if (threadIdx.x == 0) s_big = 0;
+    __syncthreads();
+    unsigned long long acc = 0, z = 0;
+    bool big = false;
+    for (uint64_t j = threadIdx.x; j < m; j += blockDim.x) {
         const uint32_t v = r[j];
-        s = __dadd_rn(s, __longlong_as_double((long long)(1023 - (int)v) << 52));
+        big |= v > V;
+        acc += v <= V ? 1ULL << (V - v) : 0ULL;
         z += (v == 0);
     }
+    if (big) atomicOr(&s_big, 1u);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        acc += __shfl_down_sync(0xffffffffu, acc, off);
+        z += __shfl_down_sync(0xffffffffu, z, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_sum[threadIdx.x >> 5] = acc;
+        s_zero[threadIdx.x >> 5] = z;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    unsigned long long tot = 0, tz = 0;
+    for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) {
+        tot += s_sum[w];
+        tz += s_zero[w];
+    }
+    zeros[i] = tz;
+    if (!s_big) {
+        sums[i] = ldexp(__ull2double_rn(tot), -(int)V);  // tot <= 2^53: both steps exact
+        return;
+    }
+    double s = 0.0;
+    for (uint64_t j = 0; j < m; ++j) s = __dadd_rn(s, __longlong_as_double((long long)(1023 - (int)r[j]) << 52));
     sums[i] = s;
-    zeros[i] = z;
 }
 
 // HyperLogLog::add_hash / add_canonical_hash (sketch.rs:49-70) over device hashes.
@@ -253,9 +289,7 @@ cudaError_t launch_est_prefix(const Launch& L, uint32_t* regs, uint32_t p, uint3
 }
 cudaError_t launch_est_sums(const Launch& L, const uint32_t* regs_total, const uint32_t* regs_solid, uint32_t p,
                             uint32_t n_segs, double* sums, unsigned long long* zeros) {
-    const int threads = 64;
-    const int blocks = (int)((2 * n_segs + threads - 1) / threads);
-    k_est_sums<<<blocks, threads, 0, L.stream>>>(regs_total, regs_solid, 1ULL << p, n_segs, sums, zeros);
+    k_est_sums<<<2 * n_segs, 256, 0, L.stream>>>(regs_total, regs_solid, p, n_segs, sums, zeros);
     return cudaGetLastError();
 }
 cudaError_t launch_hll_add(const Launch& L, uint32_t* regs, uint32_t p, const uint64_t* hashes, uint64_t n, int mix) {
