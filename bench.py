@@ -237,8 +237,8 @@ def run_ours(args, rank, world, local):
     ctx.sync()
     torch.cuda.synchronize()
     launches = ctx.launch_count() - launches0
-    kernel_ms = {n: ctx.timing(n) for n in ("pass1", "solid", "pass2_emit", "pass2_upsert", "pass2_direct", "convert",
-                                             "table_init", "est_", "clamp", "cms_clamp", "subsample")}
+    kernel_ms = {n: ctx.timing(n) for n in ("pass1", "solid", "pass2_emit", "pass2_count", "pass2_upsert", "pass2_direct",
+                                             "convert", "table_init", "est_", "clamp", "cms_clamp", "subsample")}
     ctx.set_timing(False)
     if world > 1:
         t = torch.tensor([ms], dtype=torch.float64, device="cuda")
@@ -258,8 +258,8 @@ def run_ours(args, rank, world, local):
     pushes = {k: pu for (k, _, _, pu) in res}
     fam_ms = {
         "pass1": kernel_ms["pass1"][0],
-        "pass2": kernel_ms["solid"][0] + kernel_ms["pass2_emit"][0] + kernel_ms["pass2_upsert"][0]
-                 + kernel_ms["pass2_direct"][0],
+        "pass2": kernel_ms["solid"][0] + kernel_ms["pass2_emit"][0] + kernel_ms["pass2_count"][0]
+                 + kernel_ms["pass2_upsert"][0] + kernel_ms["pass2_direct"][0],
     }
     alg = {
         "pass1": sum(bank_bytes + kmers_pass[k][0] * 8 * c_b for k in KS),
@@ -357,7 +357,8 @@ def run_ours(args, rank, world, local):
             "roofline": {"kernel": ({"pass1": "pass 1 (k_pass1_sweep: 4 row-slice sweeps)",
                                      "pass2": "pass 2 (k_solid_sweep + k_emit + k_upsert)"} if kernel_ms["solid"][0] > 0 else
                                     {"pass1": "pass 1 (k_ladder_pass1: one sweep, t_solid-level gate ladder)",
-                                     "pass2": "pass 2 (k_emit_ladder + k_upsert)"})[dom],
+                                     "pass2": "pass 2 (k_emit_ladder2 + k_count_records + k_upsert)"
+                                     if kernel_ms["pass2_count"][0] > 0 else "pass 2 (k_emit_ladder2 + k_upsert)"})[dom],
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
                          "alg_bytes_per_pass": per_pass_bytes, "ms_per_pass": per_pass_ms,

@@ -178,6 +178,7 @@ SIGNATURES = {
     "fbk_table_export": (S, [vp, u64p, u16p, u8p, C.c_uint64, u64p]),
     "fbk_table_export_acc": (S, [vp, u64p, u16p, u16p, C.c_uint64, u64p]),
     "fbk_table_pushes": (S, [vp, u64p]),
+    "fbk_table_flags": (S, [vp, u32p]),
     "fbk_table_digest": (S, [vp, u64p, u64p]),
     "fbk_table_release": (S, [vp]),
     "fbk_estimator_defaults": (None, [P(EstimatorParams)]),

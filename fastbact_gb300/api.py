@@ -676,6 +676,13 @@ class SolidTable:
                                            C.byref(n)), self.ctx.handle, "table export_acc")
         return sort_rows(keys, cov, edges) if sort else (keys, cov, edges)
 
+    def filtered(self) -> bool:
+        """True when the accumulator holds only keys that may become SolidKmerNodes
+        (keys seen in fewer than min_trans_cov windows were kept out of the table)."""
+        f = C.c_uint32()
+        check(N.lib().fbk_table_flags(self._h, C.byref(f)))
+        return bool(f.value & 1)
+
     def pushes(self) -> int:
         n = C.c_uint64()
         check(N.lib().fbk_table_pushes(self._h, C.byref(n)))

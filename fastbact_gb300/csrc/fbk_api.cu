@@ -307,6 +307,7 @@ FBK_API fbk_status fbk_ctx_fork(fbk_ctx* parent, fbk_ctx** out) {
     c->sketch_mode = parent->sketch_mode;
     c->ladder_ilp = parent->ladder_ilp;
     c->emit_lookahead = parent->emit_lookahead;
+    c->acc_filter = parent->acc_filter;
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_status, 64);
@@ -405,6 +406,7 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "sketch_mode" && (v == 0 || v == 1)) ctx->sketch_mode = (int)v;
     else if (n == "ladder_ilp" && (v == 1 || v == 2)) ctx->ladder_ilp = (int)v;
     else if (n == "emit_lookahead" && v >= 1 && v <= 3) ctx->emit_lookahead = (int)v;
+    else if (n == "acc_filter" && (v == 0 || v == 1)) ctx->acc_filter = (int)v;
     // the pass kernels are compiled for blocks of at most 256 threads
     else if (n == "block_pass1" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_pass1 = (int)v;
     else if (n == "grid_pass1" && v >= 0) ctx->grid_pass1 = (int)v;
@@ -426,6 +428,7 @@ FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, doub
     else if (n == "sketch_mode") *v = ctx->sketch_mode;
     else if (n == "ladder_ilp") *v = ctx->ladder_ilp;
     else if (n == "emit_lookahead") *v = ctx->emit_lookahead;
+    else if (n == "acc_filter") *v = ctx->acc_filter;
     else if (n == "block_pass1") *v = ctx->block_pass1;
     else if (n == "grid_pass1") *v = ctx->grid_pass1;
     else if (n == "block_pass2") *v = ctx->block_pass2;
@@ -1134,7 +1137,7 @@ static fbk_status table_convert(fbk_table* t, uint64_t* acc_keys, uint16_t* acc_
         t->n_keys = h[0];
         t->n_solid = h[1];
         t->digest = h[2];
-        t->pushes = h[3];
+        t->pushes = h[3] + t->skipped_pushes;
         if (t->n_solid <= t->out_cap) return FBK_OK;
         table_free_out(t);
         uint64_t cap = t->n_solid + 1024;
@@ -1255,6 +1258,21 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
         }
     } bmg{ctx, &bm};
     const bool inline_gate = lad && ctx->pass2_mode == 1;
+    struct DevBuf {
+        fbk_ctx* c = nullptr;
+        void* p = nullptr;
+        void alloc(fbk_ctx* ctx, uint64_t bytes) {
+            if (!p) {
+                c = ctx;
+                p = dev_alloc(ctx, bytes);
+            }
+        }
+        ~DevBuf() {
+            if (!p) return;
+            cudaStreamSynchronize(c->stream);
+            dev_free(c, p);
+        }
+    } fbuf;
     auto need_bitmap = [&]() -> fbk_status {
         if (bm) return FBK_OK;
         fbk_status s2 = solidity_bitmap(ctx, b, cms, p, nw, keep_bits, &bm, lad);
@@ -1302,6 +1320,22 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
         Buckets bk;
         const bool use_buckets = max_records && ctx->pass2_mode == 1;
         st = use_buckets ? buckets_alloc(ctx, cap, slot_bytes, nw, max_records, bk) : FBK_OK;
+        // the record filter needs every record of the pass in one bucket pass: one
+        // read chunk and no prior contigs (their pushes weigh 1000)
+        RecordFilter flt{};
+        const bool filter = st == FBK_OK && use_buckets && ctx->acc_filter && !contigs && b->chunk_starts.size() == 2 &&
+                            p->min_trans_cov >= 2;
+        if (filter) {
+            uint32_t log2m = 10;
+            while (log2m < 22 && (1ULL << log2m) < max_records / bk.d.n_buckets) ++log2m;
+            fbuf.alloc(ctx, (2ULL << log2m) * 4 + 8);
+            if (!fbuf.p) st = set_err(ctx, FBK_ERR_OOM, "pass-2 record filter");
+            flt.cnt = (uint32_t*)fbuf.p;
+            flt.log2m = log2m;
+            flt.min_records = p->min_trans_cov;
+            flt.skipped = (unsigned long long*)((char*)fbuf.p + (2ULL << log2m) * 4);
+            if (st == FBK_OK) CK(ctx, cudaMemsetAsync(flt.skipped, 0, 8, ctx->stream));
+        }
         if (st) {
             table_free_storage(t);
             table_free_out(t);
@@ -1319,14 +1353,26 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
                                                                      ctx->emit_lookahead));
             else
                 TIMED(ctx, "pass2_emit", launch_emit(nw, L, bv, p->k, bm, 1, td, bk.d));
-            for (uint32_t bu = 0; bu < bk.d.n_buckets; ++bu)
-                TIMED(ctx, "pass2_upsert", launch_upsert(nw, L, bk.d, bu, 1, 1, td, ctx->d_status));
+            for (uint32_t bu = 0; bu < bk.d.n_buckets; ++bu) {
+                if (filter) {
+                    CK(ctx, cudaMemsetAsync(flt.cnt, 0, (2ULL << flt.log2m) * 4, ctx->stream));
+                    TIMED(ctx, "pass2_count", launch_count_records(nw, L, bk.d, bu, flt));
+                }
+                TIMED(ctx, "pass2_upsert", launch_upsert(nw, L, bk.d, bu, 1, 1, td, ctx->d_status, flt));
+            }
         }
         uint32_t ovf = use_buckets ? 0 : 1;  // without buckets every chunk takes the direct sweep
+        t->filtered = false;
+        t->skipped_pushes = 0;
         if (use_buckets) {
             CK(ctx, cudaMemcpyAsync(ctx->h_pinned, bk.overflow, 4, cudaMemcpyDeviceToHost, ctx->stream));
+            if (filter) CK(ctx, cudaMemcpyAsync((char*)ctx->h_pinned + 8, flt.skipped, 8, cudaMemcpyDeviceToHost, ctx->stream));
             CK(ctx, cudaStreamSynchronize(ctx->stream));
             ovf = *(uint32_t*)ctx->h_pinned;
+            if (filter && !ovf) {
+                t->filtered = true;
+                t->skipped_pushes = *(uint64_t*)((char*)ctx->h_pinned + 8);
+            }
         }
         if (ovf && max_records) {
             st = need_bitmap();
@@ -1557,6 +1603,12 @@ FBK_API fbk_status fbk_table_export_acc(fbk_table* t, uint64_t* keys, uint16_t* 
     dev_free(ctx, de);
     *n_out = t->n_keys;
     return st;
+}
+
+FBK_API fbk_status fbk_table_flags(const fbk_table* t, uint32_t* flags) {
+    if (!t || !flags) return FBK_ERR_INVALID;
+    *flags = t->filtered ? FBK_TABLE_ACC_FILTERED : 0u;
+    return FBK_OK;
 }
 
 FBK_API fbk_status fbk_table_pushes(const fbk_table* t, uint64_t* pushes) {

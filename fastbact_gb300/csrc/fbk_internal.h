@@ -75,6 +75,7 @@ struct fbk_ctx {
     int sketch_mode = 1;                  // 1: a build that does not return its sketch keeps only the gate ladder
     int ladder_ilp = 1;                   // windows per lane per step in the ladder pass 1 (1 or 2)
     int emit_lookahead = 2;               // record emit: gate loads 1 or 2 chunks ahead; 3 = 2 ahead over a flattened window stream
+    int acc_filter = 1;                   // 1: keys with fewer records than min_trans_cov stay out of the table
     bool capturing = false;               // launches are being captured into a CUDA graph
 };
 
@@ -131,6 +132,8 @@ struct fbk_table {
     uint8_t* out_mask = nullptr;
     uint64_t out_cap = 0;
     uint64_t n_keys = 0, n_solid = 0, digest = 0, pushes = 0;
+    uint64_t skipped_pushes = 0;  // pushes of records the record filter kept out of the table
+    bool filtered = false;        // the accumulator holds only keys that may become solid
 };
 
 namespace fbk {

@@ -602,10 +602,8 @@ __global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, con
 // home slot and adds the pushes.  (Taking two records per thread and issuing both
 // home-slot loads first measured 18% slower: register pressure cost more occupancy
 // than the overlap gained.)
-template <int NW>
-__global__ void __launch_bounds__(256) k_upsert(BucketDev bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov, TableDev t,
-                                                uint32_t* status) {
-    __shared__ unsigned long long s_pre[257];
+// Stripe prefix of one bucket's record counts (shared), and the address of record i.
+__device__ __forceinline__ uint64_t bucket_prefix(const BucketDev& bk, uint32_t bucket, unsigned long long* s_pre) {
     const uint32_t S = bk.stripes;  // <= 256
     if (threadIdx.x == 0) {
         unsigned long long acc = 0;
@@ -617,20 +615,75 @@ __global__ void __launch_bounds__(256) k_upsert(BucketDev bk, uint32_t bucket, u
         s_pre[S] = acc;
     }
     __syncthreads();
-    const uint64_t n = s_pre[S];
+    return s_pre[S];
+}
+template <int NW>
+__device__ __forceinline__ const uint64_t* bucket_record(const BucketDev& bk, uint32_t bucket, const unsigned long long* s_pre,
+                                                         uint64_t i) {
+    uint32_t lo = 0, hi = bk.stripes;  // stripe: last s with s_pre[s] <= i
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_pre[mid] <= i) lo = mid;
+        else hi = mid;
+    }
+    return bk.recs + (((uint64_t)bucket * bk.stripes + lo) * bk.stripe_cap + (i - s_pre[lo])) * (NW + 1);
+}
+
+// Keys that cannot become SolidKmerNodes can stay out of the table when the caller
+// does not need the whole accumulator: edge counter e of a key grows by at most one
+// per record of the key (a record pushes two different edges), so a key with fewer
+// than min_trans_cov records has an empty mask (build.rs:306-314).  Before a bucket's
+// upserts, k_count_records adds 1 per record to two rows of counters; every record of
+// a key lies in the same bucket and hits the same two counters, so the smaller one
+// bounds the key's records from above, and the upsert skips the records whose bound
+// is below min_trans_cov.  Exact when the bucket holds every record of the pass (one
+// read chunk, no prior contigs, whose pushes weigh more than 1).
+constexpr uint64_t FILTER_SALT = 0x3c6ef372fe94f82bULL;
+__device__ __forceinline__ void filter_cols(uint64_t fold, uint32_t log2m, uint32_t& c0, uint32_t& c1) {
+    const uint64_t h = smix(fold ^ FILTER_SALT);
+    const uint32_t m = (1u << log2m) - 1;
+    c0 = (uint32_t)h & m;
+    c1 = ((uint32_t)(h >> 32) & m) + (1u << log2m);
+}
+
+template <int NW>
+__global__ void __launch_bounds__(256) k_count_records(BucketDev bk, uint32_t bucket, RecordFilter flt) {
+    __shared__ unsigned long long s_pre[257];
+    const uint64_t n = bucket_prefix(bk, bucket, s_pre);
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t lo = 0, hi = S;  // stripe: last s with s_pre[s] <= i
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (s_pre[mid] <= i) lo = mid;
-            else hi = mid;
-        }
-        const uint64_t* rec = bk.recs + (((uint64_t)bucket * S + lo) * bk.stripe_cap + (i - s_pre[lo])) * (NW + 1);
+        const uint64_t* rec = bucket_record<NW>(bk, bucket, s_pre, i);
+        Key<NW> key;
+#pragma unroll
+        for (int j = 0; j < NW; ++j) key.w[j] = __ldcg(rec + j);
+        uint32_t c0, c1;
+        filter_cols(key_fold<NW>(key), flt.log2m, c0, c1);
+        atomicAdd(flt.cnt + c0, 1u);
+        atomicAdd(flt.cnt + c1, 1u);
+    }
+}
+
+template <int NW>
+__global__ void __launch_bounds__(256) k_upsert(BucketDev bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov, TableDev t,
+                                                uint32_t* status, RecordFilter flt) {
+    __shared__ unsigned long long s_pre[257];
+    const uint64_t n = bucket_prefix(bk, bucket, s_pre);
+    unsigned long long skipped = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t* rec = bucket_record<NW>(bk, bucket, s_pre, i);
         Key<NW> key;
 #pragma unroll
         for (int j = 0; j < NW; ++j) key.w[j] = __ldcs(rec + j);
         const uint32_t info = (uint32_t)__ldcs(rec + NW);
         const uint64_t f = key_fold<NW>(key);
+        if (flt.cnt) {
+            uint32_t c0, c1;
+            filter_cols(f, flt.log2m, c0, c1);
+            const uint32_t a = __ldcg(flt.cnt + c0), b = __ldcg(flt.cnt + c1);
+            if ((a < b ? a : b) < flt.min_records) {
+                skipped += ((info >> 3) & 1u) + ((info >> 7) & 1u);
+                continue;
+            }
+        }
         const uint64_t home = home_slot(f, t.cap);
         int64_t s;
         if constexpr (NW == 1) s = table_slot1(t, key.w[0], home, status);
@@ -642,6 +695,11 @@ __global__ void __launch_bounds__(256) k_upsert(BucketDev bk, uint32_t bucket, u
         if (nu) atomicAdd(&c[info & 7u], w_edge);
         if (nv) atomicAdd(&c[(info >> 4) & 7u], w_edge);
         if (t.cov) atomicAdd(&t.cov[s], w_cov * (nu + nv));
+    }
+    if (flt.cnt) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) skipped += __shfl_down_sync(0xffffffffu, skipped, off);
+        if ((threadIdx.x & 31) == 0 && skipped) atomicAdd(flt.skipped, skipped);
     }
 }
 
@@ -922,15 +980,27 @@ cudaError_t launch_emit(int nw, const Launch& L, const BankDev& b, uint32_t k, c
 
 template <int NW>
 static cudaError_t upsert_nw(const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t we, uint32_t wc, const TableDev& t,
-                             uint32_t* status) {
-    k_upsert<NW><<<grid_for(k_upsert<NW>, L), L.block, 0, L.stream>>>(bk, bucket, we, wc, t, status);
+                             uint32_t* status, const RecordFilter& flt) {
+    k_upsert<NW><<<grid_for(k_upsert<NW>, L), L.block, 0, L.stream>>>(bk, bucket, we, wc, t, status, flt);
     return cudaGetLastError();
 }
 cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov,
-                          const TableDev& t, uint32_t* status) {
-    if (nw == 1) return upsert_nw<1>(L, bk, bucket, w_edge, w_cov, t, status);
-    if (nw == 2) return upsert_nw<2>(L, bk, bucket, w_edge, w_cov, t, status);
-    return upsert_nw<4>(L, bk, bucket, w_edge, w_cov, t, status);
+                          const TableDev& t, uint32_t* status, const RecordFilter& flt) {
+    if (flt.cnt && (flt.log2m < 8 || flt.log2m > 30)) return cudaErrorInvalidValue;
+    if (nw == 1) return upsert_nw<1>(L, bk, bucket, w_edge, w_cov, t, status, flt);
+    if (nw == 2) return upsert_nw<2>(L, bk, bucket, w_edge, w_cov, t, status, flt);
+    return upsert_nw<4>(L, bk, bucket, w_edge, w_cov, t, status, flt);
+}
+template <int NW>
+static cudaError_t count_nw(const Launch& L, const BucketDev& bk, uint32_t bucket, const RecordFilter& flt) {
+    k_count_records<NW><<<grid_for(k_count_records<NW>, L), L.block, 0, L.stream>>>(bk, bucket, flt);
+    return cudaGetLastError();
+}
+cudaError_t launch_count_records(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, const RecordFilter& flt) {
+    if (!flt.cnt || flt.log2m < 8 || flt.log2m > 30) return cudaErrorInvalidValue;
+    if (nw == 1) return count_nw<1>(L, bk, bucket, flt);
+    if (nw == 2) return count_nw<2>(L, bk, bucket, flt);
+    return count_nw<4>(L, bk, bucket, flt);
 }
 
 cudaError_t launch_convert(int nw, const Launch& L, const TableDev& t, uint32_t min_trans_cov, const ConvOut& o) {

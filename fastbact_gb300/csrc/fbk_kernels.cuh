@@ -62,6 +62,15 @@ struct BucketDev {
     uint32_t* overflow;          // set when a stripe runs out of room
 };
 
+// Record filter of pass 2 (see k_count_records): two rows of 2^log2m counters, the
+// threshold, and where the pushes of skipped records are counted.
+struct RecordFilter {
+    uint32_t* cnt;                 // nullptr: no filter
+    uint32_t log2m;
+    uint32_t min_records;
+    unsigned long long* skipped;  // pushes of the records the upsert skipped
+};
+
 // Output of the SolidKmerNode conversion.
 struct ConvOut {
     uint64_t* keys;             // n_solid * NW words
@@ -119,7 +128,8 @@ cudaError_t launch_pass2_sweep(int nw, const Launch& L, const BankDev& b, uint32
 cudaError_t launch_emit(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* bm, int gate, const TableDev& t,
                         const BucketDev& bk);
 cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov,
-                          const TableDev& t, uint32_t* status);
+                          const TableDev& t, uint32_t* status, const RecordFilter& flt = RecordFilter{});
+cudaError_t launch_count_records(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, const RecordFilter& flt);
 cudaError_t launch_convert(int nw, const Launch& L, const TableDev& t, uint32_t min_trans_cov, const ConvOut& o);
 cudaError_t launch_clamp_counters(const Launch& L, uint32_t* cnt, uint64_t n);
 cudaError_t launch_table_init(int nw, const Launch& L, const TableDev& t);

@@ -251,7 +251,14 @@ class DeviceEngine:
     def pass2(self, bank, k, key_bits, target_solid_cov):
         from . import api
 
-        t = api.solid_build(self.ctx, self.dbank, self.cms, k, target_solid_cov, key_bits=key_bits)
+        # the owners sum the ranks' accumulators: every accumulated key is needed, not
+        # only those that may become solid in this rank's share
+        prev = self.ctx.get_tuning("acc_filter")
+        self.ctx.set_tuning(acc_filter=0)
+        try:
+            t = api.solid_build(self.ctx, self.dbank, self.cms, k, target_solid_cov, key_bits=key_bits)
+        finally:
+            self.ctx.set_tuning(acc_filter=prev)
         keys, cov, edges = t.export_acc(sort=False)
         t.release()
         self.cms.release()

@@ -159,7 +159,12 @@ FBK_API fbk_status fbk_ctx_event_elapsed(fbk_ctx* ctx, int slot_a, int slot_b, d
  * "record_factor" (record capacity over the expected count; a full bucket falls back
  * to the direct sweep),
  * "block_pass1", "grid_pass1", "block_pass2", "grid_pass2" (blocks of 32..256 threads in
- * steps of 32; grid 0 = occupancy). */
+ * steps of 32; grid 0 = occupancy), "sketch_mode" (1: a build that does not return its
+ * sketch keeps only a threshold-ladder gate; 0: counted sketch), "ladder_ilp" (1 or 2
+ * windows per lane in the ladder pass 1), "emit_lookahead" (record emit with the gate
+ * loads 1 or 2 chunks ahead, 3 = 2 ahead over a flattened window stream), "acc_filter"
+ * (1: keys that cannot become SolidKmerNodes stay out of the table, see
+ * fbk_table_flags).  Results do not depend on any of them. */
 FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double value);
 FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, double* value);
 /* Number of kernels launched on this context since creation. */
@@ -168,8 +173,9 @@ FBK_API fbk_status fbk_ctx_mem_info(const fbk_ctx* ctx, uint64_t* pool_used, uin
 
 /* ---- read bank (ReadBank, src/common/bitseq.rs:350-399) ---------------------- */
 /* arenas[0..3] = merged_reads, pe_forward, pe_reverse (iteration order of
- * build.rs:90).  Copies host data to the device (pinned host memory is copied
- * asynchronously on the context stream). */
+ * build.rs:90).  Copies host data to the device (page-locked host memory is copied
+ * asynchronously on the context stream; larger pageable buffers through pinned
+ * staging, after which the host buffers may be reused at once). */
 FBK_API fbk_status fbk_bank_upload(fbk_ctx* ctx, const fbk_arena_view arenas[3], fbk_bank** out);
 FBK_API fbk_status fbk_bank_info(const fbk_bank* b, uint64_t* n_reads, uint64_t* n_bases);
 FBK_API fbk_status fbk_bank_release(fbk_bank* b);
@@ -231,6 +237,17 @@ FBK_API fbk_status fbk_build_front(fbk_ctx* ctx, const fbk_bank* b, const fbk_bu
                                    fbk_table** out, fbk_cms** cms_out);
 /* n_keys: accumulated keys; n_solid: SolidKmerNode entries (mask != 0). */
 FBK_API fbk_status fbk_table_info(const fbk_table* t, uint64_t* n_keys, uint64_t* n_solid, uint64_t* capacity);
+/* FBK_TABLE_ACC_FILTERED: the accumulator holds only the keys that may become
+ * SolidKmerNodes.  A key's edge counter grows by at most one per window of the key,
+ * so a key seen in fewer than min_trans_cov windows has an empty mask; with the
+ * tuning acc_filter = 1 (default) such keys are kept out of the table when the pass
+ * runs in one read chunk without prior contigs.  The SolidKmerNode rows, their
+ * digest and fbk_table_pushes are unchanged; n_keys and fbk_table_export_acc cover
+ * the kept keys only (each with its exact KmerAcc), a superset of the keys with
+ * mask != 0.  Callers that need every accumulated key (e.g. to sum accumulators
+ * across ranks) set acc_filter = 0. */
+#define FBK_TABLE_ACC_FILTERED 1u
+FBK_API fbk_status fbk_table_flags(const fbk_table* t, uint32_t* flags);
 /* Converted entries in device order (unsorted): keys (key_bits/64 big-endian words
  * each), cov, mask.  cap = rows the buffers hold. */
 FBK_API fbk_status fbk_table_export(fbk_table* t, uint64_t* keys, uint16_t* cov, uint8_t* mask, uint64_t cap, uint64_t* n_out);

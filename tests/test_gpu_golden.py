@@ -46,14 +46,27 @@ def test_golden_isolate_estimate_and_builds(ctx):
                                             ge["subsample_factor"], ge["sample_kmer_depth"], ge["confidence"],
                                             ge["pairs_sampled"], ge["m_sample"])
     assert mg.sha(rt) == ge["regs_total_sha256"] and mg.sha(rs) == ge["regs_solid_sha256"]
-    for name, exp in GOLDEN["builds"].items():
-        k, kb, cb, tsc = name.split("_")
-        k, kb, cb = int(k[1:]), int(kb[1:]), int(cb[1:])
-        tsc = None if tsc == "tNone" else int(tsc[1:])
-        t, cms = api.build_cdbg_with_contigs_ext(bank, [], k, tsc, None, ctx=ctx, key_bits=kb, counter_bits=cb,
-                                                 cms_log2_width=15, keep_cms=True)
-        assert mg.sha(cms.export()) == exp["cms_sha256"], name
-        keys, cov, edges = t.export_acc(sort=True)
-        assert (int(keys.shape[0]), mg.sha(keys), mg.sha(cov), mg.sha(edges)) == \
-               (exp["n_keys"], exp["acc_keys_sha256"], exp["acc_cov_sha256"], exp["acc_edges_sha256"]), name
-        assert t.digest() == (exp["digest"], exp["n_solid"]), name
+    prev = ctx.get_tuning("acc_filter")
+    try:
+        for name, exp in GOLDEN["builds"].items():
+            k, kb, cb, tsc = name.split("_")
+            k, kb, cb = int(k[1:]), int(kb[1:]), int(cb[1:])
+            tsc = None if tsc == "tNone" else int(tsc[1:])
+            # every accumulated key (the fixtures hash the whole accumulator) ...
+            ctx.set_tuning(acc_filter=0)
+            t, cms = api.build_cdbg_with_contigs_ext(bank, [], k, tsc, None, ctx=ctx, key_bits=kb, counter_bits=cb,
+                                                     cms_log2_width=15, keep_cms=True)
+            assert mg.sha(cms.export()) == exp["cms_sha256"], name
+            keys, cov, edges = t.export_acc(sort=True)
+            assert (int(keys.shape[0]), mg.sha(keys), mg.sha(cov), mg.sha(edges)) == \
+                   (exp["n_keys"], exp["acc_keys_sha256"], exp["acc_cov_sha256"], exp["acc_edges_sha256"]), name
+            assert t.digest() == (exp["digest"], exp["n_solid"]), name
+            t.release()
+            # ... and the default build, whose SolidKmerNode rows are the same
+            ctx.set_tuning(acc_filter=1)
+            t = api.build_cdbg_with_contigs_ext(bank, [], k, tsc, None, ctx=ctx, key_bits=kb, counter_bits=cb,
+                                                cms_log2_width=15)
+            assert t.digest() == (exp["digest"], exp["n_solid"]), name
+            t.release()
+    finally:
+        ctx.set_tuning(acc_filter=prev)

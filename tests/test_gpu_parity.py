@@ -149,6 +149,29 @@ def test_hll_registers_and_estimate(ctx, p):
 # ---------------------------------------------------------------------------
 # build front end
 # ---------------------------------------------------------------------------
+def row_view(keys: np.ndarray) -> np.ndarray:
+    keys = np.ascontiguousarray(keys)
+    return keys.view(np.dtype((np.void, keys.shape[1] * 8))).ravel()
+
+
+def assert_acc_matches(table, o_tab, mtc):
+    """The accumulated keys (KmerAcc rows) equal the oracle's; for a table built with
+    the record filter they are a subset of the oracle's rows, identical where present,
+    that holds every key with an edge count >= min_trans_cov."""
+    gk, gc, ge = table.export_acc(sort=True)
+    ok, oc, oe = api.sort_rows(*o_tab.export_acc())
+    if not table.filtered():
+        assert gk.shape == ok.shape, (gk.shape, ok.shape)
+        assert np.array_equal(gk, ok) and np.array_equal(gc, oc) and np.array_equal(ge, oe)
+        return
+    gv, ov = row_view(gk), row_view(ok)
+    common, gi, oi = np.intersect1d(gv, ov, return_indices=True)
+    assert len(common) == len(gv), "a kept key is not an accumulated key of the oracle"
+    assert np.array_equal(gc[gi], oc[oi]) and np.array_equal(ge[gi], oe[oi])
+    need = (oe.astype(np.int64) >= mtc).any(axis=1)
+    assert np.isin(ov[need], gv).all(), "a key with an edge count >= min_trans_cov was filtered out"
+
+
 def compare_build(ctx, bank, k, kb, cb, tsc, log2w, contigs=None, subsample=None, keep_mask=None):
     dbank = api.DeviceBank(ctx, bank)
     table, cms = api.build_cdbg_with_contigs_ext(dbank, contigs or [], k, tsc, None, ctx=ctx, key_bits=kb,
@@ -157,10 +180,7 @@ def compare_build(ctx, bank, k, kb, cb, tsc, log2w, contigs=None, subsample=None
     o_cms, o_tab, t_solid, mtc = orc.build_front(bank, k, kb, log2w, cb, tsc, threads=4, keep_mask=keep_mask,
                                                  contigs=contigs)
     assert np.array_equal(cms.export(), o_cms.export()), "pass-1 CMS bytes differ"
-    gk, gc, ge = table.export_acc(sort=True)
-    ok, oc, oe = api.sort_rows(*o_tab.export_acc())
-    assert gk.shape == ok.shape, (gk.shape, ok.shape)
-    assert np.array_equal(gk, ok) and np.array_equal(gc, oc) and np.array_equal(ge, oe)
+    assert_acc_matches(table, o_tab, mtc)
     sk, sc, sm = table.export(sort=True)
     xk, xc, xm = api.sort_rows(*o_tab.export_solid(mtc))
     assert np.array_equal(sk, xk) and np.array_equal(sc, xc) and np.array_equal(sm, xm)
@@ -174,10 +194,7 @@ def compare_gate_only(ctx, bank, k, kb, cb, tsc, log2w, subsample=None, keep_mas
     table = api.build_cdbg_with_contigs_ext(bank, [], k, tsc, None, ctx=ctx, key_bits=kb, counter_bits=cb,
                                             cms_log2_width=log2w, subsample=subsample)
     _, o_tab, _, mtc = orc.build_front(bank, k, kb, log2w, cb, tsc, threads=4, keep_mask=keep_mask)
-    gk, gc, ge = table.export_acc(sort=True)
-    ok, oc, oe = api.sort_rows(*o_tab.export_acc())
-    assert gk.shape == ok.shape, (gk.shape, ok.shape)
-    assert np.array_equal(gk, ok) and np.array_equal(gc, oc) and np.array_equal(ge, oe)
+    assert_acc_matches(table, o_tab, mtc)
     sk, sc, sm = table.export(sort=True)
     xk, xc, xm = api.sort_rows(*o_tab.export_solid(mtc))
     assert np.array_equal(sk, xk) and np.array_equal(sc, xc) and np.array_equal(sm, xm)
@@ -222,6 +239,36 @@ def test_emit_variants_with_subsampling_and_256_bit_keys(repeat_isolate, lookahe
         for k, kb in [(21, 64), (33, 128), (77, 256), (101, 256)]:
             compare_gate_only(c, bank, k, kb, 16, None, 14, subsample=(0.5, 77), keep_mask=keep)
         compare_gate_only(c, bank, 77, 256, 16, None, 16)
+    finally:
+        c.close()
+
+
+@pytest.mark.parametrize("k,kb", [(21, 64), (45, 128), (77, 256), (101, 256)])
+def test_record_filter_keeps_the_solid_rows(repeat_isolate, k, kb):
+    """With the record filter (default) the table holds fewer keys, and the
+    SolidKmerNode rows, digest and push count equal the unfiltered build's."""
+    bank = repeat_isolate[0]
+    c = api.Context(0)
+    try:
+        out = {}
+        for f in (1, 0):
+            c.set_tuning(acc_filter=f)
+            for tsc in (None, 2, 5):
+                t = api.build_cdbg_with_contigs_ext(bank, [], k, tsc, None, ctx=c, key_bits=kb, counter_bits=16,
+                                                    cms_log2_width=14)
+                out[f, tsc] = (t.filtered(), t.info()[0], t.export(sort=True), t.digest(), t.pushes())
+                t.release()
+        for tsc in (None, 2, 5):
+            on, off = out[1, tsc], out[0, tsc]
+            assert on[0] and not off[0]
+            assert on[1] < off[1]
+            assert all(np.array_equal(a, b) for a, b in zip(on[2], off[2]))
+            assert on[3] == off[3] and on[4] == off[4]
+        # min_trans_cov = 1 cannot filter anything
+        c.set_tuning(acc_filter=1)
+        t = api.build_cdbg_with_contigs_ext(bank, [], k, 1, None, ctx=c, key_bits=kb, counter_bits=16, cms_log2_width=14)
+        assert not t.filtered()
+        t.release()
     finally:
         c.close()
 
@@ -412,6 +459,7 @@ TUNINGS = [
     dict(ladder_ilp=2, block_pass1=128),                 # two windows per lane in the ladder pass 1
     dict(emit_lookahead=1),                               # gate loads one chunk ahead of the emit
     dict(emit_lookahead=3),                               # emit over a flattened window stream
+    dict(acc_filter=0),                                   # every accumulated key kept
 ]
 
 
