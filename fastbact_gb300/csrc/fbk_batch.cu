@@ -531,6 +531,36 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
     st = upload_wave(B, V, w);
     if (st) return st;
     const uint32_t k = B->p.k;
+    // record filter (see k_count_records): one pair of counter rows serves the wave's
+    // bucket upserts in turn; isolates whose reads span several chunks go unfiltered
+    std::vector<RecordFilter> flt(n);
+    uint32_t log2m_max = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const BatchIso* it = V[i];
+        if (!ctx->acc_filter || B->p.min_trans_cov < 2 || it->bank->chunk_starts.size() != 2) continue;
+        uint32_t log2m = 10;
+        while (log2m < 22 && (1ULL << log2m) < it->records / std::max<uint32_t>(1, it->bk.n_buckets)) ++log2m;
+        flt[i].log2m = log2m;
+        flt[i].min_records = B->p.min_trans_cov;
+        flt[i].skipped = w.cnt + 8 * i;  // word 0 of the isolate's counters is free in phase B
+        log2m_max = std::max(log2m_max, log2m);
+    }
+    struct FilterBuf {
+        fbk_ctx* c;
+        uint32_t* p = nullptr;
+        ~FilterBuf() {
+            if (p) {
+                cudaStreamSynchronize(c->stream);
+                dev_free(c, p);
+            }
+        }
+    } fbuf{ctx};
+    if (log2m_max) {
+        fbuf.p = (uint32_t*)dev_alloc(ctx, (2ULL << log2m_max) * 4);
+        if (!fbuf.p) return set_err(ctx, FBK_ERR_OOM, "batch record filter");
+        for (uint32_t i = 0; i < n; ++i)
+            if (flt[i].log2m) flt[i].cnt = fbuf.p;
+    }
     st = run_phase(B, &B->stats.ms_phase_b, [&]() -> fbk_status {
         CK(ctx, cudaMemsetAsync(w.cnt, 0, (uint64_t)n * 64, ctx->stream));
         CK(ctx, cudaMemsetAsync(w.status, 0, (uint64_t)n * 8, ctx->stream));
@@ -557,9 +587,14 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
             BatchIso* it = V[i];
             BucketDev bk = it->bk;
             bk.overflow = w.status + 2 * i + 1;
-            for (uint32_t bu = 0; bu < bk.n_buckets; ++bu)
+            for (uint32_t bu = 0; bu < bk.n_buckets; ++bu) {
+                if (flt[i].cnt) {
+                    CK(ctx, cudaMemsetAsync(flt[i].cnt, 0, (2ULL << flt[i].log2m) * 4, ctx->stream));
+                    TIMED(ctx, "batch_filter", launch_count_records(B->nw, shape_launch(ctx, B->upsert), bk, bu, flt[i]));
+                }
                 TIMED(ctx, "batch_upsert", launch_upsert(B->nw, shape_launch(ctx, B->upsert), bk, bu, 1, 1, tbl_dev(it->table),
-                                                         w.status + 2 * i));
+                                                         w.status + 2 * i, flt[i]));
+            }
         }
         for (uint32_t i = 0; i < n; ++i) {
             fbk_table* t = V[i]->table;
@@ -598,7 +633,9 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
             t->n_keys = counts[8 * i + 3];
             t->n_solid = counts[8 * i + 4];
             t->digest = counts[8 * i + 5];
-            t->pushes = counts[8 * i + 6];
+            t->skipped_pushes = counts[8 * i + 0];
+            t->pushes = counts[8 * i + 6] + t->skipped_pushes;
+            t->filtered = flt[i].cnt != nullptr;
             free_buckets(B, it);
             if (t->n_solid > t->out_cap) {
                 st = tbl_convert(t);
