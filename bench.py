@@ -471,7 +471,7 @@ def run_batch_mode(args):
 
     # ---- diagnostics: per-kernel device time of both paths (stream launches, events) --
     fams = ("batch_pass1", "batch_solid", "batch_count", "batch_emit", "batch_prefix", "batch_filter", "batch_upsert", "pass1", "solid",
-            "pass2_emit", "pass2_upsert", "pass2_direct", "table_init", "convert", "est_", "subsample", "clamp")
+            "pass2_emit", "pass2_count", "pass2_upsert", "pass2_direct", "table_init", "convert", "est_", "subsample", "clamp")
 
     def timed_families(fn):
         ctx.sync()

@@ -406,7 +406,7 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "sketch_mode" && (v == 0 || v == 1)) ctx->sketch_mode = (int)v;
     else if (n == "ladder_ilp" && (v == 1 || v == 2)) ctx->ladder_ilp = (int)v;
     else if (n == "emit_lookahead" && v >= 1 && v <= 3) ctx->emit_lookahead = (int)v;
-    else if (n == "acc_filter" && (v == 0 || v == 1)) ctx->acc_filter = (int)v;
+    else if (n == "acc_filter" && (v == 0 || v == 1 || v == 2)) ctx->acc_filter = (int)v;
     // the pass kernels are compiled for blocks of at most 256 threads
     else if (n == "block_pass1" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_pass1 = (int)v;
     else if (n == "grid_pass1" && v >= 0) ctx->grid_pass1 = (int)v;
@@ -1323,8 +1323,8 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
         // the record filter needs every record of the pass in one bucket pass: one
         // read chunk and no prior contigs (their pushes weigh 1000)
         RecordFilter flt{};
-        const bool filter = st == FBK_OK && use_buckets && ctx->acc_filter && !contigs && b->chunk_starts.size() == 2 &&
-                            p->min_trans_cov >= 2;
+        const bool filter = st == FBK_OK && use_buckets && acc_filter_on(ctx->acc_filter, nw) && !contigs &&
+                            b->chunk_starts.size() == 2 && p->min_trans_cov >= 2;
         if (filter) {
             uint32_t log2m = 10;
             while (log2m < 22 && (1ULL << log2m) < max_records / bk.d.n_buckets) ++log2m;

@@ -75,7 +75,7 @@ struct fbk_ctx {
     int sketch_mode = 1;                  // 1: a build that does not return its sketch keeps only the gate ladder
     int ladder_ilp = 1;                   // windows per lane per step in the ladder pass 1 (1 or 2)
     int emit_lookahead = 2;               // record emit: gate loads 1 or 2 chunks ahead; 3 = 2 ahead over a flattened window stream
-    int acc_filter = 1;                   // 1: keys with fewer records than min_trans_cov stay out of the table
+    int acc_filter = 1;                   // keys with fewer records than min_trans_cov stay out of the table: 0 never, 1 for 256-bit keys, 2 always
     bool capturing = false;               // launches are being captured into a CUDA graph
 };
 
@@ -185,6 +185,11 @@ BankDev bank_view(const fbk_bank* b, uint64_t r_begin, uint64_t r_end, const uin
 // 256-bit keys of k <= 96 have a zero most significant word, which then holds the
 // slot's tag (no separate tag array).
 inline bool tag_in_key(uint32_t nw, uint32_t k) { return nw == 4 && k <= 96; }
+
+// Whether the record filter applies to keys of nw words under tuning acc_filter.
+// Counting the records costs about as much as it saves for 64- and 128-bit keys
+// (measured at k = 21..55, 100x), so by default only 256-bit keys are filtered.
+inline bool acc_filter_on(int mode, int nw) { return mode == 2 || (mode == 1 && nw == 4); }
 
 // Single-isolate pieces reused by the multi-isolate host code (fbk_api.cu).
 int key_words(uint32_t key_bits);     // 64 -> 1, 128 -> 2, 256 -> 4, else 0

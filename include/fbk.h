@@ -163,8 +163,8 @@ FBK_API fbk_status fbk_ctx_event_elapsed(fbk_ctx* ctx, int slot_a, int slot_b, d
  * sketch keeps only a threshold-ladder gate; 0: counted sketch), "ladder_ilp" (1 or 2
  * windows per lane in the ladder pass 1), "emit_lookahead" (record emit with the gate
  * loads 1 or 2 chunks ahead, 3 = 2 ahead over a flattened window stream), "acc_filter"
- * (1: keys that cannot become SolidKmerNodes stay out of the table, see
- * fbk_table_flags).  Results do not depend on any of them. */
+ * (keys that cannot become SolidKmerNodes stay out of the table, see fbk_table_flags:
+ * 0 never, 1 for 256-bit keys, 2 always).  Results do not depend on any of them. */
 FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double value);
 FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, double* value);
 /* Number of kernels launched on this context since creation. */
@@ -240,8 +240,9 @@ FBK_API fbk_status fbk_table_info(const fbk_table* t, uint64_t* n_keys, uint64_t
 /* FBK_TABLE_ACC_FILTERED: the accumulator holds only the keys that may become
  * SolidKmerNodes.  A key's edge counter grows by at most one per window of the key,
  * so a key seen in fewer than min_trans_cov windows has an empty mask; with the
- * tuning acc_filter = 1 (default) such keys are kept out of the table when the pass
- * runs in one read chunk without prior contigs.  The SolidKmerNode rows, their
+ * tuning acc_filter = 2 such keys are kept out of the table when the pass runs in one
+ * read chunk without prior contigs; acc_filter = 1 (default) does so for 256-bit keys
+ * only, where the saving outweighs the cost of counting.  The SolidKmerNode rows, their
  * digest and fbk_table_pushes are unchanged; n_keys and fbk_table_export_acc cover
  * the kept keys only (each with its exact KmerAcc), a superset of the keys with
  * mask != 0.  Callers that need every accumulated key (e.g. to sum accumulators

@@ -63,7 +63,7 @@ def test_golden_isolate_estimate_and_builds(ctx):
             assert t.digest() == (exp["digest"], exp["n_solid"]), name
             t.release()
             # ... and the default build, whose SolidKmerNode rows are the same
-            ctx.set_tuning(acc_filter=1)
+            ctx.set_tuning(acc_filter=2)
             t = api.build_cdbg_with_contigs_ext(bank, [], k, tsc, None, ctx=ctx, key_bits=kb, counter_bits=cb,
                                                 cms_log2_width=15)
             assert t.digest() == (exp["digest"], exp["n_solid"]), name

@@ -251,7 +251,7 @@ def test_record_filter_keeps_the_solid_rows(repeat_isolate, k, kb):
     c = api.Context(0)
     try:
         out = {}
-        for f in (1, 0):
+        for f in (2, 0):
             c.set_tuning(acc_filter=f)
             for tsc in (None, 2, 5):
                 t = api.build_cdbg_with_contigs_ext(bank, [], k, tsc, None, ctx=c, key_bits=kb, counter_bits=16,
@@ -259,15 +259,20 @@ def test_record_filter_keeps_the_solid_rows(repeat_isolate, k, kb):
                 out[f, tsc] = (t.filtered(), t.info()[0], t.export(sort=True), t.digest(), t.pushes())
                 t.release()
         for tsc in (None, 2, 5):
-            on, off = out[1, tsc], out[0, tsc]
+            on, off = out[2, tsc], out[0, tsc]
             assert on[0] and not off[0]
             assert on[1] < off[1]
             assert all(np.array_equal(a, b) for a, b in zip(on[2], off[2]))
             assert on[3] == off[3] and on[4] == off[4]
-        # min_trans_cov = 1 cannot filter anything
-        c.set_tuning(acc_filter=1)
+        # min_trans_cov = 1 cannot filter anything; the default filters 256-bit keys only
+        c.set_tuning(acc_filter=2)
         t = api.build_cdbg_with_contigs_ext(bank, [], k, 1, None, ctx=c, key_bits=kb, counter_bits=16, cms_log2_width=14)
         assert not t.filtered()
+        t.release()
+        c.set_tuning(acc_filter=1)
+        t = api.build_cdbg_with_contigs_ext(bank, [], k, None, None, ctx=c, key_bits=kb, counter_bits=16,
+                                            cms_log2_width=14)
+        assert t.filtered() == (kb == 256)
         t.release()
     finally:
         c.close()
@@ -460,6 +465,7 @@ TUNINGS = [
     dict(emit_lookahead=1),                               # gate loads one chunk ahead of the emit
     dict(emit_lookahead=3),                               # emit over a flattened window stream
     dict(acc_filter=0),                                   # every accumulated key kept
+    dict(acc_filter=2),                                   # keys that cannot be solid dropped at every width
 ]
 
 
