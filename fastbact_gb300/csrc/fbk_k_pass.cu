@@ -663,7 +663,7 @@ __global__ void __launch_bounds__(256) k_count_records(BucketDev bk, uint32_t bu
 }
 
 template <int NW>
-__global__ void __launch_bounds__(256) k_upsert(BucketDev bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov, TableDev t,
+__global__ void __launch_bounds__(256, 8) k_upsert(BucketDev bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov, TableDev t,
                                                 uint32_t* status, RecordFilter flt) {
     __shared__ unsigned long long s_pre[257];
     const uint64_t n = bucket_prefix(bk, bucket, s_pre);

@@ -62,7 +62,7 @@ def test_golden_isolate_estimate_and_builds(ctx):
                    (exp["n_keys"], exp["acc_keys_sha256"], exp["acc_cov_sha256"], exp["acc_edges_sha256"]), name
             assert t.digest() == (exp["digest"], exp["n_solid"]), name
             t.release()
-            # ... and the default build, whose SolidKmerNode rows are the same
+            # ... and a build with the record filter at every key width: same rows
             ctx.set_tuning(acc_filter=2)
             t = api.build_cdbg_with_contigs_ext(bank, [], k, tsc, None, ctx=ctx, key_bits=kb, counter_bits=cb,
                                                 cms_log2_width=15)
