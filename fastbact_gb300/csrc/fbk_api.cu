@@ -1326,14 +1326,15 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
         const bool filter = st == FBK_OK && use_buckets && acc_filter_on(ctx->acc_filter, nw) && !contigs &&
                             b->chunk_starts.size() == 2 && p->min_trans_cov >= 2;
         if (filter) {
-            uint32_t log2m = 10;
-            while (log2m < 22 && (1ULL << log2m) < max_records / bk.d.n_buckets) ++log2m;
-            fbuf.alloc(ctx, (2ULL << log2m) * 4 + 8);
+            // one counter per record or more, at most 2^23 (32 MB: stays in L2)
+            uint32_t log2m = 11;
+            while (log2m < 23 && (1ULL << log2m) < max_records / bk.d.n_buckets) ++log2m;
+            fbuf.alloc(ctx, (1ULL << log2m) * 4 + 8);
             if (!fbuf.p) st = set_err(ctx, FBK_ERR_OOM, "pass-2 record filter");
             flt.cnt = (uint32_t*)fbuf.p;
             flt.log2m = log2m;
             flt.min_records = p->min_trans_cov;
-            flt.skipped = (unsigned long long*)((char*)fbuf.p + (2ULL << log2m) * 4);
+            flt.skipped = (unsigned long long*)((char*)fbuf.p + (1ULL << log2m) * 4);
             if (st == FBK_OK) CK(ctx, cudaMemsetAsync(flt.skipped, 0, 8, ctx->stream));
         }
         if (st) {
@@ -1355,7 +1356,7 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
                 TIMED(ctx, "pass2_emit", launch_emit(nw, L, bv, p->k, bm, 1, td, bk.d));
             for (uint32_t bu = 0; bu < bk.d.n_buckets; ++bu) {
                 if (filter) {
-                    CK(ctx, cudaMemsetAsync(flt.cnt, 0, (2ULL << flt.log2m) * 4, ctx->stream));
+                    CK(ctx, cudaMemsetAsync(flt.cnt, 0, (1ULL << flt.log2m) * 4, ctx->stream));
                     TIMED(ctx, "pass2_count", launch_count_records(nw, L, bk.d, bu, flt));
                 }
                 TIMED(ctx, "pass2_upsert", launch_upsert(nw, L, bk.d, bu, 1, 1, td, ctx->d_status, flt));

@@ -538,8 +538,8 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
     for (uint32_t i = 0; i < n; ++i) {
         const BatchIso* it = V[i];
         if (!acc_filter_on(ctx->acc_filter, B->nw) || B->p.min_trans_cov < 2 || it->bank->chunk_starts.size() != 2) continue;
-        uint32_t log2m = 10;
-        while (log2m < 22 && (1ULL << log2m) < it->records / std::max<uint32_t>(1, it->bk.n_buckets)) ++log2m;
+        uint32_t log2m = 11;
+        while (log2m < 23 && (1ULL << log2m) < it->records / std::max<uint32_t>(1, it->bk.n_buckets)) ++log2m;
         flt[i].log2m = log2m;
         flt[i].min_records = B->p.min_trans_cov;
         flt[i].skipped = w.cnt + 8 * i;  // word 0 of the isolate's counters is free in phase B
@@ -556,7 +556,7 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
         }
     } fbuf{ctx};
     if (log2m_max) {
-        fbuf.p = (uint32_t*)dev_alloc(ctx, (2ULL << log2m_max) * 4);
+        fbuf.p = (uint32_t*)dev_alloc(ctx, (1ULL << log2m_max) * 4);
         if (!fbuf.p) return set_err(ctx, FBK_ERR_OOM, "batch record filter");
         for (uint32_t i = 0; i < n; ++i)
             if (flt[i].log2m) flt[i].cnt = fbuf.p;
@@ -589,7 +589,7 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
             bk.overflow = w.status + 2 * i + 1;
             for (uint32_t bu = 0; bu < bk.n_buckets; ++bu) {
                 if (flt[i].cnt) {
-                    CK(ctx, cudaMemsetAsync(flt[i].cnt, 0, (2ULL << flt[i].log2m) * 4, ctx->stream));
+                    CK(ctx, cudaMemsetAsync(flt[i].cnt, 0, (1ULL << flt[i].log2m) * 4, ctx->stream));
                     TIMED(ctx, "batch_filter", launch_count_records(B->nw, shape_launch(ctx, B->upsert), bk, bu, flt[i]));
                 }
                 TIMED(ctx, "batch_upsert", launch_upsert(B->nw, shape_launch(ctx, B->upsert), bk, bu, 1, 1, tbl_dev(it->table),

@@ -633,17 +633,14 @@ __device__ __forceinline__ const uint64_t* bucket_record(const BucketDev& bk, ui
 // does not need the whole accumulator: edge counter e of a key grows by at most one
 // per record of the key (a record pushes two different edges), so a key with fewer
 // than min_trans_cov records has an empty mask (build.rs:306-314).  Before a bucket's
-// upserts, k_count_records adds 1 per record to two rows of counters; every record of
-// a key lies in the same bucket and hits the same two counters, so the smaller one
-// bounds the key's records from above, and the upsert skips the records whose bound
-// is below min_trans_cov.  Exact when the bucket holds every record of the pass (one
+// upserts, k_count_records adds 1 per record to a counter chosen by the key's hash;
+// every record of a key lies in the same bucket and hits the same counter, so the
+// counter bounds the key's records from above, and the upsert skips the records whose
+// bound is below min_trans_cov.  Exact when the bucket holds every record of the pass (one
 // read chunk, no prior contigs, whose pushes weigh more than 1).
 constexpr uint64_t FILTER_SALT = 0x3c6ef372fe94f82bULL;
-__device__ __forceinline__ void filter_cols(uint64_t fold, uint32_t log2m, uint32_t& c0, uint32_t& c1) {
-    const uint64_t h = smix(fold ^ FILTER_SALT);
-    const uint32_t m = (1u << log2m) - 1;
-    c0 = (uint32_t)h & m;
-    c1 = ((uint32_t)(h >> 32) & m) + (1u << log2m);
+__device__ __forceinline__ uint32_t filter_col(uint64_t fold, uint32_t log2m) {
+    return (uint32_t)(smix(fold ^ FILTER_SALT) >> (64 - log2m));
 }
 
 template <int NW>
@@ -655,10 +652,7 @@ __global__ void __launch_bounds__(256) k_count_records(BucketDev bk, uint32_t bu
         Key<NW> key;
 #pragma unroll
         for (int j = 0; j < NW; ++j) key.w[j] = __ldcg(rec + j);
-        uint32_t c0, c1;
-        filter_cols(key_fold<NW>(key), flt.log2m, c0, c1);
-        atomicAdd(flt.cnt + c0, 1u);
-        atomicAdd(flt.cnt + c1, 1u);
+        atomicAdd(flt.cnt + filter_col(key_fold<NW>(key), flt.log2m), 1u);
     }
 }
 
@@ -676,10 +670,7 @@ __global__ void __launch_bounds__(256, 8) k_upsert(BucketDev bk, uint32_t bucket
         const uint32_t info = (uint32_t)__ldcs(rec + NW);
         const uint64_t f = key_fold<NW>(key);
         if (flt.cnt) {
-            uint32_t c0, c1;
-            filter_cols(f, flt.log2m, c0, c1);
-            const uint32_t a = __ldcg(flt.cnt + c0), b = __ldcg(flt.cnt + c1);
-            if ((a < b ? a : b) < flt.min_records) {
+            if (__ldcg(flt.cnt + filter_col(f, flt.log2m)) < flt.min_records) {
                 skipped += ((info >> 3) & 1u) + ((info >> 7) & 1u);
                 continue;
             }

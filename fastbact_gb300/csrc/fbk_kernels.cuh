@@ -62,8 +62,8 @@ struct BucketDev {
     uint32_t* overflow;          // set when a stripe runs out of room
 };
 
-// Record filter of pass 2 (see k_count_records): two rows of 2^log2m counters, the
-// threshold, and where the pushes of skipped records are counted.
+// Record filter of pass 2 (see k_count_records): 2^log2m counters, the threshold, and
+// where the pushes of skipped records are counted.
 struct RecordFilter {
     uint32_t* cnt;                 // nullptr: no filter
     uint32_t log2m;
