@@ -277,9 +277,9 @@ __global__ void __launch_bounds__(256) k_batch_emit(const IsoDev* __restrict__ i
     const uint64_t total = s_base[n_iso];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint64_t* buf = emit_smem + (uint64_t)wib * EMIT_WARP_WORDS(NW);
-    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + EMIT_BUF * (NW + 1));
-    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + EMIT_BUF);
-    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + EMIT_BUF);
+    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + emit_buf(NW) * (NW + 1));
+    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + emit_buf(NW));
+    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + emit_buf(NW));
     unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(256) k_batch_emit(const IsoDev* __restrict__ i
                 bbuf[pos] = (uint8_t)bucket;
             }
             n_buf += __popc(active);
-            if (n_buf > EMIT_BUF - 32) {
+            if (n_buf > emit_buf(NW) - 32) {
                 __syncwarp();
                 emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
                 n_buf = 0;

@@ -208,9 +208,9 @@ __global__ void __launch_bounds__(256) k_emit(BankDev b, uint32_t k, const uint3
     extern __shared__ uint64_t emit_smem[];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint64_t* buf = emit_smem + (uint64_t)wib * EMIT_WARP_WORDS(NW);
-    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + EMIT_BUF * (NW + 1));      // EMIT_BUF bytes
-    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + EMIT_BUF);              // EMIT_BUF u16
-    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + EMIT_BUF);              // EMIT_MAX_BUCKETS u32
+    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + emit_buf(NW) * (NW + 1));      // emit_buf(NW) bytes
+    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + emit_buf(NW));              // emit_buf(NW) u16
+    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + emit_buf(NW));              // EMIT_MAX_BUCKETS u32
     unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(256) k_emit(BankDev b, uint32_t k, const uint3
                 bbuf[pos] = (uint8_t)bucket;
             }
             n_buf += __popc(active);
-            if (n_buf > EMIT_BUF - 32) {
+            if (n_buf > emit_buf(NW) - 32) {
                 __syncwarp();
                 emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
                 n_buf = 0;
@@ -286,9 +286,9 @@ __global__ void __launch_bounds__(256) k_emit_ladder(BankDev b, uint32_t k, cons
     extern __shared__ uint64_t emit_smem[];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint64_t* buf = emit_smem + (uint64_t)wib * EMIT_WARP_WORDS(NW);
-    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + EMIT_BUF * (NW + 1));
-    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + EMIT_BUF);
-    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + EMIT_BUF);
+    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + emit_buf(NW) * (NW + 1));
+    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + emit_buf(NW));
+    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + emit_buf(NW));
     unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
     const uint32_t* top = lad + (uint64_t)(t_solid - 1) * ((4ULL << log2w) >> 5);
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(256) k_emit_ladder(BankDev b, uint32_t k, cons
                 bbuf[pos] = (uint8_t)bucket;
             }
             n_buf += __popc(active);
-            if (n_buf > EMIT_BUF - 32) {
+            if (n_buf > emit_buf(NW) - 32) {
                 __syncwarp();
                 emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
                 n_buf = 0;
@@ -387,9 +387,9 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
     extern __shared__ uint64_t emit_smem[];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint64_t* buf = emit_smem + (uint64_t)wib * EMIT_WARP_WORDS(NW);
-    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + EMIT_BUF * (NW + 1));
-    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + EMIT_BUF);
-    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + EMIT_BUF);
+    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + emit_buf(NW) * (NW + 1));
+    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + emit_buf(NW));
+    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + emit_buf(NW));
     unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
     const uint32_t* top = lad + (uint64_t)(t_solid - 1) * ((4ULL << log2w) >> 5);
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
                 bbuf[pos] = (uint8_t)bucket;
             }
             n_buf += __popc(active);
-            if (n_buf > EMIT_BUF - 32) {
+            if (n_buf > emit_buf(NW) - 32) {
                 __syncwarp();
                 emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
                 n_buf = 0;
@@ -524,9 +524,9 @@ __global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, con
     extern __shared__ uint64_t emit_smem[];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint64_t* buf = emit_smem + (uint64_t)wib * EMIT_WARP_WORDS(NW);
-    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + EMIT_BUF * (NW + 1));
-    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + EMIT_BUF);
-    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + EMIT_BUF);
+    uint8_t* bbuf = reinterpret_cast<uint8_t*>(buf + emit_buf(NW) * (NW + 1));
+    uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + emit_buf(NW));
+    uint32_t* hist = reinterpret_cast<uint32_t*>(rank + emit_buf(NW));
     unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
     const uint32_t* top = lad + (uint64_t)(t_solid - 1) * ((4ULL << log2w) >> 5);
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -581,7 +581,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, con
                 bbuf[pos] = (uint8_t)bucket;
             }
             n_buf += __popc(active);
-            if (n_buf > EMIT_BUF - 32) {
+            if (n_buf > emit_buf(NW) - 32) {
                 __syncwarp();
                 emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
                 n_buf = 0;

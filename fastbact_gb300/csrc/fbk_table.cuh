@@ -116,14 +116,20 @@ __device__ __forceinline__ bool bm_bit(const uint32_t* __restrict__ bm, uint64_t
     return (__ldg(&bm[g >> 5]) >> (g & 31)) & 1u;
 }
 
-// Records are staged per warp in shared memory (EMIT_BUF of them) and flushed
+// Records are staged per warp in shared memory (emit_buf(NW) of them) and flushed
 // bucket by bucket: one atomic per (flush, bucket) reserves room for all of the
 // warp's records of that bucket, which are then written as one run.
-constexpr uint32_t EMIT_BUF = 128;
+// Records staged per warp: as many as fit in about 9 KB of shared memory per warp
+// (three blocks of eight warps per SM), so that a flush sends more records to each
+// bucket (a flush's cost grows with the buckets it touches, not with its records:
+// measured at k = 55, 30 buckets, a 128-record staging made the emit 1.6x slower
+// than half as many buckets).
+__host__ __device__ constexpr uint32_t emit_buf(int nw) { return nw == 1 ? 448u : nw == 2 ? 288u : 192u; }
 constexpr uint32_t EMIT_MAX_BUCKETS = 64;
 // staging words per warp: records, bucket bytes, ranks (u16), histogram (64 u32),
 // reservation bases (64 u64)
-#define EMIT_WARP_WORDS(NW) (EMIT_BUF * ((NW) + 1) + EMIT_BUF / 8 + EMIT_BUF / 4 + EMIT_MAX_BUCKETS / 2 + EMIT_MAX_BUCKETS)
+#define EMIT_WARP_WORDS(NW) \
+    (emit_buf(NW) * ((NW) + 1) + emit_buf(NW) / 8 + emit_buf(NW) / 4 + EMIT_MAX_BUCKETS / 2 + EMIT_MAX_BUCKETS)
 
 // Warp counting sort of the staged records by bucket: a shared-memory histogram
 // (one atomic per record), one parallel round of global reservations (lane j
