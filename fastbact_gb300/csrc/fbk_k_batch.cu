@@ -281,6 +281,7 @@ __global__ void __launch_bounds__(256) k_batch_emit(const IsoDev* __restrict__ i
     uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + emit_buf(NW));
     uint32_t* hist = reinterpret_cast<uint32_t*>(rank + emit_buf(NW));
     unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
+    uint16_t* perm = reinterpret_cast<uint16_t*>(gbase + EMIT_MAX_BUCKETS);
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const uint32_t stripe = (uint32_t)(gw % stripes);
@@ -294,7 +295,7 @@ __global__ void __launch_bounds__(256) k_batch_emit(const IsoDev* __restrict__ i
         if (ci != cur) {
             if (n_buf) {
                 __syncwarp();
-                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank, perm);
                 n_buf = 0;
             }
             cur = ci;
@@ -339,13 +340,13 @@ __global__ void __launch_bounds__(256) k_batch_emit(const IsoDev* __restrict__ i
             n_buf += __popc(active);
             if (n_buf > emit_buf(NW) - 32) {
                 __syncwarp();
-                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank, perm);
                 n_buf = 0;
             }
         }
     }
     __syncwarp();
-    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank, perm);
 }
 
 // ---------------------------------------------------------------------------

@@ -212,6 +212,7 @@ __global__ void __launch_bounds__(256) k_emit(BankDev b, uint32_t k, const uint3
     uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + emit_buf(NW));              // emit_buf(NW) u16
     uint32_t* hist = reinterpret_cast<uint32_t*>(rank + emit_buf(NW));              // EMIT_MAX_BUCKETS u32
     unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
+    uint16_t* perm = reinterpret_cast<uint16_t*>(gbase + EMIT_MAX_BUCKETS);
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const uint32_t stripe = (uint32_t)(gw % bk.stripes);
@@ -254,13 +255,13 @@ __global__ void __launch_bounds__(256) k_emit(BankDev b, uint32_t k, const uint3
             n_buf += __popc(active);
             if (n_buf > emit_buf(NW) - 32) {
                 __syncwarp();
-                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank, perm);
                 n_buf = 0;
             }
         }
     }
     __syncwarp();
-    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank, perm);
 }
 
 // Record emit with the gate read inline from a threshold ladder (fbk_k_ladder.cu):
@@ -290,6 +291,7 @@ __global__ void __launch_bounds__(256) k_emit_ladder(BankDev b, uint32_t k, cons
     uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + emit_buf(NW));
     uint32_t* hist = reinterpret_cast<uint32_t*>(rank + emit_buf(NW));
     unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
+    uint16_t* perm = reinterpret_cast<uint16_t*>(gbase + EMIT_MAX_BUCKETS);
     const uint32_t* top = lad + (uint64_t)(t_solid - 1) * ((4ULL << log2w) >> 5);
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -343,7 +345,7 @@ __global__ void __launch_bounds__(256) k_emit_ladder(BankDev b, uint32_t k, cons
             n_buf += __popc(active);
             if (n_buf > emit_buf(NW) - 32) {
                 __syncwarp();
-                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank, perm);
                 n_buf = 0;
             }
             mprev = mcur;
@@ -353,7 +355,7 @@ __global__ void __launch_bounds__(256) k_emit_ladder(BankDev b, uint32_t k, cons
         }
     }
     __syncwarp();
-    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank, perm);
 }
 
 // The same emit with the gate loads of chunk it + 2 in flight while chunk it is
@@ -391,6 +393,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
     uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + emit_buf(NW));
     uint32_t* hist = reinterpret_cast<uint32_t*>(rank + emit_buf(NW));
     unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
+    uint16_t* perm = reinterpret_cast<uint16_t*>(gbase + EMIT_MAX_BUCKETS);
     const uint32_t* top = lad + (uint64_t)(t_solid - 1) * ((4ULL << log2w) >> 5);
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -451,7 +454,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
             n_buf += __popc(active);
             if (n_buf > emit_buf(NW) - 32) {
                 __syncwarp();
-                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank, perm);
                 n_buf = 0;
             }
             // resolve chunk it + 2 and rotate
@@ -466,7 +469,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
         }
     }
     __syncwarp();
-    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank, perm);
 }
 
 // The same emit over a flattened window stream: a warp takes a run of EMIT_RUN
@@ -528,6 +531,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, con
     uint16_t* rank = reinterpret_cast<uint16_t*>(bbuf + emit_buf(NW));
     uint32_t* hist = reinterpret_cast<uint32_t*>(rank + emit_buf(NW));
     unsigned long long* gbase = reinterpret_cast<unsigned long long*>(hist + EMIT_MAX_BUCKETS);
+    uint16_t* perm = reinterpret_cast<uint16_t*>(gbase + EMIT_MAX_BUCKETS);
     const uint32_t* top = lad + (uint64_t)(t_solid - 1) * ((4ULL << log2w) >> 5);
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -583,7 +587,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, con
             n_buf += __popc(active);
             if (n_buf > emit_buf(NW) - 32) {
                 __syncwarp();
-                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+                emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank, perm);
                 n_buf = 0;
             }
             const uint32_t mfar = __ballot_sync(0xffffffffu, gate_resolve(gf, wf.live));
@@ -595,7 +599,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, con
         }
     }
     __syncwarp();
-    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank);
+    if (n_buf) emit_flush<NW>(bk, stripe, lane, buf, bbuf, n_buf, hist, gbase, rank, perm);
 }
 
 // Upsert of one bucket's records: every thread resolves its record's key from its

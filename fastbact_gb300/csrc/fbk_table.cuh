@@ -119,44 +119,56 @@ __device__ __forceinline__ bool bm_bit(const uint32_t* __restrict__ bm, uint64_t
 // Records are staged per warp in shared memory (emit_buf(NW) of them) and flushed
 // bucket by bucket: one atomic per (flush, bucket) reserves room for all of the
 // warp's records of that bucket, which are then written as one run.
-// Records staged per warp: as many as fit in about 9 KB of shared memory per warp
-// (three blocks of eight warps per SM), so that a flush sends more records to each
-// bucket (a flush's cost grows with the buckets it touches, not with its records:
-// measured at k = 55, 30 buckets, a 128-record staging made the emit 1.6x slower
-// than half as many buckets).
-__host__ __device__ constexpr uint32_t emit_buf(int nw) { return nw == 1 ? 448u : nw == 2 ? 288u : 192u; }
+// Records staged per warp (128).  Staging 2-3.5 times as many per warp (9 KB of
+// shared memory per warp) made the emit 3-40% slower: the shared memory comes out
+// of the L1 that serves the bank and gate loads.
+__host__ __device__ constexpr uint32_t emit_buf(int nw) { return nw > 0 ? 128u : 128u; }
 constexpr uint32_t EMIT_MAX_BUCKETS = 64;
 // staging words per warp: records, bucket bytes, ranks (u16), histogram (64 u32),
-// reservation bases (64 u64)
+// reservation bases (64 u64), bucket-order permutation (u16)
 #define EMIT_WARP_WORDS(NW) \
-    (emit_buf(NW) * ((NW) + 1) + emit_buf(NW) / 8 + emit_buf(NW) / 4 + EMIT_MAX_BUCKETS / 2 + EMIT_MAX_BUCKETS)
+    (emit_buf(NW) * ((NW) + 1) + emit_buf(NW) / 8 + emit_buf(NW) / 4 + EMIT_MAX_BUCKETS / 2 + EMIT_MAX_BUCKETS + emit_buf(NW) / 4)
 
 // Warp counting sort of the staged records by bucket: a shared-memory histogram
-// (one atomic per record), one parallel round of global reservations (lane j
-// reserves for bucket j, j+32, ...), then every lane copies records to
-// region[bucket] + rank.  Cost does not grow with the number of buckets.
+// (one atomic per record), one round of global reservations (lane j reserves for
+// buckets j and j + 32), a warp scan of the counts that places every record in
+// bucket order, then a copy in that order, one 8-byte word per lane, so the records
+// of a bucket leave as one contiguous run of stores.
 template <int NW>
 __device__ __forceinline__ void emit_flush(const BucketDev& bk, uint32_t stripe, uint32_t lane, uint64_t* buf, const uint8_t* bbuf,
-                                           uint32_t n_buf, uint32_t* hist, unsigned long long* gbase, uint16_t* rank) {
-    for (uint32_t bu = lane; bu < bk.n_buckets; bu += 32) hist[bu] = 0;
+                                           uint32_t n_buf, uint32_t* hist, unsigned long long* gbase, uint16_t* rank,
+                                           uint16_t* perm) {
+    constexpr uint32_t RW = NW + 1;  // words per record
+    const uint32_t nb = bk.n_buckets;  // <= EMIT_MAX_BUCKETS = 64
+    for (uint32_t bu = lane; bu < nb; bu += 32) hist[bu] = 0;
     __syncwarp();
     for (uint32_t j = lane; j < n_buf; j += 32) rank[j] = (uint16_t)atomicAdd(&hist[bbuf[j]], 1u);
     __syncwarp();
-    for (uint32_t bu = lane; bu < bk.n_buckets; bu += 32) {
-        const uint32_t c = hist[bu];
-        gbase[bu] = c ? atomicAdd(bk.fill + (uint64_t)bu * bk.stripes + stripe, (unsigned long long)c) : 0;
-    }
-    __syncwarp();
-    for (uint32_t j = lane; j < n_buf; j += 32) {
-        const uint32_t bu = bbuf[j];
-        const unsigned long long pos = gbase[bu] + rank[j];
-        if (pos < bk.stripe_cap) {
-            uint64_t* dst = bk.recs + (((uint64_t)bu * bk.stripes + stripe) * bk.stripe_cap + pos) * (NW + 1);
+    const uint32_t c0 = lane < nb ? hist[lane] : 0u, c1 = lane + 32 < nb ? hist[lane + 32] : 0u;
+    if (c0) gbase[lane] = atomicAdd(bk.fill + (uint64_t)lane * bk.stripes + stripe, (unsigned long long)c0);
+    if (c1) gbase[lane + 32] = atomicAdd(bk.fill + (uint64_t)(lane + 32) * bk.stripes + stripe, (unsigned long long)c1);
+    uint32_t s0 = c0, s1 = c1;  // inclusive scans over the lanes
 #pragma unroll
-            for (int i = 0; i <= NW; ++i) dst[i] = buf[j * (NW + 1) + i];
-        } else {
-            atomicOr(bk.overflow, 1u);
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t a = __shfl_up_sync(0xffffffffu, s0, off), b = __shfl_up_sync(0xffffffffu, s1, off);
+        if (lane >= (uint32_t)off) {
+            s0 += a;
+            s1 += b;
         }
+    }
+    const uint32_t tot0 = __shfl_sync(0xffffffffu, s0, 31);
+    __syncwarp();
+    if (lane < nb) hist[lane] = s0 - c0;  // first bucket-order position of each bucket
+    if (lane + 32 < nb) hist[lane + 32] = tot0 + s1 - c1;
+    __syncwarp();
+    for (uint32_t j = lane; j < n_buf; j += 32) perm[hist[bbuf[j]] + rank[j]] = (uint16_t)j;
+    __syncwarp();
+    for (uint32_t w = lane; w < n_buf * RW; w += 32) {
+        const uint32_t p = w / RW, i = w - p * RW;
+        const uint32_t j = perm[p], bu = bbuf[j];
+        const unsigned long long pos = gbase[bu] + (p - hist[bu]);
+        if (pos < bk.stripe_cap) bk.recs[(((uint64_t)bu * bk.stripes + stripe) * bk.stripe_cap + pos) * RW + i] = buf[j * RW + i];
+        else if (i == 0) atomicOr(bk.overflow, 1u);
     }
     __syncwarp();
 }
