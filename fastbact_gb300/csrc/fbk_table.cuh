@@ -119,10 +119,10 @@ __device__ __forceinline__ bool bm_bit(const uint32_t* __restrict__ bm, uint64_t
 // Records are staged per warp in shared memory (emit_buf(NW) of them) and flushed
 // bucket by bucket: one atomic per (flush, bucket) reserves room for all of the
 // warp's records of that bucket, which are then written as one run.
-// Records staged per warp (128).  Staging 2-3.5 times as many per warp (9 KB of
-// shared memory per warp) made the emit 3-40% slower: the shared memory comes out
-// of the L1 that serves the bank and gate loads.
-__host__ __device__ constexpr uint32_t emit_buf(int nw) { return nw > 0 ? 128u : 128u; }
+// Records staged per warp.  Staging 2-3.5 times as many per warp (9 KB of shared
+// memory per warp) made the emit 3-40% slower: the shared memory comes out of the L1
+// that serves the bank and gate loads.
+__host__ __device__ constexpr uint32_t emit_buf(int) { return 128u; }
 constexpr uint32_t EMIT_MAX_BUCKETS = 64;
 // staging words per warp: records, bucket bytes, ranks (u16), histogram (64 u32),
 // reservation bases (64 u64), bucket-order permutation (u16)
