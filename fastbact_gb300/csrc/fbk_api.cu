@@ -1323,7 +1323,7 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
         // the record filter needs every record of the pass in one bucket pass: one
         // read chunk and no prior contigs (their pushes weigh 1000)
         RecordFilter flt{};
-        const bool filter = st == FBK_OK && use_buckets && acc_filter_on(ctx->acc_filter, nw) && !contigs &&
+        const bool filter = st == FBK_OK && use_buckets && acc_filter_on(ctx->acc_filter, nw, distinct_hint, max_records) && !contigs &&
                             b->chunk_starts.size() == 2 && p->min_trans_cov >= 2;
         if (filter) {
             // one counter per record or more, at most 2^23 (32 MB: stays in L2)

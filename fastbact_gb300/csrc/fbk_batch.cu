@@ -537,7 +537,9 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
     uint32_t log2m_max = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const BatchIso* it = V[i];
-        if (!acc_filter_on(ctx->acc_filter, B->nw) || B->p.min_trans_cov < 2 || it->bank->chunk_starts.size() != 2) continue;
+        if (!acc_filter_on(ctx->acc_filter, B->nw, it->distinct, it->records) || B->p.min_trans_cov < 2 ||
+            it->bank->chunk_starts.size() != 2)
+            continue;
         uint32_t log2m = 11;
         while (log2m < 23 && (1ULL << log2m) < it->records / std::max<uint32_t>(1, it->bk.n_buckets)) ++log2m;
         flt[i].log2m = log2m;

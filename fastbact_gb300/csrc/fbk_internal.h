@@ -186,10 +186,14 @@ BankDev bank_view(const fbk_bank* b, uint64_t r_begin, uint64_t r_end, const uin
 // slot's tag (no separate tag array).
 inline bool tag_in_key(uint32_t nw, uint32_t k) { return nw == 4 && k <= 96; }
 
-// Whether the record filter applies to keys of nw words under tuning acc_filter.
-// Counting the records costs about as much as it saves for 64- and 128-bit keys
-// (measured at k = 21..55, 100x), so by default only 256-bit keys are filtered.
-inline bool acc_filter_on(int mode, int nw) { return mode == 2 || (mode == 1 && nw == 4); }
+// Whether the record filter applies under tuning acc_filter (0 never, 2 always, 1
+// auto).  Counting costs about one L2 atomic per record; it pays when many keys are
+// seen once or twice: for 256-bit keys, and when the distinct k-mers of pass 1 exceed
+// a fifth of the records (measured at 100x: k = 55, 24% distinct, 12.7 -> 10.1 ms; k = 33,
+// 14%, 10.6 -> 11.8 ms; k = 21, 8%, 8.5 -> 12.2 ms).
+inline bool acc_filter_on(int mode, int nw, uint64_t distinct, uint64_t records) {
+    return mode == 2 || (mode == 1 && (nw == 4 || distinct * 5 > records));
+}
 
 // Single-isolate pieces reused by the multi-isolate host code (fbk_api.cu).
 int key_words(uint32_t key_bits);     // 64 -> 1, 128 -> 2, 256 -> 4, else 0

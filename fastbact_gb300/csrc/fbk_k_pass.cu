@@ -606,31 +606,15 @@ __global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, con
 // home slot and adds the pushes.  (Taking two records per thread and issuing both
 // home-slot loads first measured 18% slower: register pressure cost more occupancy
 // than the overlap gained.)
-// Stripe prefix of one bucket's record counts (shared), and the address of record i.
-__device__ __forceinline__ uint64_t bucket_prefix(const BucketDev& bk, uint32_t bucket, unsigned long long* s_pre) {
-    const uint32_t S = bk.stripes;  // <= 256
-    if (threadIdx.x == 0) {
-        unsigned long long acc = 0;
-        for (uint32_t i = 0; i < S; ++i) {
-            s_pre[i] = acc;
-            unsigned long long f = bk.fill[(uint64_t)bucket * S + i];
-            acc += f < bk.stripe_cap ? f : bk.stripe_cap;
-        }
-        s_pre[S] = acc;
-    }
-    __syncthreads();
-    return s_pre[S];
-}
-template <int NW>
-__device__ __forceinline__ const uint64_t* bucket_record(const BucketDev& bk, uint32_t bucket, const unsigned long long* s_pre,
-                                                         uint64_t i) {
-    uint32_t lo = 0, hi = bk.stripes;  // stripe: last s with s_pre[s] <= i
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (s_pre[mid] <= i) lo = mid;
-        else hi = mid;
-    }
-    return bk.recs + (((uint64_t)bucket * bk.stripes + lo) * bk.stripe_cap + (i - s_pre[lo])) * (NW + 1);
+// Bucket upserts and record counts run on a 2D grid: blockIdx.y is the stripe, and the
+// blocks of a stripe stride over its records (the stripes of a bucket hold about the
+// same number).  A block reads its stripe's fill counter once; there is no prefix over
+// the stripes and no search for a record's stripe.
+__device__ __forceinline__ uint64_t stripe_records(const BucketDev& bk, uint32_t bucket, const uint64_t*& base, int rw) {
+    const uint32_t s = blockIdx.y;
+    const unsigned long long f = bk.fill[(uint64_t)bucket * bk.stripes + s];
+    base = bk.recs + ((uint64_t)bucket * bk.stripes + s) * bk.stripe_cap * (uint64_t)rw;
+    return f < bk.stripe_cap ? f : bk.stripe_cap;
 }
 
 // Keys that cannot become SolidKmerNodes can stay out of the table when the caller
@@ -649,10 +633,10 @@ __device__ __forceinline__ uint32_t filter_col(uint64_t fold, uint32_t log2m) {
 
 template <int NW>
 __global__ void __launch_bounds__(256) k_count_records(BucketDev bk, uint32_t bucket, RecordFilter flt) {
-    __shared__ unsigned long long s_pre[257];
-    const uint64_t n = bucket_prefix(bk, bucket, s_pre);
+    const uint64_t* base;
+    const uint64_t n = stripe_records(bk, bucket, base, NW + 1);
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t* rec = bucket_record<NW>(bk, bucket, s_pre, i);
+        const uint64_t* rec = base + i * (NW + 1);
         Key<NW> key;
 #pragma unroll
         for (int j = 0; j < NW; ++j) key.w[j] = __ldcg(rec + j);
@@ -663,11 +647,11 @@ __global__ void __launch_bounds__(256) k_count_records(BucketDev bk, uint32_t bu
 template <int NW>
 __global__ void __launch_bounds__(256, 8) k_upsert(BucketDev bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov, TableDev t,
                                                 uint32_t* status, RecordFilter flt) {
-    __shared__ unsigned long long s_pre[257];
-    const uint64_t n = bucket_prefix(bk, bucket, s_pre);
+    const uint64_t* base;
+    const uint64_t n = stripe_records(bk, bucket, base, NW + 1);
     unsigned long long skipped = 0;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t* rec = bucket_record<NW>(bk, bucket, s_pre, i);
+        const uint64_t* rec = base + i * (NW + 1);
         Key<NW> key;
 #pragma unroll
         for (int j = 0; j < NW; ++j) key.w[j] = __ldcs(rec + j);
@@ -973,10 +957,15 @@ cudaError_t launch_emit(int nw, const Launch& L, const BankDev& b, uint32_t k, c
     return emit_nw<4>(L, b, k, bm, gate, t, bk);
 }
 
+// blocks per stripe: the occupancy-sized grid spread over the stripes
+static dim3 stripe_grid(int blocks, uint32_t stripes) {
+    const uint32_t s = stripes ? stripes : 1;
+    return dim3((unsigned)std::max<int>(1, (blocks + (int)s - 1) / (int)s), s);
+}
 template <int NW>
 static cudaError_t upsert_nw(const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t we, uint32_t wc, const TableDev& t,
                              uint32_t* status, const RecordFilter& flt) {
-    k_upsert<NW><<<grid_for(k_upsert<NW>, L), L.block, 0, L.stream>>>(bk, bucket, we, wc, t, status, flt);
+    k_upsert<NW><<<stripe_grid(grid_for(k_upsert<NW>, L), bk.stripes), L.block, 0, L.stream>>>(bk, bucket, we, wc, t, status, flt);
     return cudaGetLastError();
 }
 cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov,
@@ -988,7 +977,7 @@ cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t
 }
 template <int NW>
 static cudaError_t count_nw(const Launch& L, const BucketDev& bk, uint32_t bucket, const RecordFilter& flt) {
-    k_count_records<NW><<<grid_for(k_count_records<NW>, L), L.block, 0, L.stream>>>(bk, bucket, flt);
+    k_count_records<NW><<<stripe_grid(grid_for(k_count_records<NW>, L), bk.stripes), L.block, 0, L.stream>>>(bk, bucket, flt);
     return cudaGetLastError();
 }
 cudaError_t launch_count_records(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, const RecordFilter& flt) {

@@ -164,7 +164,7 @@ FBK_API fbk_status fbk_ctx_event_elapsed(fbk_ctx* ctx, int slot_a, int slot_b, d
  * windows per lane in the ladder pass 1), "emit_lookahead" (record emit with the gate
  * loads 1 or 2 chunks ahead, 3 = 2 ahead over a flattened window stream), "acc_filter"
  * (keys that cannot become SolidKmerNodes stay out of the table, see fbk_table_flags:
- * 0 never, 1 for 256-bit keys, 2 always).  Results do not depend on any of them. */
+ * 0 never, 1 where it pays, 2 always).  Results do not depend on any of them. */
 FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double value);
 FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, double* value);
 /* Number of kernels launched on this context since creation. */
@@ -241,8 +241,9 @@ FBK_API fbk_status fbk_table_info(const fbk_table* t, uint64_t* n_keys, uint64_t
  * SolidKmerNodes.  A key's edge counter grows by at most one per window of the key,
  * so a key seen in fewer than min_trans_cov windows has an empty mask; with the
  * tuning acc_filter = 2 such keys are kept out of the table when the pass runs in one
- * read chunk without prior contigs; acc_filter = 1 (default) does so for 256-bit keys
- * only, where the saving outweighs the cost of counting.  The SolidKmerNode rows, their
+ * read chunk without prior contigs; acc_filter = 1 (default) does so where the saving
+ * outweighs the cost of counting: 256-bit keys, and passes whose distinct k-mers
+ * exceed a fifth of their windows.  The SolidKmerNode rows, their
  * digest and fbk_table_pushes are unchanged; n_keys and fbk_table_export_acc cover
  * the kept keys only (each with its exact KmerAcc), a superset of the keys with
  * mask != 0.  Callers that need every accumulated key (e.g. to sum accumulators
