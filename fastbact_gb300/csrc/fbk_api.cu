@@ -841,8 +841,9 @@ static fbk_status pass1_impl(fbk_cms* c, const fbk_bank* b, uint32_t k, uint32_t
     return FBK_OK;
 }
 
-// Distinct canonical keys added to the sketch by bank passes (p=12 HyperLogLog,
-// about 1.6% standard error); only used to size the solid table.
+// Distinct canonical keys added to the sketch by bank passes (p=12 HyperLogLog over
+// the 1 key in 16 whose hash ends in four zero bits, about 1.6% standard error at
+// isolate scale); only used to size the solid table.
 static fbk_status cms_distinct(const fbk_cms* c, uint64_t* out) {
     fbk_ctx* ctx = c->ctx;
     uint32_t* h = (uint32_t*)ctx->h_pinned;
@@ -854,7 +855,8 @@ static fbk_status cms_distinct(const fbk_cms* c, uint64_t* out) {
         sum += std::ldexp(1.0, -(int)h[i]);
         zeros += h[i] == 0;
     }
-    *out = (uint64_t)(hll_estimate_from_sum(sum, zeros, 12) * 1.05) + 1024;
+    // pass 1 counts 1 key in PASS1_HLL_SAMPLE (by hash)
+    *out = (uint64_t)(hll_estimate_from_sum(sum, zeros, 12) * PASS1_HLL_SAMPLE * 1.08) + 4096;
     return FBK_OK;
 }
 

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(256, ILP == 1 ? 6 : 2) k_ladder_pass1(BankDev 
             if (do_hll) {
 #pragma unroll
                 for (int p = 0; p < ILP; ++p)
-                    if (live[p]) {
+                    if (live[p] && (h0[p] & (PASS1_HLL_SAMPLE - 1)) == 0) {  // 1 key in 16 by hash
                         uint32_t idx, rho;
                         hll_idx_rho(h0[p], 12, idx, rho);
                         if (s_hll[idx] < rho) atomicMax(&s_hll[idx], rho);

@@ -66,10 +66,14 @@ __global__ void __launch_bounds__(256) k_pass1_sweep(BankDev b, uint32_t k, uint
                 }
             }
             if (do_hll) {
-                // any bijective hash of the key serves the distinct count
-                uint32_t idx, rho;
-                hll_idx_rho(smix(key ^ cms_seed(0)), 12, idx, rho);
-                if (s_hll[idx] < rho) atomicMax(&s_hll[idx], rho);
+                // any bijective hash of the key serves the distinct count; the keys
+                // whose hash has its low 4 bits zero (1 in 16) are counted
+                const uint64_t h = smix(key ^ cms_seed(0));
+                if ((h & (PASS1_HLL_SAMPLE - 1)) == 0) {
+                    uint32_t idx, rho;
+                    hll_idx_rho(h, 12, idx, rho);
+                    if (s_hll[idx] < rho) atomicMax(&s_hll[idx], rho);
+                }
             }
         }
     }

@@ -86,6 +86,7 @@ struct ConvOut {
 // One isolate of a multi-isolate wave (fbk_k_batch.cu).
 constexpr uint32_t BATCH_MAX_ISO = 256;
 constexpr uint32_t BATCH_HLL_SAMPLE = 16;  // 1 in 16 keys (by hash) feeds the table-sizing HyperLogLog
+constexpr uint32_t PASS1_HLL_SAMPLE = 16;  // the same sampling in the single-isolate pass 1
 struct IsoDev {
     BankDev b;                      // r_begin = 0, r_end = the isolate's reads
     uint32_t* cnt;                  // exact u32 sketch, 4 rows of 2^log2w (or null with a ladder)
