@@ -656,17 +656,6 @@ __global__ void __launch_bounds__(256, 8) k_upsert(BucketDev bk, uint32_t bucket
     unsigned long long skipped = 0;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        // The probes miss L2 about half of the time (tables of 2-3 GB): start the table
-        // lines of the record this thread takes next on their way to L2 now.
-        if (i + stride < n) {
-            const uint64_t* rn = base + (i + stride) * (NW + 1);
-            Key<NW> kn;
-#pragma unroll
-            for (int j = 0; j < NW; ++j) kn.w[j] = __ldcg(rn + j);
-            const uint64_t hn = home_slot(key_fold<NW>(kn), t.cap);
-            prefetch_l2(t.keys + hn * NW);
-            prefetch_l2(t.cnt + hn * 8);
-        }
         const uint64_t* rec = base + i * (NW + 1);
         Key<NW> key;
 #pragma unroll

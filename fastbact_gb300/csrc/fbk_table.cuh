@@ -17,9 +17,6 @@ static constexpr uint64_t KEY_EMPTY = ~0ULL;
 // ---------------------------------------------------------------------------
 // Solid table probing from a precomputed home slot
 // ---------------------------------------------------------------------------
-// L2 prefetch hint (no register result, no wait).
-__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
-
 // Home slot of a key: the high 64 bits of mix(fold) * cap (any capacity).
 __device__ __forceinline__ uint64_t home_slot(uint64_t fold, uint64_t cap) {
     return __umul64hi(smix(fold ^ TABLE_SALT), cap);
@@ -135,8 +132,8 @@ constexpr uint32_t EMIT_MAX_BUCKETS = 64;
 // Warp counting sort of the staged records by bucket: a shared-memory histogram
 // (one atomic per record), one round of global reservations (lane j reserves for
 // buckets j and j + 32), a warp scan of the counts that places every record in
-// bucket order, then a copy in that order (lane p takes the p-th record), so the
-// records of a bucket leave as one contiguous run of stores.
+// bucket order, then a copy in that order, so the records of a bucket leave as one
+// contiguous run of stores.
 template <int NW>
 __device__ __forceinline__ void emit_flush(const BucketDev& bk, uint32_t stripe, uint32_t lane, uint64_t* buf, const uint8_t* bbuf,
                                            uint32_t n_buf, uint32_t* hist, unsigned long long* gbase, uint16_t* rank,
@@ -166,17 +163,28 @@ __device__ __forceinline__ void emit_flush(const BucketDev& bk, uint32_t stripe,
     __syncwarp();
     for (uint32_t j = lane; j < n_buf; j += 32) perm[hist[bbuf[j]] + rank[j]] = (uint16_t)j;
     __syncwarp();
-    // lane p writes the p-th record in bucket order: a store instruction covers one word
-    // of 32 consecutive records of the runs
-    for (uint32_t p = lane; p < n_buf; p += 32) {
-        const uint32_t j = perm[p], bu = bbuf[j];
-        const unsigned long long pos = gbase[bu] + (p - hist[bu]);
-        if (pos < bk.stripe_cap) {
-            uint64_t* dst = bk.recs + (((uint64_t)bu * bk.stripes + stripe) * bk.stripe_cap + pos) * RW;
+    if constexpr (RW <= 3) {
+        // lane p writes the p-th record in bucket order: a store instruction covers one
+        // word of 32 consecutive records of the runs
+        for (uint32_t p = lane; p < n_buf; p += 32) {
+            const uint32_t j = perm[p], bu = bbuf[j];
+            const unsigned long long pos = gbase[bu] + (p - hist[bu]);
+            if (pos < bk.stripe_cap) {
+                uint64_t* dst = bk.recs + (((uint64_t)bu * bk.stripes + stripe) * bk.stripe_cap + pos) * RW;
 #pragma unroll
-            for (uint32_t i = 0; i < RW; ++i) dst[i] = buf[j * RW + i];
-        } else {
-            atomicOr(bk.overflow, 1u);
+                for (uint32_t i = 0; i < RW; ++i) dst[i] = buf[j * RW + i];
+            } else {
+                atomicOr(bk.overflow, 1u);
+            }
+        }
+    } else {
+        // 40-byte records: one word per lane, 32 consecutive words per store instruction
+        for (uint32_t w = lane; w < n_buf * RW; w += 32) {
+            const uint32_t p = w / RW, i = w - p * RW;
+            const uint32_t j = perm[p], bu = bbuf[j];
+            const unsigned long long pos = gbase[bu] + (p - hist[bu]);
+            if (pos < bk.stripe_cap) bk.recs[(((uint64_t)bu * bk.stripes + stripe) * bk.stripe_cap + pos) * RW + i] = buf[j * RW + i];
+            else if (i == 0) atomicOr(bk.overflow, 1u);
         }
     }
     __syncwarp();
