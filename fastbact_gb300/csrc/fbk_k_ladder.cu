@@ -95,6 +95,87 @@ __global__ void __launch_bounds__(256, ILP == 1 ? 6 : 2) k_ladder_pass1(BankDev 
     }
 }
 
+// The same pass 1 software-pipelined over a read's chunks of 32 windows: the top-level
+// loads of chunk it + 1 are issued before chunk it climbs, so their L2 latency overlaps
+// the climb's atomics and the next chunk's hashing (tuning ladder_ilp = 3).
+struct LadderChunk {
+    uint32_t wd[4], mk[4], top[4];
+    uint64_t h0;
+    bool live;
+};
+template <int NW, int WS>
+__device__ __forceinline__ void ladder_prep(const BankDev& b, uint64_t off, uint32_t q, uint32_t nk, uint32_t k, uint32_t log2w,
+                                            uint64_t wmask, const uint32_t* __restrict__ top, LadderChunk& c) {
+    c.live = q < nk;
+    c.h0 = 0;
+#pragma unroll
+    for (int row = 0; row < 4; ++row) {
+        c.wd[row] = c.mk[row] = 0;
+        c.top[row] = ~0u;
+    }
+    if (!c.live) return;
+    Key<NW> can{};
+    bool rc;
+    canonical_ws<NW, WS>(b.data, off + q, k, can, rc);
+    const uint64_t key = key_fold<NW>(can);
+    c.h0 = smix(key ^ cms_seed(0));
+#pragma unroll
+    for (int row = 0; row < 4; ++row) {
+        const uint64_t h = row == 0 ? c.h0 : smix(key ^ cms_seed(row));
+        const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
+        c.wd[row] = bit >> 5;
+        c.mk[row] = 1u << (bit & 31);
+    }
+#pragma unroll
+    for (int row = 0; row < 4; ++row) c.top[row] = __ldcg(top + c.wd[row]);
+}
+
+template <int NW, int WS>
+__global__ void __launch_bounds__(256, 4) k_ladder_pass1p(BankDev b, uint32_t k, uint32_t* __restrict__ lad, uint32_t log2w,
+                                                          uint32_t t, uint32_t* __restrict__ hll12) {
+    __shared__ uint32_t s_hll[4096];
+    const bool do_hll = hll12 != nullptr;
+    if (do_hll) {
+        for (int i = threadIdx.x; i < 4096; i += blockDim.x) s_hll[i] = 0;
+        __syncthreads();
+    }
+    const uint64_t wmask = (1ULL << log2w) - 1;
+    const uint64_t level_words = (4ULL << log2w) >> 5;
+    const uint32_t* top = lad + (uint64_t)(t - 1) * level_words;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t r = b.r_begin + gw; r < b.r_end; r += nwarps) {
+        const uint32_t len = b.len[r];
+        if (len < k || !bank_keep(b, r)) continue;
+        const uint64_t off = b.off[r];
+        const uint32_t nk = len - k + 1;
+        LadderChunk cur;
+        ladder_prep<NW, WS>(b, off, lane, nk, k, log2w, wmask, top, cur);
+        for (uint32_t it = 0; it < ((nk + 31) >> 5); ++it) {
+            LadderChunk nxt;
+            ladder_prep<NW, WS>(b, off, ((it + 1) << 5) + lane, nk, k, log2w, wmask, top, nxt);
+            bool climb[4];
+#pragma unroll
+            for (int row = 0; row < 4; ++row) climb[row] = cur.live && !(cur.top[row] & cur.mk[row]);
+            ladder_climb<4>(lad, level_words, t, cur.wd, cur.mk, climb);
+            if (do_hll && cur.live && (cur.h0 & (PASS1_HLL_SAMPLE - 1)) == 0) {
+                uint32_t idx, rho;
+                hll_idx_rho(cur.h0, 12, idx, rho);
+                if (s_hll[idx] < rho) atomicMax(&s_hll[idx], rho);
+            }
+            cur = nxt;
+        }
+    }
+    if (do_hll) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < 4096; i += blockDim.x) {
+            const uint32_t v = s_hll[i];
+            if (v) atomicMax(&hll12[i], v);
+        }
+    }
+}
+
 // Solidity bitmap from a ladder: a window's bit is cleared unless the top level is
 // set in all four rows (one sweep).
 template <int NW>
@@ -145,7 +226,10 @@ static int grid_l(K kernel, const Launch& L) {
 
 template <int NW, int ILP, int WS>
 static cudaError_t lp1(const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t, uint32_t* hll) {
-    k_ladder_pass1<NW, ILP, WS><<<grid_l(k_ladder_pass1<NW, ILP, WS>, L), L.block, 0, L.stream>>>(b, k, lad, log2w, t, hll);
+    if constexpr (ILP == 3)
+        k_ladder_pass1p<NW, WS><<<grid_l(k_ladder_pass1p<NW, WS>, L), L.block, 0, L.stream>>>(b, k, lad, log2w, t, hll);
+    else
+        k_ladder_pass1<NW, ILP, WS><<<grid_l(k_ladder_pass1<NW, ILP, WS>, L), L.block, 0, L.stream>>>(b, k, lad, log2w, t, hll);
     return cudaGetLastError();
 }
 template <int NW, int ILP>
@@ -169,6 +253,11 @@ cudaError_t launch_ladder_pass1(int nw, const Launch& L, const BankDev& b, uint3
         if (nw == 1) return lp1_ws<1, 2>(L, b, k, lad, log2w, t, hll12);
         if (nw == 2) return lp1_ws<2, 2>(L, b, k, lad, log2w, t, hll12);
         return lp1_ws<4, 2>(L, b, k, lad, log2w, t, hll12);
+    }
+    if (ilp == 3) {
+        if (nw == 1) return lp1_ws<1, 3>(L, b, k, lad, log2w, t, hll12);
+        if (nw == 2) return lp1_ws<2, 3>(L, b, k, lad, log2w, t, hll12);
+        return lp1_ws<4, 3>(L, b, k, lad, log2w, t, hll12);
     }
     if (nw == 1) return lp1_ws<1, 1>(L, b, k, lad, log2w, t, hll12);
     if (nw == 2) return lp1_ws<2, 1>(L, b, k, lad, log2w, t, hll12);

@@ -464,6 +464,7 @@ TUNINGS = [
     dict(stripes=1, record_factor=0.05),                  # stripes overflow -> direct fallback
     dict(load_factor=0.85, block_pass1=128, block_pass2=64, grid_pass1=37, grid_pass2=91),
     dict(ladder_ilp=2, block_pass1=128),                 # two windows per lane in the ladder pass 1
+    dict(ladder_ilp=3),                                   # ladder pass 1 pipelined over chunks
     dict(emit_lookahead=1),                               # gate loads one chunk ahead of the emit
     dict(emit_lookahead=3),                               # emit over a flattened window stream
     dict(acc_filter=0),                                   # every accumulated key kept
