@@ -367,12 +367,15 @@ __global__ void __launch_bounds__(256) k_emit_ladder(BankDev b, uint32_t k, cons
 // farthest one are issued before the emit work and resolved after it.
 struct GateLoads {
     uint32_t w[4], m[4];
+    uint64_t h0;  // row-0 hash, which also places the key in the table (home_slot_h)
 };
 __device__ __forceinline__ void gate_issue(const uint32_t* __restrict__ top, uint32_t log2w, uint64_t key, bool live, GateLoads& g) {
     const uint64_t wmask = (1ULL << log2w) - 1;
 #pragma unroll
     for (int row = 0; row < 4; ++row) {
-        const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(smix(key ^ cms_seed(row)) & wmask);
+        const uint64_t h = smix(key ^ cms_seed(row));
+        if (row == 0) g.h0 = h;
+        const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
         g.m[row] = 1u << (bit & 31);
         g.w[row] = live ? __ldg(top + (bit >> 5)) : 0u;
     }
@@ -422,6 +425,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
         uint32_t mnext = __ballot_sync(0xffffffffu, gate_resolve(g1, l1));
         Key<NW> kc = k0, kn = k1;
         bool rcc = rc0, rcn = rc1;
+        uint64_t hc = g0.h0, hn = g1.h0;
         for (uint32_t it = 0; it < n_it; ++it) {
             // issue chunk it + 2
             Key<NW> kf{};
@@ -444,7 +448,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
                     const uint64_t g = off + q;
                     if (sr) info |= 8u | (base_at(b.data, g + k) + (rcc ? 4u : 0u));
                     if (sl) info |= (8u | ((3u - base_at(b.data, g - 1)) + (rcc ? 0u : 4u))) << 4;
-                    bucket = (uint32_t)(home_slot(key_fold<NW>(kc), t.cap) >> bk.shift);
+                    bucket = (uint32_t)(home_slot_h(hc, t.cap) >> bk.shift);
                 }
             }
             const uint32_t active = __ballot_sync(0xffffffffu, emit);
@@ -468,8 +472,10 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
             mnext = mfar;
             kc = kn;
             rcc = rcn;
+            hc = hn;
             kn = kf;
             rcn = rcf;
+            hn = gf.h0;
         }
     }
     __syncwarp();

@@ -9,7 +9,6 @@
 
 namespace fbk {
 
-static constexpr uint64_t TABLE_SALT = 0x6a09e667f3bcc908ULL;
 static constexpr uint64_t FP_SALT = 0xbb67ae8584caa73bULL;
 static constexpr uint64_t TAG_READY = 1ULL << 63;
 static constexpr uint64_t KEY_EMPTY = ~0ULL;
@@ -17,9 +16,12 @@ static constexpr uint64_t KEY_EMPTY = ~0ULL;
 // ---------------------------------------------------------------------------
 // Solid table probing from a precomputed home slot
 // ---------------------------------------------------------------------------
-// Home slot of a key: the high 64 bits of mix(fold) * cap (any capacity).
+// Home slot of a key: the high 64 bits of h * cap (any capacity), h = splitmix64 of
+// the folded key with the sketch's row-0 seed — the hash the gate already computes
+// for row 0, whose column is its low bits, so the record emit reuses it.
+__device__ __forceinline__ uint64_t home_slot_h(uint64_t h_row0, uint64_t cap) { return __umul64hi(h_row0, cap); }
 __device__ __forceinline__ uint64_t home_slot(uint64_t fold, uint64_t cap) {
-    return __umul64hi(smix(fold ^ TABLE_SALT), cap);
+    return home_slot_h(smix(fold ^ cms_seed(0)), cap);
 }
 
 __device__ __forceinline__ int64_t table_slot1(const TableDev& t, uint64_t key, uint64_t s, uint32_t* status) {
