@@ -308,6 +308,7 @@ FBK_API fbk_status fbk_ctx_fork(fbk_ctx* parent, fbk_ctx** out) {
     c->ladder_ilp = parent->ladder_ilp;
     c->emit_lookahead = parent->emit_lookahead;
     c->acc_filter = parent->acc_filter;
+    c->upsert_all = parent->upsert_all;
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_status, 64);
@@ -407,6 +408,7 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "ladder_ilp" && (v == 1 || v == 2 || v == 3)) ctx->ladder_ilp = (int)v;
     else if (n == "emit_lookahead" && v >= 1 && v <= 3) ctx->emit_lookahead = (int)v;
     else if (n == "acc_filter" && (v == 0 || v == 1 || v == 2)) ctx->acc_filter = (int)v;
+    else if (n == "upsert_all" && (v == 0 || v == 1)) ctx->upsert_all = (int)v;
     // the pass kernels are compiled for blocks of at most 256 threads
     else if (n == "block_pass1" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_pass1 = (int)v;
     else if (n == "grid_pass1" && v >= 0) ctx->grid_pass1 = (int)v;
@@ -429,6 +431,7 @@ FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, doub
     else if (n == "ladder_ilp") *v = ctx->ladder_ilp;
     else if (n == "emit_lookahead") *v = ctx->emit_lookahead;
     else if (n == "acc_filter") *v = ctx->acc_filter;
+    else if (n == "upsert_all") *v = ctx->upsert_all;
     else if (n == "block_pass1") *v = ctx->block_pass1;
     else if (n == "grid_pass1") *v = ctx->grid_pass1;
     else if (n == "block_pass2") *v = ctx->block_pass2;
@@ -1356,12 +1359,20 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
                                                                      ctx->emit_lookahead));
             else
                 TIMED(ctx, "pass2_emit", launch_emit(nw, L, bv, p->k, bm, 1, td, bk.d));
-            for (uint32_t bu = 0; bu < bk.d.n_buckets; ++bu) {
-                if (filter) {
-                    CK(ctx, cudaMemsetAsync(flt.cnt, 0, (1ULL << flt.log2m) * 4, ctx->stream));
-                    TIMED(ctx, "pass2_count", launch_count_records(nw, L, bk.d, bu, flt));
+            if (!filter && ctx->upsert_all) {
+                // every bucket in one persistent launch; bytes 8..15 of the overflow
+                // word's buffer hand out the work items
+                unsigned long long* work = (unsigned long long*)(bk.overflow + 2);
+                CK(ctx, cudaMemsetAsync(work, 0, 8, ctx->stream));
+                TIMED(ctx, "pass2_upsert", launch_upsert_all(nw, L, bk.d, 1, 1, td, ctx->d_status, work));
+            } else {
+                for (uint32_t bu = 0; bu < bk.d.n_buckets; ++bu) {
+                    if (filter) {
+                        CK(ctx, cudaMemsetAsync(flt.cnt, 0, (1ULL << flt.log2m) * 4, ctx->stream));
+                        TIMED(ctx, "pass2_count", launch_count_records(nw, L, bk.d, bu, flt));
+                    }
+                    TIMED(ctx, "pass2_upsert", launch_upsert(nw, L, bk.d, bu, 1, 1, td, ctx->d_status, flt));
                 }
-                TIMED(ctx, "pass2_upsert", launch_upsert(nw, L, bk.d, bu, 1, 1, td, ctx->d_status, flt));
             }
         }
         uint32_t ovf = use_buckets ? 0 : 1;  // without buckets every chunk takes the direct sweep

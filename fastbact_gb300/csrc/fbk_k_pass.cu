@@ -654,42 +654,78 @@ __global__ void __launch_bounds__(256) k_count_records(BucketDev bk, uint32_t bu
     }
 }
 
+// One record's upsert: resolve the key's slot from its home slot and add its pushes.
+template <int NW>
+__device__ __forceinline__ void upsert_record(const uint64_t* rec, uint32_t w_edge, uint32_t w_cov, const TableDev& t,
+                                              uint32_t* status, const RecordFilter& flt, unsigned long long& skipped) {
+    Key<NW> key;
+#pragma unroll
+    for (int j = 0; j < NW; ++j) key.w[j] = __ldcs(rec + j);
+    const uint32_t info = (uint32_t)__ldcs(rec + NW);
+    const uint64_t f = key_fold<NW>(key);
+    if (flt.cnt) {
+        if (__ldcg(flt.cnt + filter_col(f, flt.log2m)) < flt.min_records) {
+            skipped += ((info >> 3) & 1u) + ((info >> 7) & 1u);
+            return;
+        }
+    }
+    const uint64_t home = home_slot(f, t.cap);
+    int64_t s;
+    if constexpr (NW == 1) s = table_slot1(t, key.w[0], home, status);
+    else if constexpr (NW == 2) s = table_slot2(t, key, home, status);
+    else s = table_slotw<NW>(t, key, f, home, status);
+    if (s < 0) return;
+    uint32_t* c = t.cnt + (uint64_t)s * 8;
+    const uint32_t nu = (info >> 3) & 1u, nv = (info >> 7) & 1u;
+    if (nu) atomicAdd(&c[info & 7u], w_edge);
+    if (nv) atomicAdd(&c[(info >> 4) & 7u], w_edge);
+    if (t.cov) atomicAdd(&t.cov[s], w_cov * (nu + nv));
+}
+
 template <int NW>
 __global__ void __launch_bounds__(256, 8) k_upsert(BucketDev bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov, TableDev t,
                                                 uint32_t* status, RecordFilter flt) {
     const uint64_t* base;
     const uint64_t n = stripe_records(bk, bucket, base, NW + 1);
     unsigned long long skipped = 0;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint64_t* rec = base + i * (NW + 1);
-        Key<NW> key;
-#pragma unroll
-        for (int j = 0; j < NW; ++j) key.w[j] = __ldcs(rec + j);
-        const uint32_t info = (uint32_t)__ldcs(rec + NW);
-        const uint64_t f = key_fold<NW>(key);
-        if (flt.cnt) {
-            if (__ldcg(flt.cnt + filter_col(f, flt.log2m)) < flt.min_records) {
-                skipped += ((info >> 3) & 1u) + ((info >> 7) & 1u);
-                continue;
-            }
-        }
-        const uint64_t home = home_slot(f, t.cap);
-        int64_t s;
-        if constexpr (NW == 1) s = table_slot1(t, key.w[0], home, status);
-        else if constexpr (NW == 2) s = table_slot2(t, key, home, status);
-        else s = table_slotw<NW>(t, key, f, home, status);
-        if (s < 0) continue;
-        uint32_t* c = t.cnt + (uint64_t)s * 8;
-        const uint32_t nu = (info >> 3) & 1u, nv = (info >> 7) & 1u;
-        if (nu) atomicAdd(&c[info & 7u], w_edge);
-        if (nv) atomicAdd(&c[(info >> 4) & 7u], w_edge);
-        if (t.cov) atomicAdd(&t.cov[s], w_cov * (nu + nv));
-    }
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        upsert_record<NW>(base + i * (NW + 1), w_edge, w_cov, t, status, flt, skipped);
     if (flt.cnt) {
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) skipped += __shfl_down_sync(0xffffffffu, skipped, off);
         if ((threadIdx.x & 31) == 0 && skipped) atomicAdd(flt.skipped, skipped);
+    }
+}
+
+// Every bucket of a pass in one persistent launch: blocks take work items (bucket,
+// stripe, run of UPSERT_ITEM records) from a counter in bucket order, so at any time
+// the blocks work on one or two buckets' table ranges, without a launch and its tail
+// per bucket.  No record filter (its counts must be complete before a bucket's
+// upserts start).
+constexpr uint32_t UPSERT_ITEM = 4096;
+template <int NW>
+__global__ void __launch_bounds__(256, 8) k_upsert_all(BucketDev bk, uint32_t w_edge, uint32_t w_cov, TableDev t,
+                                                    uint32_t* status, unsigned long long* work) {
+    __shared__ unsigned long long s_item;
+    const uint64_t per_stripe = (bk.stripe_cap + UPSERT_ITEM - 1) / UPSERT_ITEM;
+    const uint64_t n_items = (uint64_t)bk.n_buckets * bk.stripes * per_stripe;
+    const RecordFilter none{};
+    unsigned long long skipped = 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(work, 1ULL);
+        __syncthreads();
+        const uint64_t item = s_item;
+        __syncthreads();
+        if (item >= n_items) break;
+        const uint64_t bs = item / per_stripe;  // bucket * stripes + stripe
+        const uint64_t first = (item - bs * per_stripe) * UPSERT_ITEM;
+        const unsigned long long f = bk.fill[bs];
+        const uint64_t n = f < bk.stripe_cap ? f : bk.stripe_cap;
+        if (first >= n) continue;
+        const uint64_t last = first + UPSERT_ITEM < n ? first + UPSERT_ITEM : n;
+        const uint64_t* base = bk.recs + bs * bk.stripe_cap * (NW + 1);
+        for (uint64_t i = first + threadIdx.x; i < last; i += blockDim.x)
+            upsert_record<NW>(base + i * (NW + 1), w_edge, w_cov, t, status, none, skipped);
     }
 }
 
@@ -985,6 +1021,19 @@ cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t
     if (nw == 1) return upsert_nw<1>(L, bk, bucket, w_edge, w_cov, t, status, flt);
     if (nw == 2) return upsert_nw<2>(L, bk, bucket, w_edge, w_cov, t, status, flt);
     return upsert_nw<4>(L, bk, bucket, w_edge, w_cov, t, status, flt);
+}
+template <int NW>
+static cudaError_t upsert_all_nw(const Launch& L, const BucketDev& bk, uint32_t we, uint32_t wc, const TableDev& t,
+                                 uint32_t* status, unsigned long long* work) {
+    k_upsert_all<NW><<<grid_for(k_upsert_all<NW>, L), L.block, 0, L.stream>>>(bk, we, wc, t, status, work);
+    return cudaGetLastError();
+}
+cudaError_t launch_upsert_all(int nw, const Launch& L, const BucketDev& bk, uint32_t w_edge, uint32_t w_cov, const TableDev& t,
+                              uint32_t* status, unsigned long long* work) {
+    if (!work) return cudaErrorInvalidValue;
+    if (nw == 1) return upsert_all_nw<1>(L, bk, w_edge, w_cov, t, status, work);
+    if (nw == 2) return upsert_all_nw<2>(L, bk, w_edge, w_cov, t, status, work);
+    return upsert_all_nw<4>(L, bk, w_edge, w_cov, t, status, work);
 }
 template <int NW>
 static cudaError_t count_nw(const Launch& L, const BucketDev& bk, uint32_t bucket, const RecordFilter& flt) {

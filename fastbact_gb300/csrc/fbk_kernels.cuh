@@ -131,6 +131,9 @@ cudaError_t launch_emit(int nw, const Launch& L, const BankDev& b, uint32_t k, c
 cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov,
                           const TableDev& t, uint32_t* status, const RecordFilter& flt = RecordFilter{});
 cudaError_t launch_count_records(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, const RecordFilter& flt);
+// every bucket in one persistent launch; *work (zeroed by the caller) hands out items
+cudaError_t launch_upsert_all(int nw, const Launch& L, const BucketDev& bk, uint32_t w_edge, uint32_t w_cov, const TableDev& t,
+                              uint32_t* status, unsigned long long* work);
 cudaError_t launch_convert(int nw, const Launch& L, const TableDev& t, uint32_t min_trans_cov, const ConvOut& o);
 cudaError_t launch_clamp_counters(const Launch& L, uint32_t* cnt, uint64_t n);
 cudaError_t launch_table_init(int nw, const Launch& L, const TableDev& t);

@@ -469,6 +469,7 @@ TUNINGS = [
     dict(emit_lookahead=3),                               # emit over a flattened window stream
     dict(acc_filter=0),                                   # every accumulated key kept
     dict(acc_filter=2),                                   # keys that cannot be solid dropped at every width
+    dict(upsert_all=0, acc_filter=0),                     # one upsert launch per bucket
 ]
 
 
