@@ -563,6 +563,21 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
         for (uint32_t i = 0; i < n; ++i)
             if (flt[i].log2m) flt[i].cnt = fbuf.p;
     }
+    // work-item counters of the persistent upserts (unfiltered isolates)
+    struct WorkBuf {
+        fbk_ctx* c;
+        unsigned long long* p = nullptr;
+        ~WorkBuf() {
+            if (p) {
+                cudaStreamSynchronize(c->stream);
+                dev_free(c, p);
+            }
+        }
+    } work{ctx};
+    if (ctx->upsert_all) {
+        work.p = (unsigned long long*)dev_alloc(ctx, (uint64_t)n * 8);
+        if (!work.p) return set_err(ctx, FBK_ERR_OOM, "batch upsert counters");
+    }
     st = run_phase(B, &B->stats.ms_phase_b, [&]() -> fbk_status {
         CK(ctx, cudaMemsetAsync(w.cnt, 0, (uint64_t)n * 64, ctx->stream));
         CK(ctx, cudaMemsetAsync(w.status, 0, (uint64_t)n * 8, ctx->stream));
@@ -585,10 +600,16 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
             TIMED(ctx, "batch_emit", launch_batch_emit(B->nw, shape_launch(ctx, B->emit), w.iso, w.rb, n, k, BATCH_STRIPES));
         }
         // upserts bucket by bucket, so each launch's table range stays in L2
+        if (work.p) CK(ctx, cudaMemsetAsync(work.p, 0, (uint64_t)n * 8, ctx->stream));
         for (uint32_t i = 0; i < n; ++i) {
             BatchIso* it = V[i];
             BucketDev bk = it->bk;
             bk.overflow = w.status + 2 * i + 1;
+            if (work.p && !flt[i].cnt) {
+                TIMED(ctx, "batch_upsert", launch_upsert_all(B->nw, shape_launch(ctx, B->upsert), bk, 1, 1, tbl_dev(it->table),
+                                                             w.status + 2 * i, work.p + i));
+                continue;
+            }
             for (uint32_t bu = 0; bu < bk.n_buckets; ++bu) {
                 if (flt[i].cnt) {
                     CK(ctx, cudaMemsetAsync(flt[i].cnt, 0, (1ULL << flt[i].log2m) * 4, ctx->stream));
