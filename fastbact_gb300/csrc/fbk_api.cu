@@ -1,8 +1,6 @@
 // fbk_api.cu — host side of the C ABI: contexts, device pool, bank upload, and the
 // CountMinSketch / HyperLogLog / solid-table objects with their build passes.
 #include <algorithm>
-#include <atomic>
-#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
