@@ -1198,7 +1198,8 @@ static fbk_status solidity_bitmap(fbk_ctx* ctx, const fbk_bank* b, const fbk_cms
 struct Buckets {
     fbk_ctx* ctx = nullptr;
     BucketDev d{};
-    uint32_t* overflow = nullptr;
+    uint32_t* overflow = nullptr;      // 256 bytes: the overflow flag, then the work counter
+    unsigned long long* work = nullptr;  // work items handed out by the persistent upsert
     ~Buckets() {
         if (!ctx) return;
         cudaStreamSynchronize(ctx->stream);
@@ -1225,6 +1226,7 @@ static fbk_status buckets_alloc(fbk_ctx* ctx, uint64_t cap, uint64_t slot_bytes,
     bk.d.recs = (uint64_t*)dev_alloc(ctx, (uint64_t)P * S * per_stripe * 8 * (nw + 1));
     bk.d.fill = (unsigned long long*)dev_alloc(ctx, (uint64_t)P * S * 8);
     bk.overflow = (uint32_t*)dev_alloc(ctx, 256);
+    bk.work = bk.overflow ? (unsigned long long*)(bk.overflow + 2) : nullptr;
     bk.d.overflow = bk.overflow;
     if (!bk.d.recs || !bk.d.fill || !bk.overflow) return set_err(ctx, FBK_ERR_OOM, "pass-2 record buckets");
     CK(ctx, cudaMemsetAsync(bk.overflow, 0, 4, ctx->stream));
@@ -1358,11 +1360,9 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
             else
                 TIMED(ctx, "pass2_emit", launch_emit(nw, L, bv, p->k, bm, 1, td, bk.d));
             if (!filter && ctx->upsert_all) {
-                // every bucket in one persistent launch; bytes 8..15 of the overflow
-                // word's buffer hand out the work items
-                unsigned long long* work = (unsigned long long*)(bk.overflow + 2);
-                CK(ctx, cudaMemsetAsync(work, 0, 8, ctx->stream));
-                TIMED(ctx, "pass2_upsert", launch_upsert_all(nw, L, bk.d, 1, 1, td, ctx->d_status, work));
+                // every bucket in one persistent launch
+                CK(ctx, cudaMemsetAsync(bk.work, 0, 8, ctx->stream));
+                TIMED(ctx, "pass2_upsert", launch_upsert_all(nw, L, bk.d, 1, 1, td, ctx->d_status, bk.work));
             } else {
                 for (uint32_t bu = 0; bu < bk.d.n_buckets; ++bu) {
                     if (filter) {
