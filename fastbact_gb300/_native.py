@@ -156,6 +156,7 @@ SIGNATURES = {
     "fbk_cms_add_keys": (S, [vp, u64p, C.c_uint64]),
     "fbk_cms_estimate_keys": (S, [vp, u64p, C.c_uint64, u32p]),
     "fbk_cms_add_bank": (S, [vp, vp, C.c_uint32, C.c_uint32, P(Subsample)]),
+    "fbk_cms_build": (S, [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, P(vp)]),
     "fbk_cms_add_contigs": (S, [vp, u8p, u64p, C.c_uint64, C.c_uint32, C.c_uint32]),
     "fbk_cms_nbytes": (S, [vp, u64p]),
     "fbk_cms_export": (S, [vp, u8p, C.c_uint64]),

@@ -526,6 +526,18 @@ class CountMinSketch:
               self.ctx.handle, "cms create")
         self.ctx.adopt(self)
 
+    @classmethod
+    def build(cls, ctx: Context, bank: "DeviceBank", k: int, log2_width: int, counter_bits: int = 4,
+              key_bits: int | None = None) -> "CountMinSketch":
+        """Pass 1 in one call (fbk_cms_build): a new sketch holding every k-mer of the bank."""
+        self = cls.__new__(cls)
+        self.ctx, self.width, self.counter_bits = ctx, 1 << log2_width, counter_bits
+        self._h = C.c_void_p()
+        check(N.lib().fbk_cms_build(ctx.handle, bank.handle, k, key_bits or key_bits_for_k(k), log2_width, counter_bits,
+                                    C.byref(self._h)), ctx.handle, "cms build")
+        ctx.adopt(self)
+        return self
+
     @staticmethod
     def width_for_genome_size(g: int) -> int:
         return N.lib().fbk_cms_width_for_genome_size(g)

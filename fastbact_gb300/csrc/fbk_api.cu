@@ -876,6 +876,22 @@ FBK_API fbk_status fbk_cms_add_bank(fbk_cms* c, const fbk_bank* b, uint32_t k, u
     return st;
 }
 
+FBK_API fbk_status fbk_cms_build(fbk_ctx* ctx, const fbk_bank* b, uint32_t k, uint32_t key_bits, uint32_t log2_width,
+                                 uint32_t counter_bits, fbk_cms** out) {
+    if (!ctx || !b || !out) return FBK_ERR_INVALID;
+    *out = nullptr;
+    fbk_cms* c = nullptr;
+    fbk_status st = fbk_cms_create(ctx, log2_width, counter_bits, &c);
+    if (st) return st;
+    st = fbk_cms_add_bank(c, b, k, key_bits, nullptr);
+    if (st) {
+        fbk_cms_release(c);
+        return st;
+    }
+    *out = c;
+    return FBK_OK;
+}
+
 // Prior contigs are counted with weights up to 1000 per push, so their bank is cut
 // into ranges of fewer than 4M bases (1000 x 4M < 2^32 - 2^17).
 static const uint64_t CONTIG_CHUNK_BASES = 4000000;

@@ -191,6 +191,10 @@ FBK_API fbk_status fbk_cms_estimate_keys(fbk_cms* c, const uint64_t* keys, uint6
 /* Pass 1 of build_cdbg_with_contigs_ext (build.rs:90-116): add the canonical
  * k-mer fold of every k-mer of every read with len >= k.  ss may be NULL. */
 FBK_API fbk_status fbk_cms_add_bank(fbk_cms* c, const fbk_bank* b, uint32_t k, uint32_t key_bits, const fbk_subsample* ss);
+/* Pass 1 in one call: a new sketch of 4 x 2^log2_width counters holding every k-mer
+ * of the bank (fbk_cms_create + fbk_cms_add_bank; build.rs:74-116). */
+FBK_API fbk_status fbk_cms_build(fbk_ctx* ctx, const fbk_bank* b, uint32_t k, uint32_t key_bits, uint32_t log2_width,
+                                 uint32_t counter_bits, fbk_cms** out);
 /* Prior contigs add x10 per k-mer (build.rs:118-138); ascii concatenated, offs has n+1 entries. */
 FBK_API fbk_status fbk_cms_add_contigs(fbk_cms* c, const uint8_t* ascii, const uint64_t* offs, uint64_t n, uint32_t k, uint32_t key_bits);
 /* Raw table in the reference byte layout (4*w/2 bytes, nibble) or 4*w u16 (LE). */

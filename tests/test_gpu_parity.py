@@ -682,6 +682,17 @@ def test_bank_upload_checks_every_sequence(ctx):
             api.DeviceBank(ctx, api.BitSeqArena(words, offs, lens))
 
 
+@pytest.mark.parametrize("k,kb,cb", [(31, 64, 4), (45, 128, 16), (77, 256, 4)])
+def test_cms_build_one_call(ctx, small_isolate, k, kb, cb):
+    """fbk_cms_build (create + pass 1) gives the oracle's pass-1 sketch bytes."""
+    bank = small_isolate[0]
+    db = api.DeviceBank(ctx, bank)
+    cms = api.CountMinSketch.build(ctx, db, k, 14, cb, key_bits=kb)
+    assert np.array_equal(cms.export(), orc.build_front(bank, k, kb, 14, cb, None, threads=4)[0].export())
+    cms.release()
+    db.release()
+
+
 @pytest.mark.parametrize("cb,log2w", [(16, 22), (4, 24)])
 def test_large_sketch_export_import_round_trip(ctx, small_isolate, cb, log2w):
     """Sketches of 32 MB go through the pinned staging slots both ways (several
