@@ -300,6 +300,7 @@ FBK_API fbk_status fbk_ctx_fork(fbk_ctx* parent, fbk_ctx** out) {
     c->block_pass1 = parent->block_pass1;
     c->grid_pass1 = parent->grid_pass1;
     c->block_pass2 = parent->block_pass2;
+    c->block_emit = parent->block_emit;
     c->grid_pass2 = parent->grid_pass2;
     c->block_misc = parent->block_misc;
     c->sketch_mode = parent->sketch_mode;
@@ -411,6 +412,7 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "block_pass1" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_pass1 = (int)v;
     else if (n == "grid_pass1" && v >= 0) ctx->grid_pass1 = (int)v;
     else if (n == "block_pass2" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_pass2 = (int)v;
+    else if (n == "block_emit" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_emit = (int)v;
     else if (n == "grid_pass2" && v >= 0) ctx->grid_pass2 = (int)v;
     else return set_err(ctx, FBK_ERR_INVALID, "unknown tuning name or value out of range: " + n);
     return FBK_OK;
@@ -433,6 +435,7 @@ FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, doub
     else if (n == "block_pass1") *v = ctx->block_pass1;
     else if (n == "grid_pass1") *v = ctx->grid_pass1;
     else if (n == "block_pass2") *v = ctx->block_pass2;
+    else if (n == "block_emit") *v = ctx->block_emit;
     else if (n == "grid_pass2") *v = ctx->grid_pass2;
     else return FBK_ERR_INVALID;
     return FBK_OK;
@@ -1371,8 +1374,9 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
             const BankDev bv = bank_view(b, b->chunk_starts[c], b->chunk_starts[c + 1], keep_bits);
             CK(ctx, cudaMemsetAsync(bk.d.fill, 0, (uint64_t)bk.d.n_buckets * bk.d.stripes * 8, ctx->stream));
             if (inline_gate)
-                TIMED(ctx, "pass2_emit", launch_emit_ladder(nw, L, bv, p->k, lad->bits, lad->log2w, p->t_solid, td, bk.d,
-                                                                     ctx->emit_lookahead));
+                TIMED(ctx, "pass2_emit", launch_emit_ladder(nw, launch_cfg_persistent(ctx, ctx->block_emit, ctx->grid_pass2), bv,
+                                                            p->k, lad->bits, lad->log2w, p->t_solid, td, bk.d,
+                                                            ctx->emit_lookahead));
             else
                 TIMED(ctx, "pass2_emit", launch_emit(nw, L, bv, p->k, bm, 1, td, bk.d));
             if (!filter && ctx->upsert_all) {

@@ -158,8 +158,8 @@ FBK_API fbk_status fbk_ctx_event_elapsed(fbk_ctx* ctx, int slot_a, int slot_b, d
  * bucket), "stripes", "load_factor", "pass2_mode" (1 buckets, 0 direct sweep),
  * "record_factor" (record capacity over the expected count; a full bucket falls back
  * to the direct sweep),
- * "block_pass1", "grid_pass1", "block_pass2", "grid_pass2" (blocks of 32..256 threads in
- * steps of 32; grid 0 = occupancy), "sketch_mode" (1: a build that does not return its
+ * "block_pass1", "grid_pass1", "block_pass2", "grid_pass2", "block_emit" (blocks of
+ * 32..256 threads in steps of 32; grid 0 = occupancy), "sketch_mode" (1: a build that does not return its
  * sketch keeps only a threshold-ladder gate; 0: counted sketch), "ladder_ilp" (1 or 2
  * windows per lane in the ladder pass 1, 3 = pipelined over chunks), "emit_lookahead" (record emit with the gate
  * loads 1 or 2 chunks ahead, 3 = 2 ahead over a flattened window stream), "acc_filter"

@@ -470,6 +470,7 @@ TUNINGS = [
     dict(acc_filter=0),                                   # every accumulated key kept
     dict(acc_filter=2),                                   # keys that cannot be solid dropped at every width
     dict(upsert_all=0, acc_filter=0),                     # one upsert launch per bucket
+    dict(block_emit=256),                                 # record emit in blocks of 256
 ]
 
 
