@@ -457,8 +457,9 @@ class DeviceBank:
         self._h = C.c_void_p()
         check(N.lib().fbk_bank_upload(ctx.handle, self._views, C.byref(self._h)), ctx.handle, "bank upload")
         ctx.adopt(self)
-        self.n_bases = bank.total_bases()
-        self.n_reads = bank.total_reads()
+        nr, nb = C.c_uint64(), C.c_uint64()  # the totals the upload's scan computed
+        check(N.lib().fbk_bank_info(self._h, C.byref(nr), C.byref(nb)))
+        self.n_reads, self.n_bases = nr.value, nb.value
 
     @classmethod
     def from_handle(cls, ctx: Context, h) -> "DeviceBank":
