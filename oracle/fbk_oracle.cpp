@@ -1,9 +1,9 @@
 // fbk_oracle.cpp — ORACLE: CPU restatement of fastBact's k-mer counting front end.
 //
 // TEST INFRASTRUCTURE ONLY.  Nothing in the product (the fastbact_gb300 package and
-// its libfbk.so) links, loads or calls this file.  It is used by tests/ as the
-// parity checker, by __graft_entry__.smoke() as the checker, and by bench.py as the
-// timed CPU baseline ("kind": "port") and as the reference arm.
+// its libfbk.so) links, loads or calls this file.  It is used by tests/ to check the
+// device results, by __graft_entry__.smoke() to check its one small run, and by
+// bench.py as the timed CPU baseline ("kind": "port") and as the reference arm.
 //
 // The reference (Caizhaohui/fastBact v0.1.0) is pure Rust.  No Rust toolchain and
 // no vendored crates exist where this project is built, so the reference cannot be

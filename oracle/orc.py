@@ -1,7 +1,7 @@
 """ctypes wrapper of the oracle library (oracle/_build/liborc.so).
 
-TEST INFRASTRUCTURE ONLY: the checker for the device kernels and the timed CPU
-baseline.  Builds the library on first use with oracle/build_oracle.sh.
+TEST INFRASTRUCTURE ONLY: the oracle the device kernels are checked against, and the
+timed CPU baseline.  Builds the library on first use with oracle/build_oracle.sh.
 """
 from __future__ import annotations
 
