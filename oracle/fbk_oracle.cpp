@@ -735,7 +735,7 @@ static std::string read_id_prefix(const std::string& id) {
 }  // namespace orc
 
 // ===========================================================================
-// extern "C" surface for ctypes (tests, smoke checker, CPU baseline timing)
+// extern "C" surface for ctypes (tests, smoke(), CPU baseline timing)
 // ===========================================================================
 using namespace orc;
 
