@@ -363,6 +363,12 @@ def run_ours(args, rank, world, local):
                          "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
                          "alg_bytes_per_pass": per_pass_bytes, "ms_per_pass": per_pass_ms,
                          "note": "per pass = one k of one step; achieved = algorithmic bytes / event-timed kernel time"},
+            # the second figure the path is bound by: L2 atomics, counted as the edge-counter
+            # atomics of the upserts (one per transition push) over the upsert time
+            "l2_atomics": {"kind": "edge-counter atomics of pass 2 (one per transition push)",
+                           "ops_per_step": sum(pushes.values()),
+                           "per_s": sum(pushes.values()) * args.steps / (kernel_ms["pass2_upsert"][0] / 1e3)
+                           if kernel_ms["pass2_upsert"][0] > 0 else None},
             "gpu_launches": launches,
             "clocks": clk,
             "e2e": e2e,
