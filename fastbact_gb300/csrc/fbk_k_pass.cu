@@ -697,26 +697,26 @@ __global__ void __launch_bounds__(256, 8) k_upsert(BucketDev bk, uint32_t bucket
     }
 }
 
-// Every bucket of a pass in one persistent launch: warps take work items (bucket,
+// Every bucket of a pass in one persistent launch: blocks take work items (bucket,
 // stripe, run of UPSERT_ITEM records) from a counter in bucket order, so at any time
-// they work on one or two buckets' table ranges, without a launch and its tail per
-// bucket.  Items are taken per warp (lane 0 fetches, a shuffle shares): with items per
-// block, threads waited at the block barriers for the block's slowest probe (ncu: 15%
-// of the stall cycles).  No record filter (its counts must be complete before a
-// bucket's upserts start).
-constexpr uint32_t UPSERT_ITEM = 2048;
+// the blocks work on one or two buckets' table ranges, without a launch and its tail
+// per bucket.  (Items taken per warp instead, which removes the block barriers, made
+// the upsert 11% slower: every warp then waits on the shared counter's atomic.)  No
+// record filter (its counts must be complete before a bucket's upserts start).
+constexpr uint32_t UPSERT_ITEM = 16384;
 template <int NW>
 __global__ void __launch_bounds__(256, 8) k_upsert_all(BucketDev bk, uint32_t w_edge, uint32_t w_cov, TableDev t,
                                                     uint32_t* status, unsigned long long* work) {
-    const uint32_t lane = threadIdx.x & 31;
+    __shared__ unsigned long long s_item;
     const uint64_t per_stripe = (bk.stripe_cap + UPSERT_ITEM - 1) / UPSERT_ITEM;
     const uint64_t n_items = (uint64_t)bk.n_buckets * bk.stripes * per_stripe;
     const RecordFilter none{};
     unsigned long long skipped = 0;
     for (;;) {
-        unsigned long long item = 0;
-        if (lane == 0) item = atomicAdd(work, 1ULL);
-        item = __shfl_sync(0xffffffffu, item, 0);
+        if (threadIdx.x == 0) s_item = atomicAdd(work, 1ULL);
+        __syncthreads();
+        const uint64_t item = s_item;
+        __syncthreads();
         if (item >= n_items) break;
         const uint64_t bs = item / per_stripe;  // bucket * stripes + stripe
         const uint64_t first = (item - bs * per_stripe) * UPSERT_ITEM;
@@ -725,7 +725,7 @@ __global__ void __launch_bounds__(256, 8) k_upsert_all(BucketDev bk, uint32_t w_
         if (first >= n) continue;
         const uint64_t last = first + UPSERT_ITEM < n ? first + UPSERT_ITEM : n;
         const uint64_t* base = bk.recs + bs * bk.stripe_cap * (NW + 1);
-        for (uint64_t i = first + lane; i < last; i += 32)
+        for (uint64_t i = first + threadIdx.x; i < last; i += blockDim.x)
             upsert_record<NW>(base + i * (NW + 1), w_edge, w_cov, t, status, none, skipped);
     }
 }
