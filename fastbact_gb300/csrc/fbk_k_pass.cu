@@ -700,10 +700,12 @@ __global__ void __launch_bounds__(256, 8) k_upsert(BucketDev bk, uint32_t bucket
 // Every bucket of a pass in one persistent launch: blocks take work items (bucket,
 // stripe, run of UPSERT_ITEM records) from a counter in bucket order, so at any time
 // the blocks work on one or two buckets' table ranges, without a launch and its tail
-// per bucket.  (Items taken per warp instead, which removes the block barriers, made
-// the upsert 11% slower: every warp then waits on the shared counter's atomic.)  No
-// record filter (its counts must be complete before a bucket's upserts start).
-constexpr uint32_t UPSERT_ITEM = 16384;
+// per bucket.  Measured per step at 100x: items of 2048 records 31.9 ms, 4096 32.3,
+// 16384 37.0 (the blocks then spread over more buckets at once); items taken per warp
+// instead, which removes the block barriers, 35.9 (every warp waits on the shared
+// counter's atomic).  No record filter (its counts must be complete before a bucket's
+// upserts start).
+constexpr uint32_t UPSERT_ITEM = 2048;
 template <int NW>
 __global__ void __launch_bounds__(256, 8) k_upsert_all(BucketDev bk, uint32_t w_edge, uint32_t w_cov, TableDev t,
                                                     uint32_t* status, unsigned long long* work) {
