@@ -820,7 +820,8 @@ def cpu_arm(bank, sample, n_sample, stats, budget_s: float, threads: int = 0, si
                      f"k={KS} over the first {frac:.3%} of each arena's reads (nibble CMS, 64 mutex shards)",
            "seconds": dt + t_est, "build_value": km / max(dt, 1e-9), "estimator_seconds": t_est}
     if single_s > 0:
-        f1 = min(1.0, max(0.001, single_s * (rate / cores) / max(full, 1)))
+        km1, dt1 = run(0.001, 1)
+        f1 = min(1.0, max(0.001, single_s * (km1 / max(dt1, 1e-6)) / max(full, 1)))
         km1, dt1 = run(f1, 1)
         out["single_thread"] = {"value": (km1 + est_kmers) / (dt1 + t_est), "build_value": km1 / max(dt1, 1e-9),
                                 "sample": f"passes 1-2 over the first {f1:.3%} of each arena's reads on one thread, "
