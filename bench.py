@@ -837,7 +837,7 @@ def run_reference(args, rank, world):
 
     build()
     _, bank, _, sample, n_sample, stats, _ = make_workload(0, args.scale)
-    per_step = max(5.0, min(20.0, 150.0 / max(args.steps + args.warmup, 1)))
+    per_step = min(args.cpu_seconds, max(5.0, min(20.0, 150.0 / max(args.steps + args.warmup, 1))))
     vals = []
     for i in range(args.warmup + args.steps):
         last = i == args.warmup + args.steps - 1
