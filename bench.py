@@ -357,8 +357,8 @@ def run_ours(args, rank, world, local):
             "roofline": {"kernel": ({"pass1": "pass 1 (k_pass1_sweep: 4 row-slice sweeps)",
                                      "pass2": "pass 2 (k_solid_sweep + k_emit + k_upsert)"} if kernel_ms["solid"][0] > 0 else
                                     {"pass1": "pass 1 (k_ladder_pass1: one sweep, t_solid-level gate ladder)",
-                                     "pass2": "pass 2 (k_emit_ladder2 + k_count_records + k_upsert)"
-                                     if kernel_ms["pass2_count"][0] > 0 else "pass 2 (k_emit_ladder2 + k_upsert)"})[dom],
+                                     "pass2": "pass 2 (k_emit_flat + k_count_records + k_upsert)"
+                                     if kernel_ms["pass2_count"][0] > 0 else "pass 2 (k_emit_flat + k_upsert)"})[dom],
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
                          "alg_bytes_per_pass": per_pass_bytes, "ms_per_pass": per_pass_ms,

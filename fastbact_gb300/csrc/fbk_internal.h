@@ -75,7 +75,7 @@ struct fbk_ctx {
     double record_factor = 1.25;          // bucket capacity / expected records per stripe
     int sketch_mode = 1;                  // 1: a build that does not return its sketch keeps only the gate ladder
     int ladder_ilp = 1;                   // windows per lane per step in the ladder pass 1 (1 or 2)
-    int emit_lookahead = 2;               // record emit: gate loads 1 or 2 chunks ahead; 3 = 2 ahead over a flattened window stream
+    int emit_lookahead = 3;               // record emit: gate loads 1 or 2 chunks ahead read by read; 3 = 2 ahead over a flattened window stream
     int upsert_all = 1;                   // 1: an unfiltered pass upserts every bucket in one persistent launch
     int acc_filter = 1;                   // keys with fewer records than min_trans_cov stay out of the table: 0 never, 1 for 256-bit keys, 2 always
     bool capturing = false;               // launches are being captured into a CUDA graph

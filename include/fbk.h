@@ -162,7 +162,7 @@ FBK_API fbk_status fbk_ctx_event_elapsed(fbk_ctx* ctx, int slot_a, int slot_b, d
  * 32..256 threads in steps of 32; grid 0 = occupancy), "sketch_mode" (1: a build that does not return its
  * sketch keeps only a threshold-ladder gate; 0: counted sketch), "ladder_ilp" (1 or 2
  * windows per lane in the ladder pass 1, 3 = pipelined over chunks), "emit_lookahead" (record emit with the gate
- * loads 1 or 2 chunks ahead, 3 = 2 ahead over a flattened window stream), "acc_filter"
+ * loads 1 or 2 chunks ahead read by read, 3 = 2 ahead over a flattened window stream, the default), "acc_filter"
  * (keys that cannot become SolidKmerNodes stay out of the table, see fbk_table_flags:
  * 0 never, 1 where it pays, 2 always).  Results do not depend on any of them. */
 FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double value);

@@ -466,7 +466,7 @@ TUNINGS = [
     dict(ladder_ilp=2, block_pass1=128),                 # two windows per lane in the ladder pass 1
     dict(ladder_ilp=3),                                   # ladder pass 1 pipelined over chunks
     dict(emit_lookahead=1),                               # gate loads one chunk ahead of the emit
-    dict(emit_lookahead=3),                               # emit over a flattened window stream
+    dict(emit_lookahead=2),                               # emit read by read, gate loads two chunks ahead
     dict(acc_filter=0),                                   # every accumulated key kept
     dict(acc_filter=2),                                   # keys that cannot be solid dropped at every width
     dict(upsert_all=0, acc_filter=0),                     # one upsert launch per bucket
