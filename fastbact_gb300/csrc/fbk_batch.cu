@@ -1373,7 +1373,9 @@ FBK_API fbk_status fbk_server_wait(fbk_server* S, uint64_t id, double timeout_ms
     auto f = S->reqs.find(id);
     if (f == S->reqs.end()) return FBK_ERR_INVALID;
     Req* r = f->second.get();
-    const auto until = std::chrono::steady_clock::now() + std::chrono::microseconds((int64_t)(timeout_ms * 1000.0));
+    // NaN or negative: no wait; infinite or huge: 1e12 ms (the microsecond count stays in int64)
+    const double tmo = timeout_ms > 0.0 ? std::min(timeout_ms, 1e12) : 0.0;
+    const auto until = std::chrono::steady_clock::now() + std::chrono::microseconds((int64_t)(tmo * 1000.0));
     while (r->state >= 0 && r->state < 4) {
         if (S->cv.wait_until(lk, until) == std::cv_status::timeout && r->state >= 0 && r->state < 4) {
             if (out) request_info(S, r, out);

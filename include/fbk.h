@@ -512,7 +512,8 @@ FBK_API fbk_status fbk_server_create(fbk_ctx* ctx, const fbk_server_params* p, f
 FBK_API fbk_status fbk_server_submit(fbk_server* s, const fbk_arena_view bank[3], const fbk_arena_view* sample,
                                      uint64_t sample_pairs, const fbk_count_stats* stats, uint64_t* id);
 FBK_API fbk_status fbk_server_poll(fbk_server* s, uint64_t id, fbk_request_info* out);
-/* Waits until the request is done or failed; FBK_ERR_NOT_READY after timeout_ms. */
+/* Waits until the request is done or failed; FBK_ERR_NOT_READY after timeout_ms
+ * (NaN or <= 0: no wait; values above 1e12, infinity included, count as 1e12). */
 FBK_API fbk_status fbk_server_wait(fbk_server* s, uint64_t id, double timeout_ms, fbk_request_info* out);
 /* Hands a done request's table to the caller (release it with fbk_table_release before
  * destroying the context) and frees the request's remaining device state. */
