@@ -708,6 +708,7 @@ FBK_API fbk_status fbk_bank_release(fbk_bank* b) {
 // CountMinSketch
 // ===========================================================================
 FBK_API uint64_t fbk_cms_width_for_genome_size(uint64_t g) {
+    if (g > (1ULL << 27) / 16) return 1ULL << 27;  // above the clamp (and no overflow of g * 16)
     uint64_t x = g * 16, t = 1;
     while (t < x) t <<= 1;
     return std::min<uint64_t>(std::max<uint64_t>(t, 1ULL << 21), 1ULL << 27);
@@ -1058,6 +1059,7 @@ FBK_API fbk_status fbk_hll_export(fbk_hll* h, uint8_t* regs, uint64_t n) {
 }
 
 FBK_API double fbk_hll_estimate_registers(const uint8_t* regs, uint32_t p) {
+    if (!regs || p < 4 || p > 18) return std::nan("");
     const uint64_t n = 1ULL << p;
     double sum = 0.0;
     uint64_t zeros = 0;
@@ -1173,12 +1175,6 @@ static fbk_status table_convert(fbk_table* t, uint64_t* acc_keys, uint16_t* acc_
         t->out_cap = cap;
     }
     return FBK_OK;
-}
-
-static uint64_t next_pow2(uint64_t x) {
-    uint64_t t = 1;
-    while (t < x) t <<= 1;
-    return t;
 }
 
 // The pass-1 gate kept as a threshold ladder instead of counts (fbk_k_ladder.cu).

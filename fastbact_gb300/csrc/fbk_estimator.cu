@@ -79,6 +79,7 @@ struct Buffers {
 extern "C" {
 
 FBK_API void fbk_estimator_defaults(fbk_estimator_params* p) {
+    if (!p) return;
     memset(p, 0, sizeof(*p));
     p->k = 21;
     p->cms_log2_width = 23;
@@ -90,7 +91,7 @@ FBK_API void fbk_estimator_defaults(fbk_estimator_params* p) {
 
 FBK_API int fbk_compute_dynamic_kmers(uint64_t median_len, int64_t target_max_k, uint64_t* out, int cap) {
     std::vector<uint64_t> v = dynamic_kmers(median_len, target_max_k);
-    for (int i = 0; i < (int)v.size() && i < cap; ++i) out[i] = v[i];
+    for (int i = 0; out && i < (int)v.size() && i < cap; ++i) out[i] = v[i];
     return (int)v.size();
 }
 

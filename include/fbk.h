@@ -217,7 +217,7 @@ FBK_API fbk_status fbk_hll_export(fbk_hll* h, uint8_t* regs, uint64_t n);
 FBK_API fbk_status fbk_hll_estimate(fbk_hll* h, double* out);
 FBK_API fbk_status fbk_hll_release(fbk_hll* h);
 /* HyperLogLog::estimate over host registers (f64, register order). */
-FBK_API double fbk_hll_estimate_registers(const uint8_t* regs, uint32_t p);
+FBK_API double fbk_hll_estimate_registers(const uint8_t* regs, uint32_t p); /* NaN unless regs and 4 <= p <= 18 */
 
 /* ---- ntHash (src/common/kmer.rs:385-477) --------------------------------------
  * Canonical ntHash of every window of length k of each read in the arena

@@ -249,3 +249,23 @@ def test_subsample_policy_branches():  # src/main.rs:76-180
         api.subsample_decide(api.subsample_policy(threshold_ratio=0.5), hi)
     with pytest.raises(N.FbkError):
         api.subsample_decide(api.subsample_policy(threshold_ratio=float("nan")), hi)
+
+
+def test_host_only_calls_at_their_edges():
+    """Host-only calls on edge inputs: sketch widths clamp at both ends (sketch.rs:165-168)
+    without overflowing g * 16; register estimates refuse what they cannot read; the
+    k ladder can be counted without an output buffer."""
+    lib = N.lib()
+    assert lib.fbk_cms_width_for_genome_size(0) == 1 << 21
+    assert lib.fbk_cms_width_for_genome_size(1_000_000) == 1 << 24
+    assert lib.fbk_cms_width_for_genome_size(5_000_000) == 1 << 27
+    for g in ((1 << 27) // 16, (1 << 27) // 16 + 1, 1 << 59, (1 << 60) + 1, (1 << 64) - 1):
+        assert lib.fbk_cms_width_for_genome_size(g) == 1 << 27
+    regs = np.zeros(1 << 14, dtype=np.uint8)
+    ptr = regs.ctypes.data_as(C.POINTER(C.c_uint8))
+    assert lib.fbk_hll_estimate_registers(ptr, 14) == 0.0   # all registers empty: zero cardinality
+    for p in (3, 19, 64):
+        assert np.isnan(lib.fbk_hll_estimate_registers(ptr, p))
+    assert np.isnan(lib.fbk_hll_estimate_registers(None, 14))
+    n = lib.fbk_compute_dynamic_kmers(150, -1, None, 16)
+    assert n == len(api.compute_dynamic_kmers(150)) and n > 0
