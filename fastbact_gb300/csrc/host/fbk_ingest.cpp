@@ -417,15 +417,17 @@ FBK_API fbk_status fbk_hbank_stats(const fbk_hbank* hb, uint64_t* input_pairs, u
 
 FBK_API void fbk_hbank_free(fbk_hbank* hb) { delete hb; }
 
-FBK_API uint64_t fbk_trim_adapter(const uint8_t* seq, uint64_t len) { return trim_adapter_len(seq, len); }
+FBK_API uint64_t fbk_trim_adapter(const uint8_t* seq, uint64_t len) { return seq ? trim_adapter_len(seq, len) : 0; }
 
 FBK_API int64_t fbk_trim_quality(const uint8_t* seq, const uint8_t* qual, uint64_t len, uint32_t min_qual, uint64_t min_len) {
+    if (!qual && len) return -1;
     return trim_quality_len(seq, qual, len, len, min_qual, min_len);
 }
 
 FBK_API int64_t fbk_merge_read_pair(const uint8_t* r1, const uint8_t* q1, uint64_t l1, const uint8_t* r2, const uint8_t* q2,
                                     uint64_t l2, uint64_t min_overlap, double max_mismatch_ratio, uint8_t* merged_out,
                                     uint64_t* overlap_len, uint64_t* mismatches) {
+    if ((!r1 && l1) || (!r2 && l2) || !merged_out) return -1;
     return merge_pair(r1, q1, l1, q1 ? l1 : 0, r2, q2, l2, q2 ? l2 : 0, min_overlap, max_mismatch_ratio, merged_out, overlap_len,
                       mismatches);
 }

@@ -134,6 +134,7 @@ using namespace fbk;
 extern "C" {
 
 FBK_API void fbk_synth_defaults(fbk_synth_params* p) {
+    if (!p) return;
     memset(p, 0, sizeof(*p));
     p->seed = 42;
     p->genome_len = 1000000;
@@ -154,6 +155,7 @@ FBK_API void fbk_synth_defaults(fbk_synth_params* p) {
 }
 
 FBK_API uint64_t fbk_synth_n_pairs(const fbk_synth_params* p) {
+    if (!p || p->read_len == 0) return 0;
     return (uint64_t)std::llround(p->coverage * (double)p->genome_len / (2.0 * (double)p->read_len));
 }
 

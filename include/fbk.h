@@ -548,7 +548,10 @@ FBK_API fbk_status fbk_hbank_arena(const fbk_hbank* hb, int arena, fbk_arena_vie
 FBK_API fbk_status fbk_hbank_stats(const fbk_hbank* hb, uint64_t* input_pairs, uint64_t* retained_pairs, uint64_t* merged_pairs,
                                    uint64_t* unmerged_pairs, uint64_t* bases_before_trim, uint64_t* bases_after_trim);
 FBK_API void fbk_hbank_free(fbk_hbank* hb);
-/* Single-pair helpers exposed for their known-answer tests. */
+/* Single-pair helpers exposed for their known-answer tests.  fbk_trim_adapter returns
+ * the kept length; fbk_trim_quality the kept length or -1 (read dropped, or no quality
+ * string); fbk_merge_read_pair the merged length (merged_out holds l1 + l2 bytes) or -1
+ * (no acceptable overlap, or a missing buffer). */
 FBK_API uint64_t fbk_trim_adapter(const uint8_t* seq, uint64_t len);
 FBK_API int64_t fbk_trim_quality(const uint8_t* seq, const uint8_t* qual, uint64_t len, uint32_t min_qual, uint64_t min_len);
 FBK_API int64_t fbk_merge_read_pair(const uint8_t* r1, const uint8_t* q1, uint64_t l1, const uint8_t* r2, const uint8_t* q2,

@@ -269,3 +269,13 @@ def test_host_only_calls_at_their_edges():
     assert np.isnan(lib.fbk_hll_estimate_registers(None, 14))
     n = lib.fbk_compute_dynamic_kmers(150, -1, None, 16)
     assert n == len(api.compute_dynamic_kmers(150)) and n > 0
+
+
+def test_single_pair_helpers_refuse_missing_buffers():
+    lib = N.lib()
+    assert lib.fbk_trim_adapter(None, 10) == 0
+    assert lib.fbk_trim_quality(None, None, 10, 20, 5) == -1
+    seq = np.frombuffer(b"ACGT" * 10, dtype=np.uint8)
+    ptr = seq.ctypes.data_as(C.POINTER(C.c_uint8))
+    assert lib.fbk_merge_read_pair(ptr, None, len(seq), None, None, len(seq), 10, 0.1, None, None, None) == -1
+    assert lib.fbk_merge_read_pair(ptr, None, len(seq), ptr, None, len(seq), 10, 0.1, None, None, None) == -1
