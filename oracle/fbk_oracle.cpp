@@ -784,7 +784,6 @@ ORC_API uint64_t orc_rev_comp_word(uint64_t w, unsigned n) { return rev_comp_wor
 ORC_API uint64_t orc_cms_width_for_genome_size(uint64_t g) { return CMS::width_for_genome_size(g); }
 
 // K-mer integer helpers; words are big-endian (most significant first), nw = 1, 2, 4.
-static int nw_for(int key_bits) { return key_bits == 64 ? 1 : key_bits == 128 ? 2 : key_bits == 256 ? 4 : 0; }
 
 ORC_API int orc_kmer_from_ascii(int key_bits, const uint8_t* s, unsigned k, uint64_t* out) {
     if (key_bits == 64) K64::from_ascii(s, k).words(out);
