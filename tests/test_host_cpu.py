@@ -279,3 +279,25 @@ def test_single_pair_helpers_refuse_missing_buffers():
     ptr = seq.ctypes.data_as(C.POINTER(C.c_uint8))
     assert lib.fbk_merge_read_pair(ptr, None, len(seq), None, None, len(seq), 10, 0.1, None, None, None) == -1
     assert lib.fbk_merge_read_pair(ptr, None, len(seq), ptr, None, len(seq), 10, 0.1, None, None, None) == -1
+
+
+def test_cohort_draws_stay_in_their_ranges():
+    """Cohort members (batches and serving) come from a splitmix64 stream per seed:
+    genome 2-7 Mbp, GC 0.30-0.68, depth 30-200x, the same values on every call."""
+    from fastbact_gb300 import cohort
+
+    draws = [cohort.draw(1000 + i) for i in range(64)]
+    assert draws == [cohort.draw(1000 + i) for i in range(64)]
+    for d in draws:
+        assert 2_000_000 <= d["genome_len"] <= 7_000_000
+        assert 0.30 <= d["gc"] <= 0.68
+        assert 30.0 <= d["coverage"] <= 200.0
+    assert len({d["genome_len"] for d in draws}) == 64
+    assert any(d["coverage"] > 150.0 for d in draws) and any(d["coverage"] < 110.0 for d in draws)
+    small = cohort.draw(1000, scale=0.001)
+    assert small["genome_len"] == 20_000 and small["gc"] == draws[0]["gc"]
+    m = cohort.make(1, first_seed=1000, scale=0.002, sample_pairs=5000)[0]
+    assert m.params == cohort.draw(1000, scale=0.002)
+    assert m.sample_pairs == min(5000, m.stats.exact_read_pairs) and len(m.sample) == 2 * m.sample_pairs
+    assert m.ingest.input_read_pairs == m.stats.exact_read_pairs
+    assert cohort.policy().threshold_ratio == 150.0 / 110.0
