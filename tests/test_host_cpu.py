@@ -301,3 +301,32 @@ def test_cohort_draws_stay_in_their_ranges():
     assert m.sample_pairs == min(5000, m.stats.exact_read_pairs) and len(m.sample) == 2 * m.sample_pairs
     assert m.ingest.input_read_pairs == m.stats.exact_read_pairs
     assert cohort.policy().threshold_ratio == 150.0 / 110.0
+
+
+def test_headers_compile_as_strict_c_and_link(tmp_path):
+    """The C ABI is usable from plain C (cgo, bindgen and ctypes callers see the same
+    declarations): both headers compile as C11 with -pedantic -Werror, and a C program
+    links against the library and calls host-only entry points."""
+    import shutil
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    lib_dir = Path(N.lib()._name).parent
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include "fbk.h"\n#include "fbk_synth.h"\n#include <stdio.h>\n'
+        "int main(void) {\n"
+        '    printf("%s %llu %d\\n", fbk_status_str(FBK_ERR_INVALID),\n'
+        "           (unsigned long long)fbk_cms_width_for_genome_size(1000000),\n"
+        "           fbk_ctx_set_tuning(NULL, \"stripes\", 8.0));\n"
+        "    return 0;\n}\n")
+    exe = tmp_path / "caller"
+    r = subprocess.run([gcc, "-std=c11", "-Wall", "-Wextra", "-Werror", "-pedantic", f"-I{ROOT / 'include'}",
+                        str(src), f"-L{lib_dir}", "-lfbk", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    msg, width, st = out.stdout.split()[:-2], int(out.stdout.split()[-2]), int(out.stdout.split()[-1])
+    assert " ".join(msg) == N.lib().fbk_status_str(1).decode()
+    assert width == 1 << 24 and st == 1
