@@ -330,3 +330,53 @@ def test_headers_compile_as_strict_c_and_link(tmp_path):
     msg, width, st = out.stdout.split()[:-2], int(out.stdout.split()[-2]), int(out.stdout.split()[-1])
     assert " ".join(msg) == N.lib().fbk_status_str(1).decode()
     assert width == 1 << 24 and st == 1
+
+
+STRUCT_MIRRORS = {
+    "fbk_arena_view": "ArenaView", "fbk_count_stats": "CountStats", "fbk_genome_estimate": "GenomeEstimate",
+    "fbk_estimator_params": "EstimatorParams", "fbk_subsample": "Subsample", "fbk_build_params": "BuildParams",
+    "fbk_subsample_policy": "SubsamplePolicy", "fbk_batch_params": "BatchParams", "fbk_batch_result": "BatchResult",
+    "fbk_batch_stats": "BatchStats", "fbk_ingest_stats": "IngestStatsC", "fbk_server_params": "ServerParams",
+    "fbk_request_info": "RequestInfo", "fbk_server_stats": "ServerStats", "fbk_synth_params": "SynthParams",
+}
+
+
+def test_ctypes_mirrors_match_the_c_layouts(tmp_path):
+    """Every struct of the C headers has a ctypes mirror with the same size and the same
+    field offsets (measured by the C compiler), and every declared function is bound with
+    as many arguments as the header declares."""
+    import shutil
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    declared = set()
+    for h in (ROOT / "include").glob("*.h"):
+        declared |= set(re.findall(r"\}\s*(fbk_\w+);", h.read_text()))
+    assert declared == set(STRUCT_MIRRORS)
+    lines = ['#include "fbk.h"', '#include "fbk_synth.h"', "#include <stddef.h>", "#include <stdio.h>",
+             "int main(void) {"]
+    for cname, pyname in STRUCT_MIRRORS.items():
+        py = getattr(N, pyname)
+        lines.append(f'    printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'    printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run([gcc, "-std=c11", f"-I{ROOT / 'include'}", str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60).stdout.split("\n")
+    for ln in filter(None, out):
+        cname, what, val = ln.split()
+        py = getattr(N, STRUCT_MIRRORS[cname])
+        got = C.sizeof(py) if what == "size" else getattr(py, what).offset
+        assert got == int(val), (cname, what, got, val)
+    # argument counts of every declared function
+    for h in (ROOT / "include").glob("*.h"):
+        txt = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"FBK_API\s+[^;{]*?\b(fbk_\w+)\s*\(([^;]*?)\)\s*;", txt, flags=re.S):
+            name, params = m.group(1), m.group(2).strip()
+            n = 0 if params in ("", "void") else params.count(",") + 1
+            assert name in N.SIGNATURES, name
+            assert len(N.SIGNATURES[name][1]) == n, (name, len(N.SIGNATURES[name][1]), n)
