@@ -1,28 +1,33 @@
 // fbk_noalloc.cu — the genome-estimator sample loop for callers that cannot
 // allocate device memory.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is being
-// captured on its stream (an allocation there breaks or invalidates the capture),
-// hosts whose device memory is owned by another runtime's allocator (a Rust or Go
-// service with its own pool, a framework that has reserved the whole GPU), and
-// latency-critical loops that must not take the allocator's locks or trigger an
-// implicit device synchronisation.  fbk_estimate_sample_noalloc serves them: it
-// needs no context and makes no allocating call.  Its scratch memory is the
-// file-scope device array below, FBK_NOALLOC_SCRATCH_BYTES (8 MiB) in size, which
-// every GPU that loads this library holds until the process exits.
+// Some callers cannot call cudaMalloc: hosts whose device memory is owned by another
+// runtime's allocator (a Rust or Go service with its own pool, a framework that has
+// reserved the whole GPU, so a cudaMalloc of ours would fail or fragment its pool),
+// and latency-critical loops that must not take the allocator's locks or trigger the
+// implicit device synchronisation a cudaFree can cause.  fbk_estimate_sample_noalloc
+// serves them: it needs no context and makes no allocating call.  Its scratch memory
+// is the file-scope device array below, FBK_NOALLOC_SCRATCH_BYTES (8 MiB) in size,
+// which every GPU that loads this library holds until the process exits.
+//
+// It is a blocking call: it copies the caller's host buffers to the array on the
+// caller's stream, waits for the stream (cudaStreamSynchronize) and evaluates the
+// estimator's checkpoints on the host.  So it cannot be recorded into a CUDA graph;
+// a call made on a stream that is being captured fails (the synchronisation is
+// refused there) and ends that capture.
 //
 // The sizes that fit: at most 20000 read pairs (40000 reads), at most 2^23 bases in
 // the sample, a count-min sketch of at most 2^18 columns per row, HyperLogLog
 // precision at most 14.  Larger requests are rejected with FBK_ERR_INVALID and a
-// message; nothing is launched for them.
+// message; nothing is copied or launched for them.
 //
 // The first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (with that device current) and caches it; make that first
-// call before any stream capture begins.  Every call on a device shares the same
-// array and leaves its contents behind; each call re-initialises every region it
-// reads before use (the first-occurrence table, the register segments, the padding
-// after the packed reads).  Calls whose GPU work overlaps — different streams, or
-// different host threads without ordering — race on the array, so serialise them.
+// cudaGetSymbolAddress (with that device current) and caches it.  Every call on a
+// device shares the same array and leaves its contents behind; each call
+// re-initialises every region it reads before use (the first-occurrence table, the
+// register segments, the padding after the packed reads).  Calls whose GPU work
+// overlaps — different streams, or different host threads without ordering — race on
+// the array, so serialise them.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -235,10 +240,11 @@ extern "C" FBK_API fbk_status fbk_estimate_sample_noalloc(int device, void* stre
     bv.keep_bits = nullptr;
     bv.r_begin = 0;
     bv.r_end = n_reads;
-    Launch L;
+    Launch L{};
     L.grid = sms * 4;
     L.block = 256;
     L.stream = st;
+    L.sms = sms;
     if (e == cudaSuccess) e = launch_est_firstpos(L, bv, d_kbase, k, d_first, log2w);
     if (e == cudaSuccess) e = launch_est_hll(L, bv, d_kbase, k, d_first, log2w, p, n_segs, d_rt, d_rs);
     if (e == cudaSuccess) e = launch_est_prefix(L, d_rt, p, n_segs);

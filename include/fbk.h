@@ -9,8 +9,7 @@
  * time; separate contexts are independent.  Each context owns one CUDA stream.
  *
  * Reference interfaces (paths inside the fastBact repository) that each group
- * replaces are cited next to the declarations.  The Rust-side binding a maintainer
- * adds to call these functions is shown in INTEGRATION.md.
+ * replaces are cited next to the declarations.
  */
 #ifndef FBK_H
 #define FBK_H
@@ -281,18 +280,20 @@ FBK_API fbk_status fbk_estimate_sample(fbk_ctx* ctx, const fbk_arena_view* sampl
 FBK_API fbk_status fbk_estimate_bank(fbk_ctx* ctx, const fbk_bank* sample, const uint32_t* read_lengths, uint64_t n_pairs,
                                      const fbk_count_stats* stats, const fbk_estimator_params* p, fbk_genome_estimate* out,
                                      uint8_t* regs_total, uint8_t* regs_solid);
-/* fbk_estimate_sample for callers that cannot allocate device memory (code running
- * during a CUDA graph capture, hosts whose device memory belongs to another
- * runtime's allocator, loops that must not take allocator locks).  This entry
- * point has no counterpart in the reference.  It takes no context and allocates
- * nothing: its scratch is one fixed device array of FBK_NOALLOC_SCRATCH_BYTES that
- * every GPU loading the library holds until exit.  Limits: at most 20000 sampled
- * pairs, 2^23 sample bases, cms_log2_width <= 18, hll_p <= 14 — larger requests
- * return FBK_ERR_INVALID with a message in err.  The first call on a device looks
- * up the array's address (cudaGetSymbolAddress); make it before any stream
- * capture.  Calls share the array: each clears what it reads, and calls whose GPU
- * work overlaps race, so serialise them.  stream: a cudaStream_t (NULL = default);
- * the call returns after its work on that stream has finished. */
+/* fbk_estimate_sample for callers that cannot allocate device memory: hosts whose
+ * device memory belongs to another runtime's allocator (a service with its own pool,
+ * a framework that reserved the GPU), and loops that must not take allocator locks
+ * or the synchronisation a cudaFree can cause.  This entry point has no counterpart
+ * in the reference.  It takes no context and allocates nothing: its scratch is one
+ * fixed device array of FBK_NOALLOC_SCRATCH_BYTES that every GPU loading the library
+ * holds until exit.  Limits: at most 20000 sampled pairs, 2^23 sample bases,
+ * cms_log2_width <= 18, hll_p <= 14 — larger requests return FBK_ERR_INVALID with a
+ * message in err, before anything is copied or launched.  The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress).  Calls share the array: each
+ * clears what it reads, and calls whose GPU work overlaps race, so serialise them.
+ * stream: a cudaStream_t (NULL = default).  The call blocks: it synchronises the
+ * stream and finishes the estimate on the host, so it cannot be recorded into a CUDA
+ * graph (on a capturing stream it fails and ends the capture). */
 #define FBK_NOALLOC_SCRATCH_BYTES (8u << 20)
 FBK_API fbk_status fbk_estimate_sample_noalloc(int device, void* stream, const fbk_arena_view* sample, uint64_t n_pairs,
                                                const fbk_count_stats* stats, const fbk_estimator_params* p,

@@ -1,10 +1,11 @@
 """The allocation-free estimator entry point (fbk_estimate_sample_noalloc) agrees
 exactly with fbk_estimate_sample on the same sample, on two calls in a row.
 
-It exists for callers that cannot call cudaMalloc — code running while a CUDA graph
-is captured, or hosts whose device memory belongs to another runtime's allocator —
-so it is called here through the C ABI with host buffers only.  This file is
-collected last so that a failure here does not stop the rest of the suite."""
+It exists for callers that cannot call cudaMalloc — hosts whose device memory belongs
+to another runtime's allocator, or loops that must not take allocator locks — so it is
+called here through the C ABI with host buffers only.  Requests beyond its fixed
+scratch (pairs, bases, sketch width, HLL precision) are refused before any copy.  This
+file is collected last so that a failure here does not stop the rest of the suite."""
 import ctypes as C
 
 import numpy as np
@@ -63,3 +64,24 @@ def test_noalloc_rejects_oversized_requests():
     assert st == 1 and "cms_log2_width" in msg
     st, _, _, _, msg = _noalloc(sample, n_pairs, stats, hll_p=16)
     assert st == 1 and "hll_p" in msg
+
+
+def test_noalloc_rejects_too_many_pairs():
+    # 30000 pairs at 150x of a 60 kb genome: 25000 sampled pairs exceed the 20000 limit
+    sample, n_pairs, stats = _sample(8, 60_000, 150.0, 25_000)
+    assert n_pairs > 20_000
+    st, _, _, _, msg = _noalloc(sample, n_pairs, stats, max_pairs=250_000)
+    assert st == 1 and "20000 sampled pairs" in msg
+
+
+def test_noalloc_rejects_too_many_bases():
+    # two pairs whose last read ends past base 2^23 (the sample's extent, not its
+    # length, sizes the packed copy)
+    n_words = ((1 << 23) + 256) // 32 + 1
+    data = np.zeros(n_words, np.uint64)
+    offsets = np.array([0, 100, 200, (1 << 23) + 10], np.uint64)
+    lengths = np.array([100, 100, 100, 100], np.uint32)
+    sample = api.BitSeqArena(data, offsets, lengths)
+    stats = api.ExactCountStats(2, 200, 200, 400, 100, 100, 100.0, 100)
+    st, _, _, _, msg = _noalloc(sample, 2, stats, max_pairs=250_000)
+    assert st == 1 and "2^23 sample bases" in msg
