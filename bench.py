@@ -35,12 +35,10 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-KS = [21, 33, 55, 77]
-WORKLOAD = dict(seed=43, genome_len=5_000_000, gc=0.51, n_repeats=7, repeat_len=5000, repeat_identity=0.99,
-                coverage=100.0, sub_rate=0.005, indel_rate=0.0)
-CMS_LOG2W = 24
+from fastbact_gb300 import workloads  # noqa: E402
+
+PLAIN_MODES = {"plain": workloads.ISOLATE_5MBP, "plain1m": workloads.PLAIN_1MBP}
 COUNTER_BITS = 16
-HLL_P = 14
 
 
 def parse():
@@ -54,9 +52,13 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
-    ap.add_argument("--mode", choices=["plain", "batch", "serve", "stress"], default="plain",
-                    help="plain: one isolate per step (the headline line); batch: a cohort in multi-isolate waves; "
-                         "serve: Poisson arrivals through the request loop")
+    ap.add_argument("--mode", choices=["plain", "plain1m", "batch", "serve", "stress"], default="plain",
+                    help="plain: the isolate-scale workload, one isolate per step (the headline line); plain1m: the "
+                         "1 Mbp 50x workload; batch: a cohort in multi-isolate waves; serve: Poisson arrivals through "
+                         "the request loop; stress: 12 Mbp at 300x, k = 127")
+    ap.add_argument("--no-check", action="store_true",
+                    help="skip the parity check of the timed step's outputs against the oracle")
+    ap.add_argument("--no-counted", action="store_true", help="skip timing the counted-sketch form of the step")
     ap.add_argument("--isolates", type=int, default=64, help="cohort size (batch and serve modes)")
     ap.add_argument("--genome-scale", type=float, default=1.0, help="cohort genome-size multiplier (quick runs)")
     return ap.parse_args()
@@ -135,17 +137,22 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # workload
 # ---------------------------------------------------------------------------
-def make_workload(rank: int, scale: float):
-    from fastbact_gb300 import api
-
-    wl = dict(WORKLOAD)
-    wl["seed"] = WORKLOAD["seed"] + 1000 * rank  # independent isolate per rank (weak scaling)
-    wl["coverage"] = WORKLOAD["coverage"] * scale
-    p = api.synth_params(**wl)
+def make_workload(wl: dict, rank: int, scale: float):
     t0 = time.time()
-    bank, st, sample, n_sample, stats = api.synth_isolate(p, threads=0, sample_pairs=150_000)
-    gen_s = time.time() - t0
-    return p, bank, st, sample, n_sample, stats, gen_s
+    p, bank, st, sample, n_sample, stats = workloads.generate(wl, rank=rank, coverage_scale=scale)
+    return p, bank, st, sample, n_sample, stats, time.time() - t0
+
+
+def plain_config(wl: dict, p, bank, stats, scale: float) -> dict:
+    """The workload as both arms name it: what was generated, not what came out."""
+    return {"workload": wl["text"] + (f" (coverage x{scale})" if scale != 1.0 else ""),
+            "genome_len": int(p.genome_len), "pairs": int(stats.exact_read_pairs), "bank_reads": bank.total_reads(),
+            "bank_bases": bank.total_bases(), "ks": list(wl["ks"]),
+            "cms": f"4 x 2^{wl['cms_log2w']} u16", "hll_p": wl["hll_p"], "t_solid": 2, "min_trans_cov": 3}
+
+
+def step_kmers(bank, ks) -> dict:
+    return {k: (kmers_in(bank, k, k), kmers_in(bank, k, k + 1)) for k in ks}
 
 
 _PINNED: list = []  # keeps the page-locked blocks alive for the process
@@ -172,6 +179,55 @@ def pinned_bank(bank):
     return api.ReadBank(*arenas)
 
 
+def ascii_reads(arena, n: int) -> list:
+    """The first n reads of an arena as ASCII (vectorised decode, for the oracle)."""
+    if n == 0:
+        return []
+    end = int(arena.offsets[n - 1]) + int(arena.lengths[n - 1])
+    g = np.arange(end, dtype=np.uint64)
+    codes = (arena.data[g >> np.uint64(5)] >> ((g & np.uint64(31)) << np.uint64(1))) & np.uint64(3)
+    s = np.frombuffer(b"ACGT", np.uint8)[codes.astype(np.intp)].tobytes()
+    return [s[int(o):int(o) + int(L)] for o, L in zip(arena.offsets[:n], arena.lengths[:n])]
+
+
+EST_FIELDS = ("genome_size", "exact_read_pairs", "total_bases", "median_read_len", "max_read_len", "estimated_cov",
+              "subsample_factor", "kmers", "n_kmers", "confidence", "u_ge_1", "u_ge_2", "sample_kmer_depth",
+              "pairs_sampled", "m_sample")
+
+
+def parity_check(wl, bank, sample, n_sample, stats, ge, regs, res) -> dict:
+    """Checks the timed step's outputs against the oracle on the same inputs: every
+    GenomeEstimate field and both HLL register arrays, and per k the SolidKmerNode
+    digest and row count (the same order-free digest the device computes)."""
+    from fastbact_gb300 import api
+    from oracle import orc
+
+    t0 = time.perf_counter()
+    out = {"estimate": True, "registers": True, "tables": {}}
+    rc, oe, ort, ors = orc.estimate_from_reads(ascii_reads(sample, 2 * n_sample), orc.count_stats(**stats.__dict__),
+                                               workloads.EST_MAX_PAIRS, workloads.EST_TARGET_COV, hll_p=wl["hll_p"])
+    gc = ge.to_c()
+    for f in EST_FIELDS:
+        g, o = getattr(gc, f), getattr(oe, f)
+        if f == "kmers":
+            g, o = list(g), list(o)
+        if rc != 0 or g != o:
+            out["estimate"] = False
+            out.setdefault("estimate_mismatch", []).append(f)
+    out["registers"] = bool(np.array_equal(regs[0], ort) and np.array_equal(regs[1], ors))
+    for (k, _, n_solid, _, digest) in res:
+        _, o_tab, _, mtc = orc.build_front(bank, k, api.key_bits_for_k(k), wl["cms_log2w"], 16, None, threads=0)
+        od, on = o_tab.digest(mtc)
+        del o_tab
+        out["tables"][str(k)] = {"digest_equal": od == digest, "n_solid": n_solid, "n_solid_equal": on == n_solid}
+    out["ok"] = out["estimate"] and out["registers"] and all(
+        v["digest_equal"] and v["n_solid_equal"] for v in out["tables"].values())
+    out["seconds"] = time.perf_counter() - t0
+    out["what"] = ("oracle (C++ restatement of the reference) on the same inputs: every GenomeEstimate field, both "
+                   "HLL register arrays, per k the SolidKmerNode digest and count of the last timed step")
+    return out
+
+
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
@@ -186,7 +242,9 @@ def run_ours(args, rank, world, local):
     if world > 1:
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    p, bank, ist, sample, n_sample, stats, gen_s = make_workload(rank, args.scale)
+    wl = PLAIN_MODES[args.mode]
+    KS, LOG2W, HLL_P = wl["ks"], wl["cms_log2w"], wl["hll_p"]
+    p, bank, ist, sample, n_sample, stats, gen_s = make_workload(wl, rank, args.scale)
     ctx = api.Context(local, pool_bytes=int(os.environ.get("FBK_POOL_BYTES", str(60 << 30))))
     tune = {}
     for kv in filter(None, os.environ.get("FBK_TUNE", "").split(",")):
@@ -197,15 +255,16 @@ def run_ours(args, rank, world, local):
     dbank = api.DeviceBank(ctx, bank)
     dsample = api.DeviceBank(ctx, sample)
     ctx.sync()
-    cb = args.counter_bits
+    cb = COUNTER_BITS
 
     def step(ctx, dbank, dsample, sample_lengths, export=False, outs=None):
-        ge, _, _ = api.estimate_bank(ctx, dsample, sample_lengths, n_sample, stats, max_pairs=250_000, target_cov=110.0)
+        ge, _, _ = api.estimate_bank(ctx, dsample, sample_lengths, n_sample, stats, max_pairs=workloads.EST_MAX_PAIRS,
+                                     target_cov=workloads.EST_TARGET_COV, hll_p=HLL_P)
         res = []
         for k in KS:
-            t = api.build_cdbg_ext(dbank, k, None, ge.genome_size, ctx=ctx, counter_bits=cb, cms_log2_width=CMS_LOG2W)
+            t = api.build_cdbg_ext(dbank, k, None, ge.genome_size, ctx=ctx, counter_bits=cb, cms_log2_width=LOG2W)
             info = t.info()
-            res.append((k, info[0], info[1], t.pushes()))
+            res.append((k, info[0], info[1], t.pushes(), t.digest()[0]))
             if export:
                 t.export(out=outs.get(k) if outs else None)
             t.release()
@@ -215,47 +274,69 @@ def run_ours(args, rank, world, local):
     for _ in range(args.warmup):
         ge, res = step(ctx, dbank, dsample, sample_len)
     kmers_est = ge.m_sample
-    kmers_pass = {k: (kmers_in(bank, k, k), kmers_in(bank, k, k + 1)) for k in KS}
-    kmers_step = kmers_est + sum(a + b for a, b in kmers_pass.values())
+    kmers_pass = step_kmers(bank, KS)
+    kmers_build = sum(a + b for a, b in kmers_pass.values())
+    kmers_step = kmers_est + kmers_build
+
+    def timed_region(n_steps):
+        clocks = ClockSampler(local)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        ctx.sync()
+        ctx.timing_reset()
+        ctx.set_timing(True)
+        launches0 = ctx.launch_count()
+        clocks.start()
+        ctx.record(0)
+        for _ in range(n_steps):
+            out = step(ctx, dbank, dsample, sample_len)
+        ctx.record(1)
+        ms = ctx.elapsed_ms(0, 1)
+        clk = clocks.stop()
+        ctx.sync()
+        torch.cuda.synchronize()
+        launches = ctx.launch_count() - launches0
+        kms = {n: ctx.timing(n) for n in ("pass1", "solid", "pass2_emit", "pass2_count", "pass2_upsert", "pass2_direct",
+                                          "convert", "table_init", "est_", "clamp", "cms_clamp", "subsample", "")}
+        ctx.set_timing(False)
+        if world > 1:
+            t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return out, ms, clk, launches, kms
 
     # ---- device-resident timed region -------------------------------------------
-    clocks = ClockSampler(local)
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    ctx.sync()
-    ctx.timing_reset()
-    ctx.set_timing(True)
-    launches0 = ctx.launch_count()
-    clocks.start()
-    ctx.record(0)
-    for _ in range(args.steps):
-        ge, res = step(ctx, dbank, dsample, sample_len)
-    ctx.record(1)
-    ms = ctx.elapsed_ms(0, 1)
-    clk = clocks.stop()
-    ctx.sync()
-    torch.cuda.synchronize()
-    launches = ctx.launch_count() - launches0
-    kernel_ms = {n: ctx.timing(n) for n in ("pass1", "solid", "pass2_emit", "pass2_count", "pass2_upsert", "pass2_direct",
-                                             "convert", "table_init", "est_", "clamp", "cms_clamp", "subsample")}
-    ctx.set_timing(False)
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    (ge, res), ms, clk, launches, kernel_ms = timed_region(args.steps)
     total_kmers = kmers_step * args.steps * world
     value = total_kmers / (ms / 1e3)
+
+    # ---- the same step with the counted u16 sketch (what a caller asking for the
+    # sketch gets); the headline keeps only the t_solid-level gate ladder -----------
+    counted = None
+    if not args.no_counted:
+        old_mode = ctx.get_tuning("sketch_mode")
+        ctx.set_tuning(sketch_mode=0)
+        step(ctx, dbank, dsample, sample_len)
+        (_, res_c), ms_c, clk_c, _, kms_c = timed_region(max(1, min(args.steps, 5)))
+        ctx.set_tuning(sketch_mode=old_mode)
+        n_c = max(1, min(args.steps, 5))
+        counted = {"value": kmers_step * n_c * world / (ms_c / 1e3), "unit": "k-mers/s", "ms_per_step": ms_c / n_c,
+                   "steps": n_c, "same_tables": [r[4] for r in res_c] == [r[4] for r in res],
+                   "kernel_ms_per_step": {k: v[0] / n_c for k, v in kms_c.items() if v[0] > 0 and k},
+                   "clocks": clk_c,
+                   "what": "pass 1 keeps exact u32 counts (read as u16 saturating), 4 row-slice sweeps, solidity "
+                           "bitmap from the counts; same tables as the ladder gate"}
 
     # ---- roofline of the dominant pass --------------------------------------------
     # Algorithmic bytes per pass (per k-mer occurrence): pass 1 = packed input +
     # 4 counters read and written (8 c_b); pass 2 = packed input + 4 counters read
     # (4 c_b) + 2 x (entry read + written) per transition push, entry = key + cov (2)
-    # + 8 edge counters (16).  c_b = 2 bytes (u16 sketch) or 0.5 (nibble).
-    c_b = 0.5 if cb == 4 else 2.0
+    # + 8 edge counters (16); c_b = 2 bytes (u16 sketch).
+    c_b = 2.0
     bank_bytes = bank.total_bases() / 4.0
-    key_bytes = {21: 8, 33: 16, 55: 16, 77: 32}
-    pushes = {k: pu for (k, _, _, pu) in res}
+    key_bytes = {k: 8 * (api.key_bits_for_k(k) // 64) for k in KS}
+    pushes = {r[0]: r[3] for r in res}
     fam_ms = {
         "pass1": kernel_ms["pass1"][0],
         "pass2": kernel_ms["solid"][0] + kernel_ms["pass2_emit"][0] + kernel_ms["pass2_count"][0]
@@ -276,13 +357,13 @@ def run_ours(args, rank, world, local):
     else:
         peak = 6800.0
         peak_src = "fallback"
-    traffic = None
+    traffic, traffic_src = None, None
     tpath = ROOT / "profiles" / "traffic.txt"
-    if tpath.exists():
+    if tpath.exists() and args.mode == "plain":
         for ln in tpath.read_text().splitlines():
             f = ln.split()
-            if len(f) >= 2 and f[0] == f"{dom}_{'u16' if cb == 16 else 'nibble'}":
-                traffic = float(f[1])
+            if len(f) >= 2 and f[0] == f"{dom}_u16":
+                traffic, traffic_src = float(f[1]), "profiles/traffic.txt (ncu dram__bytes, one pass of one k)"
 
     # ---- end to end through the C ABI from pinned host memory ------------------------
     e2e = None
@@ -305,7 +386,7 @@ def run_ours(args, rank, world, local):
             return ge2, res2
 
         _, res0 = e2e_step()
-        for (k, _, n_solid, _) in res0:
+        for (k, _, n_solid, _, _) in res0:
             nw = key_bytes[k] // 8
             outs[k] = (pinned_copy(np.zeros((n_solid, nw), np.uint64)), pinned_copy(np.zeros(n_solid, np.uint16)),
                        pinned_copy(np.zeros(n_solid, np.uint8)))
@@ -325,35 +406,50 @@ def run_ours(args, rank, world, local):
             t = torch.tensor([e_ms], dtype=torch.float64, device="cuda")
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             e_ms = float(t.item())
-        d2h = sum(n_solid * ((key_bytes[k]) + 2 + 1) for (k, _, n_solid, _) in res2)
+        d2h = sum(n_solid * ((key_bytes[k]) + 2 + 1) for (k, _, n_solid, _, _) in res2)
         e2e = {"value": total_kmers / (e_ms / 1e3), "unit": "k-mers/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": e_ms / args.steps}
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e_ms / args.steps,
+               "same_tables": [r[4] for r in res2] == [r[4] for r in res]}
+
+    # ---- parity of the timed step against the oracle ----------------------------
+    parity = None
+    if rank == 0 and not args.no_check:
+        _, rt, rs = api.estimate_bank(ctx, dsample, sample_len, n_sample, stats, want_registers=True,
+                                      max_pairs=workloads.EST_MAX_PAIRS, target_cov=workloads.EST_TARGET_COV,
+                                      hll_p=HLL_P)
+        parity = parity_check(wl, bank, sample, n_sample, stats, ge, (rt, rs), res)
 
     # ---- CPU baseline (oracle restatement, bounded sample) ------------------------
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_arm(bank, sample, n_sample, stats, budget_s=args.cpu_seconds, single_s=3.0)
+        cpu = cpu_arm(wl, bank, sample, n_sample, stats, budget_s=args.cpu_seconds, single_s=3.0)
 
     if rank == 0:
+        est_ms = kernel_ms["est_"][0] / args.steps
+        build_ms = ms / args.steps - est_ms
         line = {
             "metric": "k-mers/s ntHash+CMS+HLL+count (estimator + multi-k build front end)",
             "value": value, "unit": "k-mers/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "u64/u16 integer", "data": "synthetic (seeded generator; no dataset)",
-            "config": {
-                "workload": "isolate-scale plain method: 5 Mbp genome GC 0.51, 7x5 kb repeats >=99% id, "
-                            "PE150 100x (1.67M pairs), N(350,30) fragments, 0.5% subs, Phred tail decay; "
-                            "multi-k 21,33,55 (64/128-bit) + 77 (256-bit)",
-                "genome_len": p.genome_len, "pairs": stats.exact_read_pairs, "bank_reads": bank.total_reads(),
-                "bank_bases": bank.total_bases(), "ks": KS, "cms": f"4 x 2^{CMS_LOG2W} {'u16' if cb == 16 else 'nibble'}",
-                "hll_p": HLL_P, "estimator_kmers": kmers_est,
-                "pass_kmers": {str(k): kmers_pass[k] for k in KS},
-                "solid": {str(k): n for (k, _, n, _) in res}, "table_keys": {str(k): n for (k, n, _, _) in res},
-                "genome_size_est": ge.genome_size, "parallelism": f"replicas x{world} (one isolate per GPU)",
-                "l2": "per-step working set exceeds L2 (bank 115 MB + CMS 128 MB + solid tables >= 1 GB)",
-                "generation_s": round(gen_s, 1), "tuning": tune,
-            },
-            "kernel_ms": {k: {"ms": v[0], "launches": v[1]} for k, v in kernel_ms.items()},
+            "config": dict(plain_config(wl, p, bank, stats, args.scale),
+                           parallelism=f"replicas x{world} (one isolate per GPU)",
+                           l2="inputs larger than L2: bank + 4 x 2^w sketch gate + solid tables of GBs per k"),
+            "parity_checked": bool(parity and parity["ok"]),
+            "parity": parity,
+            "results": {"estimator_kmers": kmers_est, "pass_kmers": {str(k): kmers_pass[k] for k in KS},
+                        "solid": {str(r[0]): r[2] for r in res}, "table_keys": {str(r[0]): r[1] for r in res},
+                        "digests": {str(r[0]): hex(r[4]) for r in res}, "genome_size_est": ge.genome_size,
+                        "generation_s": round(gen_s, 1), "tuning": tune,
+                        "gate": "t_solid-level threshold ladder (exact: the gate reads only min_r count_r >= t_solid)"},
+            "stages": {"estimator": {"kmers": kmers_est, "ms_per_step": est_ms,
+                                     "kmers_per_s": kmers_est / (est_ms / 1e3) if est_ms > 0 else None,
+                                     "note": "device kernel time of the estimator stages"},
+                       "build": {"kmers": kmers_build, "ms_per_step": build_ms,
+                                 "kmers_per_s": kmers_build / (build_ms / 1e3),
+                                 "note": "step time minus the estimator kernels"}},
+            "counted_sketch": counted,
+            "kernel_ms": {k or "all": {"ms": v[0], "launches": v[1]} for k, v in kernel_ms.items()},
             "roofline": {"kernel": ({"pass1": "pass 1 (k_pass1_sweep: 4 row-slice sweeps)",
                                      "pass2": "pass 2 (k_solid_sweep + k_emit + k_upsert)"} if kernel_ms["solid"][0] > 0 else
                                     {"pass1": "pass 1 (k_ladder_pass1: one sweep, t_solid-level gate ladder)",
@@ -361,6 +457,7 @@ def run_ours(args, rank, world, local):
                                      if kernel_ms["pass2_count"][0] > 0 else "pass 2 (k_emit_flat + k_upsert)"})[dom],
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+                         "traffic_source": traffic_src,
                          "alg_bytes_per_pass": per_pass_bytes, "ms_per_pass": per_pass_ms,
                          "note": "per pass = one k of one step; achieved = algorithmic bytes / event-timed kernel time"},
             # the second figure the path is bound by: L2 atomics, counted as the edge-counter
@@ -378,6 +475,8 @@ def run_ours(args, rank, world, local):
     if world > 1:
         torch.distributed.destroy_process_group()
     ctx.close()
+    if parity is not None and not parity["ok"]:
+        sys.exit(1)
 
 
 # ---------------------------------------------------------------------------
@@ -539,8 +638,7 @@ def run_batch_mode(args):
 # ---------------------------------------------------------------------------
 # stress mode: 12 Mbp GC 0.66 genome, repeats and a tandem array, 300x, k = 127
 # ---------------------------------------------------------------------------
-STRESS = dict(seed=46, genome_len=12_000_000, gc=0.66, n_repeats=10, repeat_len=5000, repeat_identity=0.99,
-              tandem_copies=200, tandem_unit=60, coverage=300.0, sub_rate=0.01, indel_rate=0.0005)
+STRESS = workloads.STRESS_12MBP["gen"]
 
 
 def run_stress_mode(args):
@@ -768,19 +866,26 @@ def run_serve_mode(args):
 # ---------------------------------------------------------------------------
 # CPU arm: the oracle restatement of the reference algorithm, multithreaded
 # ---------------------------------------------------------------------------
-def cpu_arm(bank, sample, n_sample, stats, budget_s: float, threads: int = 0, single_s: float = 0.0):
-    """Times the reference algorithm (estimator sample loop + build passes 1-2 for each
-    k) on a bounded prefix of the bank's reads; returns k-mers/s.  With single_s > 0 the
-    build passes also run on one thread for about single_s seconds (the estimator's
-    sample loop is sequential in the reference, so its time is shared by both figures)."""
+def cpu_arm(wl, bank, sample, n_sample, stats, budget_s: float, threads: int = 0, single_s: float = 0.0):
+    """Times the reference algorithm on the host cores, with the GPU step's mix of work.
+
+    The estimator's sample loop (sequential in the reference, estimator.rs:309-379) runs
+    on its whole sample; the build passes 1-2 for each k (rayon-parallel in the
+    reference, build.rs:93-116,243-289) run on a bounded prefix of each arena's reads,
+    sized to the budget.  `value` is the step's k-mers (estimator + every pass of every
+    k, the GPU step's own count) over the estimator's measured time plus the build
+    k-mers at the measured build rate: the same estimator:build mix as the GPU step.
+    With single_s > 0 the build passes are also timed on one thread."""
     from fastbact_gb300 import api
     from oracle import orc
 
+    ks, log2w = wl["ks"], wl["cms_log2w"]
     cores = threads or os.cpu_count() or 1
-    reads = [sample.extract_ascii(i) for i in range(2 * min(n_sample, 150_000))]
+    reads = ascii_reads(sample, 2 * min(n_sample, 150_000))
     ost = orc.count_stats(**stats.__dict__)
     t0 = time.perf_counter()
-    rc, oe, _, _ = orc.estimate_from_reads(reads, ost, 250_000, 110.0)
+    rc, oe, _, _ = orc.estimate_from_reads(reads, ost, workloads.EST_MAX_PAIRS, workloads.EST_TARGET_COV,
+                                           hll_p=wl["hll_p"])
     t_est = time.perf_counter() - t0
     est_kmers = oe.m_sample
 
@@ -802,30 +907,35 @@ def cpu_arm(bank, sample, n_sample, stats, budget_s: float, threads: int = 0, si
         b = sub_bank(frac)
         t = time.perf_counter()
         km = 0
-        for k in KS:
+        for k in ks:
             kb = api.key_bits_for_k(k)
-            cms, tab, _, _ = orc.build_front(b, k, kb, CMS_LOG2W, 4, None, threads=nt)
+            cms, tab, _, _ = orc.build_front(b, k, kb, log2w, 4, None, threads=nt)
             del cms, tab
             km += kmers_in(b, k, k) + kmers_in(b, k, k + 1)
         return km, time.perf_counter() - t
 
     km, dt = run(0.005, cores)
     rate = km / max(dt, 1e-6)
-    full = sum(kmers_in(bank, k, k) + kmers_in(bank, k, k + 1) for k in KS)
+    full = sum(kmers_in(bank, k, k) + kmers_in(bank, k, k + 1) for k in ks)
     frac = min(1.0, max(0.005, (budget_s - t_est) * rate / max(full, 1)))
     km, dt = run(frac, cores)
-    value = (km + est_kmers) / (dt + t_est)
-    out = {"value": value, "unit": "k-mers/s", "cores": cores, "kind": "port",
-           "sample": f"estimator sample loop ({est_kmers} k-mers, sequential as in the reference) + passes 1-2 at "
-                     f"k={KS} over the first {frac:.3%} of each arena's reads (nibble CMS, 64 mutex shards)",
-           "seconds": dt + t_est, "build_value": km / max(dt, 1e-9), "estimator_seconds": t_est}
+    build_rate = km / max(dt, 1e-9)
+    step_s = t_est + full / build_rate  # the whole step at the measured stage rates
+    out = {"value": (est_kmers + full) / step_s, "unit": "k-mers/s", "cores": cores, "kind": "port",
+           "sample": f"estimator sample loop over its whole sample ({est_kmers} k-mers, sequential as in the "
+                     f"reference) + passes 1-2 at k={ks} over the first {frac:.3%} of each arena's reads (nibble CMS, "
+                     f"64 mutex shards); value = the step's k-mers over estimator time + build k-mers at the build rate",
+           "seconds": dt + t_est, "projected_step_s": step_s,
+           "stages": {"estimator": {"kmers": est_kmers, "seconds": t_est, "kmers_per_s": est_kmers / max(t_est, 1e-9)},
+                      "build": {"kmers_sampled": km, "kmers_step": full, "seconds": dt, "kmers_per_s": build_rate}}}
     if single_s > 0:
         km1, dt1 = run(0.001, 1)
         f1 = min(1.0, max(0.001, single_s * (km1 / max(dt1, 1e-6)) / max(full, 1)))
         km1, dt1 = run(f1, 1)
-        out["single_thread"] = {"value": (km1 + est_kmers) / (dt1 + t_est), "build_value": km1 / max(dt1, 1e-9),
+        r1 = km1 / max(dt1, 1e-9)
+        out["single_thread"] = {"value": (est_kmers + full) / (t_est + full / r1), "build_kmers_per_s": r1,
                                 "sample": f"passes 1-2 over the first {f1:.3%} of each arena's reads on one thread, "
-                                          f"plus the same estimator sample loop",
+                                          f"plus the same estimator sample loop (which is sequential anyway)",
                                 "seconds": dt1 + t_est}
     return out
 
@@ -833,26 +943,38 @@ def cpu_arm(bank, sample, n_sample, stats, budget_s: float, threads: int = 0, si
 def run_reference(args, rank, world):
     if rank != 0:
         return
+    if args.mode not in PLAIN_MODES:
+        print(json.dumps({"impl": "reference", "unavailable": f"--mode {args.mode} has no CPU counterpart in the "
+                          "reference (it counts one isolate per process)"}), flush=True)
+        return
     from fastbact_gb300.build import build
+    from oracle import orc
 
-    build()
-    _, bank, _, sample, n_sample, stats, _ = make_workload(0, args.scale)
+    build()  # compiles; loads nothing (the generator and the oracle are host-only libraries)
+    orc.build()
+    wl = PLAIN_MODES[args.mode]
+    p, bank, _, sample, n_sample, stats, _ = make_workload(wl, 0, args.scale)
     per_step = min(args.cpu_seconds, max(5.0, min(20.0, 150.0 / max(args.steps + args.warmup, 1))))
     vals = []
     for i in range(args.warmup + args.steps):
         last = i == args.warmup + args.steps - 1
-        r = cpu_arm(bank, sample, n_sample, stats, budget_s=per_step, single_s=3.0 if last else 0.0)
+        r = cpu_arm(wl, bank, sample, n_sample, stats, budget_s=per_step, single_s=3.0 if last else 0.0)
         if i >= args.warmup:
             vals.append(r)
     v = float(np.mean([r["value"] for r in vals]))
+    est_rate = float(np.mean([r["stages"]["estimator"]["kmers_per_s"] for r in vals]))
+    build_rate = float(np.mean([r["stages"]["build"]["kmers_per_s"] for r in vals]))
     line = {"impl": "reference", "metric": "k-mers/s ntHash+CMS+HLL+count (estimator + multi-k build front end)",
             "value": v, "unit": "k-mers/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": float(np.mean([r["seconds"] for r in vals])) * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u64/u8 integer", "data": "synthetic (seeded generator)",
-            "config": {"workload": "isolate-scale plain method (same as the GPU arm), bounded sample per step",
-                       "ks": KS},
+            "ms_per_step": float(np.mean([r["projected_step_s"] for r in vals])) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64/u8 integer", "data": "synthetic (seeded generator; no dataset)",
+            "config": dict(plain_config(wl, p, bank, stats, args.scale),
+                           parallelism=f"replicas x{world} (one isolate per GPU)",
+                           l2="inputs larger than L2: bank + 4 x 2^w sketch gate + solid tables of GBs per k"),
+            "stages": {"estimator": {"kmers_per_s": est_rate}, "build": {"kmers_per_s": build_rate}},
             "cpu_baseline": {"value": v, "unit": "k-mers/s", "cores": vals[0]["cores"], "kind": "port",
-                             "sample": vals[0]["sample"], "single_thread": vals[-1].get("single_thread")},
+                             "sample": vals[0]["sample"], "stages": vals[-1]["stages"],
+                             "single_thread": vals[-1].get("single_thread")},
             "e2e": {"value": v, "unit": "k-mers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

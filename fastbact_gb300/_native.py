@@ -1,9 +1,9 @@
 """ctypes binding of the C ABI in include/fbk.h and include/fbk_synth.h.
 
-The library is loaded from fastbact_gb300/_lib/libfbk.so (built in-tree by
-fastbact_gb300.build).  There is no fallback: if the library is missing the
-import of anything that needs it raises, so no CPU path can stand in for the
-device kernels.
+The device library is loaded from fastbact_gb300/_lib/libfbk.so and the seeded
+input generator from fastbact_gb300/_lib/libfbk_synth.so (both built in-tree by
+fastbact_gb300.build).  There is no fallback: if a library is missing, anything
+that needs it raises, so no CPU path can stand in for the device kernels.
 """
 from __future__ import annotations
 
@@ -14,6 +14,7 @@ from pathlib import Path
 import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libfbk.so"
+SYNTH_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libfbk_synth.so"
 
 u8p = C.POINTER(C.c_uint8)
 u16p = C.POINTER(C.c_uint16)
@@ -181,6 +182,7 @@ SIGNATURES = {
     "fbk_table_pushes": (S, [vp, u64p]),
     "fbk_table_flags": (S, [vp, u32p]),
     "fbk_table_digest": (S, [vp, u64p, u64p]),
+    "fbk_table_acc_digest": (S, [vp, u64p, u64p]),
     "fbk_table_release": (S, [vp]),
     "fbk_estimator_defaults": (None, [P(EstimatorParams)]),
     "fbk_estimate_sample": (S, [vp, P(ArenaView), C.c_uint64, P(CountStats), P(EstimatorParams), P(GenomeEstimate), u8p, u8p]),
@@ -235,6 +237,11 @@ SIGNATURES = {
     "fbk_trim_adapter": (C.c_uint64, [u8p, C.c_uint64]),
     "fbk_trim_quality": (C.c_int64, [u8p, u8p, C.c_uint64, C.c_uint32, C.c_uint64]),
     "fbk_merge_read_pair": (C.c_int64, [u8p, u8p, C.c_uint64, u8p, u8p, C.c_uint64, C.c_uint64, C.c_double, u8p, u64p, u64p]),
+}
+
+# include/fbk_synth.h, exported by libfbk_synth.so (with the host-bank accessors of
+# the banks it returns)
+SYNTH_SIGNATURES = {
     "fbk_synth_defaults": (None, [P(SynthParams)]),
     "fbk_synth_n_pairs": (C.c_uint64, [P(SynthParams)]),
     "fbk_synth_genome": (S, [P(SynthParams), u8p]),
@@ -242,6 +249,9 @@ SIGNATURES = {
     "fbk_synth_write_fastq": (S, [P(SynthParams), C.c_char_p, C.c_char_p]),
     "fbk_synth_isolate": (S, [P(SynthParams), C.c_int, C.c_uint64, C.c_uint32, C.c_int, C.c_int, P(vp), C.c_uint64, P(vp),
                               P(CountStats)]),
+    "fbk_hbank_arena": (S, [vp, C.c_int, P(ArenaView)]),
+    "fbk_hbank_stats": (S, [vp, u64p, u64p, u64p, u64p, u64p, u64p]),
+    "fbk_hbank_free": (None, [vp]),
 }
 
 _lib = None
@@ -261,6 +271,24 @@ def lib() -> C.CDLL:
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+_synth_lib = None
+
+
+def synth_lib() -> C.CDLL:
+    """Loads libfbk_synth.so, the seeded input generator (raises if it was not built)."""
+    global _synth_lib
+    if _synth_lib is None:
+        if not SYNTH_LIB_PATH.exists():
+            raise RuntimeError(f"{SYNTH_LIB_PATH} is missing: run fastbact_gb300.build.build()")
+        L = C.CDLL(str(SYNTH_LIB_PATH))
+        for name, (res, args) in SYNTH_SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _synth_lib = L
+    return _synth_lib
 
 
 class FbkError(RuntimeError):
@@ -304,7 +332,7 @@ def arena_view(data: np.ndarray, offsets: np.ndarray, lengths: np.ndarray, pair_
 
 
 def exported_symbols() -> list[str]:
-    return sorted(SIGNATURES)
+    return sorted(set(SIGNATURES) | set(SYNTH_SIGNATURES))
 
 
 os.environ.setdefault("CUDA_MODULE_LOADING", "LAZY")

@@ -238,8 +238,9 @@ def _arena_from_view(v: N.ArenaView) -> BitSeqArena:
                        cp(v.lengths, v.n_seqs, np.uint32), cp(v.pair_idx, v.n_seqs, np.uint32))
 
 
-def _bank_from_hbank(h) -> tuple[ReadBank, IngestStats]:
-    L = N.lib()
+def _bank_from_hbank(h, L=None) -> tuple[ReadBank, IngestStats]:
+    """Copies a host bank out; L is the library that made it (libfbk or libfbk_synth)."""
+    L = L or N.lib()
     arenas = []
     for i in range(3):
         v = N.ArenaView()
@@ -701,6 +702,12 @@ class SolidTable:
         check(N.lib().fbk_table_pushes(self._h, C.byref(n)))
         return n.value
 
+    def acc_digest(self) -> tuple[int, int]:
+        """(order-free digest of every accumulated key with its KmerAcc, n_keys)."""
+        d, n = C.c_uint64(), C.c_uint64()
+        check(N.lib().fbk_table_acc_digest(self._h, C.byref(d), C.byref(n)), self.ctx.handle, "accumulator digest")
+        return d.value, n.value
+
     def digest(self) -> tuple[int, int]:
         d, n = C.c_uint64(), C.c_uint64()
         check(N.lib().fbk_table_digest(self._h, C.byref(d), C.byref(n)))
@@ -1111,7 +1118,7 @@ class Server:
 # ---------------------------------------------------------------------------
 def synth_params(**kw) -> N.SynthParams:
     p = N.SynthParams()
-    N.lib().fbk_synth_defaults(C.byref(p))
+    N.synth_lib().fbk_synth_defaults(C.byref(p))
     for k, v in kw.items():
         setattr(p, k, v)
     return p
@@ -1124,30 +1131,30 @@ def synth_isolate(params: N.SynthParams, threads: int = 0, min_len: int = 30, mi
     pairs, ExactCountStats)."""
     hb, hs = C.c_void_p(), C.c_void_p()
     cs = N.CountStats()
-    check(N.lib().fbk_synth_isolate(C.byref(params), threads, min_len, min_qual, int(enable_trim), int(enable_merge),
+    check(N.synth_lib().fbk_synth_isolate(C.byref(params), threads, min_len, min_qual, int(enable_trim), int(enable_merge),
                                     C.byref(hb), sample_pairs, C.byref(hs) if sample_pairs else None, C.byref(cs)),
           None, "synth isolate")
     try:
-        bank, st = _bank_from_hbank(hb)
+        bank, st = _bank_from_hbank(hb, N.synth_lib())
         sample = None
         if sample_pairs:
-            sbank, _ = _bank_from_hbank(hs)
+            sbank, _ = _bank_from_hbank(hs, N.synth_lib())
             sample = sbank.merged_reads
     finally:
-        N.lib().fbk_hbank_free(hb)
+        N.synth_lib().fbk_hbank_free(hb)
         if sample_pairs:
-            N.lib().fbk_hbank_free(hs)
+            N.synth_lib().fbk_hbank_free(hs)
     n_sample = len(sample) // 2 if sample is not None else 0
     return bank, st, sample, n_sample, ExactCountStats.from_c(cs)
 
 
 def synth_write_fastq(params: N.SynthParams, r1: str, r2: str) -> None:
-    check(N.lib().fbk_synth_write_fastq(C.byref(params), str(r1).encode(), str(r2).encode()), None, "synth fastq")
+    check(N.synth_lib().fbk_synth_write_fastq(C.byref(params), str(r1).encode(), str(r2).encode()), None, "synth fastq")
 
 
 def synth_genome(params: N.SynthParams) -> bytes:
     g = np.zeros(params.genome_len, np.uint8)
-    check(N.lib().fbk_synth_genome(C.byref(params), ptr(g)))
+    check(N.synth_lib().fbk_synth_genome(C.byref(params), ptr(g)))
     return g.tobytes()
 
 
@@ -1155,7 +1162,7 @@ def synth_pairs(params: N.SynthParams, genome: bytes, first: int, n: int):
     L = params.read_len
     bufs = [np.zeros(n * L, np.uint8) for _ in range(4)]
     g = np.frombuffer(genome, np.uint8).copy()
-    check(N.lib().fbk_synth_pairs(C.byref(params), ptr(g), first, n, *[ptr(b) for b in bufs]))
+    check(N.synth_lib().fbk_synth_pairs(C.byref(params), ptr(g), first, n, *[ptr(b) for b in bufs]))
     return [b.reshape(n, L) for b in bufs]
 
 

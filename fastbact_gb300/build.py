@@ -1,4 +1,7 @@
-"""Builds the native library fastbact_gb300/_lib/libfbk.so in-tree.
+"""Builds the native libraries in-tree: fastbact_gb300/_lib/libfbk.so (the device
+path and its host side) and fastbact_gb300/_lib/libfbk_synth.so (the seeded input
+generator, a host-only library of its own so that a CPU-only caller generating
+workloads never maps the device library).
 
 CUDA translation units are compiled for sm_103a only; host C++ units with g++.
 -ffp-contract=off keeps the estimator's f64 host arithmetic free of fused
@@ -21,6 +24,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 LIB_DIR = PKG / "_lib"
 LIB = LIB_DIR / "libfbk.so"
+SYNTH_LIB = LIB_DIR / "libfbk_synth.so"
 BUILD_DIR = ROOT / "_build" / "fbk"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -44,6 +48,11 @@ def sources() -> tuple[list[Path], list[Path]]:
     return cu, cpp
 
 
+def synth_sources() -> list[Path]:
+    """The generator plus the host ingest it runs to make a read bank."""
+    return sorted((CSRC / "synth").glob("*.cpp")) + [CSRC / "host" / "fbk_ingest.cpp", CSRC / "host" / "fbk_workers.cpp"]
+
+
 def _digest(files: list[Path]) -> str:
     h = hashlib.sha256()
     for f in sorted(files):
@@ -55,13 +64,16 @@ def _digest(files: list[Path]) -> str:
 
 def build(verbose: bool = False, force: bool = False) -> Path:
     cu, cpp = sources()
+    synth = synth_sources()
     headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((CSRC / "host").glob("*.h")) + list(
         (ROOT / "include").glob("*.h"))
-    digest = _digest(cu + cpp + headers)
+    digest = _digest(cu + cpp + synth + headers)
     stamp = LIB_DIR / "libfbk.sha256"
-    if not force and LIB.exists() and stamp.exists() and stamp.read_text().strip() == digest:
+    if (not force and LIB.exists() and SYNTH_LIB.exists() and stamp.exists()
+            and stamp.read_text().strip() == digest):
         return LIB
     nvcc = _nvcc()
+    cxx = os.environ.get("CXX", "g++")
     BUILD_DIR.mkdir(parents=True, exist_ok=True)
     LIB_DIR.mkdir(parents=True, exist_ok=True)
     jobs = []
@@ -70,7 +82,12 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         jobs.append([nvcc, *NVCC_FLAGS, "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)])
     for src in cpp:
         obj = BUILD_DIR / (src.stem + ".o")
-        jobs.append([os.environ.get("CXX", "g++"), *CXX_FLAGS, "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)])
+        jobs.append([cxx, *CXX_FLAGS, "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)])
+    synth_tmp = LIB_DIR / "libfbk_synth.so.tmp"
+    # -Bsymbolic: the generator's own copy of the host ingest binds to itself even
+    # when libfbk.so (which exports the same ingest entry points) is loaded first
+    jobs.append([cxx, *CXX_FLAGS, "-shared", "-Wl,--no-undefined", "-Wl,-Bsymbolic", "-I", str(ROOT / "include"),
+                 *[str(s) for s in synth], "-o", str(synth_tmp)])
 
     def run(cmd):
         if verbose:
@@ -88,6 +105,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     tmp = LIB_DIR / "libfbk.so.tmp"
     run([nvcc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lpthread"])
     os.replace(tmp, LIB)
+    os.replace(synth_tmp, SYNTH_LIB)
     stamp.write_text(digest)
     return LIB
 

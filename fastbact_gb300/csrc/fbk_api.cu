@@ -1140,11 +1140,13 @@ static fbk_status table_alloc(fbk_table* t, uint64_t cap, bool with_cov) {
 }
 
 // Runs the conversion kernel, (re)allocating the compact output when needed.
-static fbk_status table_convert(fbk_table* t, uint64_t* acc_keys, uint16_t* acc_cov, uint16_t* acc_edges, uint64_t acc_cap) {
+static fbk_status table_convert(fbk_table* t, uint64_t* acc_keys, uint16_t* acc_cov, uint16_t* acc_edges, uint64_t acc_cap,
+                                uint64_t* acc_digest = nullptr) {
     fbk_ctx* ctx = t->ctx;
     for (int attempt = 0; attempt < 2; ++attempt) {
         CK(ctx, cudaMemsetAsync(ctx->d_counts, 0, 8 * sizeof(unsigned long long), ctx->stream));
-        ConvOut o;
+        ConvOut o{};
+        o.acc_digest = acc_digest != nullptr;
         o.keys = t->out_keys;
         o.cov = t->out_cov;
         o.mask = t->out_mask;
@@ -1156,12 +1158,13 @@ static fbk_status table_convert(fbk_table* t, uint64_t* acc_keys, uint16_t* acc_
         o.counts = ctx->d_counts;
         TIMED(ctx, "convert", launch_convert((int)t->nw, launch_cfg(ctx, 256, 0), table_dev(t), t->min_trans_cov, o));
         unsigned long long* h = (unsigned long long*)ctx->h_pinned;
-        CK(ctx, cudaMemcpyAsync(h, ctx->d_counts, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(ctx, cudaMemcpyAsync(h, ctx->d_counts, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
         CK(ctx, cudaStreamSynchronize(ctx->stream));
         t->n_keys = h[0];
         t->n_solid = h[1];
         t->digest = h[2];
         t->pushes = h[3] + t->skipped_pushes;
+        if (acc_digest) *acc_digest = h[5];
         if (t->n_solid <= t->out_cap) return FBK_OK;
         table_free_out(t);
         uint64_t cap = t->n_solid + 1024;
@@ -1643,6 +1646,16 @@ FBK_API fbk_status fbk_table_pushes(const fbk_table* t, uint64_t* pushes) {
     if (!t || !pushes) return FBK_ERR_INVALID;
     *pushes = t->pushes;
     return FBK_OK;
+}
+
+FBK_API fbk_status fbk_table_acc_digest(fbk_table* t, uint64_t* digest, uint64_t* n_keys) {
+    if (!t || !digest) return FBK_ERR_INVALID;
+    fbk_ctx* ctx = t->ctx;
+    if (!t->cnt) return set_err(ctx, FBK_ERR_INVALID, "the accumulator slots of this table were released after conversion");
+    CK(ctx, cudaSetDevice(ctx->device));
+    fbk_status st = table_convert(t, nullptr, nullptr, nullptr, 0, digest);
+    if (st == FBK_OK && n_keys) *n_keys = t->n_keys;
+    return st;
 }
 
 FBK_API fbk_status fbk_table_digest(fbk_table* t, uint64_t* digest, uint64_t* n_solid) {

@@ -771,13 +771,30 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp
     return before + x - v;
 }
 
+// Order-free digest term of one accumulated key (KmerAcc, build.rs:145-149): the key's
+// words (big-endian order) folded through splitmix64, then cov and the 8 capped edge
+// counts packed as u16 fields.  Summed over keys mod 2^64, it compares a whole
+// accumulator without exporting it (the oracle computes the same sum).
+template <int NW>
+__device__ __forceinline__ uint64_t acc_row_digest(const Key<NW>& key, uint16_t cov, const uint32_t* cnt) {
+    uint64_t kd = 0;
+#pragma unroll
+    for (int i = 0; i < NW; ++i) kd = smix(kd ^ key.w[i]);
+    uint64_t e[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) e[i] = cnt[i] > 0xFFFFu ? 0xFFFFu : cnt[i];
+    const uint64_t v0 = (uint64_t)cov | (e[0] << 16) | (e[1] << 32) | (e[2] << 48);
+    const uint64_t v1 = e[3] | (e[4] << 16) | (e[5] << 32) | (e[6] << 48);
+    return smix(kd ^ smix(v0 ^ smix(v1 ^ smix(e[7]))));
+}
+
 template <int NW>
 __global__ void __launch_bounds__(256) k_convert(TableDev t, uint32_t min_trans_cov, ConvOut o) {
     __shared__ uint32_t s_warp[32];
     __shared__ unsigned long long s_base[2];
     const uint64_t cap = t.cap;
     const uint64_t tile = (uint64_t)blockDim.x * CONV_SLOTS;
-    unsigned long long n_keys = 0, digest = 0, raw_total = 0;
+    unsigned long long n_keys = 0, digest = 0, raw_total = 0, acc_digest = 0;
     for (uint64_t base = (uint64_t)blockIdx.x * tile; base < cap; base += (uint64_t)gridDim.x * tile) {
         const uint64_t s0 = base + (uint64_t)threadIdx.x * CONV_SLOTS;
         uint32_t occ_bits = 0, keep_bits = 0;
@@ -835,6 +852,7 @@ __global__ void __launch_bounds__(256) k_convert(TableDev t, uint32_t min_trans_
 #pragma unroll
             for (int i = 0; i < NW; ++i) key.w[i] = t.keys[s * NW + i];
             if (NW == 4 && t.tag_stride == NW) key.w[0] = 0;  // word 0 holds the tag
+            if (o.acc_digest) acc_digest += acc_row_digest<NW>(key, covs[j], t.cnt + s * 8);
             if (o.acc_keys) {
                 if (wa < o.cap_acc) {
 #pragma unroll
@@ -870,8 +888,10 @@ __global__ void __launch_bounds__(256) k_convert(TableDev t, uint32_t min_trans_
         digest += __shfl_down_sync(0xffffffffu, digest, off);
         raw_total += __shfl_down_sync(0xffffffffu, raw_total, off);
         n_keys += __shfl_down_sync(0xffffffffu, n_keys, off);
+        acc_digest += __shfl_down_sync(0xffffffffu, acc_digest, off);
     }
     if ((threadIdx.x & 31) == 0) {
+        if (acc_digest) atomicAdd(&o.counts[5], acc_digest);
         if (n_keys) atomicAdd(&o.counts[0], n_keys);
         if (digest) atomicAdd(&o.counts[2], digest);
         if (raw_total) atomicAdd(&o.counts[3], raw_total);

@@ -79,8 +79,10 @@ struct ConvOut {
     uint64_t* acc_keys;         // optional: every accumulated key
     uint16_t* acc_cov;
     uint16_t* acc_edges;        // 8 per key
-    unsigned long long* counts; // [0] n_keys, [1] n_solid, [2] digest, [3] raw edge total, [4] acc rows
+    unsigned long long* counts; // [0] n_keys, [1] n_solid, [2] digest, [3] raw edge total, [4] acc rows,
+                                // [5] accumulator digest (when acc_digest)
     uint64_t cap_solid, cap_acc;
+    int acc_digest;             // also sum the order-free digest of every accumulated key
 };
 
 // One isolate of a multi-isolate wave (fbk_k_batch.cu).

@@ -8,7 +8,7 @@
 #include <thread>
 
 #include "../../../include/fbk_synth.h"
-#include "fbk_host.h"
+#include "../host/fbk_host.h"
 
 namespace fbk {
 

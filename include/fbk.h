@@ -263,6 +263,14 @@ FBK_API fbk_status fbk_table_export_acc(fbk_table* t, uint64_t* keys, uint16_t* 
 FBK_API fbk_status fbk_table_pushes(const fbk_table* t, uint64_t* pushes);
 /* Order-independent digest of the converted entries (same formula as the oracle's). */
 FBK_API fbk_status fbk_table_digest(fbk_table* t, uint64_t* digest, uint64_t* n_solid);
+/* Order-independent digest of the whole accumulator — every key of the
+ * FxHashMap<K, KmerAcc> shards with its cov and 8 edge counts (build.rs:145-196) — as
+ * the sum mod 2^64 over keys of splitmix64(kd ^ splitmix64(v0 ^ splitmix64(v1 ^
+ * splitmix64(e7)))), kd = the key's big-endian words folded through splitmix64,
+ * v0 = cov | e0<<16 | e1<<32 | e2<<48, v1 = e3 | e4<<16 | e5<<32 | e6<<48.  Compares
+ * accumulators of tens of millions of keys without exporting them.  For a table built
+ * with the record filter (fbk_table_flags) it covers the kept keys only. */
+FBK_API fbk_status fbk_table_acc_digest(fbk_table* t, uint64_t* digest, uint64_t* n_keys);
 FBK_API fbk_status fbk_table_release(fbk_table* t);
 
 /* ---- estimator (src/ingest/estimator.rs:104-440) ----------------------------- */

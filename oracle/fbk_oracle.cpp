@@ -1057,6 +1057,40 @@ ORC_API uint64_t orc_table_solid_digest(void* h, unsigned min_trans_cov, uint64_
     return solid_digest<K256>(ot->t, min_trans_cov, n_out);
 }
 
+// Order-independent digest of the whole accumulator (every key of the 64 shard maps with
+// its KmerAcc, build.rs:145-196): sum over keys of
+// splitmix64(kd ^ splitmix64(v0 ^ splitmix64(v1 ^ splitmix64(e7)))), kd = the key's
+// big-endian words folded through splitmix64, v0 = cov | e0<<16 | e1<<32 | e2<<48,
+// v1 = e3 | e4<<16 | e5<<32 | e6<<48.  Compares accumulators of tens of millions of
+// keys at full size without exporting them.
+template <class K>
+static uint64_t acc_digest(void* t, uint64_t* n_out) {
+    uint64_t d = 0, n = 0;
+    for (auto& sh : ((SolidTable<K>*)t)->shards)
+        for (uint64_t i = 0; i < sh.cap; ++i) {
+            if (!sh.used[i]) continue;
+            const KmerAcc& a = sh.vals[i];
+            uint64_t w[4] = {0, 0, 0, 0};
+            sh.keys[i].words(w);
+            uint64_t kd = 0;
+            for (int j = 0; j < K::NW; ++j) kd = splitmix64(kd ^ w[j]);
+            const uint64_t v0 = (uint64_t)a.cov | ((uint64_t)a.edge_counts[0] << 16) | ((uint64_t)a.edge_counts[1] << 32) |
+                                ((uint64_t)a.edge_counts[2] << 48);
+            const uint64_t v1 = (uint64_t)a.edge_counts[3] | ((uint64_t)a.edge_counts[4] << 16) |
+                                ((uint64_t)a.edge_counts[5] << 32) | ((uint64_t)a.edge_counts[6] << 48);
+            d += splitmix64(kd ^ splitmix64(v0 ^ splitmix64(v1 ^ splitmix64((uint64_t)a.edge_counts[7]))));
+            n++;
+        }
+    *n_out = n;
+    return d;
+}
+ORC_API uint64_t orc_table_acc_digest(void* h, uint64_t* n_out) {
+    OrcTable* ot = (OrcTable*)h;
+    if (ot->key_bits == 64) return acc_digest<K64>(ot->t, n_out);
+    if (ot->key_bits == 128) return acc_digest<K128>(ot->t, n_out);
+    return acc_digest<K256>(ot->t, n_out);
+}
+
 // compute_dynamic_kmers — estimator.rs:104-161; target_max_k < 0 means None.
 ORC_API int orc_compute_dynamic_kmers(uint64_t median_len, int64_t target_max_k, uint64_t* out, int cap) {
     std::vector<uint64_t> v;

@@ -87,6 +87,7 @@ _SIG = {
     "orc_table_export_acc": (C.c_uint64, [vp, u64p, u16p, u16p, C.c_uint64]),
     "orc_table_export_solid": (C.c_uint64, [vp, C.c_uint, u64p, u16p, u8p, C.c_uint64]),
     "orc_table_solid_digest": (C.c_uint64, [vp, C.c_uint, u64p]),
+    "orc_table_acc_digest": (C.c_uint64, [vp, u64p]),
     "orc_compute_dynamic_kmers": (C.c_int, [C.c_uint64, C.c_int64, u64p, C.c_int]),
     "orc_subsample_keep": (C.c_int, [C.c_uint64, C.c_double, C.c_uint64]),
     "orc_estimate_from_reads": (C.c_int, [u8p, u64p, C.c_uint64, C.POINTER(OrcCountStats), C.c_uint64, C.c_double, C.c_uint,
@@ -230,6 +231,12 @@ class Table:
     def digest(self, min_trans_cov: int):
         n = C.c_uint64()
         d = lib().orc_table_solid_digest(self.h, min_trans_cov, C.byref(n))
+        return d, n.value
+
+    def acc_digest(self):
+        """(order-free digest of every accumulated key with its KmerAcc, n_keys)."""
+        n = C.c_uint64()
+        d = lib().orc_table_acc_digest(self.h, C.byref(n))
         return d, n.value
 
     def __del__(self):

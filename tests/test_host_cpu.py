@@ -27,14 +27,29 @@ def declared_symbols():
     return names
 
 
+def _exports(path):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(path)], capture_output=True, text=True, check=True).stdout
+    return {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+
+
 def test_library_exports_every_declared_symbol():
+    """fbk.h is exported by libfbk.so, fbk_synth.h by the generator's libfbk_synth.so,
+    and the generator library does not need the device library."""
     declared = declared_symbols()
     assert len(declared) > 50
-    out = subprocess.run(["nm", "-D", "--defined-only", str(N.LIB_PATH)], capture_output=True, text=True, check=True).stdout
-    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
-    assert declared <= exported, sorted(declared - exported)
-    assert declared == set(N.SIGNATURES), sorted(declared ^ set(N.SIGNATURES))
+    synth_declared = {n for n in declared if n.startswith("fbk_synth_")}
+    dev_declared = declared - synth_declared
+    dev_exported = _exports(N.LIB_PATH)
+    assert dev_declared <= dev_exported, sorted(dev_declared - dev_exported)
+    assert not (synth_declared & dev_exported), "the generator must live outside the device library"
+    synth_exported = _exports(N.SYNTH_LIB_PATH)
+    assert synth_declared <= synth_exported, sorted(synth_declared - synth_exported)
+    assert dev_declared == set(N.SIGNATURES), sorted(dev_declared ^ set(N.SIGNATURES))
+    assert synth_declared == {n for n in N.SYNTH_SIGNATURES if n.startswith("fbk_synth_")}
+    needed = subprocess.run(["readelf", "-d", str(N.SYNTH_LIB_PATH)], capture_output=True, text=True, check=True).stdout
+    assert "libfbk.so" not in needed and "libcuda" not in needed and "libcudart" not in needed
     N.lib()  # binds every signature
+    N.synth_lib()
 
 
 def test_no_device_is_reported_not_faked():
@@ -179,7 +194,7 @@ def test_synth_is_deterministic_and_thread_independent():
         assert np.array_equal(a.data, b.data) and np.array_equal(a.offsets, b.offsets)
         assert np.array_equal(a.lengths, b.lengths) and np.array_equal(a.pair_idx, b.pair_idx)
     assert np.array_equal(smp1.data, smp2.data) and n1 == n2 == 500
-    assert c1 == c2 and c1.exact_read_pairs == api.N.lib().fbk_synth_n_pairs(C.byref(p))
+    assert c1 == c2 and c1.exact_read_pairs == api.N.synth_lib().fbk_synth_n_pairs(C.byref(p))
     # tail trimming and merging happened
     assert s1.retained_read_pairs <= s1.input_read_pairs
     assert len(b1.pe_forward) == len(b1.pe_reverse) > 0
@@ -378,5 +393,6 @@ def test_ctypes_mirrors_match_the_c_layouts(tmp_path):
         for m in re.finditer(r"FBK_API\s+[^;{]*?\b(fbk_\w+)\s*\(([^;]*?)\)\s*;", txt, flags=re.S):
             name, params = m.group(1), m.group(2).strip()
             n = 0 if params in ("", "void") else params.count(",") + 1
-            assert name in N.SIGNATURES, name
-            assert len(N.SIGNATURES[name][1]) == n, (name, len(N.SIGNATURES[name][1]), n)
+            sig = N.SIGNATURES.get(name) or N.SYNTH_SIGNATURES.get(name)
+            assert sig is not None, name
+            assert len(sig[1]) == n, (name, len(sig[1]), n)
