@@ -79,8 +79,15 @@ __device__ __forceinline__ uint32_t code_of(uint8_t c) {  // ASCII_TO_2BIT
     c = up(c);
     return c == 'C' ? 1u : c == 'G' ? 2u : c == 'T' ? 3u : 0u;
 }
-__device__ __forceinline__ uint8_t rc_char(uint8_t c) {
-    return (c == 'A' || c == 'a') ? 'T' : (c == 'C' || c == 'c') ? 'G' : (c == 'G' || c == 'g') ? 'C' : 'A';
+// Complement for the merge's reverse complement of R2: a base other than ACGT becomes
+// 'A' when R2 has at most 512 bases (trim_merge.rs:152-162) and 'T' when it is longer
+// (reverse_complement_ascii, bitseq.rs:90-98, reads it as A and complements it).
+__device__ __forceinline__ uint8_t rc_char(uint8_t c, uint64_t l2) {
+    return (c == 'A' || c == 'a')   ? 'T'
+           : (c == 'C' || c == 'c') ? 'G'
+           : (c == 'G' || c == 'g') ? 'C'
+           : (c == 'T' || c == 't') ? 'A'
+                                    : (l2 <= 512 ? 'A' : 'T');
 }
 
 __constant__ uint8_t c_truseq[14] = "AGATCGGAAGAGC";
@@ -139,7 +146,7 @@ __device__ uint64_t d_merge_overlap(const uint8_t* r1, uint64_t l1, const uint8_
         const uint64_t allowed = (uint64_t)((double)d * ratio);
         uint64_t mm = 0;
         for (uint64_t i = 0; i < d; ++i)
-            if (up(s1[i]) != up(rc_char(r2[l2 - 1 - i])) && ++mm > allowed) break;
+            if (up(s1[i]) != up(rc_char(r2[l2 - 1 - i], l2)) && ++mm > allowed) break;
         if (mm <= allowed) {
             const double score = (double)d - 2.5 * (double)mm;
             if (score > best) {
@@ -246,12 +253,12 @@ __global__ void k_pair_write(IngestArgs A, WriteArgs W, const uint8_t* __restric
             uint64_t g = g0;
             for (uint64_t i = 0; i < t1 - d; ++i) put_code(W.data, g++, code_of(s1[i]));
             for (uint64_t i = 0; i < d; ++i) {
-                const uint8_t b1 = s1[t1 - d + i], b2 = rc_char(s2[t2 - 1 - i]);
+                const uint8_t b1 = s1[t1 - d + i], b2 = rc_char(s2[t2 - 1 - i], t2);
                 const uint8_t qa = q1[t1 - d + i], qb = q2[t2 - 1 - i];
                 const uint8_t c = (up(b1) == up(b2)) ? up(b1) : (qa >= qb ? up(b1) : up(b2));
                 put_code(W.data, g++, code_of(c));
             }
-            for (uint64_t i = d; i < t2; ++i) put_code(W.data, g++, code_of(rc_char(s2[t2 - 1 - i])));
+            for (uint64_t i = d; i < t2; ++i) put_code(W.data, g++, code_of(rc_char(s2[t2 - 1 - i], t2)));
         } else {
             const uint64_t r1i = W.rbase[1] + read_no[p], r2i = W.rbase[2] + read_no[p];
             const uint64_t g1 = W.wbase[1] * 32 + base_no[p], g2 = W.wbase[2] * 32 + base_no[A.n_pairs + p];

@@ -252,10 +252,14 @@ int64_t merge_pair(const uint8_t* r1, const uint8_t* q1, uint64_t l1, uint64_t q
                    uint64_t l2, uint64_t ql2, uint64_t min_overlap, double max_mismatch_ratio, uint8_t* out,
                    uint64_t* overlap_len, uint64_t* mismatches) {
     if (l1 < min_overlap || l2 < min_overlap) return -1;
+    // a base other than ACGT becomes 'A' when R2 has at most 512 bases (the stack path,
+    // trim_merge.rs:152-162) and 'T' when it is longer (reverse_complement_ascii,
+    // bitseq.rs:90-98, reads it as A and complements it)
+    const uint8_t other = l2 <= 512 ? 'A' : 'T';
     std::vector<uint8_t> rc2(l2);
     for (uint64_t i = 0; i < l2; ++i) {
         const uint8_t c = r2[l2 - 1 - i];
-        rc2[i] = (c == 'A' || c == 'a') ? 'T' : (c == 'C' || c == 'c') ? 'G' : (c == 'G' || c == 'g') ? 'C' : 'A';
+        rc2[i] = (c == 'A' || c == 'a') ? 'T' : (c == 'C' || c == 'c') ? 'G' : (c == 'G' || c == 'g') ? 'C' : (c == 'T' || c == 't') ? 'A' : other;
     }
     const uint64_t max_d = std::min(l1, l2);
     uint64_t best_d = 0, best_mm = 0;

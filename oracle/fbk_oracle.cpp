@@ -27,6 +27,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -1755,3 +1756,239 @@ ORC_API uint64_t orc_index_terminal_kmers(int key_bits, unsigned k, const uint8_
     if (key_bits == 128) return term_index_impl<K128>(k, useq, uoff, n, keys, unitig, is_rc, pos, cap);
     return term_index_impl<K256>(k, useq, uoff, n, keys, unitig, is_rc, pos, cap);
 }
+
+// ===========================================================================
+// Read ingest — src/ingest/trim_merge.rs:17-238 (adapter clip, quality trim,
+// FLASH-style overlap merge) and :307-417 (the ingest loop that fills a ReadBank).
+// A literal restatement over ASCII records, kept apart from the library's own host
+// and device ingest so that both can be checked against it.
+// ===========================================================================
+namespace orc_ingest {
+
+static const char* ADAPTERS_AGAT[2] = {"AGATCGGAAGAGC", "AGATGTGTATAAGAGACAG"};  // trim_merge.rs:12-13
+static const char* ADAPTER_CTGT = "CTGTCTCTTATACACATCT";                          // trim_merge.rs:14
+
+static inline uint8_t upper(uint8_t c) { return (c >= 'a' && c <= 'z') ? (uint8_t)(c - 32) : c; }
+static inline bool eq_nocase(uint8_t a, uint8_t b) { return upper(a) == upper(b); }
+
+// At most one mismatch over the adapter's first min(10, len) bases at seq + i.
+static bool adapter_at(const uint8_t* seq, uint64_t i, const char* adapter) {
+    const uint64_t n = std::min<uint64_t>(10, strlen(adapter));
+    unsigned mm = 0;
+    for (uint64_t j = 0; j < n; ++j)
+        if (!eq_nocase(seq[i + j], (uint8_t)adapter[j]) && ++mm > 1) return false;
+    return true;
+}
+
+// trim_adapter — trim_merge.rs:17-76: the kept length.
+static uint64_t trim_adapter(const uint8_t* seq, uint64_t len) {
+    if (len < 10) return len;
+    uint64_t cut = len;
+    const uint64_t start = len > 100 ? len - 100 : 0;
+    for (uint64_t i = start; i + 10 <= len; ++i) {
+        const uint8_t b0 = upper(seq[i]), b1 = upper(seq[i + 1]);
+        const bool agat = (b0 == 'A' && b1 == 'G') || b0 == 'A' || b1 == 'G';
+        const bool ctgt = (b0 == 'C' && b1 == 'T') || b0 == 'C' || b1 == 'T';
+        if (!agat && !ctgt) continue;
+        if (agat)
+            for (const char* a : ADAPTERS_AGAT)
+                if (adapter_at(seq, i, a)) {
+                    cut = std::min(cut, i);
+                    break;
+                }
+        if (ctgt && cut > i && adapter_at(seq, i, ADAPTER_CTGT)) cut = std::min(cut, i);
+    }
+    return cut;
+}
+
+// trim_quality — trim_merge.rs:79-115: the kept length, or -1 for None.
+static int64_t trim_quality(const uint8_t* qual, uint64_t len, uint64_t qual_len, unsigned min_qual, uint64_t min_len) {
+    if (len < min_len || qual_len != len) return -1;
+    uint64_t cut = len;
+    const uint64_t W = 4;
+    auto wsum = [&](uint64_t end) {
+        uint64_t s = 0;
+        for (uint64_t j = end - W; j < end; ++j) s += qual[j] > 33 ? qual[j] - 33 : 0;
+        return s;
+    };
+    if (qual_len >= W) {
+        if (wsum(cut) >= (uint64_t)min_qual * W) return (int64_t)len;
+        while (cut >= W) {
+            if (wsum(cut) / W >= min_qual) break;
+            --cut;
+        }
+    }
+    return cut < min_len ? -1 : (int64_t)cut;
+}
+
+// merge_read_pair — trim_merge.rs:135-238.  Returns the merged sequence's length
+// (written to out) or -1 for Unmerged.
+static int64_t merge_read_pair(const uint8_t* r1, const uint8_t* q1, uint64_t l1, uint64_t q1_len, const uint8_t* r2,
+                               const uint8_t* q2, uint64_t l2, uint64_t q2_len, uint64_t min_overlap, double max_ratio,
+                               std::vector<uint8_t>& out, uint64_t* overlap, uint64_t* mismatches) {
+    if (l1 < min_overlap || l2 < min_overlap) return -1;
+    // Reverse complement of R2.  A base other than ACGT (either case) becomes 'A' for
+    // reads of up to 512 bases (the stack path, trim_merge.rs:152-162) but 'T' for longer
+    // ones (reverse_complement_ascii, bitseq.rs:90-98, reads it as A and complements it).
+    std::vector<uint8_t> rc2(l2);
+    const uint8_t other = l2 <= 512 ? 'A' : TWO_BIT_TO_ASCII[COMPLEMENT_2BIT[A2B.t['N']]];
+    for (uint64_t i = 0; i < l2; ++i) {
+        switch (r2[l2 - 1 - i]) {
+            case 'A': case 'a': rc2[i] = 'T'; break;
+            case 'C': case 'c': rc2[i] = 'G'; break;
+            case 'G': case 'g': rc2[i] = 'C'; break;
+            case 'T': case 't': rc2[i] = 'A'; break;
+            default: rc2[i] = other;
+        }
+    }
+    const uint64_t max_d = std::min(l1, l2);
+    uint64_t best_d = 0, best_mm = 0;
+    double best_score = -INFINITY;
+    for (uint64_t d = max_d; d >= min_overlap; --d) {
+        const uint8_t* s1 = r1 + (l1 - d);
+        const uint64_t allowed = (uint64_t)((double)d * max_ratio);
+        uint64_t mm = 0;
+        for (uint64_t i = 0; i < d; ++i)
+            if (!eq_nocase(s1[i], rc2[i]) && ++mm > allowed) break;
+        if (mm <= allowed) {
+            const double score = (double)d - 2.5 * (double)mm;
+            if (score > best_score) {
+                best_score = score;
+                best_d = d;
+                best_mm = mm;
+            }
+        }
+        if ((double)d <= best_score) break;
+        if (d == 0) break;
+    }
+    if (best_d < min_overlap) return -1;
+    out.clear();
+    out.insert(out.end(), r1, r1 + (l1 - best_d));
+    for (uint64_t i = 0; i < best_d; ++i) {
+        const uint8_t b1 = r1[l1 - best_d + i], b2 = rc2[i];
+        const uint8_t qa = (l1 - best_d + i) < q1_len ? q1[l1 - best_d + i] : 'I';
+        const uint8_t qb = i < l2 ? ((l2 - 1 - i) < q2_len ? q2[l2 - 1 - i] : 'I') : 'I';
+        if (eq_nocase(b1, b2) || qa >= qb) out.push_back(upper(b1));
+        else out.push_back(upper(b2));
+    }
+    out.insert(out.end(), rc2.begin() + best_d, rc2.end());
+    *overlap = best_d;
+    *mismatches = best_mm;
+    return (int64_t)out.size();
+}
+
+// BitSeqArena::push_seq — bitseq.rs:195-222, plus the input pair of the read.
+struct OArena {
+    std::vector<uint64_t> data, offsets;
+    std::vector<uint32_t> lengths, pair_idx;
+    uint64_t total = 0;
+    void push(const uint8_t* s, uint64_t n, uint32_t pair) {
+        offsets.push_back(total);
+        lengths.push_back((uint32_t)n);
+        pair_idx.push_back(pair);
+        if (!n) return;
+        const uint64_t end = total + n;
+        if (data.size() < (end + 31) / 32) data.resize((end + 31) / 32, 0);
+        for (uint64_t i = 0; i < n; ++i) {
+            const uint64_t g = total + i;
+            data[g >> 5] |= (uint64_t)A2B.t[s[i]] << ((g & 31) << 1);
+        }
+        total = end;
+    }
+};
+
+struct OIngest {
+    OArena a[3];  // merged_reads, pe_forward, pe_reverse (bitseq.rs:350-355)
+    uint64_t stats[7] = {};  // IngestStats fields in declaration order, trim_merge.rs:262-271
+};
+
+}  // namespace orc_ingest
+
+using namespace orc_ingest;
+
+ORC_API uint64_t orc_trim_adapter(const uint8_t* seq, uint64_t len) { return orc_ingest::trim_adapter(seq, len); }
+ORC_API int64_t orc_trim_quality(const uint8_t* qual, uint64_t len, unsigned min_qual, uint64_t min_len) {
+    return orc_ingest::trim_quality(qual, len, len, min_qual, min_len);
+}
+ORC_API int64_t orc_merge_read_pair(const uint8_t* r1, const uint8_t* q1, uint64_t l1, const uint8_t* r2, const uint8_t* q2,
+                                    uint64_t l2, uint64_t min_overlap, double max_ratio, uint8_t* out, uint64_t* overlap,
+                                    uint64_t* mismatches) {
+    std::vector<uint8_t> m;
+    const int64_t n = orc_ingest::merge_read_pair(r1, q1, l1, l1, r2, q2, l2, l2, min_overlap, max_ratio, m, overlap, mismatches);
+    if (n > 0) memcpy(out, m.data(), (size_t)n);
+    return n;
+}
+
+// ingest_reads_ext_with_seed — trim_merge.rs:307-417.  Returns a handle, or null with
+// the reference's error text in err.
+ORC_API void* orc_ingest_fastq(const char* r1p, const char* r2p, double factor, uint64_t min_len, unsigned min_qual,
+                               int enable_trim, int enable_merge, uint64_t seed, char* err, int errlen) {
+    auto fail = [&](const std::string& m) -> void* {
+        if (err && errlen > 0) snprintf(err, errlen, "%s", m.c_str());
+        return nullptr;
+    };
+    FastqReader a(r1p), b(r2p);
+    if (!a.f) return fail(std::string("Failed to open file ") + r1p);
+    if (!b.f) return fail(std::string("Failed to open file ") + r2p);
+    std::unique_ptr<OIngest> ing(new OIngest());
+    uint64_t* st = ing->stats;  // input, retained, before, after, merged pairs, merged bases, unmerged
+    const bool subsample = factor < 0.999;
+    const uint64_t keep = f64_to_u64_sat(factor * 18446744073709551616.0);  // (f * u64::MAX as f64) as u64
+    uint64_t pair = 0;
+    std::string e1, e2;
+    std::vector<uint8_t> merged;
+    for (;;) {
+        const int x = a.next(e1), y = b.next(e2);
+        if (x == 0 && y == 0) break;
+        if (x < 0) return fail("Corrupted record in R1 FASTQ: " + e1);
+        if (y < 0) return fail("Corrupted record in R2 FASTQ: " + e2);
+        if (x != y) return fail("Mismatched paired-end FASTQ mate counts between R1 and R2");
+        ++pair;
+        st[0]++;
+        const uint8_t *s1 = (const uint8_t*)a.seq.data(), *q1 = (const uint8_t*)a.qual.data();
+        const uint8_t *s2 = (const uint8_t*)b.seq.data(), *q2 = (const uint8_t*)b.qual.data();
+        uint64_t l1 = a.seq.size(), l2 = b.seq.size();
+        st[2] += l1 + l2;
+        if (subsample && splitmix64(pair ^ seed) > keep) continue;
+        if (enable_trim) {
+            const uint64_t c1 = orc_ingest::trim_adapter(s1, l1), c2 = orc_ingest::trim_adapter(s2, l2);
+            const int64_t t1 = orc_ingest::trim_quality(q1, c1, std::min<uint64_t>(c1, a.qual.size()), min_qual, min_len);
+            const int64_t t2 = orc_ingest::trim_quality(q2, c2, std::min<uint64_t>(c2, b.qual.size()), min_qual, min_len);
+            if (t1 < 0 || t2 < 0) continue;
+            l1 = (uint64_t)t1;
+            l2 = (uint64_t)t2;
+        } else if (l1 < min_len || l2 < min_len) {
+            continue;
+        }
+        st[1]++;
+        st[3] += l1 + l2;
+        uint64_t ov = 0, mm = 0;
+        const int64_t n = enable_merge ? orc_ingest::merge_read_pair(s1, q1, l1, l1, s2, q2, l2, l2, 15, 0.10, merged, &ov, &mm) : -1;
+        if (n >= 0) {
+            st[4]++;
+            st[5] += (uint64_t)n;
+            ing->a[0].push(merged.data(), (uint64_t)n, (uint32_t)(pair - 1));
+        } else {
+            st[6]++;
+            ing->a[1].push(s1, l1, (uint32_t)(pair - 1));
+            ing->a[2].push(s2, l2, (uint32_t)(pair - 1));
+        }
+    }
+    if (ing->a[0].lengths.empty() && ing->a[1].lengths.empty())
+        return fail("No valid reads survived trimming and quality filtering (check input FASTQ files)");
+    return ing.release();
+}
+ORC_API void orc_ingest_sizes(const void* h, int arena, uint64_t* n_words, uint64_t* n_seqs) {
+    const OArena& a = ((const OIngest*)h)->a[arena];
+    *n_words = a.data.size();
+    *n_seqs = a.lengths.size();
+}
+ORC_API void orc_ingest_export(const void* h, int arena, uint64_t* data, uint64_t* offsets, uint32_t* lengths, uint32_t* pair_idx) {
+    const OArena& a = ((const OIngest*)h)->a[arena];
+    std::copy(a.data.begin(), a.data.end(), data);
+    std::copy(a.offsets.begin(), a.offsets.end(), offsets);
+    std::copy(a.lengths.begin(), a.lengths.end(), lengths);
+    std::copy(a.pair_idx.begin(), a.pair_idx.end(), pair_idx);
+}
+ORC_API void orc_ingest_stats(const void* h, uint64_t* out7) { memcpy(out7, ((const OIngest*)h)->stats, 7 * sizeof(uint64_t)); }
+ORC_API void orc_ingest_free(void* h) { delete (OIngest*)h; }

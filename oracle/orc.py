@@ -88,6 +88,16 @@ _SIG = {
     "orc_table_export_solid": (C.c_uint64, [vp, C.c_uint, u64p, u16p, u8p, C.c_uint64]),
     "orc_table_solid_digest": (C.c_uint64, [vp, C.c_uint, u64p]),
     "orc_table_acc_digest": (C.c_uint64, [vp, u64p]),
+    "orc_trim_adapter": (C.c_uint64, [u8p, C.c_uint64]),
+    "orc_trim_quality": (C.c_int64, [u8p, C.c_uint64, C.c_uint, C.c_uint64]),
+    "orc_merge_read_pair": (C.c_int64, [u8p, u8p, C.c_uint64, u8p, u8p, C.c_uint64, C.c_uint64, C.c_double, u8p, u64p,
+                                        u64p]),
+    "orc_ingest_fastq": (vp, [C.c_char_p, C.c_char_p, C.c_double, C.c_uint64, C.c_uint, C.c_int, C.c_int, C.c_uint64,
+                              C.c_char_p, C.c_int]),
+    "orc_ingest_sizes": (None, [vp, C.c_int, u64p, u64p]),
+    "orc_ingest_export": (None, [vp, C.c_int, u64p, u64p, u32p, u32p]),
+    "orc_ingest_stats": (None, [vp, u64p]),
+    "orc_ingest_free": (None, [vp]),
     "orc_compute_dynamic_kmers": (C.c_int, [C.c_uint64, C.c_int64, u64p, C.c_int]),
     "orc_subsample_keep": (C.c_int, [C.c_uint64, C.c_double, C.c_uint64]),
     "orc_estimate_from_reads": (C.c_int, [u8p, u64p, C.c_uint64, C.POINTER(OrcCountStats), C.c_uint64, C.c_double, C.c_uint,
@@ -378,3 +388,61 @@ def index_terminal_kmers(seqs: list, k: int, key_bits: int):
     rc, pos = np.zeros(cap, np.uint8), np.zeros(cap, np.uint32)
     m = lib().orc_index_terminal_kmers(key_bits, k, p(useq), p(uoff), n, p(keys), p(uni), p(rc), p(pos), cap)
     return keys[:m], uni[:m], rc[:m], pos[:m]
+
+
+# ---------------------------------------------------------------------------
+# read ingest (trim_merge.rs:17-238, 307-417)
+# ---------------------------------------------------------------------------
+def _u8(b: bytes) -> np.ndarray:
+    return np.frombuffer(b, np.uint8).copy() if b else np.zeros(1, np.uint8)
+
+
+def trim_adapter(seq: bytes) -> int:
+    """Kept length after 3' adapter clipping."""
+    return int(lib().orc_trim_adapter(p(_u8(seq)), len(seq)))
+
+
+def trim_quality(qual: bytes, min_qual: int, min_len: int):
+    """Kept length after the 4-base window trim, or None."""
+    n = lib().orc_trim_quality(p(_u8(qual)), len(qual), min_qual, min_len)
+    return None if n < 0 else int(n)
+
+
+def merge_read_pair(r1: bytes, q1: bytes, r2: bytes, q2: bytes, min_overlap: int = 15, ratio: float = 0.10):
+    """(merged sequence, overlap, mismatches), or None when the pair stays unmerged."""
+    out = np.zeros(len(r1) + len(r2) + 1, np.uint8)
+    ov, mm = C.c_uint64(), C.c_uint64()
+    n = lib().orc_merge_read_pair(p(_u8(r1)), p(_u8(q1)), len(r1), p(_u8(r2)), p(_u8(q2)), len(r2), min_overlap, ratio,
+                                  p(out), C.byref(ov), C.byref(mm))
+    return None if n < 0 else (out[:n].tobytes(), ov.value, mm.value)
+
+
+INGEST_STATS = ("input_read_pairs", "retained_read_pairs", "bases_before_trim", "bases_after_trim", "merged_pairs_count",
+                "merged_bases", "unmerged_pairs_count")
+
+
+def ingest_fastq(r1: str, r2: str, subsample_factor: float = 1.0, min_len: int = 30, min_qual: int = 20,
+                 enable_trim: bool = True, enable_merge: bool = True, seed: int = 0):
+    """ingest_reads_ext_with_seed: ([3 arenas as (data, offsets, lengths, pair_idx)], stats dict).
+    Raises RuntimeError with the reference's message on failure."""
+    err = C.create_string_buffer(1024)
+    h = lib().orc_ingest_fastq(str(r1).encode(), str(r2).encode(), subsample_factor, min_len, min_qual, int(enable_trim),
+                               int(enable_merge), seed, err, len(err))
+    if not h:
+        raise RuntimeError(err.value.decode(errors="replace"))
+    try:
+        arenas = []
+        for a in range(3):
+            nw, ns = C.c_uint64(), C.c_uint64()
+            lib().orc_ingest_sizes(h, a, C.byref(nw), C.byref(ns))
+            d = np.zeros(max(nw.value, 1), np.uint64)
+            o = np.zeros(max(ns.value, 1), np.uint64)
+            L = np.zeros(max(ns.value, 1), np.uint32)
+            pi = np.zeros(max(ns.value, 1), np.uint32)
+            lib().orc_ingest_export(h, a, p(d), p(o), p(L), p(pi))
+            arenas.append((d[:nw.value], o[:ns.value], L[:ns.value], pi[:ns.value]))
+        st = np.zeros(7, np.uint64)
+        lib().orc_ingest_stats(h, p(st))
+        return arenas, dict(zip(INGEST_STATS, (int(x) for x in st)))
+    finally:
+        lib().orc_ingest_free(h)

@@ -607,45 +607,66 @@ def test_terminal_kmer_index_matches_oracle(ctx, repeat_isolate, k, kb):
 
 
 # ---------------------------------------------------------------------------
-# ingest on the device (trim_merge.rs:307-417) equals the host ingest
+# ingest on the device (trim_merge.rs:307-417) equals the oracle's restatement
 # ---------------------------------------------------------------------------
-def _host_bank_concat(bank):
-    """The device bank layout of a host ReadBank: words of the three arenas back to
-    back, offsets rebased by the preceding arenas' words."""
+def _oracle_bank_concat(arenas):
+    """The device bank layout of the oracle's three arenas: words back to back, offsets
+    rebased by the preceding arenas' words."""
     words, offs, lens, pidx, wbase = [], [], [], [], 0
-    for a in bank.arenas:
-        words.append(a.data)
-        offs.append(a.offsets.astype(np.uint64) + np.uint64(wbase * 32))
-        lens.append(a.lengths)
-        pidx.append(a.pair_idx)
-        wbase += len(a.data)
+    for d, o, L, pi in arenas:
+        words.append(d)
+        offs.append(o.astype(np.uint64) + np.uint64(wbase * 32))
+        lens.append(L)
+        pidx.append(pi)
+        wbase += len(d)
     return np.concatenate(words), np.concatenate(offs), np.concatenate(lens), np.concatenate(pidx)
+
+
+def _check_device_ingest(ctx, r1, r2, kw):
+    o_arenas, o_st = orc.ingest_fastq(r1, r2, **kw)
+    dbank, dst, merged_bases = api.ingest_fastq_device(ctx, r1, r2, **kw)
+    for f in ("input_read_pairs", "retained_read_pairs", "bases_before_trim", "bases_after_trim", "merged_pairs_count",
+              "unmerged_pairs_count"):
+        assert getattr(dst, f) == o_st[f], f
+    assert merged_bases == o_st["merged_bases"]
+    words, offs, lens, pidx, counts = dbank.export()
+    ow, oo, ol, op = _oracle_bank_concat(o_arenas)
+    assert counts == [len(a[2]) for a in o_arenas]
+    assert np.array_equal(lens, ol) and np.array_equal(offs, oo) and np.array_equal(pidx, op)
+    assert np.array_equal(words[: ow.size], ow) and not words[ow.size:].any()
+    return dbank, o_st
 
 
 @pytest.mark.parametrize("opts", [dict(), dict(subsample_factor=0.4, seed=11), dict(enable_merge=False),
                                   dict(enable_trim=False, min_len=100), dict(min_qual=35, min_len=60)])
-def test_device_ingest_matches_host(ctx, tmp_path, opts):
+def test_device_ingest_matches_oracle(ctx, tmp_path, opts):
     p = api.synth_params(seed=303, genome_len=30_000, coverage=20.0, gc=0.45, sub_rate=0.01)
     r1, r2 = tmp_path / "d_1.fq", tmp_path / "d_2.fq"
     api.synth_write_fastq(p, r1, r2)
     kw = dict(subsample_factor=1.0, min_len=30, min_qual=20, enable_trim=True, enable_merge=True, seed=0)
     kw.update(opts)
-    hbank, hst = api.ingest_reads_ext_with_seed(r1, r2, kw["subsample_factor"], kw["min_len"], kw["min_qual"], kw["enable_trim"],
-                                                kw["enable_merge"], kw["seed"])
-    dbank, dst, merged_bases = api.ingest_fastq_device(ctx, r1, r2, **kw)
-    assert dst == hst
-    words, offs, lens, pidx, counts = dbank.export()
-    hw, ho, hl, hp = _host_bank_concat(hbank)
-    assert counts == [len(a) for a in hbank.arenas]
-    assert np.array_equal(lens, hl) and np.array_equal(offs, ho) and np.array_equal(pidx, hp)
-    assert np.array_equal(words, hw)
-    assert merged_bases == hbank.merged_reads.total_bases()
+    dbank, o_st = _check_device_ingest(ctx, r1, r2, kw)
     if not opts:
-        assert len(hbank.merged_reads) > 0  # the default settings merge overlapping pairs
-    # the device bank counts like the uploaded one
+        assert o_st["merged_pairs_count"] > 0  # the default settings merge overlapping pairs
+    # the device bank counts like the uploaded host bank
+    hbank, _ = api.ingest_reads_ext_with_seed(r1, r2, kw["subsample_factor"], kw["min_len"], kw["min_qual"], kw["enable_trim"],
+                                              kw["enable_merge"], kw["seed"])
     t1 = api.build_cdbg_ext(dbank, 31, None, ctx=ctx, key_bits=64, counter_bits=16, cms_log2_width=16)
     t2 = api.build_cdbg_ext(hbank, 31, None, ctx=ctx, key_bits=64, counter_bits=16, cms_log2_width=16)
     assert t1.digest() == t2.digest()
+
+
+def test_device_ingest_matches_oracle_on_odd_reads(ctx, tmp_path):
+    """Lowercase, N, planted adapters, short reads and pairs over 512 bases (whose
+    reverse complement turns a non-ACGT base into 'T', not 'A')."""
+    from _ingest_cases import OPTS, odd_pairs_fastq
+
+    r1, r2 = tmp_path / "o_1.fq", tmp_path / "o_2.fq"
+    odd_pairs_fastq(r1, r2, 78, 400)
+    for opts in OPTS:
+        kw = dict(subsample_factor=1.0, min_len=30, min_qual=20, enable_trim=True, enable_merge=True, seed=0)
+        kw.update(opts)
+        _check_device_ingest(ctx, r1, r2, kw)
 
 
 def test_device_ingest_rejects_bad_records(ctx, tmp_path):
