@@ -70,7 +70,7 @@ def test_noalloc_rejects_too_many_pairs():
     # 30000 pairs at 150x of a 60 kb genome: 25000 sampled pairs exceed the 20000 limit
     sample, n_pairs, stats = _sample(8, 60_000, 150.0, 25_000)
     assert n_pairs > 20_000
-    st, _, _, _, msg = _noalloc(sample, n_pairs, stats, max_pairs=250_000)
+    st, _, _, _, msg = _noalloc(sample, n_pairs, stats, cms_log2_width=18, hll_p=14, max_pairs=250_000)
     assert st == 1 and "20000 sampled pairs" in msg
 
 
@@ -83,5 +83,5 @@ def test_noalloc_rejects_too_many_bases():
     lengths = np.array([100, 100, 100, 100], np.uint32)
     sample = api.BitSeqArena(data, offsets, lengths)
     stats = api.ExactCountStats(2, 200, 200, 400, 100, 100, 100.0, 100)
-    st, _, _, _, msg = _noalloc(sample, 2, stats, max_pairs=250_000)
+    st, _, _, _, msg = _noalloc(sample, 2, stats, cms_log2_width=18, hll_p=14, max_pairs=250_000)
     assert st == 1 and "2^23 sample bases" in msg
