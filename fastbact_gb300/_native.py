@@ -183,6 +183,10 @@ SIGNATURES = {
     "fbk_table_flags": (S, [vp, u32p]),
     "fbk_table_digest": (S, [vp, u64p, u64p]),
     "fbk_table_acc_digest": (S, [vp, u64p, u64p]),
+    "fbk_table_export_acc_owned": (S, [vp, C.c_uint32, vp, C.c_uint64, u64p]),
+    "fbk_table_from_acc_rows": (S, [vp, C.c_uint32, C.c_uint32, C.c_uint32, vp, C.c_uint64, P(vp)]),
+    "fbk_cms_counts_device": (S, [vp, P(vp), u64p]),
+    "fbk_cms_clamp_counts": (S, [vp]),
     "fbk_table_release": (S, [vp]),
     "fbk_estimator_defaults": (None, [P(EstimatorParams)]),
     "fbk_estimate_sample": (S, [vp, P(ArenaView), C.c_uint64, P(CountStats), P(EstimatorParams), P(GenomeEstimate), u8p, u8p]),

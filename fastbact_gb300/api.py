@@ -579,6 +579,19 @@ class CountMinSketch:
         raw = np.ascontiguousarray(raw, dtype=np.uint8)
         check(N.lib().fbk_cms_import(self._h, ptr(raw), raw.size), self.ctx.handle, "cms import")
 
+    def counts_tensor(self):
+        """The device counters (4 rows of 2^log2w u32, each <= 65535 between calls) as
+        an int32 CUDA tensor that aliases them (no copy): a collective can reduce the
+        sketches of several ranks in place.  Call clamp_counts() afterwards."""
+        import torch
+
+        ptr_, n = C.c_void_p(), C.c_uint64()
+        check(N.lib().fbk_cms_counts_device(self._h, C.byref(ptr_), C.byref(n)), self.ctx.handle, "cms counters")
+        return torch.as_tensor(_CudaArray(ptr_.value, (n.value,), "<i4"), device="cuda")
+
+    def clamp_counts(self) -> None:
+        check(N.lib().fbk_cms_clamp_counts(self._h), self.ctx.handle, "cms clamp")
+
     def merge(self, other: "CountMinSketch") -> None:
         check(N.lib().fbk_cms_merge(self._h, other._h), self.ctx.handle, "cms merge")
 
@@ -701,6 +714,21 @@ class SolidTable:
         n = C.c_uint64()
         check(N.lib().fbk_table_pushes(self._h, C.byref(n)))
         return n.value
+
+    def export_acc_owned(self, world: int):
+        """Every accumulated key with its 8 edge counts, grouped by owner rank
+        (splitmix64(fold(key)) mod world), as an int64 CUDA tensor of
+        (n, key_bits/64 + 2) rows (key words, then the edge counts packed as u16
+        fields), and the rows per owner."""
+        import torch
+
+        n = self.info()[0]
+        rows = torch.empty((max(n, 1), self.nw + 2), dtype=torch.int64, device="cuda")
+        counts = np.zeros(world, np.uint64)
+        torch.cuda.synchronize()
+        check(N.lib().fbk_table_export_acc_owned(self._h, world, C.c_void_p(rows.data_ptr()), n, ptr(counts)),
+              self.ctx.handle, "owner rows")
+        return rows[:n], [int(c) for c in counts]
 
     def acc_digest(self) -> tuple[int, int]:
         """(order-free digest of every accumulated key with its KmerAcc, n_keys)."""
@@ -901,6 +929,28 @@ def solid_build(ctx: Context, bank: DeviceBank, cms: CountMinSketch, k: int, tar
     check(N.lib().fbk_solid_build(ctx.handle, bank.handle, cms._h, C.byref(p), _subsample(subsample), ptr(ascii), ptr(offs),
                                   len(contigs), C.byref(t)), ctx.handle, "solid build")
     return SolidTable(ctx, t, k, p.key_bits)
+
+
+def table_from_acc_rows(ctx: Context, k: int, key_bits: int, min_trans_cov: int, rows) -> SolidTable:
+    """An owner's table from the accumulated rows it received from every rank (a
+    contiguous int64 CUDA tensor of (n, key_bits/64 + 2) rows, as export_acc_owned
+    writes them): equal keys add up, then the SolidKmerNode conversion."""
+    import torch
+
+    rows = rows.contiguous()
+    t = C.c_void_p()
+    torch.cuda.synchronize()
+    check(N.lib().fbk_table_from_acc_rows(ctx.handle, k, key_bits, min_trans_cov, C.c_void_p(rows.data_ptr() if len(rows) else 0),
+                                          len(rows), C.byref(t)), ctx.handle, "table from rows")
+    return SolidTable(ctx, t, k, key_bits)
+
+
+class _CudaArray:
+    """A device buffer owned by the library, described for torch.as_tensor."""
+
+    def __init__(self, ptr_: int, shape: tuple, typestr: str):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (ptr_, False), "version": 2,
+                                         "strides": None}
 
 
 def subsample_mask(ctx: Context, n_pairs: int, factor: float, seed: int) -> np.ndarray:

@@ -994,6 +994,22 @@ FBK_API fbk_status fbk_cms_merge(fbk_cms* dst, const fbk_cms* src) {
     return FBK_OK;
 }
 
+FBK_API fbk_status fbk_cms_counts_device(fbk_cms* c, uint32_t** counts, uint64_t* n) {
+    if (!c || !counts || !n) return FBK_ERR_INVALID;
+    *counts = c->cnt;
+    *n = c->n;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_cms_clamp_counts(fbk_cms* c) {
+    if (!c) return FBK_ERR_INVALID;
+    fbk_ctx* ctx = c->ctx;
+    CK(ctx, cudaSetDevice(ctx->device));
+    fbk_status st = cms_clamp(c);
+    if (st == FBK_OK) CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return st;
+}
+
 FBK_API fbk_status fbk_cms_release(fbk_cms* c) {
     if (!c) return FBK_OK;
     cudaStreamSynchronize(c->ctx->stream);
@@ -1646,6 +1662,105 @@ FBK_API fbk_status fbk_table_pushes(const fbk_table* t, uint64_t* pushes) {
     if (!t || !pushes) return FBK_ERR_INVALID;
     *pushes = t->pushes;
     return FBK_OK;
+}
+
+FBK_API fbk_status fbk_table_export_acc_owned(fbk_table* t, uint32_t world, uint64_t* rows, uint64_t cap_rows,
+                                              uint64_t* owner_counts) {
+    if (!t || !owner_counts || world == 0 || world > 65536) return FBK_ERR_INVALID;
+    fbk_ctx* ctx = t->ctx;
+    if (!t->cnt) return set_err(ctx, FBK_ERR_INVALID, "the accumulator slots of this table were released after conversion");
+    CK(ctx, cudaSetDevice(ctx->device));
+    const uint64_t n = t->n_keys;
+    if (n > cap_rows || (n && !rows)) return set_err(ctx, FBK_ERR_INVALID, "owner rows: buffer smaller than the accumulator");
+    const int nw = (int)t->nw;
+    uint64_t* dk = n ? (uint64_t*)dev_alloc(ctx, n * 8 * nw) : nullptr;
+    uint16_t* dc = n ? (uint16_t*)dev_alloc(ctx, n * 2) : nullptr;
+    uint16_t* de = n ? (uint16_t*)dev_alloc(ctx, n * 16) : nullptr;
+    unsigned long long* cnt = (unsigned long long*)dev_alloc(ctx, (uint64_t)world * 16);
+    fbk_status st = (n && (!dk || !dc || !de)) || !cnt ? set_err(ctx, FBK_ERR_OOM, "owner rows: staging") : FBK_OK;
+    if (st == FBK_OK) st = table_convert(t, dk, dc, de, n);
+    if (st == FBK_OK) {
+        const Launch L = launch_cfg(ctx, 256, 0);
+        cudaError_t e = cudaMemsetAsync(cnt, 0, (uint64_t)world * 8, ctx->stream);
+        if (e == cudaSuccess) e = launch_owner_hist(nw, L, dk, n, world, cnt);
+        std::vector<unsigned long long> h(world);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), cnt, (uint64_t)world * 8, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e == cudaSuccess) {
+            std::vector<unsigned long long> start(world);
+            unsigned long long acc = 0;
+            for (uint32_t o = 0; o < world; ++o) {
+                start[o] = acc;
+                acc += h[o];
+                owner_counts[o] = h[o];
+            }
+            unsigned long long* cursor = cnt + world;
+            e = cudaMemcpyAsync(cursor, start.data(), (uint64_t)world * 8, cudaMemcpyHostToDevice, ctx->stream);
+            if (e == cudaSuccess) e = launch_owner_scatter(nw, L, dk, de, n, world, cursor, rows);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        }
+        if (e != cudaSuccess) st = cuda_err(ctx, e, "owner rows");
+    }
+    cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, dk);
+    dev_free(ctx, dc);
+    dev_free(ctx, de);
+    dev_free(ctx, cnt);
+    return st;
+}
+
+FBK_API fbk_status fbk_table_from_acc_rows(fbk_ctx* ctx, uint32_t k, uint32_t key_bits, uint32_t min_trans_cov,
+                                           const uint64_t* rows, uint64_t n, fbk_table** out) {
+    if (!ctx || !out || (n && !rows)) return FBK_ERR_INVALID;
+    *out = nullptr;
+    const int nw = nw_of(key_bits);
+    if (!nw || k < 1 || k > max_k_of(key_bits)) return set_err(ctx, FBK_ERR_INVALID, "k out of range for key_bits");
+    if (min_trans_cov > 0xFFFF) return set_err(ctx, FBK_ERR_INVALID, "min_trans_cov must fit u16");
+    CK(ctx, cudaSetDevice(ctx->device));
+    fbk_table* t = new fbk_table();
+    t->ctx = ctx;
+    t->nw = (uint32_t)nw;
+    t->k = k;
+    t->min_trans_cov = min_trans_cov;
+    uint64_t cap = std::max<uint64_t>(1024, (uint64_t)((double)n / ctx->load_factor) + 1024);
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        fbk_status st = table_alloc(t, cap, false);
+        if (st == FBK_OK && !t->out_keys) {
+            const uint64_t oc = n + 4096;  // converted rows are a subset of the keys
+            t->out_keys = (uint64_t*)dev_alloc(ctx, oc * 8 * nw);
+            t->out_cov = (uint16_t*)dev_alloc(ctx, oc * 2);
+            t->out_mask = (uint8_t*)dev_alloc(ctx, oc);
+            if (!t->out_keys || !t->out_cov || !t->out_mask) table_free_out(t);
+            else t->out_cap = oc;
+        }
+        if (st == FBK_OK) {
+            cudaError_t e = cudaMemsetAsync(ctx->d_status, 0, 4, ctx->stream);
+            if (e == cudaSuccess)
+                e = launch_rows_upsert(nw, launch_cfg(ctx, 256, 0), rows, n, table_dev(t), ctx->d_status);
+            if (e != cudaSuccess) st = cuda_err(ctx, e, "rows upsert");
+        }
+        uint32_t bits = 0;
+        if (st == FBK_OK) st = ctx_check_status(ctx, &bits);
+        if (st == FBK_OK && (bits & ST_SPIN_TIMEOUT))
+            st = set_err(ctx, FBK_ERR_TIMEOUT, "solid table: a bounded wait for a key publication gave up");
+        if (st == FBK_OK && !(bits & ST_TABLE_FULL)) {
+            st = table_convert(t, nullptr, nullptr, nullptr, 0);
+            if (st == FBK_OK) {
+                *out = t;
+                return FBK_OK;
+            }
+        }
+        table_free_storage(t);
+        if (st != FBK_OK) {
+            table_free_out(t);
+            delete t;
+            return st;
+        }
+        cap *= 2;
+    }
+    table_free_out(t);
+    delete t;
+    return set_err(ctx, FBK_ERR_TABLE_FULL, "solid table still full after growing it 3 times");
 }
 
 FBK_API fbk_status fbk_table_acc_digest(fbk_table* t, uint64_t* digest, uint64_t* n_keys) {

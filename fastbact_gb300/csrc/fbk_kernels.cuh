@@ -140,6 +140,15 @@ cudaError_t launch_convert(int nw, const Launch& L, const TableDev& t, uint32_t 
 cudaError_t launch_clamp_counters(const Launch& L, uint32_t* cnt, uint64_t n);
 cudaError_t launch_table_init(int nw, const Launch& L, const TableDev& t);
 
+// ---- one isolate across ranks (fbk_shard.cu) -------------------------------------
+// Rows are NW key words and two words of packed u16 edge counts; the owner of a key
+// is splitmix64(fold(key)) mod world.
+cudaError_t launch_owner_hist(int nw, const Launch& L, const uint64_t* keys, uint64_t n, uint32_t world,
+                              unsigned long long* counts);
+cudaError_t launch_owner_scatter(int nw, const Launch& L, const uint64_t* keys, const uint16_t* edges, uint64_t n, uint32_t world,
+                                 unsigned long long* cursor, uint64_t* rows);
+cudaError_t launch_rows_upsert(int nw, const Launch& L, const uint64_t* rows, uint64_t n, const TableDev& t, uint32_t* status);
+
 // ---- threshold ladders (fbk_k_ladder.cu) -----------------------------------------
 // The CMS gate of pass 2 without counts: t levels x 4 rows x 2^log2w bits, level j of
 // (row, col) set once the count reached j + 1.  1 <= t <= LADDER_MAX_LEVELS.

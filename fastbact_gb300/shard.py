@@ -23,9 +23,15 @@ counter (all-reduce MIN; occurrence t's estimate is >= 2 iff every row's counter
 touched before t), then the HLL register maxima per checkpoint segment (all-reduce
 MAX); the checkpoints and the post-math run on the merged registers.
 
-The engine is what counts one rank's reads: DeviceEngine runs this library's
-kernels; any object with the same three methods (pass1, load, pass2) can stand
-in, which is how the exchange logic is tested on hosts without a GPU.
+The engine is what counts one rank's reads.  With DeviceEngine (this library's
+kernels) the data plane stays on the GPU: the rank sketches are reduced in place on
+the device counters (fbk_cms_counts_device), the accumulated rows leave the table
+already grouped by owner (fbk_table_export_acc_owned) and the owner rebuilds and
+converts its table from the received rows on the device (fbk_table_from_acc_rows).
+The collectives move CUDA tensors when the process group is NCCL and host tensors
+otherwise (gloo).  Any other object with the three host methods (pass1, load,
+pass2) can stand in for the engine, which is how the exchange logic is tested on
+hosts without a GPU.
 """
 from __future__ import annotations
 
@@ -157,14 +163,94 @@ def digest(keys: np.ndarray, cov: np.ndarray, mask: np.ndarray) -> int:
         return int(np.sum(v, dtype=np.uint64))
 
 
+class DistComm:
+    """The two collectives of the exchange over a torch.distributed group: CUDA
+    tensors go to the collective as they are when the backend is NCCL; with any other
+    backend they are staged through host memory."""
+
+    def __init__(self, group=None):
+        import torch.distributed as dist
+
+        self.group = group
+        self.on_device = dist.get_backend(group) == "nccl"
+
+    def _dev(self, t):
+        return t if self.on_device else t.cpu()
+
+    def all_reduce_sum_(self, t):
+        import torch.distributed as dist
+
+        x = self._dev(t)
+        dist.all_reduce(x, op=dist.ReduceOp.SUM, group=self.group)
+        if x is not t:
+            t.copy_(x)
+
+    def all_to_all_rows(self, rows, send_counts):
+        """rows: (n, w) tensor grouped by destination rank, send_counts[r] rows for rank
+        r; returns (received rows on rows' device, received counts)."""
+        import torch
+        import torch.distributed as dist
+
+        w = rows.shape[1]
+        dev = rows.device if self.on_device else torch.device("cpu")
+        send = torch.tensor([int(c) for c in send_counts], dtype=torch.int64, device=dev)
+        recv = torch.zeros_like(send)
+        dist.all_to_all_single(recv, send, group=self.group)
+        recv_l = [int(x) for x in recv.cpu()]
+        src = rows.contiguous().to(dev)
+        dst = torch.empty((sum(recv_l), w), dtype=rows.dtype, device=dev)
+        dist.all_to_all_single(dst.view(-1), src.view(-1), output_split_sizes=[x * w for x in recv_l],
+                               input_split_sizes=[int(x) * w for x in send_counts], group=self.group)
+        return dst.to(rows.device), recv_l
+
+    def sum_u64(self, v: int) -> int:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([v - (1 << 64) if v >= (1 << 63) else v], dtype=torch.int64)
+        t = t.cuda() if self.on_device else t
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=self.group)  # wraps: the sum mod 2^64
+        return int(t.item()) & ((1 << 64) - 1)
+
+
+def _sharded_build_device(engine, bank, k, key_bits, log2w, counter_bits, target_solid_cov, rank, world, comm):
+    import torch
+
+    from . import api
+
+    min_trans_cov = 3 if target_solid_cov is None else target_solid_cov
+    mine = shard_bank(bank, rank, world)
+    engine.pass1_device(mine, k, key_bits, log2w, counter_bits)
+    counts = engine.sketch_tensor()  # the device counters, reduced in place
+    engine.ctx.sync()
+    comm.all_reduce_sum_(counts)
+    torch.cuda.synchronize()
+    engine.clamp()
+    rows, send = engine.owned_rows(mine, k, key_bits, target_solid_cov, world)
+    got, _ = comm.all_to_all_rows(rows, send)
+    torch.cuda.synchronize()
+    table = api.table_from_acc_rows(engine.ctx, k, key_bits, min_trans_cov, got)
+    merged = engine.cms.export()
+    engine.release()
+    d = comm.sum_u64(table.digest()[0])
+    nkeys, ncov, nmask = table.export(sort=True)
+    table.release()
+    return (nkeys, ncov, nmask), merged, d
+
+
 def sharded_build(engine, bank, k: int, key_bits: int, log2w: int, counter_bits: int, target_solid_cov: int | None,
-                  rank: int, world: int, group=None):
+                  rank: int, world: int, group=None, comm=None):
     """Counts this rank's share of `bank` and runs the exchange steps.  Returns the
     SolidKmerNode rows this rank owns (sorted by key), the merged sketch bytes and
-    the global digest.  target_solid_cov as in build_cdbg (None: gate 2, mask 3)."""
+    the global digest.  target_solid_cov as in build_cdbg (None: gate 2, mask 3).
+    A DeviceEngine keeps the data plane on the GPU; `comm` (default: DistComm over
+    `group`) carries its collectives."""
     import torch
     import torch.distributed as dist
 
+    if isinstance(engine, DeviceEngine):
+        return _sharded_build_device(engine, bank, k, key_bits, log2w, counter_bits, target_solid_cov, rank, world,
+                                     comm or DistComm(group))
     min_trans_cov = 3 if target_solid_cov is None else target_solid_cov
     mine = shard_bank(bank, rank, world)
     raw = engine.pass1(mine, k, key_bits, log2w, counter_bits)
@@ -231,11 +317,54 @@ class DeviceEstimatorEngine:
 
 
 class DeviceEngine:
-    """Counts one rank's reads on its GPU with this library's kernels."""
+    """Counts one rank's reads on its GPU with this library's kernels.  The host
+    methods (pass1, load, pass2) export to numpy; the device methods keep the sketch
+    and the accumulated rows on the GPU for the collectives."""
 
     def __init__(self, ctx):
         self.ctx = ctx
         self.cms = None
+        self.dbank = None
+
+    # ---- device data plane -------------------------------------------------------
+    def pass1_device(self, bank, k, key_bits, log2w, counter_bits):
+        from . import api
+
+        self.dbank = api.DeviceBank(self.ctx, bank)
+        self.cms = api.CountMinSketch(1 << log2w, self.ctx, counter_bits)
+        self.cms.add_bank(self.dbank, k, key_bits)
+
+    def sketch_tensor(self):
+        """The sketch's u32 device counters as an int32 CUDA tensor (no copy)."""
+        return self.cms.counts_tensor()
+
+    def clamp(self):
+        self.cms.clamp_counts()
+
+    def owned_rows(self, bank, k, key_bits, target_solid_cov, world):
+        """Pass 2 against the merged sketch; every accumulated row, grouped by owner
+        rank, as a (n, key_bits/64 + 2) int64 CUDA tensor, and the rows per owner."""
+        from . import api
+
+        prev = self.ctx.get_tuning("acc_filter")
+        self.ctx.set_tuning(acc_filter=0)  # the owners need every accumulated key
+        try:
+            t = api.solid_build(self.ctx, self.dbank, self.cms, k, target_solid_cov, key_bits=key_bits)
+        finally:
+            self.ctx.set_tuning(acc_filter=prev)
+        rows, counts = t.export_acc_owned(world)
+        t.release()
+        return rows, counts
+
+    def release(self):
+        if self.cms is not None:
+            self.cms.release()
+            self.cms = None
+        if self.dbank is not None:
+            self.dbank.release()
+            self.dbank = None
+
+    # ---- host data plane (gloo tests; the oracle engine has the same three) --------
 
     def pass1(self, bank, k, key_bits, log2w, counter_bits):
         from . import api

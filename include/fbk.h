@@ -205,6 +205,15 @@ FBK_API fbk_status fbk_cms_export(fbk_cms* c, uint8_t* out, uint64_t nbytes);
  * sketch of reads counted on several ranks (no counterpart in the reference). */
 FBK_API fbk_status fbk_cms_import(fbk_cms* c, const uint8_t* in, uint64_t nbytes);
 FBK_API fbk_status fbk_cms_merge(fbk_cms* dst, const fbk_cms* src);
+/* The sketch's device counters — 4 rows of 2^log2_width u32 counts, row-major, each
+ * at most 65535 between calls — so that a collective library can reduce them in place
+ * (an all-reduce SUM over ranks that counted disjoint read shares: the merged gate is
+ * exact, min(cap, sum of min(65535, a_r)) = min(cap, sum a_r)).  Synchronise the
+ * context before handing the pointer to another stream; call fbk_cms_clamp_counts
+ * after the reduction.  Replaces the CountMinSketch merge of build.rs:93-116 across
+ * processes (no counterpart in the reference, which runs in one process). */
+FBK_API fbk_status fbk_cms_counts_device(fbk_cms* c, uint32_t** counts, uint64_t* n);
+FBK_API fbk_status fbk_cms_clamp_counts(fbk_cms* c);
 FBK_API fbk_status fbk_cms_release(fbk_cms* c);
 
 /* ---- HyperLogLog (src/common/sketch.rs:24-115) ------------------------------ */
@@ -271,6 +280,19 @@ FBK_API fbk_status fbk_table_digest(fbk_table* t, uint64_t* digest, uint64_t* n_
  * accumulators of tens of millions of keys without exporting them.  For a table built
  * with the record filter (fbk_table_flags) it covers the kept keys only. */
 FBK_API fbk_status fbk_table_acc_digest(fbk_table* t, uint64_t* digest, uint64_t* n_keys);
+/* One isolate across ranks (the 64 FxHashMap shards of build.rs:141-196 partitioned by
+ * rank instead of by mutex).  fbk_table_export_acc_owned writes every accumulated key
+ * of a table into the DEVICE buffer rows (cap_rows rows of key_bits/64 + 2 u64 words:
+ * the key's big-endian words, then the 8 edge counts as u16 fields, e0 | e1 << 16 |
+ * e2 << 32 | e3 << 48 and e4 .. e7 likewise), grouped by owner rank
+ * splitmix64(fold(key)) mod world, and the rows per owner into owner_counts[world]
+ * (host).  fbk_table_from_acc_rows builds an owner's table from the rows it received
+ * from every rank (DEVICE buffer; equal keys add up, capped at 65535 when read) and
+ * converts it to SolidKmerNodes (build.rs:295-328). */
+FBK_API fbk_status fbk_table_export_acc_owned(fbk_table* t, uint32_t world, uint64_t* rows, uint64_t cap_rows,
+                                              uint64_t* owner_counts);
+FBK_API fbk_status fbk_table_from_acc_rows(fbk_ctx* ctx, uint32_t k, uint32_t key_bits, uint32_t min_trans_cov,
+                                           const uint64_t* rows, uint64_t n, fbk_table** out);
 FBK_API fbk_status fbk_table_release(fbk_table* t);
 
 /* ---- estimator (src/ingest/estimator.rs:104-440) ----------------------------- */

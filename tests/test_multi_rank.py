@@ -106,6 +106,54 @@ def test_sharded_count_equals_single_process(world):
 
 
 
+def _comm_rank_main(rank, world, port, q):
+    """DistComm over gloo: the collectives the device data plane uses, on host tensors."""
+    import torch
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        comm = shard.DistComm()
+        assert not comm.on_device
+        t = torch.arange(10, dtype=torch.int32) * (rank + 1)
+        comm.all_reduce_sum_(t)
+        # rank r sends r + 1 + d rows to rank d, each row (r, d, i)
+        rows, counts = [], []
+        for d in range(world):
+            n = rank + 1 + d
+            rows += [[rank, d, i] for i in range(n)]
+            counts.append(n)
+        got, recv = comm.all_to_all_rows(torch.tensor(rows, dtype=torch.int64), counts)
+        s = comm.sum_u64((1 << 64) - 5 + rank)  # wraps mod 2^64
+        q.put((rank, t.tolist(), got.tolist(), recv, s))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_dist_comm_collectives_over_gloo():
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_comm_rank_main, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    try:
+        res = dict((r[0], r[1:]) for r in (q.get(timeout=300) for _ in range(world)))
+    finally:
+        for p in procs:
+            p.join(timeout=120)
+    for p in procs:
+        assert p.exitcode == 0
+    for rank in range(world):
+        t, got, recv, s = res[rank]
+        assert t == [3 * i for i in range(10)]  # (1 + 2) * i
+        want = [[r, rank, i] for r in range(world) for i in range(r + 1 + rank)]
+        assert got == want and recv == [r + 1 + rank for r in range(world)]
+        assert s == (2 * ((1 << 64) - 5) + 1) % (1 << 64)
+
+
 def test_owner_partition_is_balanced():
     keys = np.arange(1, 200_001, dtype=np.uint64).reshape(-1, 1) * np.uint64(0x9E3779B97F4A7C15)
     for world in (2, 3, 8):
