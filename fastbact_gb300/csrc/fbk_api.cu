@@ -1243,7 +1243,9 @@ struct Buckets {
     }
 };
 
-static fbk_status buckets_alloc(fbk_ctx* ctx, uint64_t cap, uint64_t slot_bytes, int nw, uint64_t max_records, Buckets& bk) {
+static fbk_status buckets_alloc(fbk_ctx* ctx, uint64_t cap, uint64_t slot_bytes, int nw, uint32_t k, uint64_t max_records,
+                                Buckets& bk) {
+    const RecFmt fmt = record_format(k, nw);
     // at most 64 buckets (the emit kernel's per-warp staging holds 64 counters)
     uint32_t shift = 0;
     while (shift < 40 && (2ULL << shift) * slot_bytes <= ctx->bucket_bytes) ++shift;
@@ -1257,7 +1259,10 @@ static fbk_status buckets_alloc(fbk_ctx* ctx, uint64_t cap, uint64_t slot_bytes,
     bk.d.n_buckets = P;
     bk.d.stripes = S;
     bk.d.stripe_cap = per_stripe;
-    bk.d.recs = (uint64_t*)dev_alloc(ctx, (uint64_t)P * S * per_stripe * 8 * (nw + 1));
+    bk.d.rw = fmt.rw;
+    bk.d.ws = fmt.ws;
+    bk.d.packed = fmt.packed;
+    bk.d.recs = (uint64_t*)dev_alloc(ctx, (uint64_t)P * S * per_stripe * 8 * fmt.rw);
     bk.d.fill = (unsigned long long*)dev_alloc(ctx, (uint64_t)P * S * 8);
     bk.overflow = (uint32_t*)dev_alloc(ctx, 256);
     bk.work = bk.overflow ? (unsigned long long*)(bk.overflow + 2) : nullptr;
@@ -1358,7 +1363,7 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
         };
         Buckets bk;
         const bool use_buckets = max_records && ctx->pass2_mode == 1;
-        st = use_buckets ? buckets_alloc(ctx, cap, slot_bytes, nw, max_records, bk) : FBK_OK;
+        st = use_buckets ? buckets_alloc(ctx, cap, slot_bytes, nw, p->k, max_records, bk) : FBK_OK;
         // the record filter needs every record of the pass in one bucket pass: one
         // read chunk and no prior contigs (their pushes weigh 1000)
         RecordFilter flt{};

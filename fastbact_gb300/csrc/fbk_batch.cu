@@ -450,8 +450,8 @@ PlanB plan_b(const fbk_batch* B, const BatchIso* it) {
     q.shift = shift;
     q.n_buckets = (uint32_t)((q.cap + (1ULL << shift) - 1) >> shift);
     q.per_stripe = (uint64_t)(1.15 * (double)it->records / ((double)q.n_buckets * BATCH_STRIPES)) + 2048;
-    q.bytes = q.cap * sb + q.out_cap * (8ULL * B->nw + 3) + (uint64_t)q.n_buckets * BATCH_STRIPES * (q.per_stripe * 8 * (B->nw + 1) + 8) +
-              8192;
+    q.bytes = q.cap * sb + q.out_cap * (8ULL * B->nw + 3) +
+              (uint64_t)q.n_buckets * BATCH_STRIPES * (q.per_stripe * 8 * record_format(B->p.k, B->nw).rw + 8) + 8192;
     return q;
 }
 
@@ -472,7 +472,8 @@ fbk_status alloc_b(fbk_batch* B, BatchIso* it, const PlanB& q) {
     t->out_cov = (uint16_t*)dev_alloc(ctx, q.out_cap * 2);
     t->out_mask = (uint8_t*)dev_alloc(ctx, q.out_cap);
     t->out_cap = q.out_cap;
-    it->recs = (uint64_t*)dev_alloc(ctx, (uint64_t)q.n_buckets * BATCH_STRIPES * q.per_stripe * 8 * (B->nw + 1));
+    const RecFmt fmt = record_format(B->p.k, B->nw);
+    it->recs = (uint64_t*)dev_alloc(ctx, (uint64_t)q.n_buckets * BATCH_STRIPES * q.per_stripe * 8 * fmt.rw);
     it->fill = (unsigned long long*)dev_alloc(ctx, (uint64_t)q.n_buckets * BATCH_STRIPES * 8);
     if (!t->keys || (t->nw > 2 && !t->tags) || !t->cnt || !t->out_keys || !t->out_cov || !t->out_mask || !it->recs || !it->fill)
         return set_err(ctx, FBK_ERR_OOM, "batch table");
@@ -483,6 +484,9 @@ fbk_status alloc_b(fbk_batch* B, BatchIso* it, const PlanB& q) {
     it->bk.shift = q.shift;
     it->bk.n_buckets = q.n_buckets;
     it->bk.stripes = BATCH_STRIPES;
+    it->bk.rw = fmt.rw;
+    it->bk.ws = fmt.ws;
+    it->bk.packed = fmt.packed;
     return FBK_OK;
 }
 
@@ -1014,7 +1018,8 @@ uint64_t request_estimate(const fbk_batch_params& p, int nw, uint64_t n_bases, u
     const uint64_t sample = sample_bases / 4 + 65536;
     const uint64_t a = (4ULL << p.cms_log2_width) * 4 + 4096 * 4 + n_bases / 8 + n_reads / 8 + 8192;
     const double w = (double)n_bases;
-    const double b = w * (0.9 * 1.15 * 8.0 * (nw + 1) + 0.25 / 0.62 * (double)slot_bytes_of(nw) + 0.275 * (8.0 * nw + 3));
+    const double b = w * (0.9 * 1.15 * 8.0 * record_format(p.k, nw).rw + 0.25 / 0.62 * (double)slot_bytes_of(nw) +
+                          0.275 * (8.0 * nw + 3));
     return reads + sample + a + (uint64_t)b + (16ULL << 20);
 }
 

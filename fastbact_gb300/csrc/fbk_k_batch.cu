@@ -332,9 +332,7 @@ __global__ void __launch_bounds__(256) k_batch_emit(const IsoDev* __restrict__ i
             const uint32_t active = __ballot_sync(0xffffffffu, emit);
             if (emit) {
                 const uint32_t pos = n_buf + __popc(active & ((1u << lane) - 1));
-#pragma unroll
-                for (int i = 0; i < NW; ++i) buf[pos * (NW + 1) + i] = key.w[i];
-                buf[pos * (NW + 1) + NW] = info;
+                rec_put<NW>(buf + pos * (NW + 1), key, info, bk);
                 bbuf[pos] = (uint8_t)bucket;
             }
             n_buf += __popc(active);

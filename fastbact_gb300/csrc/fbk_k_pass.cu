@@ -251,9 +251,7 @@ __global__ void __launch_bounds__(256) k_emit(BankDev b, uint32_t k, const uint3
             const uint32_t active = __ballot_sync(0xffffffffu, emit);
             if (emit) {
                 const uint32_t pos = n_buf + __popc(active & ((1u << lane) - 1));
-#pragma unroll
-                for (int i = 0; i < NW; ++i) buf[pos * (NW + 1) + i] = key.w[i];
-                buf[pos * (NW + 1) + NW] = info;
+                rec_put<NW>(buf + pos * (NW + 1), key, info, bk);
                 bbuf[pos] = (uint8_t)bucket;
             }
             n_buf += __popc(active);
@@ -341,9 +339,7 @@ __global__ void __launch_bounds__(256) k_emit_ladder(BankDev b, uint32_t k, cons
             const uint32_t active = __ballot_sync(0xffffffffu, emit);
             if (emit) {
                 const uint32_t pos = n_buf + __popc(active & ((1u << lane) - 1));
-#pragma unroll
-                for (int i = 0; i < NW; ++i) buf[pos * (NW + 1) + i] = kc.w[i];
-                buf[pos * (NW + 1) + NW] = info;
+                rec_put<NW>(buf + pos * (NW + 1), kc, info, bk);
                 bbuf[pos] = (uint8_t)bucket;
             }
             n_buf += __popc(active);
@@ -454,9 +450,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
             const uint32_t active = __ballot_sync(0xffffffffu, emit);
             if (emit) {
                 const uint32_t pos = n_buf + __popc(active & ((1u << lane) - 1));
-#pragma unroll
-                for (int i = 0; i < NW; ++i) buf[pos * (NW + 1) + i] = kc.w[i];
-                buf[pos * (NW + 1) + NW] = info;
+                rec_put<NW>(buf + pos * (NW + 1), kc, info, bk);
                 bbuf[pos] = (uint8_t)bucket;
             }
             n_buf += __popc(active);
@@ -521,17 +515,19 @@ struct StreamWindow {
     bool live, rc;
     bool has_l, has_r;  // neighbours inside the read
 };
-template <int NW>
+template <int NW, int WS>
 __device__ __forceinline__ void stream_window(const BankDev& b, uint32_t k, const StreamCursor& c, StreamWindow<NW>& w) {
     w.live = c.r < c.r_end;
     w.rc = false;
     w.g = c.off + c.q;
     w.has_l = c.q > 0;
     w.has_r = c.q + 1 < c.nk;
-    if (w.live) window_canonical<NW>(b.data, w.g, k, w.key, w.rc);
+    if (w.live) canonical_ws<NW, WS>(b.data, w.g, k, w.key, w.rc);
 }
 
-template <int NW>
+// WS = (64*NW - 2k) / 64 as in k_emit_ladder2; the record's bucket comes from the
+// row-0 hash the gate computed for the window (GateLoads::h0).
+template <int NW, int WS>
 __global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, const uint32_t* __restrict__ lad, uint32_t log2w,
                                                       uint32_t t_solid, TableDev t, BucketDev bk) {
     extern __shared__ uint64_t emit_smem[];
@@ -557,19 +553,20 @@ __global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, con
         stream_advance(b, k, cur, lane);
         // chunks 0 and 1 resolved up front
         StreamWindow<NW> wc, wn;
-        stream_window<NW>(b, k, cur, wc);
+        stream_window<NW, WS>(b, k, cur, wc);
         stream_advance(b, k, cur, 32);
-        stream_window<NW>(b, k, cur, wn);
+        stream_window<NW, WS>(b, k, cur, wn);
         stream_advance(b, k, cur, 32);
         GateLoads g0, g1;
         gate_issue(top, log2w, wc.live ? key_fold<NW>(wc.key) : 0, wc.live, g0);
         gate_issue(top, log2w, wn.live ? key_fold<NW>(wn.key) : 0, wn.live, g1);
         uint32_t mprev = 0, mcur = __ballot_sync(0xffffffffu, gate_resolve(g0, wc.live));
         uint32_t mnext = __ballot_sync(0xffffffffu, gate_resolve(g1, wn.live));
+        uint64_t hc = g0.h0, hn = g1.h0;
         // the stream of a run is contiguous: once a chunk has no live lane, none has
         while (__any_sync(0xffffffffu, wc.live)) {
             StreamWindow<NW> wf;
-            stream_window<NW>(b, k, cur, wf);
+            stream_window<NW, WS>(b, k, cur, wf);
             stream_advance(b, k, cur, 32);
             GateLoads gf;
             gate_issue(top, log2w, wf.live ? key_fold<NW>(wf.key) : 0, wf.live, gf);
@@ -583,15 +580,13 @@ __global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, con
                 if (emit) {
                     if (sr) info |= 8u | (base_at(b.data, wc.g + k) + (wc.rc ? 4u : 0u));
                     if (sl) info |= (8u | ((3u - base_at(b.data, wc.g - 1)) + (wc.rc ? 0u : 4u))) << 4;
-                    bucket = (uint32_t)(home_slot(key_fold<NW>(wc.key), t.cap) >> bk.shift);
+                    bucket = (uint32_t)(home_slot_h(hc, t.cap) >> bk.shift);
                 }
             }
             const uint32_t active = __ballot_sync(0xffffffffu, emit);
             if (emit) {
                 const uint32_t pos = n_buf + __popc(active & ((1u << lane) - 1));
-#pragma unroll
-                for (int i = 0; i < NW; ++i) buf[pos * (NW + 1) + i] = wc.key.w[i];
-                buf[pos * (NW + 1) + NW] = info;
+                rec_put<NW, WS>(buf + pos * (NW + 1), wc.key, info, bk);
                 bbuf[pos] = (uint8_t)bucket;
             }
             n_buf += __popc(active);
@@ -606,6 +601,8 @@ __global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, con
             mnext = mfar;
             wc = wn;
             wn = wf;
+            hc = hn;
+            hn = gf.h0;
         }
     }
     __syncwarp();
@@ -644,24 +641,21 @@ __device__ __forceinline__ uint32_t filter_col(uint64_t fold, uint32_t log2m) {
 template <int NW>
 __global__ void __launch_bounds__(256) k_count_records(BucketDev bk, uint32_t bucket, RecordFilter flt) {
     const uint64_t* base;
-    const uint64_t n = stripe_records(bk, bucket, base, NW + 1);
+    const uint64_t n = stripe_records(bk, bucket, base, bk.rw);
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t* rec = base + i * (NW + 1);
         Key<NW> key;
-#pragma unroll
-        for (int j = 0; j < NW; ++j) key.w[j] = __ldcg(rec + j);
+        rec_key<NW>(base + i * bk.rw, key, bk);
         atomicAdd(flt.cnt + filter_col(key_fold<NW>(key), flt.log2m), 1u);
     }
 }
 
 // One record's upsert: resolve the key's slot from its home slot and add its pushes.
 template <int NW>
-__device__ __forceinline__ void upsert_record(const uint64_t* rec, uint32_t w_edge, uint32_t w_cov, const TableDev& t,
-                                              uint32_t* status, const RecordFilter& flt, unsigned long long& skipped) {
+__device__ __forceinline__ void upsert_record(const uint64_t* rec, const BucketDev& bk, uint32_t w_edge, uint32_t w_cov,
+                                              const TableDev& t, uint32_t* status, const RecordFilter& flt,
+                                              unsigned long long& skipped) {
     Key<NW> key;
-#pragma unroll
-    for (int j = 0; j < NW; ++j) key.w[j] = __ldcs(rec + j);
-    const uint32_t info = (uint32_t)__ldcs(rec + NW);
+    const uint32_t info = rec_get<NW>(rec, key, bk);
     const uint64_t f = key_fold<NW>(key);
     if (flt.cnt) {
         if (__ldcg(flt.cnt + filter_col(f, flt.log2m)) < flt.min_records) {
@@ -686,10 +680,10 @@ template <int NW>
 __global__ void __launch_bounds__(256, 8) k_upsert(BucketDev bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov, TableDev t,
                                                 uint32_t* status, RecordFilter flt) {
     const uint64_t* base;
-    const uint64_t n = stripe_records(bk, bucket, base, NW + 1);
+    const uint64_t n = stripe_records(bk, bucket, base, bk.rw);
     unsigned long long skipped = 0;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        upsert_record<NW>(base + i * (NW + 1), w_edge, w_cov, t, status, flt, skipped);
+        upsert_record<NW>(base + i * bk.rw, bk, w_edge, w_cov, t, status, flt, skipped);
     if (flt.cnt) {
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) skipped += __shfl_down_sync(0xffffffffu, skipped, off);
@@ -726,9 +720,9 @@ __global__ void __launch_bounds__(256, 8) k_upsert_all(BucketDev bk, uint32_t w_
         const uint64_t n = f < bk.stripe_cap ? f : bk.stripe_cap;
         if (first >= n) continue;
         const uint64_t last = first + UPSERT_ITEM < n ? first + UPSERT_ITEM : n;
-        const uint64_t* base = bk.recs + bs * bk.stripe_cap * (NW + 1);
+        const uint64_t* base = bk.recs + bs * bk.stripe_cap * bk.rw;
         for (uint64_t i = first + threadIdx.x; i < last; i += blockDim.x)
-            upsert_record<NW>(base + i * (NW + 1), w_edge, w_cov, t, status, none, skipped);
+            upsert_record<NW>(base + i * bk.rw, bk, w_edge, w_cov, t, status, none, skipped);
     }
 }
 
@@ -995,9 +989,21 @@ template <int NW>
 static cudaError_t emitl_nw(const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w, uint32_t ts,
                             const TableDev& t, const BucketDev& bk, int lookahead) {
     const size_t smem = (size_t)(L.block / 32) * EMIT_WARP_WORDS(NW) * 8;
-    if (lookahead == 3) return emit_launch(k_emit_flat<NW>, L, b, k, lad, log2w, ts, t, bk, smem);
+    const uint32_t ws = (64u * NW - 2u * k) >> 6;
+    if (lookahead == 3) {
+        if constexpr (NW == 1) {
+            return emit_launch(k_emit_flat<1, 0>, L, b, k, lad, log2w, ts, t, bk, smem);
+        } else if constexpr (NW == 2) {
+            if (ws == 0) return emit_launch(k_emit_flat<2, 0>, L, b, k, lad, log2w, ts, t, bk, smem);
+            return emit_launch(k_emit_flat<2, 1>, L, b, k, lad, log2w, ts, t, bk, smem);
+        } else {
+            if (ws == 0) return emit_launch(k_emit_flat<4, 0>, L, b, k, lad, log2w, ts, t, bk, smem);
+            if (ws == 1) return emit_launch(k_emit_flat<4, 1>, L, b, k, lad, log2w, ts, t, bk, smem);
+            if (ws == 2) return emit_launch(k_emit_flat<4, 2>, L, b, k, lad, log2w, ts, t, bk, smem);
+            return emit_launch(k_emit_flat<4, 3>, L, b, k, lad, log2w, ts, t, bk, smem);
+        }
+    }
     if (lookahead == 2) {
-        const uint32_t ws = (64u * NW - 2u * k) >> 6;
         if constexpr (NW == 1) {
             return emit_launch(k_emit_ladder2<1, 0>, L, b, k, lad, log2w, ts, t, bk, smem);
         } else if constexpr (NW == 2) {

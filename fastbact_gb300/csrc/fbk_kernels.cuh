@@ -50,17 +50,39 @@ struct TableDev {
 
 // Pass-2 records, grouped by the slot range of their key's home slot.  Bucket b
 // holds S stripes of stripe_cap records; warps append to stripe (warp % S) with one
-// atomic per (warp iteration, bucket).  A record is the canonical key (NW words)
-// and the pushes it makes: bits 0-2 edge as u, bit 3 present; bits 4-6 edge as v,
-// bit 7 present.
+// atomic per (warp iteration, bucket).  A record is the canonical key and the pushes
+// it makes (the info byte: bits 0-2 edge as u, bit 3 present; bits 4-6 edge as v,
+// bit 7 present), packed into rw = ceil((2k + 8) / 64) words (record_format).
 struct BucketDev {
-    uint64_t* recs;              // (NW + 1) words per record
+    uint64_t* recs;              // rw words per record
     unsigned long long* fill;    // P * S append counters
     uint64_t stripe_cap;
     uint32_t shift;              // bucket of a home slot = home >> shift
     uint32_t n_buckets, stripes;
     uint32_t* overflow;          // set when a stripe runs out of room
+    uint32_t rw, ws, packed;     // record layout (record_format)
 };
+
+// Record layout of a pass at k with NW-word keys.  The key's leading ws = (64 NW - 2k)
+// / 64 words are zero and not stored; its significant words follow in big-endian
+// order.  When the first significant word leaves its top 8 bits free (2k - 64 (NK - 1)
+// <= 56 for NK = NW - ws significant words) the info byte goes there and a record is
+// NK words (packed); otherwise the info byte takes a word of its own before the key
+// (NK + 1 words).  k = 21: 1 word; k = 31: 2; k = 33 and 55: 2; k = 63: 3; k = 77: 3;
+// k = 127: 5.
+struct RecFmt {
+    uint32_t rw, ws, packed;
+};
+__host__ __device__ inline RecFmt record_format(uint32_t k, int nw) {
+    const uint32_t ws = (64u * (uint32_t)nw - 2u * k) >> 6;
+    const uint32_t nk = (uint32_t)nw - ws;
+    const uint32_t top_bits = 2u * k - 64u * (nk - 1);
+    RecFmt f;
+    f.ws = ws;
+    f.packed = top_bits <= 56 ? 1u : 0u;
+    f.rw = nk + (f.packed ? 0u : 1u);
+    return f;
+}
 
 // Record filter of pass 2 (see k_count_records): 2^log2m counters, the threshold, and
 // where the pushes of skipped records are counted.

@@ -54,15 +54,26 @@ __device__ __forceinline__ void cas128(uint64_t* addr, uint64_t cmp_lo, uint64_t
         : "memory");
 }
 
+// A slot goes from EMPTY to its key in one 16-byte CAS and never changes again, so a
+// word read that is neither EMPTY nor ours proves the slot belongs to another key and
+// needs no CAS.  Word 0 of a k <= 63 key is below 2^62, so word 0 != EMPTY proves the
+// slot is claimed; word 1 can be all ones in a real key (a 32-base poly-T suffix), so a
+// word 1 of EMPTY proves nothing and such slots, like every EMPTY-looking one, are
+// decided by the CAS, which returns the slot's whole current value.  A key whose word 1
+// is all ones is also confirmed by the CAS when it seems found, since a read of the two
+// words could straddle another key's claim.
 __device__ __forceinline__ int64_t table_slot2(const TableDev& t, const Key<2>& key, uint64_t s, uint32_t* status) {
+    const bool w1_empty = key.w[1] == KEY_EMPTY;
     for (uint32_t probe = 0; probe < t.max_probe; ++probe) {
         uint64_t* a = t.keys + s * 2;
-        const uint64_t c0 = __ldcg(a), c1 = __ldcg(a + 1);
-        if (c0 == key.w[0] && c1 == key.w[1]) return (int64_t)s;
-        // Anything but our key or EMPTY may be a slot being written: decide with the CAS.
-        uint64_t o0, o1;
-        cas128(a, KEY_EMPTY, KEY_EMPTY, key.w[0], key.w[1], o0, o1);
-        if ((o0 == KEY_EMPTY && o1 == KEY_EMPTY) || (o0 == key.w[0] && o1 == key.w[1])) return (int64_t)s;
+        const ulonglong2 c = __ldcg(reinterpret_cast<const ulonglong2*>(a));
+        const bool other = (c.x != KEY_EMPTY && c.x != key.w[0]) || (c.y != KEY_EMPTY && c.y != key.w[1]);
+        if (!other) {
+            if (c.x == key.w[0] && c.y == key.w[1] && !w1_empty) return (int64_t)s;
+            uint64_t o0, o1;
+            cas128(a, KEY_EMPTY, KEY_EMPTY, key.w[0], key.w[1], o0, o1);
+            if ((o0 == KEY_EMPTY && o1 == KEY_EMPTY) || (o0 == key.w[0] && o1 == key.w[1])) return (int64_t)s;
+        }
         s = s + 1 == t.cap ? 0 : s + 1;
     }
     atomicOr(status, ST_TABLE_FULL);
@@ -118,6 +129,50 @@ __device__ __forceinline__ bool bm_bit(const uint32_t* __restrict__ bm, uint64_t
     return (__ldg(&bm[g >> 5]) >> (g & 31)) & 1u;
 }
 
+// Writes a record (key, info byte) in the bucket's layout at dst.  WS_T >= 0 is the
+// word shift known at compile time (it equals bk.ws); -1 reads it from bk.
+template <int NW, int WS_T = -1>
+__device__ __forceinline__ void rec_put(uint64_t* dst, const Key<NW>& key, uint32_t info, const BucketDev& bk) {
+    const uint32_t ws = WS_T >= 0 ? (uint32_t)WS_T : bk.ws;
+    const uint32_t base = bk.packed ? 0u : 1u;
+    if (!bk.packed) dst[0] = info;
+#pragma unroll
+    for (int i = 0; i < NW; ++i)
+        if ((uint32_t)i >= ws)
+            dst[base + i - ws] = key.w[i] | ((bk.packed && (uint32_t)i == ws) ? ((uint64_t)info << 56) : 0ULL);
+}
+// Reads a record written by rec_put; returns its info byte.  Streaming loads: every
+// record is read once.
+template <int NW>
+__device__ __forceinline__ uint32_t rec_get(const uint64_t* src, Key<NW>& key, const BucketDev& bk) {
+    const uint32_t ws = bk.ws, base = bk.packed ? 0u : 1u;
+    uint32_t info = 0;
+    if (!bk.packed) info = (uint32_t)__ldcs(src);
+#pragma unroll
+    for (int i = 0; i < NW; ++i) {
+        uint64_t w = 0;
+        if ((uint32_t)i >= ws) w = __ldcs(src + base + i - ws);
+        if (bk.packed && (uint32_t)i == ws) {
+            info = (uint32_t)(w >> 56);
+            w &= (1ULL << 56) - 1;
+        }
+        key.w[i] = w;
+    }
+    return info;
+}
+// The key of a record only (the record filter's count).
+template <int NW>
+__device__ __forceinline__ void rec_key(const uint64_t* src, Key<NW>& key, const BucketDev& bk) {
+    const uint32_t ws = bk.ws, base = bk.packed ? 0u : 1u;
+#pragma unroll
+    for (int i = 0; i < NW; ++i) {
+        uint64_t w = 0;
+        if ((uint32_t)i >= ws) w = __ldcg(src + base + i - ws);
+        if (bk.packed && (uint32_t)i == ws) w &= (1ULL << 56) - 1;
+        key.w[i] = w;
+    }
+}
+
 // Records are staged per warp in shared memory (emit_buf(NW) of them) and flushed
 // bucket by bucket: one atomic per (flush, bucket) reserves room for all of the
 // warp's records of that bucket, which are then written as one run.
@@ -126,8 +181,9 @@ __device__ __forceinline__ bool bm_bit(const uint32_t* __restrict__ bm, uint64_t
 // that serves the bank and gate loads.
 __host__ __device__ constexpr uint32_t emit_buf(int) { return 128u; }
 constexpr uint32_t EMIT_MAX_BUCKETS = 64;
-// staging words per warp: records, bucket bytes, ranks (u16), histogram (64 u32),
-// reservation bases (64 u64), bucket-order permutation (u16)
+// staging words per warp: records (NW + 1 words apart, bk.rw of them used), bucket
+// bytes, ranks (u16), histogram (64 u32), reservation bases (64 u64), bucket-order
+// permutation (u16)
 #define EMIT_WARP_WORDS(NW) \
     (emit_buf(NW) * ((NW) + 1) + emit_buf(NW) / 8 + emit_buf(NW) / 4 + EMIT_MAX_BUCKETS / 2 + EMIT_MAX_BUCKETS + emit_buf(NW) / 4)
 
@@ -140,7 +196,8 @@ template <int NW>
 __device__ __forceinline__ void emit_flush(const BucketDev& bk, uint32_t stripe, uint32_t lane, uint64_t* buf, const uint8_t* bbuf,
                                            uint32_t n_buf, uint32_t* hist, unsigned long long* gbase, uint16_t* rank,
                                            uint16_t* perm) {
-    constexpr uint32_t RW = NW + 1;  // words per record
+    constexpr uint32_t SW = NW + 1;  // staging stride in words
+    const uint32_t RW = bk.rw;       // words per record (<= SW)
     const uint32_t nb = bk.n_buckets;  // <= EMIT_MAX_BUCKETS = 64
     for (uint32_t bu = lane; bu < nb; bu += 32) hist[bu] = 0;
     __syncwarp();
@@ -165,7 +222,7 @@ __device__ __forceinline__ void emit_flush(const BucketDev& bk, uint32_t stripe,
     __syncwarp();
     for (uint32_t j = lane; j < n_buf; j += 32) perm[hist[bbuf[j]] + rank[j]] = (uint16_t)j;
     __syncwarp();
-    if constexpr (RW <= 3) {
+    if (RW <= 2) {
         // lane p writes the p-th record in bucket order: a store instruction covers one
         // word of 32 consecutive records of the runs
         for (uint32_t p = lane; p < n_buf; p += 32) {
@@ -173,19 +230,19 @@ __device__ __forceinline__ void emit_flush(const BucketDev& bk, uint32_t stripe,
             const unsigned long long pos = gbase[bu] + (p - hist[bu]);
             if (pos < bk.stripe_cap) {
                 uint64_t* dst = bk.recs + (((uint64_t)bu * bk.stripes + stripe) * bk.stripe_cap + pos) * RW;
-#pragma unroll
-                for (uint32_t i = 0; i < RW; ++i) dst[i] = buf[j * RW + i];
+                dst[0] = buf[j * SW];
+                if (RW == 2) dst[1] = buf[j * SW + 1];
             } else {
                 atomicOr(bk.overflow, 1u);
             }
         }
     } else {
-        // 40-byte records: one word per lane, 32 consecutive words per store instruction
+        // records of 3 words or more: one word per lane, 32 consecutive words per store
         for (uint32_t w = lane; w < n_buf * RW; w += 32) {
             const uint32_t p = w / RW, i = w - p * RW;
             const uint32_t j = perm[p], bu = bbuf[j];
             const unsigned long long pos = gbase[bu] + (p - hist[bu]);
-            if (pos < bk.stripe_cap) bk.recs[(((uint64_t)bu * bk.stripes + stripe) * bk.stripe_cap + pos) * RW + i] = buf[j * RW + i];
+            if (pos < bk.stripe_cap) bk.recs[(((uint64_t)bu * bk.stripes + stripe) * bk.stripe_cap + pos) * RW + i] = buf[j * SW + i];
             else if (i == 0) atomicOr(bk.overflow, 1u);
         }
     }
