@@ -404,8 +404,8 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "pass2_mode" && (v == 0 || v == 1)) ctx->pass2_mode = (int)v;
     else if (n == "record_factor" && v > 0 && v <= 16) ctx->record_factor = v;
     else if (n == "sketch_mode" && (v == 0 || v == 1)) ctx->sketch_mode = (int)v;
-    else if (n == "ladder_ilp" && (v == 1 || v == 2 || v == 3)) ctx->ladder_ilp = (int)v;
-    else if (n == "emit_lookahead" && v >= 1 && v <= 3) ctx->emit_lookahead = (int)v;
+    else if (n == "ladder_ilp" && (v == 1 || v == 2 || v == 3 || v == 4)) ctx->ladder_ilp = (int)v;
+    else if (n == "emit_lookahead" && v >= 1 && v <= 4) ctx->emit_lookahead = (int)v;
     else if (n == "acc_filter" && (v == 0 || v == 1 || v == 2)) ctx->acc_filter = (int)v;
     else if (n == "upsert_all" && (v == 0 || v == 1)) ctx->upsert_all = (int)v;
     // the pass kernels are compiled for blocks of at most 256 threads

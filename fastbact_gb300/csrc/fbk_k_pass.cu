@@ -360,29 +360,8 @@ __global__ void __launch_bounds__(256) k_emit_ladder(BankDev b, uint32_t k, cons
 
 // The same emit with the gate loads of chunk it + 2 in flight while chunk it is
 // emitted: a lane holds three keys (chunks it, it + 1, it + 2), the loads of the
-// farthest one are issued before the emit work and resolved after it.
-struct GateLoads {
-    uint32_t w[4], m[4];
-    uint64_t h0;  // row-0 hash, which also places the key in the table (home_slot_h)
-};
-__device__ __forceinline__ void gate_issue(const uint32_t* __restrict__ top, uint32_t log2w, uint64_t key, bool live, GateLoads& g) {
-    const uint64_t wmask = (1ULL << log2w) - 1;
-#pragma unroll
-    for (int row = 0; row < 4; ++row) {
-        const uint64_t h = smix(key ^ cms_seed(row));
-        if (row == 0) g.h0 = h;
-        const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
-        g.m[row] = 1u << (bit & 31);
-        g.w[row] = live ? __ldg(top + (bit >> 5)) : 0u;
-    }
-}
-__device__ __forceinline__ bool gate_resolve(const GateLoads& g, bool live) {
-    bool ok = live;
-#pragma unroll
-    for (int row = 0; row < 4; ++row) ok &= (g.w[row] & g.m[row]) != 0;
-    return ok;
-}
-
+// farthest one are issued before the emit work and resolved after it (GateLoads,
+// fbk_table.cuh).
 // WS = (64*NW - 2k) / 64 is a template parameter: key words below WS are constant
 // zeros, which saves their registers and instructions (k = 77 in 256-bit keys: one
 // word of four).
@@ -990,6 +969,11 @@ static cudaError_t emitl_nw(const Launch& L, const BankDev& b, uint32_t k, const
                             const TableDev& t, const BucketDev& bk, int lookahead) {
     const size_t smem = (size_t)(L.block / 32) * EMIT_WARP_WORDS(NW) * 8;
     const uint32_t ws = (64u * NW - 2u * k) >> 6;
+    if (lookahead == 4) {  // one lane per read, rolled (fbk_k_roll.cu)
+        Launch L2 = L;
+        L2.block = 256;
+        return launch_emit_roll(NW, L2, b, k, lad, log2w, ts, t, bk);
+    }
     if (lookahead == 3) {
         if constexpr (NW == 1) {
             return emit_launch(k_emit_flat<1, 0>, L, b, k, lad, log2w, ts, t, bk, smem);

@@ -186,6 +186,14 @@ cudaError_t launch_ladder_solid(int nw, const Launch& L, const BankDev& b, uint3
 cudaError_t launch_emit_ladder(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
                                uint32_t t_solid, const TableDev& t, const BucketDev& bk, int lookahead);
 
+// One lane per read, k-mers rolled base by base, each warp's run of 32 reads staged in
+// shared memory (fbk_k_roll.cu); the same results as launch_ladder_pass1 and
+// launch_emit_ladder.  Blocks of 256 threads.
+cudaError_t launch_ladder_pass1_roll(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w,
+                                     uint32_t t, uint32_t* hll12);
+cudaError_t launch_emit_roll(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
+                             uint32_t t_solid, const TableDev& t, const BucketDev& bk);
+
 // ---- multi-isolate waves (fbk_k_batch.cu) ----------------------------------------
 // read_base: n_iso + 1 global read indices (isolate i owns [read_base[i], read_base[i+1])).
 cudaError_t launch_batch_pass1(int nw, const Launch& L, const IsoDev* iso, const unsigned long long* read_base, uint32_t n_iso,

@@ -125,6 +125,31 @@ __device__ __forceinline__ int64_t table_slotw(const TableDev& t, const Key<NW>&
 }
 
 
+// The ladder gate of pass 2 (fbk_k_ladder.cu) for one window, in two halves so that
+// the four L2 loads can be in flight while other work runs: gate_issue hashes the key
+// for the four rows and loads the top level's words, gate_resolve tests the bits.
+struct GateLoads {
+    uint32_t w[4], m[4];
+    uint64_t h0;  // row-0 hash, which also places the key in the table (home_slot_h)
+};
+__device__ __forceinline__ void gate_issue(const uint32_t* __restrict__ top, uint32_t log2w, uint64_t key, bool live, GateLoads& g) {
+    const uint64_t wmask = (1ULL << log2w) - 1;
+#pragma unroll
+    for (int row = 0; row < 4; ++row) {
+        const uint64_t h = smix(key ^ cms_seed(row));
+        if (row == 0) g.h0 = h;
+        const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
+        g.m[row] = 1u << (bit & 31);
+        g.w[row] = live ? __ldg(top + (bit >> 5)) : 0u;
+    }
+}
+__device__ __forceinline__ bool gate_resolve(const GateLoads& g, bool live) {
+    bool ok = live;
+#pragma unroll
+    for (int row = 0; row < 4; ++row) ok &= (g.w[row] & g.m[row]) != 0;
+    return ok;
+}
+
 __device__ __forceinline__ bool bm_bit(const uint32_t* __restrict__ bm, uint64_t g) {
     return (__ldg(&bm[g >> 5]) >> (g & 31)) & 1u;
 }

@@ -225,7 +225,7 @@ def test_gate_only_with_subsampling(ctx, repeat_isolate):
     compare_gate_only(ctx, bank, 31, 64, 16, None, 16, subsample=(0.35, 1234), keep_mask=keep)
 
 
-@pytest.mark.parametrize("lookahead", [1, 2, 3])
+@pytest.mark.parametrize("lookahead", [1, 2, 3, 4])
 def test_emit_variants_with_subsampling_and_256_bit_keys(repeat_isolate, lookahead):
     """Every record-emit form (gate one or two chunks ahead, read by read or over the
     flattened window stream) with skipped reads and keys of every width, including
@@ -344,6 +344,31 @@ def test_build_edge_cases(ctx):
     empty = api.ReadBank()
     t = api.build_cdbg_ext(empty, 31, None, 100000, ctx=ctx)
     assert t.info()[:2] == (0, 0)
+
+
+EDGE_SEQS = [b"", b"A", b"ACGT" * 7, b"C" * 31, b"G" * 32, b"T" * 1000, b"ACGTTGCA" * 600] + rand_seqs(3, 50, 1, 70)
+
+
+@pytest.mark.parametrize("k,kb", [(1, 64), (5, 64), (21, 64), (28, 64), (29, 64), (31, 64), (33, 128), (55, 128), (60, 128),
+                                  (61, 128), (63, 128), (65, 256), (77, 256), (92, 256), (93, 256), (96, 256), (97, 256),
+                                  (124, 256), (125, 256), (127, 256)])
+@pytest.mark.parametrize("rolled", [False, True])
+def test_gate_only_every_record_layout(repeat_isolate, k, kb, rolled):
+    """Every pass-2 record layout (records of ceil((2k + 8) / 64) words, the info byte
+    packed into the key's free top bits or in a word of its own: the boundaries are
+    k = 28/29, 60/61, 92/93, 124/125), with the per-window kernels and with the rolled
+    one-lane-per-read kernels; an edge-case bank whose runs include reads too long to
+    stage (the global-memory path), empty and shorter-than-k reads."""
+    c = api.Context(0)
+    try:
+        if rolled:
+            c.set_tuning(ladder_ilp=4, emit_lookahead=4)
+        compare_gate_only(c, repeat_isolate[0], k, kb, 16, None, 14)
+        edge = api.ReadBank(api.BitSeqArena.from_seqs(EDGE_SEQS[:4]), api.BitSeqArena.from_seqs(EDGE_SEQS[4:30]),
+                            api.BitSeqArena.from_seqs(EDGE_SEQS[30:]))
+        compare_gate_only(c, edge, k, kb, 4, 1, 12)
+    finally:
+        c.close()
 
 
 def test_build_rc_bank_invariance(ctx, small_isolate):
@@ -467,6 +492,7 @@ TUNINGS = [
     dict(ladder_ilp=3),                                   # ladder pass 1 pipelined over chunks
     dict(emit_lookahead=1),                               # gate loads one chunk ahead of the emit
     dict(emit_lookahead=2),                               # emit read by read, gate loads two chunks ahead
+    dict(ladder_ilp=4, emit_lookahead=4),                 # one lane per read, k-mers rolled, runs staged in smem
     dict(acc_filter=0),                                   # every accumulated key kept
     dict(acc_filter=2),                                   # keys that cannot be solid dropped at every width
     dict(upsert_all=0, acc_filter=0),                     # one upsert launch per bucket
