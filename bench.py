@@ -311,6 +311,19 @@ def run_ours(args, rank, world, local):
     total_kmers = kmers_step * args.steps * world
     value = total_kmers / (ms / 1e3)
 
+    # ---- one more (untimed) step with the device time of each k's kernel families ----
+    per_k = {}
+    ctx.set_timing(True)
+    for k in KS:
+        ctx.sync()
+        ctx.timing_reset()
+        t = api.build_cdbg_ext(dbank, k, None, ge.genome_size, ctx=ctx, counter_bits=cb, cms_log2_width=LOG2W)
+        t.release()
+        ctx.sync()
+        per_k[str(k)] = {f: round(ctx.timing(f)[0], 3) for f in ("pass1", "pass2_emit", "pass2_count", "pass2_upsert",
+                                                                  "convert", "table_init") if ctx.timing(f)[0] > 0}
+    ctx.set_timing(False)
+
     # ---- the same step with the counted u16 sketch (what a caller asking for the
     # sketch gets); the headline keeps only the t_solid-level gate ladder -----------
     counted = None
@@ -450,6 +463,7 @@ def run_ours(args, rank, world, local):
                                  "note": "step time minus the estimator kernels"}},
             "counted_sketch": counted,
             "kernel_ms": {k or "all": {"ms": v[0], "launches": v[1]} for k, v in kernel_ms.items()},
+            "kernel_ms_per_k": per_k,
             "roofline": {"kernel": ({"pass1": "pass 1 (k_pass1_sweep: 4 row-slice sweeps)",
                                      "pass2": "pass 2 (k_solid_sweep + k_emit + k_upsert)"} if kernel_ms["solid"][0] > 0 else
                                     {"pass1": "pass 1 (k_ladder_pass1: one sweep, t_solid-level gate ladder)",

@@ -21,8 +21,10 @@
 
 namespace fbk {
 
-constexpr uint32_t ROLL_RUN = 32;         // reads per warp run (one per lane)
-constexpr uint32_t ROLL_STAGE_WORDS = 320;  // staged packed words per warp (2.5 KB)
+constexpr uint32_t ROLL_RUN = 32;           // reads per warp run (one per lane)
+constexpr uint32_t ROLL_STAGE_WORDS = 320;  // staged packed words per warp in the emit (2.5 KB)
+constexpr uint32_t P1_STAGE_WORDS = 160;    // in pass 1 (1.25 KB: six blocks of 256 fit an SM);
+                                            // a run of 32 mate reads of ~146 bases spans ~150
 
 // The run's packed words in shared memory: words [lo, lo + n) of the bank.
 struct RunStage {
@@ -36,8 +38,8 @@ struct RunStage {
 // read's first base and length (len 0 for lanes without a read).  NK + 1 words past the
 // last base are included (a window cut from the packed words reads that far).  Returns
 // a stage with n = 0 when the span does not fit: the caller then reads global memory.
-__device__ __forceinline__ RunStage stage_run(const uint64_t* __restrict__ d, uint64_t* s, uint32_t lane, uint64_t my_off,
-                                              uint32_t my_len, uint32_t nk_words) {
+__device__ __forceinline__ RunStage stage_run(const uint64_t* __restrict__ d, uint64_t* s, uint32_t cap_words, uint32_t lane,
+                                              uint64_t my_off, uint32_t my_len, uint32_t nk_words) {
     const bool has = my_len > 0;
     // first and last word of the run: reads are stored in increasing order
     const unsigned long long lo_c = has ? (my_off >> 5) : ~0ULL;
@@ -54,7 +56,7 @@ __device__ __forceinline__ RunStage stage_run(const uint64_t* __restrict__ d, ui
     const uint64_t lo2 = lo & ~1ULL;  // 16-byte aligned start
     const uint64_t end = hi + 1 + nk_words + 1;
     const uint64_t n = (end - lo2 + 1) & ~1ULL;
-    if (n > ROLL_STAGE_WORDS) return st;
+    if (n > cap_words) return st;
     const ulonglong2* src = reinterpret_cast<const ulonglong2*>(d + lo2);
     ulonglong2* dst = reinterpret_cast<ulonglong2*>(s);
     for (uint32_t i = lane; i < n / 2; i += 32) dst[i] = __ldg(src + i);
@@ -154,11 +156,11 @@ __device__ __forceinline__ uint32_t cursor_next(BaseCursor& c, const RunStage& s
 // Pass 1 with the threshold-ladder gate (fbk_k_ladder.cu), rolled.
 // ---------------------------------------------------------------------------
 template <int NW, int WS>
-__global__ void __launch_bounds__(256, 5) k_ladder_pass1_roll(BankDev b, uint32_t k, uint32_t* __restrict__ lad, uint32_t log2w,
+__global__ void __launch_bounds__(256, 6) k_ladder_pass1_roll(BankDev b, uint32_t k, uint32_t* __restrict__ lad, uint32_t log2w,
                                                               uint32_t t, uint32_t* __restrict__ hll12) {
     constexpr int NK = NW - WS;
     __shared__ uint32_t s_hll[4096];
-    __shared__ __align__(16) uint64_t s_stage[8][ROLL_STAGE_WORDS];
+    __shared__ __align__(16) uint64_t s_stage[8][P1_STAGE_WORDS];
     const bool do_hll = hll12 != nullptr;
     if (do_hll) {
         for (int i = threadIdx.x; i < 4096; i += blockDim.x) s_hll[i] = 0;
@@ -183,7 +185,7 @@ __global__ void __launch_bounds__(256, 5) k_ladder_pass1_roll(BankDev b, uint32_
         }
         const uint32_t nk = len ? len - k + 1 : 0;
         __syncwarp();
-        const RunStage st = stage_run(b.data, s_stage[wib], lane, off, len, NK);
+        const RunStage st = stage_run(b.data, s_stage[wib], P1_STAGE_WORDS, lane, off, len, NK);
         const uint32_t steps = __reduce_max_sync(0xffffffffu, nk);
         uint64_t F[NK], R[NK];
         BaseCursor cur;
@@ -269,7 +271,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_roll(BankDev b, uint32_t k, con
         }
         const uint32_t nk = len ? len - k + 1 : 0;
         __syncwarp();
-        const RunStage st = stage_run(b.data, stage, lane, off, len, NK);
+        const RunStage st = stage_run(b.data, stage, ROLL_STAGE_WORDS, lane, off, len, NK);
         const uint32_t steps = __reduce_max_sync(0xffffffffu, nk);
         uint64_t F[NK], R[NK];
         BaseCursor cur;
