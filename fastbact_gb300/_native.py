@@ -90,7 +90,7 @@ class BatchStats(C.Structure):
                 ("pass1_block", C.c_int32), ("pass1_grid", C.c_int32), ("pass1_rows", C.c_int32),
                 ("solid_block", C.c_int32), ("solid_grid", C.c_int32), ("solid_rows", C.c_int32),
                 ("emit_block", C.c_int32), ("emit_grid", C.c_int32), ("upsert_block", C.c_int32),
-                ("upsert_grid", C.c_int32), ("tuned", C.c_int32), ("_pad", C.c_int32), ("tune_ms", C.c_double)]
+                ("upsert_grid", C.c_int32), ("tuned", C.c_int32), ("emit_form", C.c_int32), ("tune_ms", C.c_double)]
 
 
 class IngestStatsC(C.Structure):

@@ -404,8 +404,8 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "pass2_mode" && (v == 0 || v == 1)) ctx->pass2_mode = (int)v;
     else if (n == "record_factor" && v > 0 && v <= 16) ctx->record_factor = v;
     else if (n == "sketch_mode" && (v == 0 || v == 1)) ctx->sketch_mode = (int)v;
-    else if (n == "ladder_ilp" && (v == 1 || v == 2 || v == 3 || v == 4)) ctx->ladder_ilp = (int)v;
-    else if (n == "emit_lookahead" && v >= 1 && v <= 4) ctx->emit_lookahead = (int)v;
+    else if (n == "ladder_ilp" && v >= 0 && v <= 4 && v == (int)v) ctx->ladder_ilp = (int)v;
+    else if (n == "emit_lookahead" && v >= 0 && v <= 4 && v == (int)v) ctx->emit_lookahead = (int)v;
     else if (n == "acc_filter" && (v == 0 || v == 1 || v == 2)) ctx->acc_filter = (int)v;
     else if (n == "upsert_all" && (v == 0 || v == 1)) ctx->upsert_all = (int)v;
     // the pass kernels are compiled for blocks of at most 256 threads
@@ -1396,7 +1396,7 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
             if (inline_gate)
                 TIMED(ctx, "pass2_emit", launch_emit_ladder(nw, launch_cfg_persistent(ctx, ctx->block_emit, ctx->grid_pass2), bv,
                                                             p->k, lad->bits, lad->log2w, p->t_solid, td, bk.d,
-                                                            ctx->emit_lookahead));
+                                                            emit_form(ctx, nw)));
             else
                 TIMED(ctx, "pass2_emit", launch_emit(nw, L, bv, p->k, bm, 1, td, bk.d));
             if (!filter && ctx->upsert_all) {
@@ -1545,7 +1545,7 @@ static fbk_status build_front_ladder(fbk_ctx* ctx, const fbk_bank* b, const fbk_
         TimedLaunch tl;
         time_begin(ctx, "pass1", tl);
         cudaError_t e = launch_ladder_pass1(nw, L, bank_view(b, b->chunk_starts[c], b->chunk_starts[c + 1], keep), p->k, lad.bits,
-                                            log2w, p->t_solid, hll, ctx->ladder_ilp);
+                                            log2w, p->t_solid, hll, ladder_form(ctx, nw));
         time_end(ctx, tl);
         if (e != cudaSuccess) st = cuda_err(ctx, e, "pass1 ladder");
     }

@@ -72,7 +72,9 @@ struct fbk_batch {
     std::vector<std::unique_ptr<BatchIso>> isos;
     fbk_batch_stats stats{};
     Shape pass1{256, 0, 4}, solid{256, 0, 4}, emit{256, 0, 0}, upsert{256, 0, 0};
-    bool tuned = false;
+    int emit_form = 0;     // 0: the context's choice (emit_form); else the phase-B autotuner's
+    bool tuned = false;    // pass-1 shape tuned
+    bool tuned_b = false;  // emit form and shape, persistent-upsert shape tuned
     cudaEvent_t ev[2] = {nullptr, nullptr};
     void* h_stage = nullptr;  // pinned staging for descriptors and read-backs
     uint64_t h_stage_bytes = 0;
@@ -350,6 +352,99 @@ fbk_status autotune(fbk_batch* B, BatchIso* it) {
     return FBK_OK;
 }
 
+// Phase-B autotuner (ladder gate): on the first phase-B isolate, with its table and
+// record buckets allocated, time the record emit in each form and block shape — flat
+// window stream with blocks of 128 or 256, one lane per read (rolled) — and, when the
+// isolate's pass upserts every bucket in one persistent launch, that launch with blocks
+// of 128 or 256 at the occupancy grid or 2 or 4 blocks per SM.  Each trial starts from
+// cleared bucket counters (and, for the upsert, a cleared table); phase B itself clears
+// both again before it runs, so the trials leave nothing behind.
+fbk_status autotune_b(fbk_batch* B, BatchIso* it, bool persistent_upsert) {
+    fbk_ctx* ctx = B->ctx;
+    const double t0 = now_ms();
+    auto timed = [&](auto&& launch, float* ms) -> fbk_status {
+        CK(ctx, cudaEventRecord(B->ev[0], ctx->stream));
+        fbk_status s2 = launch();
+        if (s2) return s2;
+        CK(ctx, cudaEventRecord(B->ev[1], ctx->stream));
+        CK(ctx, cudaEventSynchronize(B->ev[1]));
+        CK(ctx, cudaEventElapsedTime(ms, B->ev[0], B->ev[1]));
+        return FBK_OK;
+    };
+    uint32_t* flags = (uint32_t*)dev_alloc(ctx, 256);  // overflow flag, status word, work counter
+    if (!flags) return set_err(ctx, FBK_ERR_OOM, "batch autotuner");
+    BucketDev bk = it->bk;
+    bk.overflow = flags;
+    unsigned long long* work = (unsigned long long*)(flags + 2);
+    const BankDev bv = bank_view(it->bank, 0, it->bank->n_reads, it->keep);
+    struct Cand {
+        int form, block;
+    };
+    const Cand emits[] = {{3, 128}, {3, 256}, {4, 256}};
+    float best = 1e30f;
+    Cand best_e = emits[0];
+    fbk_status st = FBK_OK;
+    for (const Cand& c : emits) {
+        cudaError_t e = cudaMemsetAsync(it->fill, 0, (uint64_t)bk.n_buckets * bk.stripes * 8, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, 16, ctx->stream);
+        if (e != cudaSuccess) {
+            st = cuda_err(ctx, e, "batch autotuner");
+            break;
+        }
+        float ms = 0;
+        st = timed([&]() -> fbk_status {
+            TIMED(ctx, "tune_emit", launch_emit_ladder(B->nw, launch_cfg_persistent(ctx, c.block, 0), bv, B->p.k, it->lad,
+                                                       B->p.cms_log2_width, B->p.t_solid, tbl_dev(it->table), bk, c.form));
+            return FBK_OK;
+        }, &ms);
+        if (st) break;
+        if (ms < best) {
+            best = ms;
+            best_e = c;
+        }
+    }
+    if (st == FBK_OK && persistent_upsert) {
+        // the buckets hold the last trial's records (every form writes the same records)
+        const int blocks[] = {128, 256};
+        const int per_sm[] = {0, 2, 4};
+        best = 1e30f;
+        Shape best_u = B->upsert;
+        for (int bl : blocks)
+            for (int ps : per_sm) {
+                const Shape sh{bl, ps ? ps * ctx->num_sms : 0, 0};
+                cudaError_t e = cudaSuccess;
+                st = FBK_OK;
+                TIMED(ctx, "table_init", launch_table_init(B->nw, launch_cfg(ctx, 256, 0), tbl_dev(it->table)));
+                e = cudaMemsetAsync(it->table->cnt, 0, it->table->cap * 32, ctx->stream);
+                if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, 24, ctx->stream);
+                if (e != cudaSuccess) {
+                    st = cuda_err(ctx, e, "batch autotuner");
+                    break;
+                }
+                float ms = 0;
+                st = timed([&]() -> fbk_status {
+                    TIMED(ctx, "tune_upsert", launch_upsert_all(B->nw, shape_launch(ctx, sh), bk, 1, 1, tbl_dev(it->table),
+                                                                flags + 1, work));
+                    return FBK_OK;
+                }, &ms);
+                if (st) break;
+                if (ms < best) {
+                    best = ms;
+                    best_u = sh;
+                }
+            }
+        if (st == FBK_OK) B->upsert = best_u;
+    }
+    cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, flags);
+    if (st) return st;
+    B->emit = Shape{best_e.block, 0, 0};
+    B->emit_form = best_e.form;
+    B->tuned_b = true;
+    B->stats.tune_ms += now_ms() - t0;
+    return FBK_OK;
+}
+
 // Phase A of a wave: pass 1, solidity bitmap, counts; then the host reads each
 // isolate's distinct-key estimate and record count.
 fbk_status phase_a(fbk_batch* B, const std::vector<BatchIso*>& W) {
@@ -582,6 +677,11 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
         work.p = (unsigned long long*)dev_alloc(ctx, (uint64_t)n * 8);
         if (!work.p) return set_err(ctx, FBK_ERR_OOM, "batch upsert counters");
     }
+    if (B->p.autotune && B->ladder && !B->tuned_b) {
+        st = autotune_b(B, V[0], work.p != nullptr && !flt[0].cnt);
+        if (st) return st;
+    }
+    const int eform = B->emit_form ? B->emit_form : emit_form(ctx, B->nw);
     st = run_phase(B, &B->stats.ms_phase_b, [&]() -> fbk_status {
         CK(ctx, cudaMemsetAsync(w.cnt, 0, (uint64_t)n * 64, ctx->stream));
         CK(ctx, cudaMemsetAsync(w.status, 0, (uint64_t)n * 8, ctx->stream));
@@ -598,7 +698,7 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
                 TIMED(ctx, "batch_emit", launch_emit_ladder(B->nw, shape_launch(ctx, B->emit),
                                                             bank_view(it->bank, 0, it->bank->n_reads, it->keep), k, it->lad,
                                                             B->p.cms_log2_width, B->p.t_solid, tbl_dev(it->table), bk,
-                                                            ctx->emit_lookahead));
+                                                            eform));
             }
         } else {
             TIMED(ctx, "batch_emit", launch_batch_emit(B->nw, shape_launch(ctx, B->emit), w.iso, w.rb, n, k, BATCH_STRIPES));
@@ -977,6 +1077,7 @@ FBK_API fbk_status fbk_batch_get_stats(const fbk_batch* B, fbk_batch_stats* out)
     out->emit_grid = B->emit.grid;
     out->upsert_block = B->upsert.block;
     out->upsert_grid = B->upsert.grid;
+    out->emit_form = B->emit_form ? B->emit_form : emit_form(B->ctx, B->nw);
     out->kernel_launches = B->ctx->launches;
     return FBK_OK;
 }

@@ -477,7 +477,8 @@ typedef struct {
     /* launch shapes in use: block, grid (0 = occupancy), and sketch rows per sweep */
     int32_t pass1_block, pass1_grid, pass1_rows, solid_block, solid_grid, solid_rows;
     int32_t emit_block, emit_grid, upsert_block, upsert_grid;
-    int32_t tuned, _pad;
+    int32_t tuned;
+    int32_t emit_form;  /* record emit in use: 3 flat window stream, 4 one lane per read (rolled) */
     double tune_ms;
 } fbk_batch_stats;
 
