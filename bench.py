@@ -640,7 +640,8 @@ def run_batch_mode(args):
                   "tune_ms": tune_ms,
                   "shapes": {"pass1": [st.pass1_block, st.pass1_grid, st.pass1_rows],
                              "solid": [st.solid_block, st.solid_grid, st.solid_rows],
-                             "emit": [st.emit_block, st.emit_grid], "upsert": [st.upsert_block, st.upsert_grid]}},
+                             "emit": [st.emit_block, st.emit_grid], "emit_form": st.emit_form,
+                             "upsert": [st.upsert_block, st.upsert_grid]}},
         "gpu_launches": s1.kernel_launches - launches0 if s1.kernel_launches >= launches0 else None,
         "kernel_ms": diag,
         "clocks": clk,
