@@ -24,12 +24,9 @@ __device__ __forceinline__ uint64_t home_slot(uint64_t fold, uint64_t cap) {
     return home_slot_h(smix(fold ^ cms_seed(0)), cap);
 }
 
-// The probes take the first slot's word(s) from the caller when it loaded them early
-// (first_ok), so that load can overlap another (the record filter's counter).
-__device__ __forceinline__ int64_t table_slot1(const TableDev& t, uint64_t key, uint64_t s, uint32_t* status,
-                                               bool first_ok = false, uint64_t first = 0) {
+__device__ __forceinline__ int64_t table_slot1(const TableDev& t, uint64_t key, uint64_t s, uint32_t* status) {
     for (uint32_t probe = 0; probe < t.max_probe; ++probe) {
-        const uint64_t cur = (probe == 0 && first_ok) ? first : __ldcg(&t.keys[s]);
+        const uint64_t cur = __ldcg(&t.keys[s]);
         if (cur == key) return (int64_t)s;
         if (cur == KEY_EMPTY) {
             const uint64_t old = atomicCAS((unsigned long long*)&t.keys[s], KEY_EMPTY, key);
@@ -65,12 +62,11 @@ __device__ __forceinline__ void cas128(uint64_t* addr, uint64_t cmp_lo, uint64_t
 // decided by the CAS, which returns the slot's whole current value.  A key whose word 1
 // is all ones is also confirmed by the CAS when it seems found, since a read of the two
 // words could straddle another key's claim.
-__device__ __forceinline__ int64_t table_slot2(const TableDev& t, const Key<2>& key, uint64_t s, uint32_t* status,
-                                               bool first_ok = false, ulonglong2 first = ulonglong2{0, 0}) {
+__device__ __forceinline__ int64_t table_slot2(const TableDev& t, const Key<2>& key, uint64_t s, uint32_t* status) {
     const bool w1_empty = key.w[1] == KEY_EMPTY;
     for (uint32_t probe = 0; probe < t.max_probe; ++probe) {
         uint64_t* a = t.keys + s * 2;
-        const ulonglong2 c = (probe == 0 && first_ok) ? first : __ldcg(reinterpret_cast<const ulonglong2*>(a));
+        const ulonglong2 c = __ldcg(reinterpret_cast<const ulonglong2*>(a));
         const bool other = (c.x != KEY_EMPTY && c.x != key.w[0]) || (c.y != KEY_EMPTY && c.y != key.w[1]);
         if (!other) {
             if (c.x == key.w[0] && c.y == key.w[1] && !w1_empty) return (int64_t)s;
@@ -84,23 +80,15 @@ __device__ __forceinline__ int64_t table_slot2(const TableDev& t, const Key<2>& 
     return -1;
 }
 
-// The tag of the key's home slot, loaded with acquire ordering (the key words are read
-// after it); table_slotw can take it as its first probe's tag.
-__device__ __forceinline__ uint64_t tag_acquire(const TableDev& t, uint64_t s) {
-    cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> tag_ref(*(unsigned long long*)&t.tags[s * t.tag_stride]);
-    return tag_ref.load(cuda::memory_order_acquire);
-}
-
 template <int NW>
-__device__ __forceinline__ int64_t table_slotw(const TableDev& t, const Key<NW>& key, uint64_t f, uint64_t s, uint32_t* status,
-                                               bool first_ok = false, uint64_t first = 0) {
+__device__ __forceinline__ int64_t table_slotw(const TableDev& t, const Key<NW>& key, uint64_t f, uint64_t s, uint32_t* status) {
     const uint64_t fp = (smix(f ^ FP_SALT) | 1ULL) & ~TAG_READY;
     // with the tag in word 0 (tag_stride == NW) the key's word 0 is zero and not stored
     const int w0 = t.tag_stride == NW ? 1 : 0;
     for (uint32_t probe = 0; probe < t.max_probe; ++probe) {
         unsigned long long* tp = (unsigned long long*)&t.tags[s * t.tag_stride];
         cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> tag_ref(*tp);
-        uint64_t tag = (probe == 0 && first_ok) ? first : tag_ref.load(cuda::memory_order_acquire);
+        uint64_t tag = tag_ref.load(cuda::memory_order_acquire);
         if (tag == 0) {
             const uint64_t old = atomicCAS(tp, 0ULL, fp);
             if (old == 0) {
@@ -141,24 +129,26 @@ __device__ __forceinline__ int64_t table_slotw(const TableDev& t, const Key<NW>&
 // the four L2 loads can be in flight while other work runs: gate_issue hashes the key
 // for the four rows and loads the top level's words, gate_resolve tests the bits.
 struct GateLoads {
-    uint32_t w[4], m[4];
-    uint64_t h0;  // row-0 hash, which also places the key in the table (home_slot_h)
+    uint32_t w[4];  // the loaded words of the four rows
+    uint32_t bits;  // each row's bit within its word, 5 bits per row (one register, not four)
+    uint64_t h0;    // row-0 hash, which also places the key in the table (home_slot_h)
 };
 __device__ __forceinline__ void gate_issue(const uint32_t* __restrict__ top, uint32_t log2w, uint64_t key, bool live, GateLoads& g) {
     const uint64_t wmask = (1ULL << log2w) - 1;
+    g.bits = 0;
 #pragma unroll
     for (int row = 0; row < 4; ++row) {
         const uint64_t h = smix(key ^ cms_seed(row));
         if (row == 0) g.h0 = h;
         const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
-        g.m[row] = 1u << (bit & 31);
+        g.bits |= (bit & 31u) << (5 * row);
         g.w[row] = live ? __ldg(top + (bit >> 5)) : 0u;
     }
 }
 __device__ __forceinline__ bool gate_resolve(const GateLoads& g, bool live) {
     bool ok = live;
 #pragma unroll
-    for (int row = 0; row < 4; ++row) ok &= (g.w[row] & g.m[row]) != 0;
+    for (int row = 0; row < 4; ++row) ok &= ((g.w[row] >> ((g.bits >> (5 * row)) & 31u)) & 1u) != 0;
     return ok;
 }
 
