@@ -466,9 +466,10 @@ def run_ours(args, rank, world, local):
             "kernel_ms_per_k": per_k,
             "roofline": {"kernel": ({"pass1": "pass 1 (k_pass1_sweep: 4 row-slice sweeps)",
                                      "pass2": "pass 2 (k_solid_sweep + k_emit + k_upsert)"} if kernel_ms["solid"][0] > 0 else
-                                    {"pass1": "pass 1 (k_ladder_pass1: one sweep, t_solid-level gate ladder)",
-                                     "pass2": "pass 2 (k_emit_flat + k_count_records + k_upsert)"
-                                     if kernel_ms["pass2_count"][0] > 0 else "pass 2 (k_emit_flat + k_upsert)"})[dom],
+                                    {"pass1": "pass 1 (k_ladder_pass1 / k_ladder_pass1_roll: one sweep, t_solid-level "
+                                               "gate ladder)",
+                                     "pass2": "pass 2 (record emit k_emit_roll / k_emit_flat + k_count_records + "
+                                              "k_upsert / k_upsert_all)"})[dom],
                          "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
                          "traffic_source": traffic_src,

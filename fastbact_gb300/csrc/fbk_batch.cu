@@ -73,6 +73,7 @@ struct fbk_batch {
     fbk_batch_stats stats{};
     Shape pass1{256, 0, 4}, solid{256, 0, 4}, emit{256, 0, 0}, upsert{256, 0, 0};
     int emit_form = 0;     // 0: the context's choice (emit_form); else the phase-B autotuner's
+    bool pass1_single = false;  // ladder pass 1 as one single-isolate launch per isolate (autotuned)
     bool tuned = false;    // pass-1 shape tuned
     bool tuned_b = false;  // emit form and shape, persistent-upsert shape tuned
     cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -322,6 +323,23 @@ fbk_status autotune(fbk_batch* B, BatchIso* it) {
                     best1 = s;
                 }
             }
+    // With a ladder gate the single-isolate pass 1 (its form chosen per key width by the
+    // context) is a candidate too: one launch per isolate of the wave.
+    bool single = false;
+    if (B->ladder) {
+        CK(ctx, cudaMemsetAsync(gate, 0, cms_bytes, ctx->stream));
+        CK(ctx, cudaMemsetAsync(it->hll12, 0, 4096 * 4, ctx->stream));
+        float ms = 0;
+        st = timed([&]() -> fbk_status {
+            TIMED(ctx, "tune_pass1", launch_ladder_pass1(B->nw, launch_cfg_persistent(ctx, 256, 0),
+                                                         bank_view(it->bank, 0, it->bank->n_reads, it->keep), B->p.k, it->lad,
+                                                         B->p.cms_log2_width, B->p.t_solid, it->hll12,
+                                                         ladder_form(ctx, B->nw)));
+            return FBK_OK;
+        }, &ms);
+        if (st) return st;
+        single = ms < best;
+    }
     // the sketch now holds the isolate's full counts: tune the solidity sweep on it
     // (a ladder gate has no solidity sweep: the emit evaluates it)
     const uint64_t bm_bytes = (it->bank->n_words + 9) * 4;
@@ -345,6 +363,7 @@ fbk_status autotune(fbk_batch* B, BatchIso* it) {
                 }
             }
     B->pass1 = best1;
+    B->pass1_single = single;
     B->solid = best2;
     B->tuned = true;
     B->stats.tuned = 1;
@@ -482,7 +501,15 @@ fbk_status phase_a(fbk_batch* B, const std::vector<BatchIso*>& W) {
         if (B->ladder) {
             // the gate is evaluated inside the record emit: no bitmap, and the
             // records are bounded by the windows the count kernel tallies
-            TIMED(ctx, "batch_pass1", launch_batch_lpass1(B->nw, shape_launch(ctx, B->pass1), w.iso, w.rb, n, k));
+            if (B->pass1_single) {
+                for (BatchIso* it : W)
+                    TIMED(ctx, "batch_pass1", launch_ladder_pass1(B->nw, launch_cfg_persistent(ctx, 256, 0),
+                                                                  bank_view(it->bank, 0, it->bank->n_reads, it->keep), k, it->lad,
+                                                                  B->p.cms_log2_width, B->p.t_solid, it->hll12,
+                                                                  ladder_form(ctx, B->nw)));
+            } else {
+                TIMED(ctx, "batch_pass1", launch_batch_lpass1(B->nw, shape_launch(ctx, B->pass1), w.iso, w.rb, n, k));
+            }
             TIMED(ctx, "batch_count", launch_batch_count(shape_launch(ctx, B->solid), w.iso, w.rb, n, k));
             return FBK_OK;
         }
@@ -1069,7 +1096,7 @@ FBK_API fbk_status fbk_batch_get_stats(const fbk_batch* B, fbk_batch_stats* out)
     *out = B->stats;
     out->pass1_block = B->pass1.block;
     out->pass1_grid = B->pass1.grid;
-    out->pass1_rows = B->pass1.rows;
+    out->pass1_rows = B->pass1_single ? 0 : B->pass1.rows;
     out->solid_block = B->solid.block;
     out->solid_grid = B->solid.grid;
     out->solid_rows = B->solid.rows;

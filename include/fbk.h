@@ -474,7 +474,8 @@ typedef struct {
 typedef struct {
     uint64_t isolates_done, waves, fallbacks, graph_launches, kernel_launches;
     double ms_estimate, ms_phase_a, ms_phase_b, ms_host;   /* device time (events) and host planning */
-    /* launch shapes in use: block, grid (0 = occupancy), and sketch rows per sweep */
+    /* launch shapes in use: block, grid (0 = occupancy), and sketch rows per sweep
+     * (pass1_rows 0: the ladder pass 1 runs as one single-isolate launch per isolate) */
     int32_t pass1_block, pass1_grid, pass1_rows, solid_block, solid_grid, solid_rows;
     int32_t emit_block, emit_grid, upsert_block, upsert_grid;
     int32_t tuned;
