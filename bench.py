@@ -376,7 +376,8 @@ def run_ours(args, rank, world, local):
         for ln in tpath.read_text().splitlines():
             f = ln.split()
             if len(f) >= 2 and f[0] == f"{dom}_u16":
-                traffic, traffic_src = float(f[1]), "profiles/traffic.txt (ncu dram__bytes, one pass of one k)"
+                traffic, traffic_src = float(f[1]), ("mean DRAM bytes of one pass (one k) of pass 2 in the full-size "
+                                                      "ncu capture of profiles/pass2_traffic_isolate5M_100x.md")
 
     # ---- end to end through the C ABI from pinned host memory ------------------------
     e2e = None
@@ -674,6 +675,8 @@ def run_stress_mode(args):
     dbank, dsample = api.DeviceBank(ctx, bank), api.DeviceBank(ctx, sample)
     k, kb, log2w = 127, 256, 26
     runs = {}
+    clocks = ClockSampler(0)
+    clocks.start()
 
     def timed(name, fn, kmers):
         ctx.sync()
@@ -717,6 +720,7 @@ def run_stress_mode(args):
     runs["subsampled_110x"]["factor"] = f
     runs["subsampled_110x"]["policy"] = why
     t.release()
+    clk = clocks.stop()
     line = {
         "metric": "k-mers/s at k = 127 (stress: 12 Mbp GC 0.66, repeats + tandem array, 300x, 1% subs, 0.05% indels)",
         "value": runs["full_input"]["kmers_per_s"], "unit": "k-mers/s", "n_gpus": 1, "steps": 1, "warmup": 1,
@@ -728,6 +732,7 @@ def run_stress_mode(args):
                    "bank_reads": bank.total_reads(), "bank_bases": bank.total_bases(), "generation_s": round(gen_s, 1),
                    "genome_size_est": ge.genome_size, "estimated_cov": ge.estimated_cov},
         "runs": runs,
+        "clocks": clk,
     }
     print(json.dumps(line), flush=True)
     ctx.close()
