@@ -231,6 +231,17 @@ def parity_check(wl, bank, sample, n_sample, stats, ge, regs, res) -> dict:
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
+def env_tuning(ctx) -> dict:
+    """Tuning values from FBK_TUNE ("name=value,name=value"), set on the context."""
+    tune = {}
+    for kv in filter(None, os.environ.get("FBK_TUNE", "").split(",")):
+        name, v = kv.split("=")
+        tune[name] = float(v)
+    if tune:
+        ctx.set_tuning(**tune)
+    return tune
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -246,12 +257,7 @@ def run_ours(args, rank, world, local):
     KS, LOG2W, HLL_P = wl["ks"], wl["cms_log2w"], wl["hll_p"]
     p, bank, ist, sample, n_sample, stats, gen_s = make_workload(wl, rank, args.scale)
     ctx = api.Context(local, pool_bytes=int(os.environ.get("FBK_POOL_BYTES", str(60 << 30))))
-    tune = {}
-    for kv in filter(None, os.environ.get("FBK_TUNE", "").split(",")):
-        name, v = kv.split("=")
-        tune[name] = float(v)
-    if tune:
-        ctx.set_tuning(**tune)
+    tune = env_tuning(ctx)
     dbank = api.DeviceBank(ctx, bank)
     dsample = api.DeviceBank(ctx, sample)
     ctx.sync()
@@ -525,6 +531,7 @@ def run_batch_mode(args):
     members = cohort.make(args.isolates, scale=args.genome_scale)
     gen_s = time.time() - t0
     ctx = api.Context(0, pool_bytes=int(os.environ.get("FBK_POOL_BYTES", str(200 << 30))))
+    tune = env_tuning(ctx)
     params = api.batch_params(policy=cohort.policy(), k=BATCH_K, cms_log2_width=BATCH_LOG2W, counter_bits=16)
     b = api.Batch(ctx, params)
     # warm-up (and autotuning) on the first two members
@@ -629,7 +636,7 @@ def run_batch_mode(args):
                                "depth 30-200x, PE150; >150x subsampled to 110x; k=31, CMS 4 x 2^22 u16, HLL p=14",
                    "isolates": args.isolates, "bank_bases": int(sum(m.bank.total_bases() for m in members)),
                    "subsampled": int(sum(1 for r in res if r.subsample_factor < 1.0)),
-                   "generation_s": round(gen_s, 1)},
+                   "generation_s": round(gen_s, 1), "tuning": tune},
         "plain": {"value": args.isolates / plain_s * 3600.0, "unit": "isolates/h", "seconds": plain_s},
         "kmers_per_s": kmers / batch_s,
         "identical_to_plain": mismatches == 0, "mismatches": mismatches,

@@ -306,6 +306,8 @@ FBK_API fbk_status fbk_ctx_fork(fbk_ctx* parent, fbk_ctx** out) {
     c->sketch_mode = parent->sketch_mode;
     c->ladder_ilp = parent->ladder_ilp;
     c->emit_lookahead = parent->emit_lookahead;
+    c->upsert_queue = parent->upsert_queue;
+    c->batch_pass1 = parent->batch_pass1;
     c->acc_filter = parent->acc_filter;
     c->upsert_all = parent->upsert_all;
     cudaError_t e = cudaSetDevice(c->device);
@@ -404,8 +406,10 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "pass2_mode" && (v == 0 || v == 1)) ctx->pass2_mode = (int)v;
     else if (n == "record_factor" && v > 0 && v <= 16) ctx->record_factor = v;
     else if (n == "sketch_mode" && (v == 0 || v == 1)) ctx->sketch_mode = (int)v;
-    else if (n == "ladder_ilp" && v >= 0 && v <= 4 && v == (int)v) ctx->ladder_ilp = (int)v;
+    else if (n == "ladder_ilp" && v >= 0 && v <= 5 && v == (int)v) ctx->ladder_ilp = (int)v;
     else if (n == "emit_lookahead" && v >= 0 && v <= 4 && v == (int)v) ctx->emit_lookahead = (int)v;
+    else if (n == "upsert_queue" && (v == 0 || v == 1 || v == 2)) ctx->upsert_queue = (int)v;
+    else if (n == "batch_pass1" && (v == 0 || v == 1 || v == 2)) ctx->batch_pass1 = (int)v;
     else if (n == "acc_filter" && (v == 0 || v == 1 || v == 2)) ctx->acc_filter = (int)v;
     else if (n == "upsert_all" && (v == 0 || v == 1)) ctx->upsert_all = (int)v;
     // the pass kernels are compiled for blocks of at most 256 threads
@@ -430,6 +434,8 @@ FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, doub
     else if (n == "sketch_mode") *v = ctx->sketch_mode;
     else if (n == "ladder_ilp") *v = ctx->ladder_ilp;
     else if (n == "emit_lookahead") *v = ctx->emit_lookahead;
+    else if (n == "upsert_queue") *v = ctx->upsert_queue;
+    else if (n == "batch_pass1") *v = ctx->batch_pass1;
     else if (n == "acc_filter") *v = ctx->acc_filter;
     else if (n == "upsert_all") *v = ctx->upsert_all;
     else if (n == "block_pass1") *v = ctx->block_pass1;
@@ -1409,7 +1415,7 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
                         CK(ctx, cudaMemsetAsync(flt.cnt, 0, (1ULL << flt.log2m) * 4, ctx->stream));
                         TIMED(ctx, "pass2_count", launch_count_records(nw, L, bk.d, bu, flt));
                     }
-                    TIMED(ctx, "pass2_upsert", launch_upsert(nw, L, bk.d, bu, 1, 1, td, ctx->d_status, flt));
+                    TIMED(ctx, "pass2_upsert", launch_upsert(nw, L, bk.d, bu, 1, 1, td, ctx->d_status, flt, ctx->upsert_queue));
                 }
             }
         }

@@ -501,7 +501,7 @@ fbk_status phase_a(fbk_batch* B, const std::vector<BatchIso*>& W) {
         if (B->ladder) {
             // the gate is evaluated inside the record emit: no bitmap, and the
             // records are bounded by the windows the count kernel tallies
-            if (B->pass1_single) {
+            if (ctx->batch_pass1 ? ctx->batch_pass1 == 2 : B->pass1_single) {
                 for (BatchIso* it : W)
                     TIMED(ctx, "batch_pass1", launch_ladder_pass1(B->nw, launch_cfg_persistent(ctx, 256, 0),
                                                                   bank_view(it->bank, 0, it->bank->n_reads, it->keep), k, it->lad,
@@ -747,7 +747,7 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
                     TIMED(ctx, "batch_filter", launch_count_records(B->nw, shape_launch(ctx, B->upsert), bk, bu, flt[i]));
                 }
                 TIMED(ctx, "batch_upsert", launch_upsert(B->nw, shape_launch(ctx, B->upsert), bk, bu, 1, 1, tbl_dev(it->table),
-                                                         w.status + 2 * i, flt[i]));
+                                                         w.status + 2 * i, flt[i], ctx->upsert_queue));
             }
         }
         for (uint32_t i = 0; i < n; ++i) {
@@ -1096,7 +1096,7 @@ FBK_API fbk_status fbk_batch_get_stats(const fbk_batch* B, fbk_batch_stats* out)
     *out = B->stats;
     out->pass1_block = B->pass1.block;
     out->pass1_grid = B->pass1.grid;
-    out->pass1_rows = B->pass1_single ? 0 : B->pass1.rows;
+    out->pass1_rows = (B->ladder && (B->ctx->batch_pass1 ? B->ctx->batch_pass1 == 2 : B->pass1_single)) ? 0 : B->pass1.rows;
     out->solid_block = B->solid.block;
     out->solid_grid = B->solid.grid;
     out->solid_rows = B->solid.rows;

@@ -75,14 +75,22 @@ struct fbk_ctx {
     double record_factor = 1.25;          // bucket capacity / expected records per stripe
     int sketch_mode = 1;                  // 1: a build that does not return its sketch keeps only the gate ladder
     // Ladder pass 1: 1 or 2 windows per lane per step, 3 pipelined over chunks, 4 one lane
-    // per read with rolled k-mers; 0 (default) picks by key width: 4 for 256-bit keys
-    // (k = 77: 5.98 -> 5.24 ms per 100x pass), else 1 (rolled: k = 21 6.64 -> 7.43 ms).
+    // per read with rolled k-mers, 5 the same with two windows per lane per step; 0
+    // (default) picks by key width: 5 for 128- and 256-bit keys, 1 for 64-bit keys.
+    // Measured per 100x pass (forms 1 / 4 / 5): k = 21 6.62 / 7.47 / 7.13 ms, k = 33
+    // 7.30 / 7.37 / 6.68, k = 55 5.71 / 6.26 / 5.59, k = 77 5.98 / 5.37 / 4.74.
     int ladder_ilp = 0;
     // Record emit: gate loads 1 or 2 chunks ahead read by read; 3 = 2 ahead over a flattened
     // window stream; 4 = one lane per read with rolled k-mers.  0 (default) picks by key
     // width: 4 for 64- and 128-bit keys (k = 21 8.57 -> 7.02 ms per 100x pass, k = 33
     // 9.04 -> 8.16, k = 55 7.38 -> 6.77), 3 for 256-bit keys (rolled: k = 77 7.14 -> 8.88).
     int emit_lookahead = 0;
+    // Filtered upserts: 1 (default) queues the filter's survivors per warp so that the
+    // probes run on full warps, 2 the same at six blocks per SM, 0 tests the filter
+    // inline.  Measured per 100x pass (0 / 1 / 2): k = 55 7.44 / 6.67 / 7.93 ms, k = 77
+    // 10.88 / 7.70 / 9.10.
+    int upsert_queue = 1;
+    int batch_pass1 = 0;                  // batches with a ladder gate: 0 autotuned, 1 one multi-isolate launch, 2 a launch per isolate
     int upsert_all = 1;                   // 1: an unfiltered pass upserts every bucket in one persistent launch
     int acc_filter = 1;                   // keys with fewer records than min_trans_cov stay out of the table: 0 never, 1 for 256-bit keys, 2 always
     bool capturing = false;               // launches are being captured into a CUDA graph
@@ -148,7 +156,7 @@ struct fbk_table {
 namespace fbk {
 
 // The pass-1 and emit forms a context's tuning selects for keys of nw words.
-inline int ladder_form(const fbk_ctx* ctx, int nw) { return ctx->ladder_ilp ? ctx->ladder_ilp : (nw == 4 ? 4 : 1); }
+inline int ladder_form(const fbk_ctx* ctx, int nw) { return ctx->ladder_ilp ? ctx->ladder_ilp : (nw == 1 ? 1 : 5); }
 inline int emit_form(const fbk_ctx* ctx, int nw) { return ctx->emit_lookahead ? ctx->emit_lookahead : (nw <= 2 ? 4 : 3); }
 
 fbk_status set_err(fbk_ctx* ctx, fbk_status st, const std::string& msg);

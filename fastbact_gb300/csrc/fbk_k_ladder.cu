@@ -249,10 +249,10 @@ static cudaError_t lp1_ws(const Launch& L, const BankDev& b, uint32_t k, uint32_
 cudaError_t launch_ladder_pass1(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t,
                                 uint32_t* hll12, int ilp) {
     if (t < 1 || t > LADDER_MAX_LEVELS || log2w > 29) return cudaErrorInvalidValue;  // bit indices fit 32 bits
-    if (ilp == 4) {  // one lane per read, rolled (fbk_k_roll.cu)
+    if (ilp == 4 || ilp == 5) {  // one lane per read, rolled (fbk_k_roll.cu); 5: two windows per step
         Launch L2 = L;
         L2.block = 256;
-        return launch_ladder_pass1_roll(nw, L2, b, k, lad, log2w, t, hll12);
+        return launch_ladder_pass1_roll(nw, L2, b, k, lad, log2w, t, hll12, ilp == 5 ? 2 : 1);
     }
     if (ilp == 2) {
         if (nw == 1) return lp1_ws<1, 2>(L, b, k, lad, log2w, t, hll12);

@@ -628,6 +628,22 @@ __global__ void __launch_bounds__(256) k_count_records(BucketDev bk, uint32_t bu
     }
 }
 
+// Resolve a key's slot from its home slot and add the record's pushes (info byte).
+template <int NW>
+__device__ __forceinline__ void upsert_key(const Key<NW>& key, uint32_t info, uint64_t f, uint64_t home, uint32_t w_edge,
+                                           uint32_t w_cov, const TableDev& t, uint32_t* status) {
+    int64_t s;
+    if constexpr (NW == 1) s = table_slot1(t, key.w[0], home, status);
+    else if constexpr (NW == 2) s = table_slot2(t, key, home, status);
+    else s = table_slotw<NW>(t, key, f, home, status);
+    if (s < 0) return;
+    uint32_t* c = t.cnt + (uint64_t)s * 8;
+    const uint32_t nu = (info >> 3) & 1u, nv = (info >> 7) & 1u;
+    if (nu) atomicAdd(&c[info & 7u], w_edge);
+    if (nv) atomicAdd(&c[(info >> 4) & 7u], w_edge);
+    if (t.cov) atomicAdd(&t.cov[s], w_cov * (nu + nv));
+}
+
 // One record's upsert: resolve the key's slot from its home slot and add its pushes.
 template <int NW>
 __device__ __forceinline__ void upsert_record(const uint64_t* rec, const BucketDev& bk, uint32_t w_edge, uint32_t w_cov,
@@ -647,16 +663,7 @@ __device__ __forceinline__ void upsert_record(const uint64_t* rec, const BucketD
             return;
         }
     }
-    int64_t s;
-    if constexpr (NW == 1) s = table_slot1(t, key.w[0], home, status);
-    else if constexpr (NW == 2) s = table_slot2(t, key, home, status);
-    else s = table_slotw<NW>(t, key, f, home, status);
-    if (s < 0) return;
-    uint32_t* c = t.cnt + (uint64_t)s * 8;
-    const uint32_t nu = (info >> 3) & 1u, nv = (info >> 7) & 1u;
-    if (nu) atomicAdd(&c[info & 7u], w_edge);
-    if (nv) atomicAdd(&c[(info >> 4) & 7u], w_edge);
-    if (t.cov) atomicAdd(&t.cov[s], w_cov * (nu + nv));
+    upsert_key<NW>(key, info, f, home, w_edge, w_cov, t, status);
 }
 
 template <int NW>
@@ -672,6 +679,61 @@ __global__ void __launch_bounds__(256, 8) k_upsert(BucketDev bk, uint32_t bucket
         for (int off = 16; off > 0; off >>= 1) skipped += __shfl_down_sync(0xffffffffu, skipped, off);
         if ((threadIdx.x & 31) == 0 && skipped) atomicAdd(flt.skipped, skipped);
     }
+}
+
+// The filtered upsert with the filter's survivors queued per warp.  A warp reads 32
+// records at a time (one per lane, coalesced) and tests their filter counters; the
+// indices of the records that pass go to the warp's queue in shared memory, and the
+// warp probes the table 32 queued records at a time, re-reading each record (an L1
+// hit), so every lane of the probe phase has a record.  With the test inline, the
+// lanes whose record the filter drops (about 40% at k = 77) wait for the others'
+// probes: 12 of 32 lanes were active per instruction.
+constexpr int UPQ_WARPS = 8;
+template <int NW, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_upsert_q(BucketDev bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov, TableDev t,
+                                                  uint32_t* status, RecordFilter flt) {
+    __shared__ uint32_t s_q[UPQ_WARPS][64];
+    const uint64_t* base;
+    const uint64_t n = stripe_records(bk, bucket, base, bk.rw);
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t* q = s_q[wib];
+    uint32_t qn = 0;  // queued records (warp-uniform), below 32 between batches
+    unsigned long long skipped = 0;
+    const uint64_t gwarp = (((uint64_t)blockIdx.x * blockDim.x) >> 5) + wib;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t r0 = gwarp * 32; r0 < n; r0 += nwarps * 32) {
+        const uint64_t i = r0 + lane;
+        bool keep = false;
+        if (i < n) {
+            Key<NW> key;
+            const uint32_t info = rec_get<NW, true>(base + i * bk.rw, key, bk);
+            keep = __ldcg(flt.cnt + filter_col(key_fold<NW>(key), flt.log2m)) >= flt.min_records;
+            if (!keep) skipped += ((info >> 3) & 1u) + ((info >> 7) & 1u);
+        }
+        const uint32_t m = __ballot_sync(0xffffffffu, keep);
+        if (keep) q[qn + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+        qn += __popc(m);
+        __syncwarp();
+        if (qn >= 32) {
+            qn -= 32;
+            const uint64_t j = q[qn + lane];
+            __syncwarp();
+            Key<NW> key;
+            const uint32_t info = rec_get<NW, true>(base + j * bk.rw, key, bk);
+            const uint64_t f = key_fold<NW>(key);
+            upsert_key<NW>(key, info, f, home_slot(f, t.cap), w_edge, w_cov, t, status);
+        }
+    }
+    if (lane < qn) {
+        const uint64_t j = q[lane];
+        Key<NW> key;
+        const uint32_t info = rec_get<NW, true>(base + j * bk.rw, key, bk);
+        const uint64_t f = key_fold<NW>(key);
+        upsert_key<NW>(key, info, f, home_slot(f, t.cap), w_edge, w_cov, t, status);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) skipped += __shfl_down_sync(0xffffffffu, skipped, off);
+    if (lane == 0 && skipped) atomicAdd(flt.skipped, skipped);
 }
 
 // Every bucket of a pass in one persistent launch: blocks take work items (bucket,
@@ -1028,16 +1090,25 @@ static dim3 stripe_grid(int blocks, uint32_t stripes) {
 }
 template <int NW>
 static cudaError_t upsert_nw(const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t we, uint32_t wc, const TableDev& t,
-                             uint32_t* status, const RecordFilter& flt) {
-    k_upsert<NW><<<stripe_grid(grid_for(k_upsert<NW>, L), bk.stripes), L.block, 0, L.stream>>>(bk, bucket, we, wc, t, status, flt);
+                             uint32_t* status, const RecordFilter& flt, int queued) {
+    if (queued == 1)
+        k_upsert_q<NW, 8><<<stripe_grid(grid_for(k_upsert_q<NW, 8>, L), bk.stripes), L.block, 0, L.stream>>>(bk, bucket, we, wc, t,
+                                                                                                             status, flt);
+    else if (queued == 2)
+        k_upsert_q<NW, 6><<<stripe_grid(grid_for(k_upsert_q<NW, 6>, L), bk.stripes), L.block, 0, L.stream>>>(bk, bucket, we, wc, t,
+                                                                                                             status, flt);
+    else
+        k_upsert<NW><<<stripe_grid(grid_for(k_upsert<NW>, L), bk.stripes), L.block, 0, L.stream>>>(bk, bucket, we, wc, t, status, flt);
     return cudaGetLastError();
 }
 cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov,
-                          const TableDev& t, uint32_t* status, const RecordFilter& flt) {
+                          const TableDev& t, uint32_t* status, const RecordFilter& flt, int queue) {
     if (flt.cnt && (flt.log2m < 8 || flt.log2m > 30)) return cudaErrorInvalidValue;
-    if (nw == 1) return upsert_nw<1>(L, bk, bucket, w_edge, w_cov, t, status, flt);
-    if (nw == 2) return upsert_nw<2>(L, bk, bucket, w_edge, w_cov, t, status, flt);
-    return upsert_nw<4>(L, bk, bucket, w_edge, w_cov, t, status, flt);
+    // the queue holds 32-bit record indices of at most UPQ_WARPS warps
+    const int queued = flt.cnt && L.block % 32 == 0 && L.block <= 32 * UPQ_WARPS && bk.stripe_cap <= 0xFFFFFFFFull ? queue : 0;
+    if (nw == 1) return upsert_nw<1>(L, bk, bucket, w_edge, w_cov, t, status, flt, queued);
+    if (nw == 2) return upsert_nw<2>(L, bk, bucket, w_edge, w_cov, t, status, flt, queued);
+    return upsert_nw<4>(L, bk, bucket, w_edge, w_cov, t, status, flt, queued);
 }
 template <int NW>
 static cudaError_t upsert_all_nw(const Launch& L, const BucketDev& bk, uint32_t we, uint32_t wc, const TableDev& t,

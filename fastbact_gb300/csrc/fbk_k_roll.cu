@@ -155,9 +155,12 @@ __device__ __forceinline__ uint32_t cursor_next(BaseCursor& c, const RunStage& s
 // ---------------------------------------------------------------------------
 // Pass 1 with the threshold-ladder gate (fbk_k_ladder.cu), rolled.
 // ---------------------------------------------------------------------------
-template <int NW, int WS>
-__global__ void __launch_bounds__(256, 6) k_ladder_pass1_roll(BankDev b, uint32_t k, uint32_t* __restrict__ lad, uint32_t log2w,
-                                                              uint32_t t, uint32_t* __restrict__ hll12) {
+// P windows per lane per step (1 or 2): with P = 2 a lane rolls two consecutive windows
+// and issues their eight gate loads together before climbing both (two increments of
+// the same counter climb correctly: every level is still claimed by one atomicOr).
+template <int NW, int WS, int P>
+__global__ void __launch_bounds__(256, P == 1 ? 6 : 4) k_ladder_pass1_roll(BankDev b, uint32_t k, uint32_t* __restrict__ lad,
+                                                                          uint32_t log2w, uint32_t t, uint32_t* __restrict__ hll12) {
     constexpr int NK = NW - WS;
     __shared__ uint32_t s_hll[4096];
     __shared__ __align__(16) uint64_t s_stage[8][P1_STAGE_WORDS];
@@ -193,33 +196,43 @@ __global__ void __launch_bounds__(256, 6) k_ladder_pass1_roll(BankDev b, uint32_
             window_strands<NW, WS>(st, b.data, off, k, F, R);
             cursor_at(cur, st, b.data, off + k);
         }
-        for (uint32_t q = 0; q < steps; ++q) {
-            const bool live = q < nk;
-            if (live && q > 0) roll_strands<NK>(F, R, cursor_next(cur, st, b.data), topb, tmask);
-            uint32_t wd[4] = {0, 0, 0, 0}, mk[4] = {0, 0, 0, 0};
-            uint64_t h0 = 0;
-            if (live) {
+        for (uint32_t q = 0; q < steps; q += P) {
+            uint32_t wd[4 * P], mk[4 * P];
+            uint64_t h0[P];
+            bool live[P], climb[4 * P];
+#pragma unroll
+            for (int p = 0; p < P; ++p) {
+                const uint32_t qq = q + (uint32_t)p;
+                live[p] = qq < nk;
+                h0[p] = 0;
+#pragma unroll
+                for (int row = 0; row < 4; ++row) wd[4 * p + row] = mk[4 * p + row] = 0;
+                if (!live[p]) continue;
+                if (qq > 0) roll_strands<NK>(F, R, cursor_next(cur, st, b.data), topb, tmask);
                 Key<NW> can;
                 bool rc;
                 strands_canonical<NW, WS>(F, R, can, rc);
                 const uint64_t key = key_fold<NW>(can);
-                h0 = smix(key ^ cms_seed(0));
+                h0[p] = smix(key ^ cms_seed(0));
 #pragma unroll
                 for (int row = 0; row < 4; ++row) {
-                    const uint64_t h = row == 0 ? h0 : smix(key ^ cms_seed(row));
+                    const uint64_t h = row == 0 ? h0[p] : smix(key ^ cms_seed(row));
                     const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
-                    wd[row] = bit >> 5;
-                    mk[row] = 1u << (bit & 31);
+                    wd[4 * p + row] = bit >> 5;
+                    mk[4 * p + row] = 1u << (bit & 31);
                 }
             }
-            bool climb[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) climb[i] = live && !(__ldcg(top + wd[i]) & mk[i]);
-            ladder_climb<4>(lad, level_words, t, wd, mk, climb);
-            if (do_hll && live && (h0 & (PASS1_HLL_SAMPLE - 1)) == 0) {  // 1 key in 16 by hash
-                uint32_t idx, rho;
-                hll_idx_rho(h0, 12, idx, rho);
-                if (s_hll[idx] < rho) atomicMax(&s_hll[idx], rho);
+            for (int i = 0; i < 4 * P; ++i) climb[i] = live[i / 4] && !(__ldcg(top + wd[i]) & mk[i]);
+            ladder_climb<4 * P>(lad, level_words, t, wd, mk, climb);
+            if (do_hll) {
+#pragma unroll
+                for (int p = 0; p < P; ++p)
+                    if (live[p] && (h0[p] & (PASS1_HLL_SAMPLE - 1)) == 0) {  // 1 key in 16 by hash
+                        uint32_t idx, rho;
+                        hll_idx_rho(h0[p], 12, idx, rho);
+                        if (s_hll[idx] < rho) atomicMax(&s_hll[idx], rho);
+                    }
             }
         }
     }
@@ -370,22 +383,28 @@ static int roll_grid(Kern kern, const Launch& L, size_t smem) {
     return per_sm * (L.sms > 0 ? L.sms : 1);
 }
 
-template <int NW, int WS>
+template <int NW, int WS, int P>
 static cudaError_t lp1r(const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t, uint32_t* hll) {
     if (L.block != 256) return cudaErrorInvalidValue;  // the staging buffers are sized for 8 warps
-    k_ladder_pass1_roll<NW, WS><<<roll_grid(k_ladder_pass1_roll<NW, WS>, L, 0), L.block, 0, L.stream>>>(b, k, lad, log2w, t, hll);
+    k_ladder_pass1_roll<NW, WS, P><<<roll_grid(k_ladder_pass1_roll<NW, WS, P>, L, 0), L.block, 0, L.stream>>>(b, k, lad, log2w, t,
+                                                                                                             hll);
     return cudaGetLastError();
 }
-cudaError_t launch_ladder_pass1_roll(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w,
-                                     uint32_t t, uint32_t* hll12) {
-    if (t < 1 || t > LADDER_MAX_LEVELS || log2w > 29) return cudaErrorInvalidValue;
+template <int P>
+static cudaError_t lp1r_p(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w, uint32_t t,
+                          uint32_t* hll12) {
     const uint32_t ws = (64u * (uint32_t)nw - 2u * k) >> 6;
-    if (nw == 1) return lp1r<1, 0>(L, b, k, lad, log2w, t, hll12);
-    if (nw == 2) return ws == 0 ? lp1r<2, 0>(L, b, k, lad, log2w, t, hll12) : lp1r<2, 1>(L, b, k, lad, log2w, t, hll12);
-    if (ws == 0) return lp1r<4, 0>(L, b, k, lad, log2w, t, hll12);
-    if (ws == 1) return lp1r<4, 1>(L, b, k, lad, log2w, t, hll12);
-    if (ws == 2) return lp1r<4, 2>(L, b, k, lad, log2w, t, hll12);
-    return lp1r<4, 3>(L, b, k, lad, log2w, t, hll12);
+    if (nw == 1) return lp1r<1, 0, P>(L, b, k, lad, log2w, t, hll12);
+    if (nw == 2) return ws == 0 ? lp1r<2, 0, P>(L, b, k, lad, log2w, t, hll12) : lp1r<2, 1, P>(L, b, k, lad, log2w, t, hll12);
+    if (ws == 0) return lp1r<4, 0, P>(L, b, k, lad, log2w, t, hll12);
+    if (ws == 1) return lp1r<4, 1, P>(L, b, k, lad, log2w, t, hll12);
+    if (ws == 2) return lp1r<4, 2, P>(L, b, k, lad, log2w, t, hll12);
+    return lp1r<4, 3, P>(L, b, k, lad, log2w, t, hll12);
+}
+cudaError_t launch_ladder_pass1_roll(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w,
+                                     uint32_t t, uint32_t* hll12, int windows_per_step) {
+    if (t < 1 || t > LADDER_MAX_LEVELS || log2w > 29) return cudaErrorInvalidValue;
+    return windows_per_step == 2 ? lp1r_p<2>(nw, L, b, k, lad, log2w, t, hll12) : lp1r_p<1>(nw, L, b, k, lad, log2w, t, hll12);
 }
 
 template <int NW, int WS>

@@ -153,7 +153,7 @@ cudaError_t launch_pass2_sweep(int nw, const Launch& L, const BankDev& b, uint32
 cudaError_t launch_emit(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* bm, int gate, const TableDev& t,
                         const BucketDev& bk);
 cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov,
-                          const TableDev& t, uint32_t* status, const RecordFilter& flt = RecordFilter{});
+                          const TableDev& t, uint32_t* status, const RecordFilter& flt = RecordFilter{}, int queue = 0);
 cudaError_t launch_count_records(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, const RecordFilter& flt);
 // every bucket in one persistent launch; *work (zeroed by the caller) hands out items
 cudaError_t launch_upsert_all(int nw, const Launch& L, const BucketDev& bk, uint32_t w_edge, uint32_t w_cov, const TableDev& t,
@@ -190,7 +190,7 @@ cudaError_t launch_emit_ladder(int nw, const Launch& L, const BankDev& b, uint32
 // shared memory (fbk_k_roll.cu); the same results as launch_ladder_pass1 and
 // launch_emit_ladder.  Blocks of 256 threads.
 cudaError_t launch_ladder_pass1_roll(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w,
-                                     uint32_t t, uint32_t* hll12);
+                                     uint32_t t, uint32_t* hll12, int windows_per_step);
 cudaError_t launch_emit_roll(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
                              uint32_t t_solid, const TableDev& t, const BucketDev& bk);
 

@@ -168,17 +168,22 @@ __device__ __forceinline__ void rec_put(uint64_t* dst, const Key<NW>& key, uint3
         if ((uint32_t)i >= ws)
             dst[base + i - ws] = key.w[i] | ((bk.packed && (uint32_t)i == ws) ? ((uint64_t)info << 56) : 0ULL);
 }
-// Reads a record written by rec_put; returns its info byte.  Streaming loads: every
-// record is read once.
-template <int NW>
+// Reads a record written by rec_put; returns its info byte.  Streaming loads (every
+// record is read once), or with CACHED loads through L1 for a record read twice.
+template <int NW, bool CACHED = false>
+__device__ __forceinline__ uint64_t rec_word(const uint64_t* p) {
+    if constexpr (CACHED) return __ldg(p);
+    else return __ldcs(p);
+}
+template <int NW, bool CACHED = false>
 __device__ __forceinline__ uint32_t rec_get(const uint64_t* src, Key<NW>& key, const BucketDev& bk) {
     const uint32_t ws = bk.ws, base = bk.packed ? 0u : 1u;
     uint32_t info = 0;
-    if (!bk.packed) info = (uint32_t)__ldcs(src);
+    if (!bk.packed) info = (uint32_t)rec_word<NW, CACHED>(src);
 #pragma unroll
     for (int i = 0; i < NW; ++i) {
         uint64_t w = 0;
-        if ((uint32_t)i >= ws) w = __ldcs(src + base + i - ws);
+        if ((uint32_t)i >= ws) w = rec_word<NW, CACHED>(src + base + i - ws);
         if (bk.packed && (uint32_t)i == ws) {
             info = (uint32_t)(w >> 56);
             w &= (1ULL << 56) - 1;

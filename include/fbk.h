@@ -160,10 +160,15 @@ FBK_API fbk_status fbk_ctx_event_elapsed(fbk_ctx* ctx, int slot_a, int slot_b, d
  * "block_pass1", "grid_pass1", "block_pass2", "grid_pass2", "block_emit" (blocks of
  * 32..256 threads in steps of 32; grid 0 = occupancy), "sketch_mode" (1: a build that does not return its
  * sketch keeps only a threshold-ladder gate; 0: counted sketch), "ladder_ilp" (1 or 2
- * windows per lane in the ladder pass 1, 3 = pipelined over chunks), "emit_lookahead" (record emit with the gate
- * loads 1 or 2 chunks ahead read by read, 3 = 2 ahead over a flattened window stream, the default), "acc_filter"
+ * windows per lane in the ladder pass 1, 3 = pipelined over chunks, 4 = one lane per read
+ * with rolled k-mers, 5 = the same rolling two windows per step; 0 = by key width),
+ * "emit_lookahead" (record emit with the gate loads 1 or 2 chunks ahead read by read,
+ * 3 = 2 ahead over a flattened window stream, 4 = one lane per read with rolled k-mers;
+ * 0 = by key width), "acc_filter"
  * (keys that cannot become SolidKmerNodes stay out of the table, see fbk_table_flags:
- * 0 never, 1 where it pays, 2 always).  Results do not depend on any of them. */
+ * 0 never, 1 where it pays, 2 always), "upsert_all" (1: an unfiltered pass upserts every
+ * bucket in one persistent launch), "upsert_queue" (1: filtered upserts queue the
+ * filter's survivors per warp before probing).  Results do not depend on any of them. */
 FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double value);
 FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, double* value);
 /* Number of kernels launched on this context since creation. */

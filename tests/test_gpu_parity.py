@@ -352,17 +352,18 @@ EDGE_SEQS = [b"", b"A", b"ACGT" * 7, b"C" * 31, b"G" * 32, b"T" * 1000, b"ACGTTG
 @pytest.mark.parametrize("k,kb", [(1, 64), (5, 64), (21, 64), (28, 64), (29, 64), (31, 64), (33, 128), (55, 128), (60, 128),
                                   (61, 128), (63, 128), (65, 256), (77, 256), (92, 256), (93, 256), (96, 256), (97, 256),
                                   (124, 256), (125, 256), (127, 256)])
-@pytest.mark.parametrize("rolled", [False, True])
+@pytest.mark.parametrize("rolled", [0, 1, 2])
 def test_gate_only_every_record_layout(repeat_isolate, k, kb, rolled):
     """Every pass-2 record layout (records of ceil((2k + 8) / 64) words, the info byte
     packed into the key's free top bits or in a word of its own: the boundaries are
     k = 28/29, 60/61, 92/93, 124/125), with the per-window kernels and with the rolled
-    one-lane-per-read kernels; an edge-case bank whose runs include reads too long to
-    stage (the global-memory path), empty and shorter-than-k reads."""
+    one-lane-per-read kernels (pass 1 rolling one or two windows per step); an
+    edge-case bank whose runs include reads too long to stage (the global-memory path),
+    empty and shorter-than-k reads, and reads of odd and even window counts."""
     c = api.Context(0)
     try:
         if rolled:
-            c.set_tuning(ladder_ilp=4, emit_lookahead=4)
+            c.set_tuning(ladder_ilp=4 if rolled == 1 else 5, emit_lookahead=4)
         compare_gate_only(c, repeat_isolate[0], k, kb, 16, None, 14)
         edge = api.ReadBank(api.BitSeqArena.from_seqs(EDGE_SEQS[:4]), api.BitSeqArena.from_seqs(EDGE_SEQS[4:30]),
                             api.BitSeqArena.from_seqs(EDGE_SEQS[30:]))
@@ -493,8 +494,12 @@ TUNINGS = [
     dict(emit_lookahead=1),                               # gate loads one chunk ahead of the emit
     dict(emit_lookahead=2),                               # emit read by read, gate loads two chunks ahead
     dict(ladder_ilp=4, emit_lookahead=4),                 # one lane per read, k-mers rolled, runs staged in smem
+    dict(ladder_ilp=5),                                   # the same pass 1 rolling two windows per step
     dict(acc_filter=0),                                   # every accumulated key kept
     dict(acc_filter=2),                                   # keys that cannot be solid dropped at every width
+    dict(acc_filter=2, block_pass2=96),                   # the filter's survivors queued per warp, 3 warps per block
+    dict(acc_filter=2, upsert_queue=2),                   # the same at six blocks per SM
+    dict(acc_filter=2, upsert_queue=0),                   # the filter tested inline
     dict(upsert_all=0, acc_filter=0),                     # one upsert launch per bucket
     dict(block_emit=256),                                 # record emit in blocks of 256
 ]
