@@ -308,6 +308,7 @@ FBK_API fbk_status fbk_ctx_fork(fbk_ctx* parent, fbk_ctx** out) {
     c->emit_lookahead = parent->emit_lookahead;
     c->upsert_queue = parent->upsert_queue;
     c->batch_pass1 = parent->batch_pass1;
+    c->filter_sizing = parent->filter_sizing;
     c->acc_filter = parent->acc_filter;
     c->upsert_all = parent->upsert_all;
     cudaError_t e = cudaSetDevice(c->device);
@@ -410,8 +411,9 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "emit_lookahead" && v >= 0 && v <= 4 && v == (int)v) ctx->emit_lookahead = (int)v;
     else if (n == "upsert_queue" && (v == 0 || v == 1 || v == 2)) ctx->upsert_queue = (int)v;
     else if (n == "batch_pass1" && (v == 0 || v == 1 || v == 2)) ctx->batch_pass1 = (int)v;
+    else if (n == "filter_sizing" && (v == 0 || v == 1)) ctx->filter_sizing = (int)v;
     else if (n == "acc_filter" && (v == 0 || v == 1 || v == 2)) ctx->acc_filter = (int)v;
-    else if (n == "upsert_all" && (v == 0 || v == 1)) ctx->upsert_all = (int)v;
+    else if (n == "upsert_all" && (v == 0 || v == 1 || v == 2)) ctx->upsert_all = (int)v;
     // the pass kernels are compiled for blocks of at most 256 threads
     else if (n == "block_pass1" && v >= 32 && v <= 256 && ((int)v % 32) == 0) ctx->block_pass1 = (int)v;
     else if (n == "grid_pass1" && v >= 0) ctx->grid_pass1 = (int)v;
@@ -436,6 +438,7 @@ FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, doub
     else if (n == "emit_lookahead") *v = ctx->emit_lookahead;
     else if (n == "upsert_queue") *v = ctx->upsert_queue;
     else if (n == "batch_pass1") *v = ctx->batch_pass1;
+    else if (n == "filter_sizing") *v = ctx->filter_sizing;
     else if (n == "acc_filter") *v = ctx->acc_filter;
     else if (n == "upsert_all") *v = ctx->upsert_all;
     else if (n == "block_pass1") *v = ctx->block_pass1;
@@ -1278,6 +1281,27 @@ static fbk_status buckets_alloc(fbk_ctx* ctx, uint64_t cap, uint64_t slot_bytes,
     return FBK_OK;
 }
 
+// Capacity of a filtered pass's table, chosen after bucket 0 of P is counted: the keys
+// that pass the filter in bucket 0 are about the counters at or above min_trans_cov
+// (keys that share a counter add a few percent), the buckets split the keys by hash
+// evenly, and the table gets 30% headroom over that estimate at the context's load
+// factor, a multiple of P slots, never more than the capacity from the distinct
+// estimate.  Allocates and initialises the table.
+static fbk_status size_filtered_table(fbk_table* t, const RecordFilter& flt, uint32_t n_buckets, uint64_t cap_distinct) {
+    fbk_ctx* ctx = t->ctx;
+    unsigned long long* d_n = ctx->d_counts + 7;
+    CK(ctx, cudaMemsetAsync(d_n, 0, 8, ctx->stream));
+    TIMED(ctx, "pass2_count", launch_count_at_least(launch_cfg(ctx, 256, 0), flt.cnt, 1ULL << flt.log2m, flt.min_records, d_n));
+    CK(ctx, cudaMemcpyAsync(ctx->h_pinned, d_n, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    const uint64_t n0 = *(const unsigned long long*)ctx->h_pinned;
+    const double keys = 1.3 * (double)n0 * (double)n_buckets;
+    uint64_t cap = (uint64_t)(keys / ctx->load_factor) + 1024;
+    cap = (cap + n_buckets - 1) / n_buckets * n_buckets;
+    if (cap > cap_distinct) cap = cap_distinct;
+    return table_alloc(t, cap, false);
+}
+
 // Pass 2 for every read chunk (and the prior contigs), with retries at twice the
 // capacity when the probe limit is hit.  Reads go through record buckets; if a
 // bucket stripe overflows, the chunk is redone by the direct sweep.
@@ -1341,8 +1365,19 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
     t->min_trans_cov = p->min_trans_cov;
     const uint64_t slot_bytes = 8ULL * nw + (nw > 2 ? 8 : 0) + 32 + (contigs ? 4 : 0);
     const uint64_t max_records = std::min(b->windows(p->k, p->k + 1), b->max_chunk_bases());
+    const bool use_buckets = max_records && ctx->pass2_mode == 1;
+    // the record filter needs every record of the pass in one bucket pass: one
+    // read chunk and no prior contigs (their pushes weigh 1000)
+    const bool filter = use_buckets && acc_filter_on(ctx->acc_filter, nw, distinct_hint, max_records) && !contigs &&
+                        b->chunk_starts.size() == 2 && p->min_trans_cov >= 2;
     for (int attempt = 0; attempt < 4; ++attempt) {
-        st = table_alloc(t, cap, contigs != nullptr);
+        // A filtered pass holds only the keys that pass the filter, typically a small
+        // part of the distinct k-mers: its first attempt sizes the table once the first
+        // bucket is counted (the record buckets do not depend on the capacity), from the
+        // counters that reach min_trans_cov.  A table that fills up reruns at the
+        // capacity from the distinct estimate.
+        const bool late_table = filter && attempt == 0 && ctx->filter_sizing && !p->table_log2_cap;
+        if (!late_table) st = table_alloc(t, cap, contigs != nullptr);
         if (st) {
             table_free_out(t);
             delete t;
@@ -1363,19 +1398,16 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
         Launch L = launch_cfg_persistent(ctx, ctx->block_pass2, ctx->grid_pass2);
         Launch Lc = launch_cfg(ctx, 256, 0);
         auto clamp = [&]() -> cudaError_t {
-            cudaError_t e = launch_clamp_counters(Lc, t->cnt, cap * 8);
-            if (e == cudaSuccess && t->cov) e = launch_clamp_counters(Lc, t->cov, cap);
+            cudaError_t e = launch_clamp_counters(Lc, t->cnt, t->cap * 8);
+            if (e == cudaSuccess && t->cov) e = launch_clamp_counters(Lc, t->cov, t->cap);
             return e;
         };
         Buckets bk;
-        const bool use_buckets = max_records && ctx->pass2_mode == 1;
+        // the buckets (their count and the table range each covers) follow the capacity
+        // from the distinct estimate in every attempt
         st = use_buckets ? buckets_alloc(ctx, cap, slot_bytes, nw, p->k, max_records, bk) : FBK_OK;
-        // the record filter needs every record of the pass in one bucket pass: one
-        // read chunk and no prior contigs (their pushes weigh 1000)
         RecordFilter flt{};
-        const bool filter = st == FBK_OK && use_buckets && acc_filter_on(ctx->acc_filter, nw, distinct_hint, max_records) && !contigs &&
-                            b->chunk_starts.size() == 2 && p->min_trans_cov >= 2;
-        if (filter) {
+        if (filter && st == FBK_OK) {
             // one counter per record or more, at most 2^23 (32 MB: stays in L2)
             uint32_t log2m = 11;
             while (log2m < 23 && (1ULL << log2m) < max_records / bk.d.n_buckets) ++log2m;
@@ -1408,12 +1440,21 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
             if (!filter && ctx->upsert_all) {
                 // every bucket in one persistent launch
                 CK(ctx, cudaMemsetAsync(bk.work, 0, 8, ctx->stream));
-                TIMED(ctx, "pass2_upsert", launch_upsert_all(nw, L, bk.d, 1, 1, td, ctx->d_status, bk.work));
+                TIMED(ctx, "pass2_upsert", launch_upsert_all(nw, L, bk.d, 1, 1, td, ctx->d_status, bk.work, ctx->upsert_all));
             } else {
                 for (uint32_t bu = 0; bu < bk.d.n_buckets; ++bu) {
                     if (filter) {
                         CK(ctx, cudaMemsetAsync(flt.cnt, 0, (1ULL << flt.log2m) * 4, ctx->stream));
                         TIMED(ctx, "pass2_count", launch_count_records(nw, L, bk.d, bu, flt));
+                    }
+                    if (late_table && bu == 0) {
+                        st = size_filtered_table(t, flt, bk.d.n_buckets, cap);
+                        if (st) {
+                            table_free_out(t);
+                            delete t;
+                            return st;
+                        }
+                        td = table_dev(t);
                     }
                     TIMED(ctx, "pass2_upsert", launch_upsert(nw, L, bk.d, bu, 1, 1, td, ctx->d_status, flt, ctx->upsert_queue));
                 }
@@ -1454,7 +1495,7 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
             for (size_t c = 0; c + 1 < b->chunk_starts.size(); ++c) {
                 if (c > 0) TIMED(ctx, "clamp", clamp());
                 TIMED(ctx, "pass2_direct", launch_pass2_sweep(nw, L, bank_view(b, b->chunk_starts[c], b->chunk_starts[c + 1], keep_bits),
-                                                              p->k, bm, 1, 0, cap, 1, 1, td, ctx->d_status));
+                                                              p->k, bm, 1, 0, t->cap, 1, 1, td, ctx->d_status));
             }
         }
         if (contigs) {
@@ -1463,7 +1504,7 @@ static fbk_status solid_build_impl(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
                 TIMED(ctx, "clamp", clamp());
                 TIMED(ctx, "pass2_contigs",
                       launch_pass2_sweep(nw, L, bank_view(contigs, contigs->chunk_starts[c], contigs->chunk_starts[c + 1], nullptr),
-                                         p->k, nullptr, 0, 0, cap, 1000, 100, td, ctx->d_status));
+                                         p->k, nullptr, 0, 0, t->cap, 1000, 100, td, ctx->d_status));
             }
         }
         uint32_t bits = 0;

@@ -74,6 +74,7 @@ struct fbk_batch {
     Shape pass1{256, 0, 4}, solid{256, 0, 4}, emit{256, 0, 0}, upsert{256, 0, 0};
     int emit_form = 0;     // 0: the context's choice (emit_form); else the phase-B autotuner's
     bool pass1_single = false;  // ladder pass 1 as one single-isolate launch per isolate (autotuned)
+    bool pass1_single_used = false;  // the form the last wave ran
     bool tuned = false;    // pass-1 shape tuned
     bool tuned_b = false;  // emit form and shape, persistent-upsert shape tuned
     cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -501,7 +502,14 @@ fbk_status phase_a(fbk_batch* B, const std::vector<BatchIso*>& W) {
         if (B->ladder) {
             // the gate is evaluated inside the record emit: no bitmap, and the
             // records are bounded by the windows the count kernel tallies
-            if (ctx->batch_pass1 ? ctx->batch_pass1 == 2 : B->pass1_single) {
+            // The autotuner compares the two forms on one isolate; a wave whose gates
+            // together outgrow half the L2 runs its isolates one launch each, since the
+            // multi-isolate launch then climbs every gate of the wave at once (64
+            // isolates of 4 MB gates: 396 vs 364 ms of pass 1 per cohort).
+            const bool single = ctx->batch_pass1 ? ctx->batch_pass1 == 2
+                                                 : B->pass1_single || (uint64_t)n * gate_bytes(B) > (64ull << 20);
+            B->pass1_single_used = single;
+            if (single) {
                 for (BatchIso* it : W)
                     TIMED(ctx, "batch_pass1", launch_ladder_pass1(B->nw, launch_cfg_persistent(ctx, 256, 0),
                                                                   bank_view(it->bank, 0, it->bank->n_reads, it->keep), k, it->lad,
@@ -1096,7 +1104,7 @@ FBK_API fbk_status fbk_batch_get_stats(const fbk_batch* B, fbk_batch_stats* out)
     *out = B->stats;
     out->pass1_block = B->pass1.block;
     out->pass1_grid = B->pass1.grid;
-    out->pass1_rows = (B->ladder && (B->ctx->batch_pass1 ? B->ctx->batch_pass1 == 2 : B->pass1_single)) ? 0 : B->pass1.rows;
+    out->pass1_rows = (B->ladder && B->pass1_single_used) ? 0 : B->pass1.rows;
     out->solid_block = B->solid.block;
     out->solid_grid = B->solid.grid;
     out->solid_rows = B->solid.rows;

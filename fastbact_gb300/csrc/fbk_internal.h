@@ -90,8 +90,11 @@ struct fbk_ctx {
     // inline.  Measured per 100x pass (0 / 1 / 2): k = 55 7.44 / 6.67 / 7.93 ms, k = 77
     // 10.88 / 7.70 / 9.10.
     int upsert_queue = 1;
+    // Filtered passes: 1 sizes the table from the keys that pass the filter in the first
+    // bucket, 0 from the distinct k-mers of pass 1
+    int filter_sizing = 0;
     int batch_pass1 = 0;                  // batches with a ladder gate: 0 autotuned, 1 one multi-isolate launch, 2 a launch per isolate
-    int upsert_all = 1;                   // 1: an unfiltered pass upserts every bucket in one persistent launch
+    int upsert_all = 1;                   // 1: an unfiltered pass upserts every bucket in one persistent launch, 2: the same with every lane's probe advanced a slot per step
     int acc_filter = 1;                   // keys with fewer records than min_trans_cov stay out of the table: 0 never, 1 for 256-bit keys, 2 always
     bool capturing = false;               // launches are being captured into a CUDA graph
 };

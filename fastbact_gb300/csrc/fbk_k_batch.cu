@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(256) k_batch_emit(const IsoDev* __restrict__ i
     BankDev b{};
     const uint32_t* bm = nullptr;
     BucketDev bk{};
-    uint64_t cap = 0, base = 0;
+    uint64_t base = 0;
     for (uint64_t R = gw; R < total; R += nwarps) {
         ci = iso_walk(s_base, n_iso, ci, R);
         if (ci != cur) {
@@ -302,7 +302,6 @@ __global__ void __launch_bounds__(256) k_batch_emit(const IsoDev* __restrict__ i
             b = iso[ci].b;
             bm = iso[ci].bm;
             bk = iso[ci].bk;
-            cap = iso[ci].t.cap;
             base = s_base[ci];
         }
         const uint64_t r = R - base;
@@ -326,7 +325,7 @@ __global__ void __launch_bounds__(256) k_batch_emit(const IsoDev* __restrict__ i
                     window_canonical<NW>(b.data, g, k, key, rc);
                     if (sr) info |= 8u | (base_at(b.data, g + k) + (rc ? 4u : 0u));
                     if (sl) info |= (8u | ((3u - base_at(b.data, g - 1)) + (rc ? 0u : 4u))) << 4;
-                    bucket = (uint32_t)(home_slot(key_fold<NW>(key), cap) >> bk.shift);
+                    bucket = bucket_of(key_fold<NW>(key), bk.n_buckets);
                 }
             }
             const uint32_t active = __ballot_sync(0xffffffffu, emit);

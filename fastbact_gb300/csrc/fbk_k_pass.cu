@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(256) k_emit(BankDev b, uint32_t k, const uint3
                     window_canonical<NW>(b.data, g, k, key, rc);
                     if (sr) info |= 8u | (base_at(b.data, g + k) + (rc ? 4u : 0u));
                     if (sl) info |= (8u | ((3u - base_at(b.data, g - 1)) + (rc ? 0u : 4u))) << 4;
-                    bucket = (uint32_t)(home_slot(key_fold<NW>(key), t.cap) >> bk.shift);
+                    bucket = bucket_of(key_fold<NW>(key), bk.n_buckets);
                 }
             }
             const uint32_t active = __ballot_sync(0xffffffffu, emit);
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(256) k_emit_ladder(BankDev b, uint32_t k, cons
                     const uint64_t g = off + q;
                     if (sr) info |= 8u | (base_at(b.data, g + k) + (rcc ? 4u : 0u));
                     if (sl) info |= (8u | ((3u - base_at(b.data, g - 1)) + (rcc ? 0u : 4u))) << 4;
-                    bucket = (uint32_t)(home_slot(key_fold<NW>(kc), t.cap) >> bk.shift);
+                    bucket = bucket_of(key_fold<NW>(kc), bk.n_buckets);
                 }
             }
             const uint32_t active = __ballot_sync(0xffffffffu, emit);
@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_ladder2(BankDev b, uint32_t k, 
                     const uint64_t g = off + q;
                     if (sr) info |= 8u | (base_at(b.data, g + k) + (rcc ? 4u : 0u));
                     if (sl) info |= (8u | ((3u - base_at(b.data, g - 1)) + (rcc ? 0u : 4u))) << 4;
-                    bucket = (uint32_t)(home_slot_h(hc, t.cap) >> bk.shift);
+                    bucket = bucket_of_h(hc, bk.n_buckets);
                 }
             }
             const uint32_t active = __ballot_sync(0xffffffffu, emit);
@@ -559,7 +559,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_flat(BankDev b, uint32_t k, con
                 if (emit) {
                     if (sr) info |= 8u | (base_at(b.data, wc.g + k) + (wc.rc ? 4u : 0u));
                     if (sl) info |= (8u | ((3u - base_at(b.data, wc.g - 1)) + (wc.rc ? 0u : 4u))) << 4;
-                    bucket = (uint32_t)(home_slot_h(hc, t.cap) >> bk.shift);
+                    bucket = bucket_of_h(hc, bk.n_buckets);
                 }
             }
             const uint32_t active = __ballot_sync(0xffffffffu, emit);
@@ -615,6 +615,17 @@ __device__ __forceinline__ uint64_t stripe_records(const BucketDev& bk, uint32_t
 constexpr uint64_t FILTER_SALT = 0x3c6ef372fe94f82bULL;
 __device__ __forceinline__ uint32_t filter_col(uint64_t fold, uint32_t log2m) {
     return (uint32_t)(smix(fold ^ FILTER_SALT) >> (64 - log2m));
+}
+
+// Number of counters at or above `min` (the filter's survivors of one bucket).
+__global__ void __launch_bounds__(256) k_count_at_least(const uint32_t* __restrict__ cnt, uint64_t n, uint32_t min,
+                                                        unsigned long long* out) {
+    unsigned long long c = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        c += __ldcg(cnt + i) >= min;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
 }
 
 template <int NW>
@@ -768,6 +779,89 @@ __global__ void __launch_bounds__(256, NW == 4 ? 6 : 8) k_upsert_all(BucketDev b
         const uint64_t* base = bk.recs + bs * bk.stripe_cap * bk.rw;
         for (uint64_t i = first + threadIdx.x; i < last; i += blockDim.x)
             upsert_record<NW>(base + i * bk.rw, bk, w_edge, w_cov, t, status, none, skipped);
+    }
+}
+
+// The persistent upsert with every lane's probe sequence advanced one slot per step:
+// a lane whose record is placed takes its next record at once instead of waiting at
+// the loop's reconvergence for the lanes with longer probe runs, so each step of a
+// warp issues one table load per busy lane.  A warp works through its own records of
+// the block's work item (lane j: records first + 32 w + j, + blockDim, ...).
+// 64- and 128-bit keys (slots claimed by one CAS, no publication wait).
+template <int NW>
+__device__ __forceinline__ int probe_step(const TableDev& t, const Key<NW>& key, uint64_t s) {
+    // 1: the key's slot is s; 0: go on with the next slot
+    if constexpr (NW == 1) {
+        const uint64_t cur = __ldcg(&t.keys[s]);
+        if (cur == key.w[0]) return 1;
+        if (cur == KEY_EMPTY) {
+            const uint64_t old = atomicCAS((unsigned long long*)&t.keys[s], KEY_EMPTY, key.w[0]);
+            if (old == KEY_EMPTY || old == key.w[0]) return 1;
+        }
+        return 0;
+    } else {
+        uint64_t* a = t.keys + s * 2;
+        const ulonglong2 c = __ldcg(reinterpret_cast<const ulonglong2*>(a));
+        const bool other = (c.x != KEY_EMPTY && c.x != key.w[0]) || (c.y != KEY_EMPTY && c.y != key.w[1]);
+        if (other) return 0;
+        if (c.x == key.w[0] && c.y == key.w[1] && key.w[1] != KEY_EMPTY) return 1;
+        uint64_t o0, o1;
+        cas128(a, KEY_EMPTY, KEY_EMPTY, key.w[0], key.w[1], o0, o1);
+        return ((o0 == KEY_EMPTY && o1 == KEY_EMPTY) || (o0 == key.w[0] && o1 == key.w[1])) ? 1 : 0;
+    }
+}
+
+template <int NW>
+__global__ void __launch_bounds__(256, 8) k_upsert_all_step(BucketDev bk, uint32_t w_edge, uint32_t w_cov, TableDev t,
+                                                         uint32_t* status, unsigned long long* work) {
+    static_assert(NW <= 2, "one-CAS slots only");
+    __shared__ unsigned long long s_item;
+    const uint64_t per_stripe = (bk.stripe_cap + UPSERT_ITEM - 1) / UPSERT_ITEM;
+    const uint64_t n_items = (uint64_t)bk.n_buckets * bk.stripes * per_stripe;
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(work, 1ULL);
+        __syncthreads();
+        const uint64_t item = s_item;
+        __syncthreads();
+        if (item >= n_items) break;
+        const uint64_t bs = item / per_stripe;  // bucket * stripes + stripe
+        const uint64_t first = (item - bs * per_stripe) * UPSERT_ITEM;
+        const unsigned long long fl = bk.fill[bs];
+        const uint64_t n = fl < bk.stripe_cap ? fl : bk.stripe_cap;
+        if (first >= n) continue;
+        const uint64_t last = first + UPSERT_ITEM < n ? first + UPSERT_ITEM : n;
+        const uint64_t* base = bk.recs + bs * bk.stripe_cap * bk.rw;
+        uint64_t i = first + 32 * wib + lane;
+        bool have = false;
+        Key<NW> key;
+        uint32_t info = 0, probe = 0;
+        uint64_t s = 0;
+        for (;;) {
+            if (!have && i < last) {
+                info = rec_get<NW>(base + i * bk.rw, key, bk);
+                s = home_slot(key_fold<NW>(key), t.cap);
+                probe = 0;
+                have = true;
+                i += blockDim.x;
+            }
+            if (!__any_sync(0xffffffffu, have)) break;
+            if (!have) continue;
+            if (probe_step<NW>(t, key, s)) {
+                uint32_t* c = t.cnt + s * 8;
+                const uint32_t nu = (info >> 3) & 1u, nv = (info >> 7) & 1u;
+                if (nu) atomicAdd(&c[info & 7u], w_edge);
+                if (nv) atomicAdd(&c[(info >> 4) & 7u], w_edge);
+                if (t.cov) atomicAdd(&t.cov[s], w_cov * (nu + nv));
+                have = false;
+            } else {
+                s = s + 1 == t.cap ? 0 : s + 1;
+                if (++probe >= t.max_probe) {
+                    atomicOr(status, ST_TABLE_FULL);
+                    have = false;
+                }
+            }
+        }
     }
 }
 
@@ -1112,20 +1206,32 @@ cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t
 }
 template <int NW>
 static cudaError_t upsert_all_nw(const Launch& L, const BucketDev& bk, uint32_t we, uint32_t wc, const TableDev& t,
-                                 uint32_t* status, unsigned long long* work) {
+                                 uint32_t* status, unsigned long long* work, bool stepped) {
+    if constexpr (NW <= 2) {
+        if (stepped) {
+            k_upsert_all_step<NW><<<grid_for(k_upsert_all_step<NW>, L), L.block, 0, L.stream>>>(bk, we, wc, t, status, work);
+            return cudaGetLastError();
+        }
+    }
     k_upsert_all<NW><<<grid_for(k_upsert_all<NW>, L), L.block, 0, L.stream>>>(bk, we, wc, t, status, work);
     return cudaGetLastError();
 }
 cudaError_t launch_upsert_all(int nw, const Launch& L, const BucketDev& bk, uint32_t w_edge, uint32_t w_cov, const TableDev& t,
-                              uint32_t* status, unsigned long long* work) {
+                              uint32_t* status, unsigned long long* work, int form) {
     if (!work) return cudaErrorInvalidValue;
-    if (nw == 1) return upsert_all_nw<1>(L, bk, w_edge, w_cov, t, status, work);
-    if (nw == 2) return upsert_all_nw<2>(L, bk, w_edge, w_cov, t, status, work);
-    return upsert_all_nw<4>(L, bk, w_edge, w_cov, t, status, work);
+    // the stepped form gives each warp 32-record runs of a work item
+    const bool stepped = form == 2 && L.block % 32 == 0;
+    if (nw == 1) return upsert_all_nw<1>(L, bk, w_edge, w_cov, t, status, work, stepped);
+    if (nw == 2) return upsert_all_nw<2>(L, bk, w_edge, w_cov, t, status, work, stepped);
+    return upsert_all_nw<4>(L, bk, w_edge, w_cov, t, status, work, false);
 }
 template <int NW>
 static cudaError_t count_nw(const Launch& L, const BucketDev& bk, uint32_t bucket, const RecordFilter& flt) {
     k_count_records<NW><<<stripe_grid(grid_for(k_count_records<NW>, L), bk.stripes), L.block, 0, L.stream>>>(bk, bucket, flt);
+    return cudaGetLastError();
+}
+cudaError_t launch_count_at_least(const Launch& L, const uint32_t* cnt, uint64_t n, uint32_t min, unsigned long long* out) {
+    k_count_at_least<<<L.grid, L.block, 0, L.stream>>>(cnt, n, min, out);
     return cudaGetLastError();
 }
 cudaError_t launch_count_records(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, const RecordFilter& flt) {

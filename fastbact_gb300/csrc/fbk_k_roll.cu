@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_roll(BankDev b, uint32_t k, con
                 if (emit) {
                     if (sr) info |= 8u | (cq1 + (rq ? 4u : 0u));
                     if (sl) info |= (8u | ((3u - lq) + (rq ? 0u : 4u))) << 4;
-                    bucket = (uint32_t)(home_slot_h(hq, t.cap) >> bk.shift);
+                    bucket = bucket_of_h(hq, bk.n_buckets);
                 }
             }
             const uint32_t active = __ballot_sync(0xffffffffu, emit);

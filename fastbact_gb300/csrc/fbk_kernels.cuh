@@ -48,7 +48,11 @@ struct TableDev {
     uint32_t spin_limit;
 };
 
-// Pass-2 records, grouped by the slot range of their key's home slot.  Bucket b
+// Pass-2 records, grouped by the slot range of their key's home slot: the bucket of a
+// key is the high 64 bits of its row-0 hash times the bucket count P, and its home slot
+// the high bits of the same hash times the table capacity, so bucket b covers the
+// home slots [b cap / P, (b + 1) cap / P) for any capacity (the table can be sized
+// after the records are written).  Bucket b
 // holds S stripes of stripe_cap records; warps append to stripe (warp % S) with one
 // atomic per (warp iteration, bucket).  A record is the canonical key and the pushes
 // it makes (the info byte: bits 0-2 edge as u, bit 3 present; bits 4-6 edge as v,
@@ -57,8 +61,8 @@ struct BucketDev {
     uint64_t* recs;              // rw words per record
     unsigned long long* fill;    // P * S append counters
     uint64_t stripe_cap;
-    uint32_t shift;              // bucket of a home slot = home >> shift
-    uint32_t n_buckets, stripes;
+    uint32_t shift;              // host sizing: a bucket's table range is at most 2^shift slots
+    uint32_t n_buckets, stripes; // bucket of a key = high 64 bits of (row-0 hash) x n_buckets
     uint32_t* overflow;          // set when a stripe runs out of room
     uint32_t rw, ws, packed;     // record layout (record_format)
 };
@@ -154,10 +158,13 @@ cudaError_t launch_emit(int nw, const Launch& L, const BankDev& b, uint32_t k, c
                         const BucketDev& bk);
 cudaError_t launch_upsert(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, uint32_t w_edge, uint32_t w_cov,
                           const TableDev& t, uint32_t* status, const RecordFilter& flt = RecordFilter{}, int queue = 0);
+// Counters of cnt[0, n) at or above min, added to *out.
+cudaError_t launch_count_at_least(const Launch& L, const uint32_t* cnt, uint64_t n, uint32_t min, unsigned long long* out);
 cudaError_t launch_count_records(int nw, const Launch& L, const BucketDev& bk, uint32_t bucket, const RecordFilter& flt);
 // every bucket in one persistent launch; *work (zeroed by the caller) hands out items
 cudaError_t launch_upsert_all(int nw, const Launch& L, const BucketDev& bk, uint32_t w_edge, uint32_t w_cov, const TableDev& t,
-                              uint32_t* status, unsigned long long* work);
+                              uint32_t* status, unsigned long long* work,
+                              int form = 1);
 cudaError_t launch_convert(int nw, const Launch& L, const TableDev& t, uint32_t min_trans_cov, const ConvOut& o);
 cudaError_t launch_clamp_counters(const Launch& L, uint32_t* cnt, uint64_t n);
 cudaError_t launch_table_init(int nw, const Launch& L, const TableDev& t);

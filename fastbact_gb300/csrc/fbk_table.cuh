@@ -23,6 +23,15 @@ __device__ __forceinline__ uint64_t home_slot_h(uint64_t h_row0, uint64_t cap) {
 __device__ __forceinline__ uint64_t home_slot(uint64_t fold, uint64_t cap) {
     return home_slot_h(smix(fold ^ cms_seed(0)), cap);
 }
+// Record bucket of a key: the same hash scaled to the bucket count, so that bucket b
+// holds the keys whose home slots lie in [b cap / P, (b + 1) cap / P) whatever the
+// capacity.
+__device__ __forceinline__ uint32_t bucket_of_h(uint64_t h_row0, uint32_t n_buckets) {
+    return (uint32_t)__umul64hi(h_row0, n_buckets);
+}
+__device__ __forceinline__ uint32_t bucket_of(uint64_t fold, uint32_t n_buckets) {
+    return bucket_of_h(smix(fold ^ cms_seed(0)), n_buckets);
+}
 
 __device__ __forceinline__ int64_t table_slot1(const TableDev& t, uint64_t key, uint64_t s, uint32_t* status) {
     for (uint32_t probe = 0; probe < t.max_probe; ++probe) {
