@@ -149,6 +149,8 @@ SIGNATURES = {
     "fbk_ctx_launch_count": (S, [vp, u64p]),
     "fbk_ctx_mem_info": (S, [vp, u64p, u64p]),
     "fbk_bank_upload": (S, [vp, P(ArenaView), P(vp)]),
+    "fbk_bank_upload_async": (S, [vp, P(ArenaView), P(vp)]),
+    "fbk_bank_wait": (S, [vp]),
     "fbk_bank_info": (S, [vp, u64p, u64p]),
     "fbk_bank_release": (S, [vp]),
     "fbk_cms_width_for_genome_size": (C.c_uint64, [C.c_uint64]),
@@ -178,6 +180,8 @@ SIGNATURES = {
     "fbk_build_front": (S, [vp, vp, P(BuildParams), P(Subsample), u8p, u64p, C.c_uint64, P(vp), P(vp)]),
     "fbk_table_info": (S, [vp, u64p, u64p, u64p]),
     "fbk_table_export": (S, [vp, u64p, u16p, u8p, C.c_uint64, u64p]),
+    "fbk_table_export_async": (S, [vp, u64p, u16p, u8p, C.c_uint64, u64p]),
+    "fbk_table_export_wait": (S, [vp]),
     "fbk_table_export_acc": (S, [vp, u64p, u16p, u16p, C.c_uint64, u64p]),
     "fbk_table_pushes": (S, [vp, u64p]),
     "fbk_table_flags": (S, [vp, u32p]),

@@ -450,13 +450,18 @@ def est_shard_finish(lengths: np.ndarray, n_use: int, stats: ExactCountStats, re
 class DeviceBank:
     """A ReadBank uploaded to device memory."""
 
-    def __init__(self, ctx: Context, bank: ReadBank | BitSeqArena):
+    def __init__(self, ctx: Context, bank: ReadBank | BitSeqArena, async_upload: bool = False):
+        """async_upload: when every array is page-locked, return once the copies are
+        queued (fbk_bank_upload_async); the bank keeps its host arrays alive, and every
+        call that reads it waits for the copies on the device."""
         self.ctx = ctx
         if isinstance(bank, BitSeqArena):
             bank = ReadBank(merged_reads=bank)
         self._views = bank.views()
+        self._host = bank if async_upload else None
         self._h = C.c_void_p()
-        check(N.lib().fbk_bank_upload(ctx.handle, self._views, C.byref(self._h)), ctx.handle, "bank upload")
+        fn = N.lib().fbk_bank_upload_async if async_upload else N.lib().fbk_bank_upload
+        check(fn(ctx.handle, self._views, C.byref(self._h)), ctx.handle, "bank upload")
         ctx.adopt(self)
         nr, nb = C.c_uint64(), C.c_uint64()  # the totals the upload's scan computed
         check(N.lib().fbk_bank_info(self._h, C.byref(nr), C.byref(nb)))
@@ -659,6 +664,7 @@ class SolidTable:
     def __init__(self, ctx: Context, handle, k: int, key_bits: int):
         self.ctx, self._h, self.k, self.key_bits = ctx, handle, k, key_bits
         self.nw = key_bits // 64
+        self._pending = None
         ctx.adopt(self)
 
     @property
@@ -673,24 +679,41 @@ class SolidTable:
     def __len__(self):
         return self.info()[1]
 
-    def export(self, sort: bool = False, out=None):
-        """(keys[n, nw] big-endian words, cov u16, mask u8).  `out` = (keys, cov, mask)
-        arrays with room for at least n rows (e.g. reused pinned buffers) receive the
-        rows; the returned arrays are views of their first n rows."""
-        n_solid = self.info()[1]
+    def _out_rows(self, n_solid: int, out):
         if out is not None and len(out[1]) >= n_solid and len(out[2]) >= n_solid and len(out[0]) >= n_solid:
             keys, cov, mask = out[0][:n_solid], out[1][:n_solid], out[2][:n_solid]
             if keys.dtype != np.uint64 or keys.shape[1:] != (self.nw,) or not keys.flags.c_contiguous \
                     or cov.dtype != np.uint16 or mask.dtype != np.uint8:
                 raise ValueError("export: out must be (uint64[n, nw], uint16[n], uint8[n]) C-contiguous arrays")
-        else:
-            keys = np.zeros((n_solid, self.nw), np.uint64)
-            cov = np.zeros(n_solid, np.uint16)
-            mask = np.zeros(n_solid, np.uint8)
+            return keys, cov, mask
+        return np.zeros((n_solid, self.nw), np.uint64), np.zeros(n_solid, np.uint16), np.zeros(n_solid, np.uint8)
+
+    def export(self, sort: bool = False, out=None):
+        """(keys[n, nw] big-endian words, cov u16, mask u8).  `out` = (keys, cov, mask)
+        arrays with room for at least n rows (e.g. reused pinned buffers) receive the
+        rows; the returned arrays are views of their first n rows."""
+        n_solid = self.info()[1]
+        keys, cov, mask = self._out_rows(n_solid, out)
         n = C.c_uint64()
         check(N.lib().fbk_table_export(self._h, ptr(keys.reshape(-1)), ptr(cov), ptr(mask), n_solid, C.byref(n)),
               self.ctx.handle, "table export")
         return sort_rows(keys, cov, mask) if sort else (keys, cov, mask)
+
+    def export_async(self, out):
+        """Queues the copy of the rows into `out` = (keys, cov, mask) page-locked arrays
+        with room for every row and returns at once; export_wait() returns the rows
+        (views of out) once they have arrived.  The next build may run meanwhile."""
+        n_solid = self.info()[1]
+        keys, cov, mask = self._out_rows(n_solid, out)
+        n = C.c_uint64()
+        check(N.lib().fbk_table_export_async(self._h, ptr(keys.reshape(-1)), ptr(cov), ptr(mask), n_solid, C.byref(n)),
+              self.ctx.handle, "table export_async")
+        self._pending = (keys, cov, mask)
+
+    def export_wait(self):
+        check(N.lib().fbk_table_export_wait(self._h), self.ctx.handle, "table export_wait")
+        rows, self._pending = self._pending, None
+        return rows
 
     def export_acc(self, sort: bool = True):
         """Every accumulated key: (keys[n, nw], cov u16, edge_counts[n, 8] u16)."""

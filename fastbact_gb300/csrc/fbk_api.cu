@@ -279,6 +279,10 @@ FBK_API fbk_status fbk_ctx_destroy(fbk_ctx* c) {
         if (c->h_stage[i]) cudaFreeHost(c->h_stage[i]);
         if (c->stage_ev[i]) cudaEventDestroy(c->stage_ev[i]);
     }
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FBK_OK;
@@ -309,6 +313,7 @@ FBK_API fbk_status fbk_ctx_fork(fbk_ctx* parent, fbk_ctx** out) {
     c->upsert_queue = parent->upsert_queue;
     c->batch_pass1 = parent->batch_pass1;
     c->filter_sizing = parent->filter_sizing;
+    c->filter_load = parent->filter_load;
     c->acc_filter = parent->acc_filter;
     c->upsert_all = parent->upsert_all;
     cudaError_t e = cudaSetDevice(c->device);
@@ -412,6 +417,7 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "upsert_queue" && (v == 0 || v == 1 || v == 2)) ctx->upsert_queue = (int)v;
     else if (n == "batch_pass1" && (v == 0 || v == 1 || v == 2)) ctx->batch_pass1 = (int)v;
     else if (n == "filter_sizing" && (v == 0 || v == 1)) ctx->filter_sizing = (int)v;
+    else if (n == "filter_load" && v >= 0.02 && v <= 0.9) ctx->filter_load = v;
     else if (n == "acc_filter" && (v == 0 || v == 1 || v == 2)) ctx->acc_filter = (int)v;
     else if (n == "upsert_all" && (v == 0 || v == 1 || v == 2)) ctx->upsert_all = (int)v;
     // the pass kernels are compiled for blocks of at most 256 threads
@@ -439,6 +445,7 @@ FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, doub
     else if (n == "upsert_queue") *v = ctx->upsert_queue;
     else if (n == "batch_pass1") *v = ctx->batch_pass1;
     else if (n == "filter_sizing") *v = ctx->filter_sizing;
+    else if (n == "filter_load") *v = ctx->filter_load;
     else if (n == "acc_filter") *v = ctx->acc_filter;
     else if (n == "upsert_all") *v = ctx->upsert_all;
     else if (n == "block_pass1") *v = ctx->block_pass1;
@@ -590,7 +597,21 @@ void scan_arenas(const fbk_arena_view* arenas, int n_arenas, ArenaScan& sc) {
     for (int a = 0; a < n_arenas; ++a) sc.n_reads += arenas[a].n_seqs;
 }
 
-fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_arenas, fbk_bank** out, uint64_t chunk_bases) {
+static cudaError_t copy_stream_of(fbk_ctx* ctx, cudaStream_t* s) {
+    if (!ctx->copy_stream) {
+        cudaError_t e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return e;
+    }
+    *s = ctx->copy_stream;
+    return cudaSuccess;
+}
+
+cudaError_t bank_wait(fbk_ctx* ctx, const fbk_bank* b) {
+    return b && b->ready ? cudaStreamWaitEvent(ctx->stream, b->ready, 0) : cudaSuccess;
+}
+
+fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_arenas, fbk_bank** out, uint64_t chunk_bases,
+                            bool async) {
     uint64_t n_words = 0;
     bool all_pairs = true;
     for (int a = 0; a < n_arenas; ++a) {
@@ -622,13 +643,34 @@ fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_ar
     }
     uint64_t wbase = 0, rbase = 0;
     Launch L = launch_cfg(ctx, 256, 0);
+    // An asynchronous upload (every arena buffer page-locked) copies and rebases on the
+    // context's copy stream and records b->ready; the calls that read the bank order
+    // the context's stream after it (bank_wait).
+    if (async) {
+        for (int a = 0; a < n_arenas && async; ++a) {
+            const fbk_arena_view& v = arenas[a];
+            async = (!v.n_words || host_page_locked(v.data)) &&
+                    (!v.n_seqs || (host_page_locked(v.offsets) && host_page_locked(v.lengths) &&
+                                   (!v.pair_idx || host_page_locked(v.pair_idx))));
+        }
+        cudaError_t e = async ? copy_stream_of(ctx, &L.stream) : cudaSuccess;
+        if (e == cudaSuccess && async) e = cudaEventCreateWithFlags(&b->ready, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            fbk_bank_release(b);
+            return cuda_err(ctx, e, "bank upload stream");
+        }
+    }
+    auto h2d = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+        if (!async) return copy_h2d(ctx, dst, src, bytes);
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, L.stream);
+    };
     for (int a = 0; a < n_arenas; ++a) {
         const fbk_arena_view& v = arenas[a];
         cudaError_t e = cudaSuccess;
-        if (v.n_words) e = copy_h2d(ctx, b->data + wbase, v.data, v.n_words * 8);
-        if (e == cudaSuccess && v.n_seqs) e = copy_h2d(ctx, b->off + rbase, v.offsets, v.n_seqs * 8);
-        if (e == cudaSuccess && v.n_seqs) e = copy_h2d(ctx, b->len + rbase, v.lengths, v.n_seqs * 4);
-        if (e == cudaSuccess && v.n_seqs && b->pair_idx) e = copy_h2d(ctx, b->pair_idx + rbase, v.pair_idx, v.n_seqs * 4);
+        if (v.n_words) e = h2d(b->data + wbase, v.data, v.n_words * 8);
+        if (e == cudaSuccess && v.n_seqs) e = h2d(b->off + rbase, v.offsets, v.n_seqs * 8);
+        if (e == cudaSuccess && v.n_seqs) e = h2d(b->len + rbase, v.lengths, v.n_seqs * 4);
+        if (e == cudaSuccess && v.n_seqs && b->pair_idx) e = h2d(b->pair_idx + rbase, v.pair_idx, v.n_seqs * 4);
         if (e == cudaSuccess && wbase && v.n_seqs) {
             TimedLaunch tl;
             time_begin(ctx, "bank_rebase", tl);
@@ -643,7 +685,8 @@ fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_ar
         rbase += v.n_seqs;
         b->arena_reads.push_back(v.n_seqs);
     }
-    cudaError_t e = cudaMemsetAsync(b->data + n_words, 0, 8 * 8, ctx->stream);
+    cudaError_t e = cudaMemsetAsync(b->data + n_words, 0, 8 * 8, L.stream);
+    if (e == cudaSuccess && async) e = cudaEventRecord(b->ready, L.stream);
     if (e != cudaSuccess) {
         fbk_bank_release(b);
         return cuda_err(ctx, e, "bank padding");
@@ -694,6 +737,18 @@ FBK_API fbk_status fbk_bank_upload(fbk_ctx* ctx, const fbk_arena_view arenas[3],
     return bank_upload_impl(ctx, arenas, 3, out);
 }
 
+FBK_API fbk_status fbk_bank_upload_async(fbk_ctx* ctx, const fbk_arena_view arenas[3], fbk_bank** out) {
+    if (!ctx || !arenas || !out) return FBK_ERR_INVALID;
+    CK(ctx, cudaSetDevice(ctx->device));
+    return bank_upload_impl(ctx, arenas, 3, out, 1ull << 30, true);
+}
+
+FBK_API fbk_status fbk_bank_wait(const fbk_bank* b) {
+    if (!b) return FBK_ERR_INVALID;
+    if (b->ready) CK(b->ctx, cudaEventSynchronize(b->ready));
+    return FBK_OK;
+}
+
 FBK_API fbk_status fbk_bank_info(const fbk_bank* b, uint64_t* n_reads, uint64_t* n_bases) {
     if (!b) return FBK_ERR_INVALID;
     if (n_reads) *n_reads = b->n_reads;
@@ -705,6 +760,10 @@ FBK_API fbk_status fbk_bank_release(fbk_bank* b) {
     if (!b) return FBK_OK;
     fbk_ctx* ctx = b->ctx;
     cudaStreamSynchronize(ctx->stream);
+    if (b->ready) {
+        cudaEventSynchronize(b->ready);
+        cudaEventDestroy(b->ready);
+    }
     dev_free(ctx, b->data);
     dev_free(ctx, b->off);
     dev_free(ctx, b->len);
@@ -878,6 +937,7 @@ FBK_API fbk_status fbk_cms_add_bank(fbk_cms* c, const fbk_bank* b, uint32_t k, u
     if (!c || !b) return FBK_ERR_INVALID;
     fbk_ctx* ctx = c->ctx;
     CK(ctx, cudaSetDevice(ctx->device));
+    CK(ctx, bank_wait(ctx, b));
     uint64_t* keep = nullptr;
     fbk_status st = make_keep_bits(ctx, b, ss, &keep);
     if (st) return st;
@@ -1168,6 +1228,9 @@ static fbk_status table_alloc(fbk_table* t, uint64_t cap, bool with_cov) {
 static fbk_status table_convert(fbk_table* t, uint64_t* acc_keys, uint16_t* acc_cov, uint16_t* acc_edges, uint64_t acc_cap,
                                 uint64_t* acc_digest = nullptr) {
     fbk_ctx* ctx = t->ctx;
+    // the rows are rewritten (or reallocated): an asynchronous export of them must have
+    // been read out
+    if (t->exported) CK(ctx, cudaEventSynchronize(t->exported));
     for (int attempt = 0; attempt < 2; ++attempt) {
         CK(ctx, cudaMemsetAsync(ctx->d_counts, 0, 8 * sizeof(unsigned long long), ctx->stream));
         ConvOut o{};
@@ -1284,8 +1347,8 @@ static fbk_status buckets_alloc(fbk_ctx* ctx, uint64_t cap, uint64_t slot_bytes,
 // Capacity of a filtered pass's table, chosen after bucket 0 of P is counted: the keys
 // that pass the filter in bucket 0 are about the counters at or above min_trans_cov
 // (keys that share a counter add a few percent), the buckets split the keys by hash
-// evenly, and the table gets 30% headroom over that estimate at the context's load
-// factor, a multiple of P slots, never more than the capacity from the distinct
+// evenly, and the table gets 30% headroom over that estimate at the load of tuning
+// filter_load, a multiple of P slots, never more than the capacity from the distinct
 // estimate.  Allocates and initialises the table.
 static fbk_status size_filtered_table(fbk_table* t, const RecordFilter& flt, uint32_t n_buckets, uint64_t cap_distinct) {
     fbk_ctx* ctx = t->ctx;
@@ -1296,7 +1359,7 @@ static fbk_status size_filtered_table(fbk_table* t, const RecordFilter& flt, uin
     CK(ctx, cudaStreamSynchronize(ctx->stream));
     const uint64_t n0 = *(const unsigned long long*)ctx->h_pinned;
     const double keys = 1.3 * (double)n0 * (double)n_buckets;
-    uint64_t cap = (uint64_t)(keys / ctx->load_factor) + 1024;
+    uint64_t cap = (uint64_t)(keys / ctx->filter_load) + 1024;
     cap = (cap + n_buckets - 1) / n_buckets * n_buckets;
     if (cap > cap_distinct) cap = cap_distinct;
     return table_alloc(t, cap, false);
@@ -1552,6 +1615,7 @@ FBK_API fbk_status fbk_solid_build(fbk_ctx* ctx, const fbk_bank* b, const fbk_cm
                                    uint64_t n_contigs, fbk_table** out) {
     if (!ctx || !b || !cms || !p || !out) return FBK_ERR_INVALID;
     CK(ctx, cudaSetDevice(ctx->device));
+    CK(ctx, bank_wait(ctx, b));
     uint64_t* keep = nullptr;
     fbk_status st = make_keep_bits(ctx, b, ss, &keep);
     if (st) return st;
@@ -1617,6 +1681,7 @@ FBK_API fbk_status fbk_build_front(fbk_ctx* ctx, const fbk_bank* b, const fbk_bu
                                    fbk_table** out, fbk_cms** cms_out) {
     if (!ctx || !b || !p || !out) return FBK_ERR_INVALID;
     CK(ctx, cudaSetDevice(ctx->device));
+    CK(ctx, bank_wait(ctx, b));
     uint32_t log2w = p->cms_log2_width;
     if (!log2w) {
         // build.rs:74-84: explicit genome size (floored at 50 kb), else read bases / 60
@@ -1668,6 +1733,37 @@ FBK_API fbk_status fbk_table_export(fbk_table* t, uint64_t* keys, uint16_t* cov,
         CK(ctx, copy_d2h(ctx, mask, t->out_mask, n));
     }
     *n_out = t->n_solid;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_table_export_async(fbk_table* t, uint64_t* keys, uint16_t* cov, uint8_t* mask, uint64_t cap, uint64_t* n_out) {
+    if (!t || !n_out) return FBK_ERR_INVALID;
+    fbk_ctx* ctx = t->ctx;
+    uint64_t n = std::min(cap, t->n_solid);
+    if (n && (!keys || !cov || !mask)) return FBK_ERR_INVALID;
+    if (n && (!host_page_locked(keys) || !host_page_locked(cov) || !host_page_locked(mask)))
+        return set_err(ctx, FBK_ERR_INVALID, "fbk_table_export_async: the row buffers must be page-locked host memory");
+    CK(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t cs = nullptr;
+    CK(ctx, copy_stream_of(ctx, &cs));
+    if (!t->converted) CK(ctx, cudaEventCreateWithFlags(&t->converted, cudaEventDisableTiming));
+    if (!t->exported) CK(ctx, cudaEventCreateWithFlags(&t->exported, cudaEventDisableTiming));
+    // the copies start once the work queued on the context's stream (the conversion) is done
+    CK(ctx, cudaEventRecord(t->converted, ctx->stream));
+    CK(ctx, cudaStreamWaitEvent(cs, t->converted, 0));
+    if (n) {
+        CK(ctx, cudaMemcpyAsync(keys, t->out_keys, n * 8 * t->nw, cudaMemcpyDeviceToHost, cs));
+        CK(ctx, cudaMemcpyAsync(cov, t->out_cov, n * 2, cudaMemcpyDeviceToHost, cs));
+        CK(ctx, cudaMemcpyAsync(mask, t->out_mask, n, cudaMemcpyDeviceToHost, cs));
+    }
+    CK(ctx, cudaEventRecord(t->exported, cs));
+    *n_out = t->n_solid;
+    return FBK_OK;
+}
+
+FBK_API fbk_status fbk_table_export_wait(fbk_table* t) {
+    if (!t) return FBK_ERR_INVALID;
+    if (t->exported) CK(t->ctx, cudaEventSynchronize(t->exported));
     return FBK_OK;
 }
 
@@ -1835,6 +1931,11 @@ FBK_API fbk_status fbk_table_digest(fbk_table* t, uint64_t* digest, uint64_t* n_
 FBK_API fbk_status fbk_table_release(fbk_table* t) {
     if (!t) return FBK_OK;
     cudaStreamSynchronize(t->ctx->stream);
+    for (cudaEvent_t* e : {&t->exported, &t->converted})
+        if (*e) {
+            cudaEventSynchronize(*e);
+            cudaEventDestroy(*e);
+        }
     table_free_storage(t);
     table_free_out(t);
     delete t;

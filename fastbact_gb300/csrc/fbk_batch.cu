@@ -444,7 +444,7 @@ fbk_status autotune_b(fbk_batch* B, BatchIso* it, bool persistent_upsert) {
                 float ms = 0;
                 st = timed([&]() -> fbk_status {
                     TIMED(ctx, "tune_upsert", launch_upsert_all(B->nw, shape_launch(ctx, sh), bk, 1, 1, tbl_dev(it->table),
-                                                                flags + 1, work));
+                                                                flags + 1, work, ctx->upsert_all));
                     return FBK_OK;
                 }, &ms);
                 if (st) break;
@@ -746,7 +746,7 @@ fbk_status phase_b(fbk_batch* B, const std::vector<BatchIso*>& V) {
             bk.overflow = w.status + 2 * i + 1;
             if (work.p && !flt[i].cnt) {
                 TIMED(ctx, "batch_upsert", launch_upsert_all(B->nw, shape_launch(ctx, B->upsert), bk, 1, 1, tbl_dev(it->table),
-                                                             w.status + 2 * i, work.p + i));
+                                                             w.status + 2 * i, work.p + i, ctx->upsert_all));
                 continue;
             }
             for (uint32_t bu = 0; bu < bk.n_buckets; ++bu) {

@@ -22,8 +22,25 @@ __host__ __device__ __forceinline__ uint64_t smix(uint64_t z) {
 }
 
 // CMS row seeds — sketch.rs:122-127
-__host__ __device__ __forceinline__ uint64_t cms_seed(int r) {
+__host__ __device__ __forceinline__ constexpr uint64_t cms_seed(int r) {
     return r == 0 ? 0x243f6a8885a308d3ULL : r == 1 ? 0x13198a2e03707344ULL : r == 2 ? 0xa4093822299f31d0ULL : 0x082efa98ec4e6c89ULL;
+}
+
+// The four row hashes smix(key ^ seed_r) of the sketch (sketch.rs:191-223).  The first
+// xor-shift distributes over the xor with the seed, (x ^ s) ^ ((x ^ s) >> 30) =
+// (x ^ (x >> 30)) ^ (s ^ (s >> 30)), so it is done once for the four rows and each row
+// xors a folded seed.
+__host__ __device__ __forceinline__ constexpr uint64_t cms_seed_folded(int r) {
+    return cms_seed(r) ^ (cms_seed(r) >> 30);
+}
+__host__ __device__ __forceinline__ void cms_row_hashes(uint64_t key, uint64_t (&h)[4]) {
+    const uint64_t x = key ^ (key >> 30);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        uint64_t z = (x ^ cms_seed_folded(r)) * 0xbf58476d1ce4e5b9ULL;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+        h[r] = z ^ (z >> 31);
+    }
 }
 
 // ntHash seeds — kmer.rs:385-391 (REV[c] == FWD[3-c])

@@ -267,6 +267,7 @@ fbk_status est_shard_stage(fbk_ctx* ctx, const fbk_bank* bank, const uint32_t* l
     if (pair_begin > pair_end || pair_end > n_use) return set_err(ctx, FBK_ERR_INVALID, "pair range outside the sample");
     if (bank->n_reads < 2 * n_use) return set_err(ctx, FBK_ERR_INVALID, "sample holds fewer than 2*n_use reads");
     CKE(cudaSetDevice(ctx->device));
+    CKE(bank_wait(ctx, bank));
     const uint32_t k = prm->k, p = prm->hll_p, log2w = prm->cms_log2_width;
     EstPlan pl;
     st = est_plan(ctx, lengths, n_use, k, pl);
@@ -333,6 +334,7 @@ FBK_API fbk_status fbk_estimate_bank(fbk_ctx* ctx, const fbk_bank* sample, const
     if (st) return st;
     if (sample->n_reads < 2 * n_pairs) return set_err(ctx, FBK_ERR_INVALID, "sample holds fewer than 2*n_pairs reads");
     CKE(cudaSetDevice(ctx->device));
+    CKE(bank_wait(ctx, sample));
     const uint64_t n_use = est_n_use(stats, prm, n_pairs);
     if (n_use == 0) return set_err(ctx, FBK_ERR_EMPTY, "Input FASTQ files contain 0 valid read pairs");
     return estimate_impl(ctx, sample, read_lengths, n_use, stats, prm, out, regs_total, regs_solid);

@@ -79,6 +79,7 @@ FBK_API fbk_status fbk_filter_active_reads(fbk_ctx* ctx, const fbk_bank* bank, c
     if (bank->arena_reads.size() != 3) return set_err(ctx, FBK_ERR_INVALID, "filter_active_reads needs a three-arena ReadBank");
     if (graph_k < 1) return set_err(ctx, FBK_ERR_INVALID, "graph k must be >= 1");
     CK(ctx, cudaSetDevice(ctx->device));
+    CK(ctx, bank_wait(ctx, bank));
     const uint32_t k = std::min<uint32_t>(graph_k, 31);
     const uint64_t WINDOW = 350;
     // pack the unitigs (ASCII_TO_2BIT: A0 C1 G2 T3, anything else 0) and list the windows

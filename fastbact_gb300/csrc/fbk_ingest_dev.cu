@@ -496,6 +496,7 @@ FBK_API fbk_status fbk_ingest_fastq_device(fbk_ctx* ctx, const uint8_t* r1, uint
 FBK_API fbk_status fbk_bank_export(const fbk_bank* b, uint64_t* words, uint64_t* offsets, uint32_t* lengths, uint32_t* pair_idx) {
     if (!b) return FBK_ERR_INVALID;
     fbk_ctx* ctx = b->ctx;
+    CK(ctx, bank_wait(ctx, b));
     if (words && b->n_words) CK(ctx, cudaMemcpyAsync(words, b->data, b->n_words * 8, cudaMemcpyDeviceToHost, ctx->stream));
     if (offsets && b->n_reads) CK(ctx, cudaMemcpyAsync(offsets, b->off, b->n_reads * 8, cudaMemcpyDeviceToHost, ctx->stream));
     if (lengths && b->n_reads) CK(ctx, cudaMemcpyAsync(lengths, b->len, b->n_reads * 4, cudaMemcpyDeviceToHost, ctx->stream));

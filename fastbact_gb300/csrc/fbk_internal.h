@@ -47,6 +47,7 @@ struct fbk_ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;      // asynchronous uploads and exports (created on first use)
     std::shared_ptr<fbk::DevicePool> pool;  // shared by contexts forked from this one
     uint32_t* d_status = nullptr;            // device status bits (4 words)
     unsigned long long* d_counts = nullptr;  // conversion counters (4)
@@ -90,11 +91,18 @@ struct fbk_ctx {
     // inline.  Measured per 100x pass (0 / 1 / 2): k = 55 7.44 / 6.67 / 7.93 ms, k = 77
     // 10.88 / 7.70 / 9.10.
     int upsert_queue = 1;
-    // Filtered passes: 1 sizes the table from the keys that pass the filter in the first
-    // bucket, 0 from the distinct k-mers of pass 1
-    int filter_sizing = 0;
+    // Filtered passes: 1 (default) sizes the table from the keys that pass the filter in
+    // the first bucket, at filter_load keys per slot (plus 30% headroom), 0 from the
+    // distinct k-mers of pass 1 at load_factor.  Measured per 100x step (ms): distinct
+    // 97.0; filter_load 0.12 94.1, 0.2 93.3, 0.3 92.8, 0.62 99.0 (probe runs grow long
+    // where a bucket holds more survivors than bucket 0 predicted).
+    int filter_sizing = 1;
+    double filter_load = 0.3;
     int batch_pass1 = 0;                  // batches with a ladder gate: 0 autotuned, 1 one multi-isolate launch, 2 a launch per isolate
-    int upsert_all = 1;                   // 1: an unfiltered pass upserts every bucket in one persistent launch, 2: the same with every lane's probe advanced a slot per step
+    // Unfiltered passes: 1 upserts every bucket in one persistent launch, 2 (default) the
+    // same with every lane's probe advanced a slot per step (64/128-bit keys; per 100x
+    // pass k = 21 5.60 -> 5.59 ms, k = 33 6.70 -> 6.58), 0 one launch per bucket
+    int upsert_all = 2;
     int acc_filter = 1;                   // keys with fewer records than min_trans_cov stay out of the table: 0 never, 1 for 256-bit keys, 2 always
     bool capturing = false;               // launches are being captured into a CUDA graph
 };
@@ -113,6 +121,7 @@ struct fbk_bank {
     uint64_t max_chunk_bases() const { return max_chunk; }
     std::vector<uint64_t> len_hist;      // read-length histogram (last bin: all longer reads)
     uint64_t long_bases = 0;             // bases of reads in the last bin
+    cudaEvent_t ready = nullptr;         // an asynchronous upload's copies (null: uploaded synchronously)
     // upper bound of the windows of length k in reads with len >= min_len
     uint64_t windows(uint32_t k, uint32_t min_len) const {
         uint64_t w = 0;
@@ -154,6 +163,7 @@ struct fbk_table {
     uint64_t n_keys = 0, n_solid = 0, digest = 0, pushes = 0;
     uint64_t skipped_pushes = 0;  // pushes of records the record filter kept out of the table
     bool filtered = false;        // the accumulator holds only keys that may become solid
+    cudaEvent_t converted = nullptr, exported = nullptr;  // an asynchronous export's order and completion
 };
 
 namespace fbk {
@@ -163,6 +173,8 @@ inline int ladder_form(const fbk_ctx* ctx, int nw) { return ctx->ladder_ilp ? ct
 inline int emit_form(const fbk_ctx* ctx, int nw) { return ctx->emit_lookahead ? ctx->emit_lookahead : (nw <= 2 ? 4 : 3); }
 
 fbk_status set_err(fbk_ctx* ctx, fbk_status st, const std::string& msg);
+// Orders the context's stream after an asynchronous upload of b (no-op otherwise).
+cudaError_t bank_wait(fbk_ctx* ctx, const fbk_bank* b);
 fbk_status cuda_err(fbk_ctx* ctx, cudaError_t e, const char* what);
 void* dev_alloc(fbk_ctx* ctx, uint64_t bytes);
 void dev_free(fbk_ctx* ctx, void* p);
@@ -203,7 +215,7 @@ cudaError_t copy_d2h(fbk_ctx* ctx, void* dst, const void* src, size_t bytes);
 // sample and by prior-contig handling).
 // chunk_bases: read ranges are cut so that each holds fewer bases than this.
 fbk_status bank_upload_impl(fbk_ctx* ctx, const fbk_arena_view* arenas, int n_arenas, fbk_bank** out,
-                            uint64_t chunk_bases = 1ull << 30);
+                            uint64_t chunk_bases = 1ull << 30, bool async = false);
 BankDev bank_view(const fbk_bank* b, uint64_t r_begin, uint64_t r_end, const uint64_t* keep_bits);
 
 // 256-bit keys of k <= 96 have a zero most significant word, which then holds the

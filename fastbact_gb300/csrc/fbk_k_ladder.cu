@@ -61,12 +61,12 @@ __global__ void __launch_bounds__(256, ILP == 1 ? 6 : 2) k_ladder_pass1(BankDev 
                 Key<NW> can{};
                 bool rc;
                 canonical_ws<NW, WS>(b.data, off + q, k, can, rc);
-                const uint64_t key = key_fold<NW>(can);
-                h0[p] = smix(key ^ cms_seed(0));
+                uint64_t hr[4];
+                cms_row_hashes(key_fold<NW>(can), hr);
+                h0[p] = hr[0];
 #pragma unroll
                 for (int row = 0; row < 4; ++row) {
-                    const uint64_t h = row == 0 ? h0[p] : smix(key ^ cms_seed(row));
-                    const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
+                    const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(hr[row] & wmask);
                     wd[4 * p + row] = bit >> 5;
                     mk[4 * p + row] = 1u << (bit & 31);
                 }
@@ -117,12 +117,12 @@ __device__ __forceinline__ void ladder_prep(const BankDev& b, uint64_t off, uint
     Key<NW> can{};
     bool rc;
     canonical_ws<NW, WS>(b.data, off + q, k, can, rc);
-    const uint64_t key = key_fold<NW>(can);
-    c.h0 = smix(key ^ cms_seed(0));
+    uint64_t hr[4];
+    cms_row_hashes(key_fold<NW>(can), hr);
+    c.h0 = hr[0];
 #pragma unroll
     for (int row = 0; row < 4; ++row) {
-        const uint64_t h = row == 0 ? c.h0 : smix(key ^ cms_seed(row));
-        const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
+        const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(hr[row] & wmask);
         c.wd[row] = bit >> 5;
         c.mk[row] = 1u << (bit & 31);
     }

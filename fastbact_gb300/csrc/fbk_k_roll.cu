@@ -212,12 +212,12 @@ __global__ void __launch_bounds__(256, P == 1 ? 6 : 4) k_ladder_pass1_roll(BankD
                 Key<NW> can;
                 bool rc;
                 strands_canonical<NW, WS>(F, R, can, rc);
-                const uint64_t key = key_fold<NW>(can);
-                h0[p] = smix(key ^ cms_seed(0));
+                uint64_t hr[4];
+                cms_row_hashes(key_fold<NW>(can), hr);
+                h0[p] = hr[0];
 #pragma unroll
                 for (int row = 0; row < 4; ++row) {
-                    const uint64_t h = row == 0 ? h0[p] : smix(key ^ cms_seed(row));
-                    const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
+                    const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(hr[row] & wmask);
                     wd[4 * p + row] = bit >> 5;
                     mk[4 * p + row] = 1u << (bit & 31);
                 }

@@ -145,11 +145,12 @@ struct GateLoads {
 __device__ __forceinline__ void gate_issue(const uint32_t* __restrict__ top, uint32_t log2w, uint64_t key, bool live, GateLoads& g) {
     const uint64_t wmask = (1ULL << log2w) - 1;
     g.bits = 0;
+    uint64_t hr[4];
+    cms_row_hashes(key, hr);
+    g.h0 = hr[0];
 #pragma unroll
     for (int row = 0; row < 4; ++row) {
-        const uint64_t h = smix(key ^ cms_seed(row));
-        if (row == 0) g.h0 = h;
-        const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(h & wmask);
+        const uint32_t bit = ((uint32_t)row << log2w) + (uint32_t)(hr[row] & wmask);
         g.bits |= (bit & 31u) << (5 * row);
         g.w[row] = live ? __ldg(top + (bit >> 5)) : 0u;
     }

@@ -6,7 +6,8 @@
  * failure on a context.  The caller owns every host buffer; the library owns device
  * objects until their *_release call.  Every object (bank, sketch, table) must be
  * released before the context it was created on is destroyed.  A context is used from one host thread at a
- * time; separate contexts are independent.  Each context owns one CUDA stream.
+ * time; separate contexts are independent.  Each context owns one CUDA stream for its
+ * work, and a second one for the asynchronous upload and export calls.
  *
  * Reference interfaces (paths inside the fastBact repository) that each group
  * replaces are cited next to the declarations.
@@ -168,7 +169,10 @@ FBK_API fbk_status fbk_ctx_event_elapsed(fbk_ctx* ctx, int slot_a, int slot_b, d
  * (keys that cannot become SolidKmerNodes stay out of the table, see fbk_table_flags:
  * 0 never, 1 where it pays, 2 always), "upsert_all" (1: an unfiltered pass upserts every
  * bucket in one persistent launch), "upsert_queue" (1: filtered upserts queue the
- * filter's survivors per warp before probing).  Results do not depend on any of them. */
+ * filter's survivors per warp before probing), "filter_sizing" (1: a filtered pass sizes
+ * its table from the first bucket's survivors, at load "filter_load"), "batch_pass1"
+ * (0 autotuned, 1 one multi-isolate launch, 2 a launch per isolate).  Results do not
+ * depend on any of them. */
 FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double value);
 FBK_API fbk_status fbk_ctx_get_tuning(const fbk_ctx* ctx, const char* name, double* value);
 /* Number of kernels launched on this context since creation. */
@@ -181,6 +185,14 @@ FBK_API fbk_status fbk_ctx_mem_info(const fbk_ctx* ctx, uint64_t* pool_used, uin
  * asynchronously on the context stream; larger pageable buffers through pinned
  * staging, after which the host buffers may be reused at once). */
 FBK_API fbk_status fbk_bank_upload(fbk_ctx* ctx, const fbk_arena_view arenas[3], fbk_bank** out);
+/* The same, returning once the copies are queued when every arena buffer is
+ * page-locked (else it copies as fbk_bank_upload does): the copies run on the
+ * context's copy stream while the caller queues other work (the genome estimate of
+ * the sample, say), and every call that reads the bank orders its work after them.
+ * The host buffers must stay valid and unchanged until fbk_bank_wait returns or
+ * the bank is released. */
+FBK_API fbk_status fbk_bank_upload_async(fbk_ctx* ctx, const fbk_arena_view arenas[3], fbk_bank** out);
+FBK_API fbk_status fbk_bank_wait(const fbk_bank* b);  /* blocks until an asynchronous upload's copies are done */
 FBK_API fbk_status fbk_bank_info(const fbk_bank* b, uint64_t* n_reads, uint64_t* n_bases);
 FBK_API fbk_status fbk_bank_release(fbk_bank* b);
 
@@ -270,6 +282,13 @@ FBK_API fbk_status fbk_table_flags(const fbk_table* t, uint32_t* flags);
 /* Converted entries in device order (unsorted): keys (key_bits/64 big-endian words
  * each), cov, mask.  cap = rows the buffers hold. */
 FBK_API fbk_status fbk_table_export(fbk_table* t, uint64_t* keys, uint16_t* cov, uint8_t* mask, uint64_t cap, uint64_t* n_out);
+/* The same into page-locked buffers, returning once the copies are queued on the
+ * context's copy stream (n_out is known at once): the next build can start while the
+ * rows travel.  The buffers hold the rows after fbk_table_export_wait; releasing the
+ * table waits for the copies first. */
+FBK_API fbk_status fbk_table_export_async(fbk_table* t, uint64_t* keys, uint16_t* cov, uint8_t* mask, uint64_t cap,
+                                          uint64_t* n_out);
+FBK_API fbk_status fbk_table_export_wait(fbk_table* t);
 /* Every accumulated key with its KmerAcc (cov and edge_counts[8], saturated at 65535). */
 FBK_API fbk_status fbk_table_export_acc(fbk_table* t, uint64_t* keys, uint16_t* cov, uint16_t* edges, uint64_t cap, uint64_t* n_out);
 /* Sum over every key of its raw edge counters (= transition pushes made by pass 2,

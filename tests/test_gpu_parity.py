@@ -500,11 +500,12 @@ TUNINGS = [
     dict(acc_filter=2, block_pass2=96),                   # the filter's survivors queued per warp, 3 warps per block
     dict(acc_filter=2, upsert_queue=2),                   # the same at six blocks per SM
     dict(acc_filter=2, upsert_queue=0),                   # the filter tested inline
-    dict(load_factor=0.9, acc_filter=2),                  # long probe runs in the queued upsert
-    dict(upsert_all=2, acc_filter=0),                     # persistent upsert, every lane's probe advanced a slot per step
+    dict(filter_sizing=0, load_factor=0.9, acc_filter=2),  # long probe runs in the queued upsert
+    dict(upsert_all=1, acc_filter=0),                     # persistent upsert, probes run to the end lane by lane
     dict(upsert_all=2, acc_filter=0, load_factor=0.9),    # ... with long probe runs
-    dict(filter_sizing=1, acc_filter=2),                  # filtered tables sized from the first bucket's survivors
-    dict(filter_sizing=1, acc_filter=2, load_factor=0.9, bucket_bytes=1 << 16),  # ... from a small first bucket
+    dict(filter_sizing=0, acc_filter=2),                  # filtered tables sized from the distinct k-mers
+    dict(filter_sizing=1, filter_load=0.62, acc_filter=2),  # ... from the first bucket's survivors at a high load
+    dict(filter_sizing=1, filter_load=0.9, acc_filter=2, bucket_bytes=1 << 16),  # ... from a small first bucket
     dict(upsert_all=0, acc_filter=0),                     # one upsert launch per bucket
     dict(block_emit=256),                                 # record emit in blocks of 256
 ]
