@@ -413,7 +413,7 @@ FBK_API fbk_status fbk_ctx_set_tuning(fbk_ctx* ctx, const char* name, double v) 
     else if (n == "record_factor" && v > 0 && v <= 16) ctx->record_factor = v;
     else if (n == "sketch_mode" && (v == 0 || v == 1)) ctx->sketch_mode = (int)v;
     else if (n == "ladder_ilp" && v >= 0 && v <= 5 && v == (int)v) ctx->ladder_ilp = (int)v;
-    else if (n == "emit_lookahead" && v >= 0 && v <= 4 && v == (int)v) ctx->emit_lookahead = (int)v;
+    else if (n == "emit_lookahead" && v >= 0 && v <= 5 && v == (int)v) ctx->emit_lookahead = (int)v;
     else if (n == "upsert_queue" && (v == 0 || v == 1 || v == 2)) ctx->upsert_queue = (int)v;
     else if (n == "batch_pass1" && (v == 0 || v == 1 || v == 2)) ctx->batch_pass1 = (int)v;
     else if (n == "filter_sizing" && (v == 0 || v == 1)) ctx->filter_sizing = (int)v;

@@ -82,9 +82,10 @@ struct fbk_ctx {
     // 7.30 / 7.37 / 6.68, k = 55 5.71 / 6.26 / 5.59, k = 77 5.98 / 5.37 / 4.74.
     int ladder_ilp = 0;
     // Record emit: gate loads 1 or 2 chunks ahead read by read; 3 = 2 ahead over a flattened
-    // window stream; 4 = one lane per read with rolled k-mers.  0 (default) picks by key
-    // width: 4 for 64- and 128-bit keys (k = 21 8.57 -> 7.02 ms per 100x pass, k = 33
-    // 9.04 -> 8.16, k = 55 7.38 -> 6.77), 3 for 256-bit keys (rolled: k = 77 7.14 -> 8.88).
+    // window stream; 4 = one lane per read with rolled k-mers (5: the same at two blocks
+    // per SM for every key width).  0 (default) = 4 (per 100x pass, flat -> rolled: k = 21
+    // 8.57 -> 7.02 ms, k = 33 9.04 -> 8.16, k = 55 7.38 -> 6.77, k = 77 7.34 -> 5.74 with
+    // two blocks per SM for 256-bit keys).
     int emit_lookahead = 0;
     // Filtered upserts: 1 (default) queues the filter's survivors per warp so that the
     // probes run on full warps, 2 the same at six blocks per SM, 0 tests the filter
@@ -170,7 +171,7 @@ namespace fbk {
 
 // The pass-1 and emit forms a context's tuning selects for keys of nw words.
 inline int ladder_form(const fbk_ctx* ctx, int nw) { return ctx->ladder_ilp ? ctx->ladder_ilp : (nw == 1 ? 1 : 5); }
-inline int emit_form(const fbk_ctx* ctx, int nw) { return ctx->emit_lookahead ? ctx->emit_lookahead : (nw <= 2 ? 4 : 3); }
+inline int emit_form(const fbk_ctx* ctx, int nw) { return ctx->emit_lookahead ? ctx->emit_lookahead : 4; }
 
 fbk_status set_err(fbk_ctx* ctx, fbk_status st, const std::string& msg);
 // Orders the context's stream after an asynchronous upload of b (no-op otherwise).

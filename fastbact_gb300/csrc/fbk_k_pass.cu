@@ -1129,10 +1129,10 @@ static cudaError_t emitl_nw(const Launch& L, const BankDev& b, uint32_t k, const
                             const TableDev& t, const BucketDev& bk, int lookahead) {
     const size_t smem = (size_t)(L.block / 32) * EMIT_WARP_WORDS(NW) * 8;
     const uint32_t ws = (64u * NW - 2u * k) >> 6;
-    if (lookahead == 4) {  // one lane per read, rolled (fbk_k_roll.cu)
+    if (lookahead == 4 || lookahead == 5) {  // one lane per read, rolled (fbk_k_roll.cu); 5: two blocks per SM
         Launch L2 = L;
         L2.block = 256;
-        return launch_emit_roll(NW, L2, b, k, lad, log2w, ts, t, bk);
+        return launch_emit_roll(NW, L2, b, k, lad, log2w, ts, t, bk, lookahead == 5);
     }
     if (lookahead == 3) {
         if constexpr (NW == 1) {

@@ -253,8 +253,8 @@ __global__ void __launch_bounds__(256, P == 1 ? 6 : 4) k_ladder_pass1_roll(BankD
 // neighbour in its read; the right push carries the base after the window, the left
 // push the complement of the base before it).
 // ---------------------------------------------------------------------------
-template <int NW, int WS>
-__global__ void __launch_bounds__(256, 3) k_emit_roll(BankDev b, uint32_t k, const uint32_t* __restrict__ lad, uint32_t log2w,
+template <int NW, int WS, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_emit_roll(BankDev b, uint32_t k, const uint32_t* __restrict__ lad, uint32_t log2w,
                                                       uint32_t t_solid, TableDev t, BucketDev bk) {
     constexpr int NK = NW - WS;
     extern __shared__ __align__(16) uint64_t emit_smem[];
@@ -407,27 +407,43 @@ cudaError_t launch_ladder_pass1_roll(int nw, const Launch& L, const BankDev& b, 
     return windows_per_step == 2 ? lp1r_p<2>(nw, L, b, k, lad, log2w, t, hll12) : lp1r_p<1>(nw, L, b, k, lad, log2w, t, hll12);
 }
 
-template <int NW, int WS>
-static cudaError_t emr(const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w, uint32_t ts,
-                       const TableDev& t, const BucketDev& bk) {
+template <int NW, int WS, int MINB>
+static cudaError_t emr_b(const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w, uint32_t ts,
+                         const TableDev& t, const BucketDev& bk) {
     const size_t smem = (size_t)(L.block / 32) * (EMIT_WARP_WORDS(NW) + ROLL_STAGE_WORDS) * 8;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_emit_roll<NW, WS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(k_emit_roll<NW, WS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    k_emit_roll<NW, WS><<<roll_grid(k_emit_roll<NW, WS>, L, smem), L.block, smem, L.stream>>>(b, k, lad, log2w, ts, t, bk);
+    k_emit_roll<NW, WS, MINB><<<roll_grid(k_emit_roll<NW, WS, MINB>, L, smem), L.block, smem, L.stream>>>(b, k, lad, log2w, ts,
+                                                                                                          t, bk);
     return cudaGetLastError();
 }
+// Register budget: two blocks per SM for 256-bit keys (three windows of three key
+// words in flight spill at three blocks: k = 77 8.88 ms per 100x pass at three blocks,
+// 5.74 at two), three for narrower keys; two_blocks = two for every width.
+template <int NW, int WS>
+static cudaError_t emr(const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w, uint32_t ts,
+                       const TableDev& t, const BucketDev& bk, bool two_blocks) {
+    if constexpr (NW == 4) {
+        return emr_b<NW, WS, 2>(L, b, k, lad, log2w, ts, t, bk);
+    } else {
+        if (two_blocks) return emr_b<NW, WS, 2>(L, b, k, lad, log2w, ts, t, bk);
+        return emr_b<NW, WS, 3>(L, b, k, lad, log2w, ts, t, bk);
+    }
+}
 cudaError_t launch_emit_roll(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
-                             uint32_t t_solid, const TableDev& t, const BucketDev& bk) {
+                             uint32_t t_solid, const TableDev& t, const BucketDev& bk, bool two_blocks) {
     if (t_solid < 1 || t_solid > LADDER_MAX_LEVELS || log2w > 29) return cudaErrorInvalidValue;
     const uint32_t ws = (64u * (uint32_t)nw - 2u * k) >> 6;
-    if (nw == 1) return emr<1, 0>(L, b, k, lad, log2w, t_solid, t, bk);
-    if (nw == 2) return ws == 0 ? emr<2, 0>(L, b, k, lad, log2w, t_solid, t, bk) : emr<2, 1>(L, b, k, lad, log2w, t_solid, t, bk);
-    if (ws == 0) return emr<4, 0>(L, b, k, lad, log2w, t_solid, t, bk);
-    if (ws == 1) return emr<4, 1>(L, b, k, lad, log2w, t_solid, t, bk);
-    if (ws == 2) return emr<4, 2>(L, b, k, lad, log2w, t_solid, t, bk);
-    return emr<4, 3>(L, b, k, lad, log2w, t_solid, t, bk);
+    if (nw == 1) return emr<1, 0>(L, b, k, lad, log2w, t_solid, t, bk, two_blocks);
+    if (nw == 2)
+        return ws == 0 ? emr<2, 0>(L, b, k, lad, log2w, t_solid, t, bk, two_blocks)
+                       : emr<2, 1>(L, b, k, lad, log2w, t_solid, t, bk, two_blocks);
+    if (ws == 0) return emr<4, 0>(L, b, k, lad, log2w, t_solid, t, bk, two_blocks);
+    if (ws == 1) return emr<4, 1>(L, b, k, lad, log2w, t_solid, t, bk, two_blocks);
+    if (ws == 2) return emr<4, 2>(L, b, k, lad, log2w, t_solid, t, bk, two_blocks);
+    return emr<4, 3>(L, b, k, lad, log2w, t_solid, t, bk, two_blocks);
 }
 
 }  // namespace fbk

@@ -199,7 +199,8 @@ cudaError_t launch_emit_ladder(int nw, const Launch& L, const BankDev& b, uint32
 cudaError_t launch_ladder_pass1_roll(int nw, const Launch& L, const BankDev& b, uint32_t k, uint32_t* lad, uint32_t log2w,
                                      uint32_t t, uint32_t* hll12, int windows_per_step);
 cudaError_t launch_emit_roll(int nw, const Launch& L, const BankDev& b, uint32_t k, const uint32_t* lad, uint32_t log2w,
-                             uint32_t t_solid, const TableDev& t, const BucketDev& bk);
+                             uint32_t t_solid, const TableDev& t, const BucketDev& bk,
+                             bool two_blocks = false);
 
 // ---- multi-isolate waves (fbk_k_batch.cu) ----------------------------------------
 // read_base: n_iso + 1 global read indices (isolate i owns [read_base[i], read_base[i+1])).

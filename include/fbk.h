@@ -164,8 +164,8 @@ FBK_API fbk_status fbk_ctx_event_elapsed(fbk_ctx* ctx, int slot_a, int slot_b, d
  * windows per lane in the ladder pass 1, 3 = pipelined over chunks, 4 = one lane per read
  * with rolled k-mers, 5 = the same rolling two windows per step; 0 = by key width),
  * "emit_lookahead" (record emit with the gate loads 1 or 2 chunks ahead read by read,
- * 3 = 2 ahead over a flattened window stream, 4 = one lane per read with rolled k-mers;
- * 0 = by key width), "acc_filter"
+ * 3 = 2 ahead over a flattened window stream, 4 = one lane per read with rolled k-mers
+ * (the default), 5 = the same at two blocks per SM for every key width), "acc_filter"
  * (keys that cannot become SolidKmerNodes stay out of the table, see fbk_table_flags:
  * 0 never, 1 where it pays, 2 always), "upsert_all" (1: an unfiltered pass upserts every
  * bucket in one persistent launch), "upsert_queue" (1: filtered upserts queue the

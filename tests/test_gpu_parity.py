@@ -493,6 +493,8 @@ TUNINGS = [
     dict(ladder_ilp=3),                                   # ladder pass 1 pipelined over chunks
     dict(emit_lookahead=1),                               # gate loads one chunk ahead of the emit
     dict(emit_lookahead=2),                               # emit read by read, gate loads two chunks ahead
+    dict(emit_lookahead=3),                               # emit over the flattened window stream
+    dict(emit_lookahead=5),                               # rolled emit at two blocks per SM for every width
     dict(ladder_ilp=4, emit_lookahead=4),                 # one lane per read, k-mers rolled, runs staged in smem
     dict(ladder_ilp=5),                                   # the same pass 1 rolling two windows per step
     dict(acc_filter=0),                                   # every accumulated key kept
