@@ -64,7 +64,7 @@ struct fbk_ctx {
     // launch shapes (block size; grid 0 = 4 blocks per SM)
     int block_pass1 = 256, grid_pass1 = 0;
     int block_pass2 = 256, grid_pass2 = 0;
-    int block_emit = 128;  // record emit with the ladder gate (128 measured 2-5% faster than 256)
+    int block_emit = 128;  // flat and read-by-read record emits (128 measured 2-5% faster than 256); the rolled emit runs 256
     int block_misc = 256;
     // sweep sizing: bytes of sketch per pass-1 / solidity sweep, and bytes of table
     // per pass-2 slot range (the hot part of a range must stay L2-resident)
@@ -104,7 +104,10 @@ struct fbk_ctx {
     // same with every lane's probe advanced a slot per step (64/128-bit keys; per 100x
     // pass k = 21 5.60 -> 5.59 ms, k = 33 6.70 -> 6.58), 0 one launch per bucket
     int upsert_all = 2;
-    int acc_filter = 1;                   // keys with fewer records than min_trans_cov stay out of the table: 0 never, 1 for 256-bit keys, 2 always
+    // keys with fewer records than min_trans_cov stay out of the table: 0 never, 2 always,
+    // 1 where it pays (256-bit keys, and passes whose distinct k-mers exceed a fifth of
+    // their windows; acc_filter_on)
+    int acc_filter = 1;
     bool capturing = false;               // launches are being captured into a CUDA graph
 };
 
